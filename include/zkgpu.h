@@ -1,0 +1,149 @@
+/*
+ * zkgpu.h -- C ABI of the GB300 (sm_103a) prover hot path for pyZKP:
+ * BN254 G1 multi-scalar multiplication and the Fr NTT / iNTT / coset NTT.
+ *
+ * Drop-in boundary. The reference (fzybravery/pyZKP) reaches its GPU path through
+ * KernelFns registered under (OpType, Device.METAL, Backend.METAL)
+ * (runtime/kernels/metal/kernels.py:12-20) and called by Executor._run_node
+ * (runtime/executor.py:185-197). Those KernelFns are rebuilt in Python
+ * (pyzkp_gb300/plugin.py) on top of the entry points below, bound with ctypes
+ * (pyzkp_gb300/_native.py). Every entry point is plain C: pointers, sizes and
+ * integer status codes; no C++ exceptions cross the boundary.
+ *
+ * Data layout (identical bytes to the reference's "fr_mont_u64x4" buffers,
+ * runtime/metal/buffer.py:7-15 and runtime/kernels/cpu/kernels.py:135-141):
+ *   - a field element is 32 bytes, little endian, 8 x uint32 (= 4 x uint64) limbs;
+ *     "Montgomery" means the value a * 2^256 mod p, "canonical" the value itself;
+ *   - an affine G1 point is 64 bytes: x then y (Fq); (0, 0) denotes infinity.
+ * Device pointers are CUDA device addresses on the context's device.
+ * All functions return ZK_OK (0) or an error code; zk_last_error() describes the
+ * last failure of the calling thread.
+ */
+#ifndef ZKGPU_H
+#define ZKGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ZK_OK 0
+#define ZK_EINVAL 1 /* bad argument; the Python layer raises ValueError like the reference */
+#define ZK_ECUDA 2  /* CUDA runtime failure; RuntimeError */
+#define ZK_ENOMEM 3 /* device memory exhausted; MemoryError */
+#define ZK_ENODEV 4 /* no usable CUDA device; RuntimeError (runtime/context.py:33-34) */
+
+typedef struct zk_ctx zk_ctx;
+typedef struct zk_bases zk_bases;
+
+/* Message of the last failure on this thread ("" if none). */
+const char *zk_last_error(void);
+
+/* ABI version of this library. */
+int zk_version(void);
+
+/*
+ * Context: one device, one CUDA stream, cached NTT tables.
+ * Replaces MetalRuntime.create_default / MetalContext.create_default
+ * (runtime/metal/runtime.py:493-629, runtime/context.py:42-47).
+ */
+int zk_ctx_create(int device, zk_ctx **out);
+int zk_ctx_destroy(zk_ctx *ctx);
+/* Block until all work queued on the context stream has finished. */
+int zk_ctx_sync(zk_ctx *ctx);
+/* The context's cudaStream_t, for callers that enqueue their own work. */
+int zk_ctx_stream(zk_ctx *ctx, void **stream_out);
+/* Number of SMs of the context's device. */
+int zk_ctx_num_sms(zk_ctx *ctx, int *out);
+
+/*
+ * Device memory (stream-ordered pool of the context). Replaces
+ * MemoryPool.alloc_metal / release_metal (runtime/memory.py:56-91).
+ */
+int zk_alloc(zk_ctx *ctx, size_t bytes, void **dptr);
+int zk_free(zk_ctx *ctx, void *dptr);
+/* Copies on the context stream; both block until the copy is complete. */
+int zk_h2d(zk_ctx *ctx, void *dst_dev, const void *src_host, size_t bytes);
+int zk_d2h(zk_ctx *ctx, void *dst_host, const void *src_dev, size_t bytes);
+/* Page-locked host memory for fast copies. */
+int zk_host_alloc(size_t bytes, void **out);
+int zk_host_free(void *p);
+
+/*
+ * Fr vectors of n elements (device pointers, in-place allowed).
+ * zk_fr_to_mont / zk_fr_from_mont replace the Montgomery packing loops of
+ * _to_device / _from_device (runtime/kernels/cpu/kernels.py:98-172); to_mont
+ * reduces any 256-bit input modulo r first (int(x) % FR_MODULUS).
+ */
+int zk_fr_to_mont(zk_ctx *ctx, void *out, const void *in, size_t n);
+int zk_fr_from_mont(zk_ctx *ctx, void *out, const void *in, size_t n);
+/* Same for Fq (base-field coordinates, e.g. affine points as 2n elements). */
+int zk_fq_to_mont(zk_ctx *ctx, void *out, const void *in, size_t n);
+int zk_fq_from_mont(zk_ctx *ctx, void *out, const void *in, size_t n);
+/* out[i] = a[i] * b[i] (Montgomery in, Montgomery out): POINTWISE_MUL,
+ * runtime/kernels/metal/kernels.py:175-222 / runtime/metal/runtime.py:204-213. */
+int zk_fr_mul(zk_ctx *ctx, void *out, const void *a, const void *b, size_t n);
+/* out[i] = a[i] - b[i]: POLY_SUB on equal lengths, runtime/kernels/metal/kernels.py:122-167. */
+int zk_fr_sub(zk_ctx *ctx, void *out, const void *a, const void *b, size_t n);
+
+/*
+ * NTT family over Fr, natural order in and out, Montgomery in and out.
+ * Semantics of crypto/poly/ntt.py:103-146 and of the op KernelFns
+ * runtime/kernels/cpu/kernels.py:175-250 (which the Metal versions at
+ * runtime/kernels/metal/kernels.py:225-381,418-827 replace):
+ *   ZK_NTT_EVALS_FROM_COEFFS        evals[i] = sum_j a_j omega^(ij); the input of
+ *                                   in_len elements is zero-padded or truncated to n
+ *   ZK_NTT_COEFFS_FROM_EVALS        inverse; requires in_len == n
+ *   ZK_NTT_COSET_EVALS_FROM_COEFFS  a_j scaled by shift^j first (j < min(in_len, n))
+ *   ZK_NTT_COSET_COEFFS_FROM_EVALS  inverse, then coefficient i scaled by shift^-i
+ *                                   (by 0 for i > 0 when shift == 0, as ntt.py:136-146)
+ * omega and shift are 32-byte canonical little-endian values. omega must be a
+ * primitive n-th root of unity (omega^(n/2) == -1 for n >= 2), else ZK_EINVAL.
+ * n = 2^log_n, log_n <= 28 (2-adicity of r, crypto/poly/ntt.py:9,21-22).
+ * out holds n elements and must not overlap in.
+ */
+#define ZK_NTT_EVALS_FROM_COEFFS 0
+#define ZK_NTT_COEFFS_FROM_EVALS 1
+#define ZK_NTT_COSET_EVALS_FROM_COEFFS 2
+#define ZK_NTT_COSET_COEFFS_FROM_EVALS 3
+int zk_ntt(zk_ctx *ctx, int mode, void *out_dev, const void *in_dev, size_t in_len, uint32_t log_n,
+           const uint8_t omega[32], const uint8_t shift[32]);
+
+/*
+ * Resident G1 bases (affine, converted to Montgomery once on the device).
+ * Replaces the per-call packing of _pack_g1_point (runtime/metal/msm.py:13-34,
+ * 79-85, 200-204). Input: n affine canonical points, 64 bytes each, (0,0) = infinity,
+ * from host memory (zk_bases_create) or device memory (zk_bases_create_dev).
+ */
+int zk_bases_create(zk_ctx *ctx, const void *xy_canonical_host, size_t n, zk_bases **out);
+int zk_bases_create_dev(zk_ctx *ctx, const void *xy_canonical_dev, size_t n, zk_bases **out);
+int zk_bases_destroy(zk_bases *b);
+int zk_bases_count(const zk_bases *b, size_t *n);
+
+/*
+ * G1 MSM: sum_i scalars[i] * bases[offset + i] for i < n, returned as an affine
+ * canonical point (out_xy = x || y, 64 bytes; *out_is_inf = 1 and (0,0) for infinity).
+ * The result is the unique affine point, identical to crypto/msm/pippenger.py:10-64
+ * (through the op semantics of runtime/kernels/cpu/kernels.py:553-571) and to the
+ * Metal path metal_msm_g1 / metal_msm_g1_v2 (runtime/metal/msm.py:65-332).
+ * scalars_dev: n device elements, Montgomery (scalars_mont = 1, the TO_DEVICE form)
+ * or canonical 256-bit values (scalars_mont = 0; reduced mod r first).
+ * window_bits: 0 = automatic, else 4..20 (signed digits, 2^(c-1) buckets per window).
+ */
+int zk_msm_g1(zk_ctx *ctx, const zk_bases *bases, size_t offset, const void *scalars_dev, size_t n,
+              int scalars_mont, uint32_t window_bits, uint8_t out_xy[64], int *out_is_inf);
+
+/*
+ * out[i] = [k_i] P for one affine point P (host, canonical) and n scalars k_i
+ * (device, canonical); out is device memory of n affine canonical points.
+ * Used for synthetic bases [k_i]G and for key generation from known exponents.
+ */
+int zk_g1_fixed_base_mul(zk_ctx *ctx, const uint8_t point_xy[64], const void *k_dev, size_t n, void *out_xy_dev);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ZKGPU_H */

@@ -1,0 +1,290 @@
+// capi.cu -- extern "C" entry points declared in include/zkgpu.h.
+#include <cstring>
+#include <string>
+
+#include "zk_internal.cuh"
+
+namespace zk {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int scratch_alloc(Ctx* c, size_t bytes, void** p) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMallocAsync(p, bytes, c->stream);
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMallocAsync(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? ZK_ENOMEM : ZK_ECUDA;
+    }
+    return ZK_OK;
+}
+
+void scratch_free(Ctx* c, void* p) {
+    if (p) cudaFreeAsync(p, c->stream);
+}
+
+template <class F, int DIR>
+int convert(Ctx* c, void* out, const void* in, size_t n);
+int fr_binary(Ctx* c, int op, void* out, const void* a, const void* b, size_t n);
+int fixed_base_mul(Ctx* c, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_dev);
+
+}  // namespace zk
+
+using zk::Ctx;
+
+#define CTX_OR_FAIL(ctx)                         \
+    do {                                         \
+        if ((ctx) == nullptr) {                  \
+            zk::set_error("null zk_ctx");        \
+            return ZK_EINVAL;                    \
+        }                                        \
+        cudaError_t _e = cudaSetDevice((ctx)->impl.device); \
+        if (_e != cudaSuccess) {                 \
+            zk::set_error(cudaGetErrorString(_e)); \
+            return ZK_ECUDA;                     \
+        }                                        \
+    } while (0)
+
+extern "C" {
+
+const char* zk_last_error(void) { return zk::g_last_error.c_str(); }
+
+int zk_version(void) { return 1; }
+
+int zk_ctx_create(int device, zk_ctx** out) {
+    if (out == nullptr) {
+        zk::set_error("null output pointer");
+        return ZK_EINVAL;
+    }
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        zk::set_error(std::string("no CUDA device available: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "0"));
+        return ZK_ENODEV;
+    }
+    if (device < 0 || device >= count) {
+        zk::set_error("device index out of range");
+        return ZK_EINVAL;
+    }
+    ZK_TRY_CUDA(cudaSetDevice(device));
+    zk_ctx* c = new zk_ctx();
+    c->impl.device = device;
+    ZK_TRY_CUDA(cudaDeviceGetAttribute(&c->impl.num_sms, cudaDevAttrMultiProcessorCount, device));
+    ZK_TRY_CUDA(cudaStreamCreateWithFlags(&c->impl.stream, cudaStreamNonBlocking));
+    // keep freed stream-ordered allocations cached in the device pool
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t threshold = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+    *out = c;
+    return ZK_OK;
+}
+
+int zk_ctx_destroy(zk_ctx* ctx) {
+    if (ctx == nullptr) return ZK_OK;
+    cudaSetDevice(ctx->impl.device);
+    cudaStreamSynchronize(ctx->impl.stream);
+    for (auto& kv : ctx->impl.ntt_plans) {
+        for (void* p : kv.second->allocations) cudaFree(p);
+        delete kv.second;
+    }
+    cudaStreamDestroy(ctx->impl.stream);
+    delete ctx;
+    return ZK_OK;
+}
+
+int zk_ctx_sync(zk_ctx* ctx) {
+    CTX_OR_FAIL(ctx);
+    ZK_TRY_CUDA(cudaStreamSynchronize(ctx->impl.stream));
+    return ZK_OK;
+}
+
+int zk_ctx_stream(zk_ctx* ctx, void** stream_out) {
+    CTX_OR_FAIL(ctx);
+    *stream_out = reinterpret_cast<void*>(ctx->impl.stream);
+    return ZK_OK;
+}
+
+int zk_ctx_num_sms(zk_ctx* ctx, int* out) {
+    CTX_OR_FAIL(ctx);
+    *out = ctx->impl.num_sms;
+    return ZK_OK;
+}
+
+int zk_alloc(zk_ctx* ctx, size_t bytes, void** dptr) {
+    CTX_OR_FAIL(ctx);
+    if (dptr == nullptr) {
+        zk::set_error("null output pointer");
+        return ZK_EINVAL;
+    }
+    return zk::scratch_alloc(&ctx->impl, bytes, dptr);
+}
+
+int zk_free(zk_ctx* ctx, void* dptr) {
+    CTX_OR_FAIL(ctx);
+    zk::scratch_free(&ctx->impl, dptr);
+    return ZK_OK;
+}
+
+int zk_h2d(zk_ctx* ctx, void* dst_dev, const void* src_host, size_t bytes) {
+    CTX_OR_FAIL(ctx);
+    if (bytes == 0) return ZK_OK;
+    ZK_TRY_CUDA(cudaMemcpyAsync(dst_dev, src_host, bytes, cudaMemcpyHostToDevice, ctx->impl.stream));
+    ZK_TRY_CUDA(cudaStreamSynchronize(ctx->impl.stream));
+    return ZK_OK;
+}
+
+int zk_d2h(zk_ctx* ctx, void* dst_host, const void* src_dev, size_t bytes) {
+    CTX_OR_FAIL(ctx);
+    if (bytes == 0) return ZK_OK;
+    ZK_TRY_CUDA(cudaMemcpyAsync(dst_host, src_dev, bytes, cudaMemcpyDeviceToHost, ctx->impl.stream));
+    ZK_TRY_CUDA(cudaStreamSynchronize(ctx->impl.stream));
+    return ZK_OK;
+}
+
+int zk_host_alloc(size_t bytes, void** out) {
+    ZK_TRY_CUDA(cudaMallocHost(out, bytes ? bytes : 16));
+    return ZK_OK;
+}
+
+int zk_host_free(void* p) {
+    if (p) ZK_TRY_CUDA(cudaFreeHost(p));
+    return ZK_OK;
+}
+
+int zk_fr_to_mont(zk_ctx* ctx, void* out, const void* in, size_t n) {
+    CTX_OR_FAIL(ctx);
+    return zk::convert<zk::FrP, 1>(&ctx->impl, out, in, n);
+}
+
+int zk_fr_from_mont(zk_ctx* ctx, void* out, const void* in, size_t n) {
+    CTX_OR_FAIL(ctx);
+    return zk::convert<zk::FrP, 0>(&ctx->impl, out, in, n);
+}
+
+int zk_fq_to_mont(zk_ctx* ctx, void* out, const void* in, size_t n) {
+    CTX_OR_FAIL(ctx);
+    return zk::convert<zk::FqP, 1>(&ctx->impl, out, in, n);
+}
+
+int zk_fq_from_mont(zk_ctx* ctx, void* out, const void* in, size_t n) {
+    CTX_OR_FAIL(ctx);
+    return zk::convert<zk::FqP, 0>(&ctx->impl, out, in, n);
+}
+
+int zk_fr_mul(zk_ctx* ctx, void* out, const void* a, const void* b, size_t n) {
+    CTX_OR_FAIL(ctx);
+    return zk::fr_binary(&ctx->impl, 0, out, a, b, n);
+}
+
+int zk_fr_sub(zk_ctx* ctx, void* out, const void* a, const void* b, size_t n) {
+    CTX_OR_FAIL(ctx);
+    return zk::fr_binary(&ctx->impl, 1, out, a, b, n);
+}
+
+int zk_ntt(zk_ctx* ctx, int mode, void* out_dev, const void* in_dev, size_t in_len, uint32_t log_n,
+           const uint8_t omega[32], const uint8_t shift[32]) {
+    CTX_OR_FAIL(ctx);
+    static const uint8_t one[32] = {1};
+    if (omega == nullptr) {
+        zk::set_error("null omega");
+        return ZK_EINVAL;
+    }
+    return zk::ntt_run(&ctx->impl, mode, static_cast<zk::fe*>(out_dev), static_cast<const zk::fe*>(in_dev), in_len,
+                       log_n, omega, shift ? shift : one);
+}
+
+static int bases_from_dev_canonical(zk_ctx* ctx, const void* xy_dev, size_t n, zk_bases** out) {
+    zk_bases* b = new zk_bases();
+    b->ctx = ctx;
+    b->n = n;
+    b->dev = nullptr;
+    int rc = zk::scratch_alloc(&ctx->impl, n * sizeof(zk::affine_t), reinterpret_cast<void**>(&b->dev));
+    if (rc != ZK_OK) {
+        delete b;
+        return rc;
+    }
+    // (x, y) canonical -> Montgomery, as 2n base-field elements; (0, 0) stays (0, 0)
+    rc = zk::convert<zk::FqP, 1>(&ctx->impl, b->dev, xy_dev, 2 * n);
+    if (rc != ZK_OK) {
+        zk::scratch_free(&ctx->impl, b->dev);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return ZK_OK;
+}
+
+int zk_bases_create(zk_ctx* ctx, const void* xy_canonical_host, size_t n, zk_bases** out) {
+    CTX_OR_FAIL(ctx);
+    if (out == nullptr || (n && xy_canonical_host == nullptr)) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    void* tmp = nullptr;
+    int rc = zk::scratch_alloc(&ctx->impl, n * 64, &tmp);
+    if (rc != ZK_OK) return rc;
+    if (n) ZK_TRY_CUDA(cudaMemcpyAsync(tmp, xy_canonical_host, n * 64, cudaMemcpyHostToDevice, ctx->impl.stream));
+    rc = bases_from_dev_canonical(ctx, tmp, n, out);
+    zk::scratch_free(&ctx->impl, tmp);
+    if (rc == ZK_OK) ZK_TRY_CUDA(cudaStreamSynchronize(ctx->impl.stream));
+    return rc;
+}
+
+int zk_bases_create_dev(zk_ctx* ctx, const void* xy_canonical_dev, size_t n, zk_bases** out) {
+    CTX_OR_FAIL(ctx);
+    if (out == nullptr || (n && xy_canonical_dev == nullptr)) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    int rc = bases_from_dev_canonical(ctx, xy_canonical_dev, n, out);
+    if (rc == ZK_OK) ZK_TRY_CUDA(cudaStreamSynchronize(ctx->impl.stream));
+    return rc;
+}
+
+int zk_bases_destroy(zk_bases* b) {
+    if (b == nullptr) return ZK_OK;
+    cudaSetDevice(b->ctx->impl.device);
+    zk::scratch_free(&b->ctx->impl, b->dev);
+    delete b;
+    return ZK_OK;
+}
+
+int zk_bases_count(const zk_bases* b, size_t* n) {
+    if (b == nullptr || n == nullptr) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    *n = b->n;
+    return ZK_OK;
+}
+
+int zk_msm_g1(zk_ctx* ctx, const zk_bases* bases, size_t offset, const void* scalars_dev, size_t n, int scalars_mont,
+              uint32_t window_bits, uint8_t out_xy[64], int* out_is_inf) {
+    CTX_OR_FAIL(ctx);
+    if (bases == nullptr || out_xy == nullptr || out_is_inf == nullptr || (n && scalars_dev == nullptr)) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    if (offset > bases->n || n > bases->n - offset) {
+        zk::set_error("scalars length exceeds points length");
+        return ZK_EINVAL;
+    }
+    return zk::msm_run(&ctx->impl, bases->dev + offset, static_cast<const zk::fe*>(scalars_dev), n, scalars_mont,
+                       window_bits, out_xy, out_is_inf);
+}
+
+int zk_g1_fixed_base_mul(zk_ctx* ctx, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_xy_dev) {
+    CTX_OR_FAIL(ctx);
+    if (point_xy == nullptr) {
+        zk::set_error("null point");
+        return ZK_EINVAL;
+    }
+    return zk::fixed_base_mul(&ctx->impl, point_xy, k_dev, n, out_xy_dev);
+}
+
+}  // extern "C"

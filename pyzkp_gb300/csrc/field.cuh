@@ -1,0 +1,317 @@
+// field.cuh -- BN254 Fr / Fq arithmetic for sm_103a, 8 x 32-bit limbs, Montgomery R = 2^256.
+//
+// The Montgomery form uses R = 2^256, the same as the reference's 4 x u64 packing
+// (runtime/kernels/cpu/kernels.py:46-50,135-141; runtime/metal/runtime.py:30-40 and
+// runtime/metal/ecc_source.py:14-25 hold the same moduli), so the bytes of a device
+// element are the bytes of the reference's "fr_mont_u64x4" element.
+//
+// Multiplication is CIOS (coarsely integrated operand scanning): per limb b_i of
+// the multiplier, one carry chain adds the low halves a_j*b_i into t_j and one adds
+// the high halves into t_{j+1}; then m = t_0 * (-p^-1) and two chains add m*p and
+// shift one limb. Every carry chain is one inline-PTX block (mad.lo.cc / madc.hi.cc
+// map to IMAD with carry in/out), so carries stay in the condition-code register.
+// Both moduli are below 2^254, so the running value stays below 2^288 (9 limbs)
+// and below 2p after each row; one conditional subtraction yields the canonical
+// representative in [0, p). All results are fully reduced: equal values have equal bits.
+#pragma once
+#include <cstdint>
+
+namespace zk {
+
+// Modulus, Montgomery one (2^256 mod p) and R^2 mod p as constexpr limb accessors, so
+// unrolled code folds them into immediates.
+struct FrP {
+    __host__ __device__ static constexpr uint32_t P(int i) { return i == 0 ? 0xf0000001u : i == 1 ? 0x43e1f593u : i == 2 ? 0x79b97091u : i == 3 ? 0x2833e848u : i == 4 ? 0x8181585du : i == 5 ? 0xb85045b6u : i == 6 ? 0xe131a029u : 0x30644e72u; }
+    static constexpr uint32_t INV = 0xefffffffu  /* -r^-1 mod 2^32 */;
+    __host__ __device__ static constexpr uint32_t ONE(int i) { return i == 0 ? 0x4ffffffbu : i == 1 ? 0xac96341cu : i == 2 ? 0x9f60cd29u : i == 3 ? 0x36fc7695u : i == 4 ? 0x7879462eu : i == 5 ? 0x666ea36fu : i == 6 ? 0x9a07df2fu : 0x0e0a77c1u; }
+    __host__ __device__ static constexpr uint32_t R2(int i) { return i == 0 ? 0xae216da7u : i == 1 ? 0x1bb8e645u : i == 2 ? 0xe35c59e3u : i == 3 ? 0x53fe3ab1u : i == 4 ? 0x53bb8085u : i == 5 ? 0x8c49833du : i == 6 ? 0x7f4e44a5u : 0x0216d0b1u; }
+};
+
+struct FqP {
+    __host__ __device__ static constexpr uint32_t P(int i) { return i == 0 ? 0xd87cfd47u : i == 1 ? 0x3c208c16u : i == 2 ? 0x6871ca8du : i == 3 ? 0x97816a91u : i == 4 ? 0x8181585du : i == 5 ? 0xb85045b6u : i == 6 ? 0xe131a029u : 0x30644e72u; }
+    static constexpr uint32_t INV = 0xe4866389u  /* -q^-1 mod 2^32 */;
+    __host__ __device__ static constexpr uint32_t ONE(int i) { return i == 0 ? 0xc58f0d9du : i == 1 ? 0xd35d438du : i == 2 ? 0xf5c70b3du : i == 3 ? 0x0a78eb28u : i == 4 ? 0x7879462cu : i == 5 ? 0x666ea36fu : i == 6 ? 0x9a07df2fu : 0x0e0a77c1u; }
+    __host__ __device__ static constexpr uint32_t R2(int i) { return i == 0 ? 0x538afa89u : i == 1 ? 0xf32cfc5bu : i == 2 ? 0xd44501fbu : i == 3 ? 0xb5e71911u : i == 4 ? 0x0a417ff6u : i == 5 ? 0x47ab1effu : i == 6 ? 0xcab8351fu : 0x06d89f71u; }
+};
+
+// One field element: 8 little-endian 32-bit limbs (32 bytes, 32-byte aligned in memory).
+struct __align__(16) fe {
+    uint32_t v[8];
+};
+
+template <class F>
+__device__ __forceinline__ fe fe_one() {
+    fe r;
+#pragma unroll
+    for (int i = 0; i < 8; i++) r.v[i] = F::ONE(i);
+    return r;
+}
+
+__device__ __forceinline__ fe fe_zero() {
+    fe r;
+#pragma unroll
+    for (int i = 0; i < 8; i++) r.v[i] = 0;
+    return r;
+}
+
+__device__ __forceinline__ bool fe_is_zero(const fe& a) {
+    uint32_t x = a.v[0] | a.v[1] | a.v[2] | a.v[3] | a.v[4] | a.v[5] | a.v[6] | a.v[7];
+    return x == 0;
+}
+
+__device__ __forceinline__ bool fe_eq(const fe& a, const fe& b) {
+    uint32_t x = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) x |= a.v[i] ^ b.v[i];
+    return x == 0;
+}
+
+// r = t - p if t >= p else t, for t < 2p (< 2^255).
+template <class F>
+__device__ __forceinline__ fe fe_reduce_once(const fe& t) {
+    fe s;
+    uint32_t borrow;
+    asm("sub.cc.u32  %0, %9, %17;\n\t"
+        "subc.cc.u32 %1, %10, %18;\n\t"
+        "subc.cc.u32 %2, %11, %19;\n\t"
+        "subc.cc.u32 %3, %12, %20;\n\t"
+        "subc.cc.u32 %4, %13, %21;\n\t"
+        "subc.cc.u32 %5, %14, %22;\n\t"
+        "subc.cc.u32 %6, %15, %23;\n\t"
+        "subc.cc.u32 %7, %16, %24;\n\t"
+        "subc.u32    %8, 0, 0;"
+        : "=r"(s.v[0]), "=r"(s.v[1]), "=r"(s.v[2]), "=r"(s.v[3]), "=r"(s.v[4]), "=r"(s.v[5]), "=r"(s.v[6]),
+          "=r"(s.v[7]), "=r"(borrow)
+        : "r"(t.v[0]), "r"(t.v[1]), "r"(t.v[2]), "r"(t.v[3]), "r"(t.v[4]), "r"(t.v[5]), "r"(t.v[6]), "r"(t.v[7]),
+          "n"(F::P(0)), "n"(F::P(1)), "n"(F::P(2)), "n"(F::P(3)), "n"(F::P(4)), "n"(F::P(5)), "n"(F::P(6)),
+          "n"(F::P(7)));
+    fe r;
+#pragma unroll
+    for (int i = 0; i < 8; i++) r.v[i] = borrow ? t.v[i] : s.v[i];
+    return r;
+}
+
+template <class F>
+__device__ __forceinline__ fe fe_add(const fe& a, const fe& b) {
+    fe t;
+    asm("add.cc.u32  %0, %8, %16;\n\t"
+        "addc.cc.u32 %1, %9, %17;\n\t"
+        "addc.cc.u32 %2, %10, %18;\n\t"
+        "addc.cc.u32 %3, %11, %19;\n\t"
+        "addc.cc.u32 %4, %12, %20;\n\t"
+        "addc.cc.u32 %5, %13, %21;\n\t"
+        "addc.cc.u32 %6, %14, %22;\n\t"
+        "addc.u32    %7, %15, %23;"
+        : "=r"(t.v[0]), "=r"(t.v[1]), "=r"(t.v[2]), "=r"(t.v[3]), "=r"(t.v[4]), "=r"(t.v[5]), "=r"(t.v[6]),
+          "=r"(t.v[7])
+        : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]), "r"(a.v[7]),
+          "r"(b.v[0]), "r"(b.v[1]), "r"(b.v[2]), "r"(b.v[3]), "r"(b.v[4]), "r"(b.v[5]), "r"(b.v[6]), "r"(b.v[7]));
+    return fe_reduce_once<F>(t);
+}
+
+template <class F>
+__device__ __forceinline__ fe fe_sub(const fe& a, const fe& b) {
+    fe t;
+    uint32_t m;
+    asm("sub.cc.u32  %0, %9, %17;\n\t"
+        "subc.cc.u32 %1, %10, %18;\n\t"
+        "subc.cc.u32 %2, %11, %19;\n\t"
+        "subc.cc.u32 %3, %12, %20;\n\t"
+        "subc.cc.u32 %4, %13, %21;\n\t"
+        "subc.cc.u32 %5, %14, %22;\n\t"
+        "subc.cc.u32 %6, %15, %23;\n\t"
+        "subc.cc.u32 %7, %16, %24;\n\t"
+        "subc.u32    %8, 0, 0;"
+        : "=r"(t.v[0]), "=r"(t.v[1]), "=r"(t.v[2]), "=r"(t.v[3]), "=r"(t.v[4]), "=r"(t.v[5]), "=r"(t.v[6]),
+          "=r"(t.v[7]), "=r"(m)
+        : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]), "r"(a.v[7]),
+          "r"(b.v[0]), "r"(b.v[1]), "r"(b.v[2]), "r"(b.v[3]), "r"(b.v[4]), "r"(b.v[5]), "r"(b.v[6]), "r"(b.v[7]));
+    fe r;
+    asm("add.cc.u32  %0, %8, %16;\n\t"
+        "addc.cc.u32 %1, %9, %17;\n\t"
+        "addc.cc.u32 %2, %10, %18;\n\t"
+        "addc.cc.u32 %3, %11, %19;\n\t"
+        "addc.cc.u32 %4, %12, %20;\n\t"
+        "addc.cc.u32 %5, %13, %21;\n\t"
+        "addc.cc.u32 %6, %14, %22;\n\t"
+        "addc.u32    %7, %15, %23;"
+        : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]), "=r"(r.v[4]), "=r"(r.v[5]), "=r"(r.v[6]),
+          "=r"(r.v[7])
+        : "r"(t.v[0]), "r"(t.v[1]), "r"(t.v[2]), "r"(t.v[3]), "r"(t.v[4]), "r"(t.v[5]), "r"(t.v[6]), "r"(t.v[7]),
+          "r"(F::P(0) & m), "r"(F::P(1) & m), "r"(F::P(2) & m), "r"(F::P(3) & m), "r"(F::P(4) & m),
+          "r"(F::P(5) & m), "r"(F::P(6) & m), "r"(F::P(7) & m));
+    return r;
+}
+
+template <class F>
+__device__ __forceinline__ fe fe_neg(const fe& a) {
+    return fe_sub<F>(fe_zero(), a);
+}
+
+template <class F>
+__device__ __forceinline__ fe fe_dbl(const fe& a) {
+    return fe_add<F>(a, a);
+}
+
+// r = a * b * 2^-256 mod p (CIOS, see the file header).
+template <class F>
+__device__ __forceinline__ fe fe_mul(const fe& a, const fe& b) {
+    uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0, t8 = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const uint32_t bi = b.v[i];
+        // t += lo(a * bi)
+        asm("mad.lo.cc.u32  %0, %9, %17, %0;\n\t"
+            "madc.lo.cc.u32 %1, %10, %17, %1;\n\t"
+            "madc.lo.cc.u32 %2, %11, %17, %2;\n\t"
+            "madc.lo.cc.u32 %3, %12, %17, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %17, %4;\n\t"
+            "madc.lo.cc.u32 %5, %14, %17, %5;\n\t"
+            "madc.lo.cc.u32 %6, %15, %17, %6;\n\t"
+            "madc.lo.cc.u32 %7, %16, %17, %7;\n\t"
+            "addc.u32       %8, %8, 0;"
+            : "+r"(t0), "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8)
+            : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]),
+              "r"(a.v[7]), "r"(bi));
+        // t += hi(a * bi) << 32
+        asm("mad.hi.cc.u32  %0, %8, %16, %0;\n\t"
+            "madc.hi.cc.u32 %1, %9, %16, %1;\n\t"
+            "madc.hi.cc.u32 %2, %10, %16, %2;\n\t"
+            "madc.hi.cc.u32 %3, %11, %16, %3;\n\t"
+            "madc.hi.cc.u32 %4, %12, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.hi.cc.u32 %6, %14, %16, %6;\n\t"
+            "madc.hi.u32    %7, %15, %16, %7;"
+            : "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8)
+            : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]),
+              "r"(a.v[7]), "r"(bi));
+        const uint32_t m = t0 * F::INV;
+        // t += lo(m * p)
+        asm("mad.lo.cc.u32  %0, %9, %10, %0;\n\t"
+            "madc.lo.cc.u32 %1, %9, %11, %1;\n\t"
+            "madc.lo.cc.u32 %2, %9, %12, %2;\n\t"
+            "madc.lo.cc.u32 %3, %9, %13, %3;\n\t"
+            "madc.lo.cc.u32 %4, %9, %14, %4;\n\t"
+            "madc.lo.cc.u32 %5, %9, %15, %5;\n\t"
+            "madc.lo.cc.u32 %6, %9, %16, %6;\n\t"
+            "madc.lo.cc.u32 %7, %9, %17, %7;\n\t"
+            "addc.u32       %8, %8, 0;"
+            : "+r"(t0), "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8)
+            : "r"(m), "n"(F::P(0)), "n"(F::P(1)), "n"(F::P(2)), "n"(F::P(3)), "n"(F::P(4)), "n"(F::P(5)),
+              "n"(F::P(6)), "n"(F::P(7)));
+        // t += hi(m * p) << 32, then shift one limb (t0 is now zero)
+        asm("mad.hi.cc.u32  %0, %8, %9, %0;\n\t"
+            "madc.hi.cc.u32 %1, %8, %10, %1;\n\t"
+            "madc.hi.cc.u32 %2, %8, %11, %2;\n\t"
+            "madc.hi.cc.u32 %3, %8, %12, %3;\n\t"
+            "madc.hi.cc.u32 %4, %8, %13, %4;\n\t"
+            "madc.hi.cc.u32 %5, %8, %14, %5;\n\t"
+            "madc.hi.cc.u32 %6, %8, %15, %6;\n\t"
+            "madc.hi.u32    %7, %8, %16, %7;"
+            : "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8)
+            : "r"(m), "n"(F::P(0)), "n"(F::P(1)), "n"(F::P(2)), "n"(F::P(3)), "n"(F::P(4)), "n"(F::P(5)),
+              "n"(F::P(6)), "n"(F::P(7)));
+        t0 = t1;
+        t1 = t2;
+        t2 = t3;
+        t3 = t4;
+        t4 = t5;
+        t5 = t6;
+        t6 = t7;
+        t7 = t8;
+        t8 = 0;
+    }
+    fe t;
+    t.v[0] = t0;
+    t.v[1] = t1;
+    t.v[2] = t2;
+    t.v[3] = t3;
+    t.v[4] = t4;
+    t.v[5] = t5;
+    t.v[6] = t6;
+    t.v[7] = t7;
+    return fe_reduce_once<F>(t);
+}
+
+template <class F>
+__device__ __forceinline__ fe fe_sqr(const fe& a) {
+    return fe_mul<F>(a, a);
+}
+
+// canonical value (any 256-bit input, reduced mod p first) -> Montgomery form
+template <class F>
+__device__ __forceinline__ fe fe_to_mont(fe a) {
+    // at most floor((2^256 - 1) / p) = 5 subtractions for both BN254 moduli
+#pragma unroll 1
+    for (int k = 0; k < 5; k++) {
+        fe s;
+        uint32_t br;
+        asm("sub.cc.u32  %0, %9, %17;\n\t"
+            "subc.cc.u32 %1, %10, %18;\n\t"
+            "subc.cc.u32 %2, %11, %19;\n\t"
+            "subc.cc.u32 %3, %12, %20;\n\t"
+            "subc.cc.u32 %4, %13, %21;\n\t"
+            "subc.cc.u32 %5, %14, %22;\n\t"
+            "subc.cc.u32 %6, %15, %23;\n\t"
+            "subc.cc.u32 %7, %16, %24;\n\t"
+            "subc.u32    %8, 0, 0;"
+            : "=r"(s.v[0]), "=r"(s.v[1]), "=r"(s.v[2]), "=r"(s.v[3]), "=r"(s.v[4]), "=r"(s.v[5]), "=r"(s.v[6]),
+              "=r"(s.v[7]), "=r"(br)
+            : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]),
+              "r"(a.v[7]), "n"(F::P(0)), "n"(F::P(1)), "n"(F::P(2)), "n"(F::P(3)), "n"(F::P(4)), "n"(F::P(5)),
+              "n"(F::P(6)), "n"(F::P(7)));
+        if (br) break;  // a < p
+        a = s;
+    }
+    fe r2;
+#pragma unroll
+    for (int i = 0; i < 8; i++) r2.v[i] = F::R2(i);
+    return fe_mul<F>(a, r2);
+}
+
+template <class F>
+__device__ __forceinline__ fe fe_from_mont(const fe& a) {
+    fe one;
+#pragma unroll
+    for (int i = 0; i < 8; i++) one.v[i] = i == 0 ? 1u : 0u;
+    return fe_mul<F>(a, one);
+}
+
+// 32-byte element loads / stores as two 16-byte vector accesses
+__device__ __forceinline__ fe fe_load(const fe* p) {
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+    uint4 lo = q[0], hi = q[1];
+    fe r;
+    r.v[0] = lo.x;
+    r.v[1] = lo.y;
+    r.v[2] = lo.z;
+    r.v[3] = lo.w;
+    r.v[4] = hi.x;
+    r.v[5] = hi.y;
+    r.v[6] = hi.z;
+    r.v[7] = hi.w;
+    return r;
+}
+
+__device__ __forceinline__ fe fe_ldg(const fe* p) {
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+    uint4 lo = __ldg(q), hi = __ldg(q + 1);
+    fe r;
+    r.v[0] = lo.x;
+    r.v[1] = lo.y;
+    r.v[2] = lo.z;
+    r.v[3] = lo.w;
+    r.v[4] = hi.x;
+    r.v[5] = hi.y;
+    r.v[6] = hi.z;
+    r.v[7] = hi.w;
+    return r;
+}
+
+__device__ __forceinline__ void fe_store(fe* p, const fe& a) {
+    uint4* q = reinterpret_cast<uint4*>(p);
+    q[0] = make_uint4(a.v[0], a.v[1], a.v[2], a.v[3]);
+    q[1] = make_uint4(a.v[4], a.v[5], a.v[6], a.v[7]);
+}
+
+}  // namespace zk

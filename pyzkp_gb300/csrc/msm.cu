@@ -1,0 +1,414 @@
+// msm.cu -- BN254 G1 multi-scalar multiplication (Pippenger, signed digits, CSR buckets).
+//
+// Result semantics: the unique affine point sum_i s_i P_i, identical to
+// crypto/msm/pippenger.py:10-64 and runtime/metal/msm.py:179-332 (metal_msm_g1_v2).
+// The reference's Metal v2 pipeline is: signed-digit encode in Python
+// (runtime/metal/msm.py:145-177), histogram / single-thread prefix sum / scatter
+// into CSR (runtime/metal/ecc_source.py:437-496), one thread per bucket
+// (:499-535), one thread per window reduce (:540-566), CPU Horner (msm.py:322-332).
+//
+// This pipeline (all on the device except the last ~W*13 point additions):
+//  1. msm_digits_kernel   scalar -> W signed c-bit digits (|d| <= 2^(c-1)); CSR
+//                         histogram with warp-aggregated atomics (__match_any_sync).
+//  2. device scan         counters -> CSR row pointers (scan.cu).
+//  3. msm_scatter_kernel  (window, |digit|) buckets: entry = point index | sign << 31.
+//  4. msm_accumulate_*    equal-size segments of S entries per thread (load balanced
+//                         even when one bucket holds 5% of all points); buckets wholly
+//                         inside a segment are final; a bucket that straddles segment
+//                         boundaries leaves partial sums that tree rounds over groups
+//                         of 32 units merge, deciding "straddles" from the row pointers.
+//  5. msm_bucket_blocks   per window, blocks of g buckets: sum_b b*B_b = sum_j E_j + g*WS(Y)
+//                         with Y_j the block sums and E_j = -(sum of the g-1 prefix sums).
+//  6. msm_targets_kernel  WS(Y) = sum_j Y_j + sum_k 2^k M_k with M_k the sum of the Y_j
+//                         whose index has bit k set: plain sums, reduced by CTA trees.
+//  7. host: per window S_w = T_E + g (T_Y + sum_k 2^k M_k), then Horner over windows.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "zk_internal.cuh"
+
+namespace zk {
+
+int device_exclusive_scan(Ctx* c, uint32_t* data, size_t n, uint32_t* total);
+
+static constexpr uint32_t kNone = 0xffffffffu;
+static constexpr uint32_t kSegment = 32;   // entries per thread in the first accumulation round
+static constexpr uint32_t kGroup = 32;     // units merged per thread in later rounds
+static constexpr uint32_t kBlockG = 16;    // buckets per block in the window reduction
+static constexpr int kTargetThreads = 256;
+
+struct MsmShape {
+    uint32_t c;        // window bits
+    uint32_t W;        // windows
+    uint32_t B;        // buckets per window (|digit| in 1..B)
+    uint32_t g;        // block size of the window reduction (<= B)
+    uint32_t G;        // blocks per window
+    uint32_t K;        // log2(G)
+    uint32_t targets;  // 2 + K
+};
+
+static MsmShape make_shape(uint32_t c) {
+    MsmShape s;
+    s.c = c;
+    s.W = (255 + c - 1) / c;  // W*c >= 255 so the top window never carries out (scalars < r < 2^254)
+    s.B = 1u << (c - 1);
+    s.g = std::min<uint32_t>(kBlockG, s.B);
+    s.G = s.B / s.g;
+    s.K = 0;
+    while ((1u << s.K) < s.G) s.K++;
+    s.targets = 2 + s.K;
+    return s;
+}
+
+uint32_t msm_auto_window(size_t n) {
+    uint32_t lg = 0;
+    while ((1ull << lg) < n) lg++;
+    int c = (int)lg - 3;
+    if (c < 4) c = 4;
+    if (c > 16) c = 16;
+    return (uint32_t)c;
+}
+
+// ---- 1. digits + histogram ----------------------------------------------------
+__device__ __forceinline__ uint32_t bits_at(const fe& s, uint32_t k, uint32_t c) {
+    const uint32_t limb = k >> 5, off = k & 31;
+    uint64_t v = s.v[limb];
+    if (limb + 1 < 8) v |= (uint64_t)s.v[limb + 1] << 32;
+    // c <= 20 and off <= 31 keep off + c <= 51 bits: two limbs always suffice
+    return (uint32_t)((v >> off) & ((1ull << c) - 1));
+}
+
+__device__ __forceinline__ void warp_aggregated_inc(uint32_t* counters, uint32_t key, bool active) {
+    const uint32_t live = __ballot_sync(0xffffffffu, active);
+    if (!active) return;
+    const uint32_t peers = __match_any_sync(live, key);
+    const int leader = __ffs(peers) - 1;
+    if ((int)(threadIdx.x & 31) == leader) atomicAdd(counters + key, (uint32_t)__popc(peers));
+}
+
+__global__ void msm_digits_kernel(const fe* __restrict__ scalars, const affine_t* __restrict__ bases, uint32_t n,
+                                  int scalars_mont, MsmShape sh, uint32_t* __restrict__ digits,
+                                  uint32_t* __restrict__ counts) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    fe s = fe_zero();
+    if (valid) {
+        s = fe_ldg(scalars + i);
+        s = scalars_mont ? fe_from_mont<FrP>(s) : fe_from_mont<FrP>(fe_to_mont<FrP>(s));
+        if (affine_is_inf(affine_load(bases + i))) s = fe_zero();
+    }
+    uint32_t carry = 0;
+    const uint32_t half = 1u << (sh.c - 1);
+    for (uint32_t w = 0; w < sh.W; w++) {
+        uint32_t v = bits_at(s, w * sh.c, sh.c) + carry;
+        uint32_t mag, neg;
+        if (w + 1 < sh.W && v > half) {  // v in (2^(c-1), 2^c]: digit v - 2^c in [-2^(c-1)+1, 0]
+            mag = (1u << sh.c) - v;
+            neg = 1;
+            carry = 1;
+        } else {  // v in [0, 2^(c-1)] (the top window is at most 2^(c-1), see make_shape)
+            mag = v;
+            neg = 0;
+            carry = 0;
+        }
+        const bool nz = valid && mag != 0;
+        if (valid) digits[(size_t)w * n + i] = nz ? (mag | (neg << 31)) : 0u;
+        warp_aggregated_inc(counts, w * sh.B + (mag - 1), nz);
+    }
+}
+
+// ---- 3. scatter into CSR ------------------------------------------------------
+__global__ void msm_scatter_kernel(const uint32_t* __restrict__ digits, uint32_t n, MsmShape sh,
+                                   uint32_t* __restrict__ cursor, uint32_t* __restrict__ entries,
+                                   uint32_t* __restrict__ keys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    for (uint32_t w = 0; w < sh.W; w++) {
+        const uint32_t d = valid ? digits[(size_t)w * n + i] : 0u;
+        const bool nz = d != 0;
+        const uint32_t key = w * sh.B + (d & 0x7fffffffu) - 1;
+        const uint32_t live = __ballot_sync(0xffffffffu, nz);
+        if (nz) {
+            const uint32_t peers = __match_any_sync(live, key);
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(peers) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(cursor + key, (uint32_t)__popc(peers));
+            base = __shfl_sync(peers, base, leader);
+            const uint32_t rank = __popc(peers & ((1u << lane) - 1));
+            entries[base + rank] = i | (d & 0x80000000u);
+            keys[base + rank] = key;
+        }
+    }
+}
+
+// ---- 4. accumulation ------------------------------------------------------------
+// Emit the accumulated sum of `key` over entry range [e0, e1): final if the bucket
+// lies inside the range, else into the unit's first (bucket began earlier) or last
+// (bucket continues later) slot.
+__device__ __forceinline__ void emit_piece(uint32_t key, const xyzz_t& acc, uint32_t e0, uint32_t e1,
+                                           const uint32_t* __restrict__ row_ptr, xyzz_t* __restrict__ buckets,
+                                           uint32_t* slot_keys, xyzz_t* slot_pts, uint32_t unit) {
+    if (row_ptr[key] < e0) {
+        slot_keys[2 * unit] = key;
+        xyzz_store(slot_pts + 2 * unit, acc);
+    } else if (row_ptr[key + 1] > e1) {
+        slot_keys[2 * unit + 1] = key;
+        xyzz_store(slot_pts + 2 * unit + 1, acc);
+    } else {
+        xyzz_store(buckets + key, acc);
+    }
+}
+
+__global__ void __launch_bounds__(128) msm_accumulate_kernel(const uint32_t* __restrict__ entries,
+                                                             const uint32_t* __restrict__ keys,
+                                                             const uint32_t* __restrict__ d_total,
+                                                             const uint32_t* __restrict__ row_ptr,
+                                                             const affine_t* __restrict__ bases, uint32_t units,
+                                                             xyzz_t* __restrict__ buckets,
+                                                             uint32_t* __restrict__ slot_keys,
+                                                             xyzz_t* __restrict__ slot_pts) {
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= units) return;
+    slot_keys[2 * u] = kNone;
+    slot_keys[2 * u + 1] = kNone;
+    const uint32_t M = *d_total;
+    const uint32_t e0 = u * kSegment;
+    if (e0 >= M) return;
+    const uint32_t e1 = min(e0 + kSegment, M);
+    uint32_t cur = keys[e0];
+    xyzz_t acc = xyzz_inf();
+    for (uint32_t e = e0; e < e1; e++) {
+        const uint32_t k = keys[e];
+        if (k != cur) {
+            emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
+            cur = k;
+            acc = xyzz_inf();
+        }
+        const uint32_t ent = entries[e];
+        affine_t p = affine_load(bases + (ent & 0x7fffffffu));
+        if (ent >> 31) p.y = fe_neg<FqP>(p.y);
+        acc = xyzz_madd(acc, p.x, p.y);
+    }
+    emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
+}
+
+// Round r >= 2: unit u merges the slots of units [u*kGroup, (u+1)*kGroup) of the previous
+// round, covering entries [u * span, (u+1) * span) with span = kSegment * kGroup^(r-1).
+__global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restrict__ in_keys,
+                                                        const xyzz_t* __restrict__ in_pts, uint32_t in_units,
+                                                        const uint32_t* __restrict__ d_total,
+                                                        const uint32_t* __restrict__ row_ptr, uint64_t span,
+                                                        uint32_t units, xyzz_t* __restrict__ buckets,
+                                                        uint32_t* __restrict__ slot_keys,
+                                                        xyzz_t* __restrict__ slot_pts) {
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= units) return;
+    slot_keys[2 * u] = kNone;
+    slot_keys[2 * u + 1] = kNone;
+    const uint64_t M = *d_total;
+    const uint64_t e0l = (uint64_t)u * span;
+    if (e0l >= M) return;
+    const uint32_t e0 = (uint32_t)e0l;
+    const uint32_t e1 = (uint32_t)min(e0l + span, M);
+    const uint32_t s0 = 2 * u * kGroup;
+    const uint32_t s1 = min(2 * (u + 1) * kGroup, 2 * in_units);
+    uint32_t cur = kNone;
+    xyzz_t acc = xyzz_inf();
+    for (uint32_t s = s0; s < s1; s++) {
+        const uint32_t k = in_keys[s];
+        if (k == kNone) continue;
+        if (k != cur) {
+            if (cur != kNone) emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
+            cur = k;
+            acc = xyzz_inf();
+        }
+        acc = xyzz_add(acc, xyzz_load(in_pts + s));
+    }
+    if (cur != kNone) emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
+}
+
+// ---- 5. window reduction, level 1 -------------------------------------------------
+// Block j of window w holds buckets b = j*g + 1 .. j*g + g (stored at index b - 1).
+// Y_j = sum of the block, E_j = -(s_1 + ... + s_{g-1}) with s_u the prefix sums.
+__global__ void __launch_bounds__(128) msm_bucket_blocks_kernel(const xyzz_t* __restrict__ buckets, MsmShape sh,
+                                                                xyzz_t* __restrict__ Y, xyzz_t* __restrict__ E) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= sh.W * sh.G) return;
+    const xyzz_t* b = buckets + (size_t)t * sh.g;
+    xyzz_t s = xyzz_inf();
+    xyzz_t e = xyzz_inf();
+    for (uint32_t u = 0; u < sh.g; u++) {
+        s = xyzz_add(s, xyzz_load(b + u));
+        if (u + 1 < sh.g) e = xyzz_add(e, s);
+    }
+    xyzz_store(Y + t, s);
+    xyzz_store(E + t, xyzz_neg(e));
+}
+
+// ---- 6. plain sums per (window, target) ---------------------------------------------
+// target 0: sum_j E_j; target 1: sum_j Y_j; target 2 + k: sum of Y_j over j with bit k set.
+__global__ void __launch_bounds__(kTargetThreads) msm_targets_kernel(const xyzz_t* __restrict__ Y,
+                                                                     const xyzz_t* __restrict__ E, MsmShape sh,
+                                                                     xyzz_t* __restrict__ out) {
+    __shared__ xyzz_t red[kTargetThreads];
+    const uint32_t w = blockIdx.x / sh.targets;
+    const uint32_t tg = blockIdx.x % sh.targets;
+    const xyzz_t* src = (tg == 0 ? E : Y) + (size_t)w * sh.G;
+    const uint32_t count = tg >= 2 ? sh.G / 2 : sh.G;
+    const uint32_t k = tg >= 2 ? tg - 2 : 0;
+    xyzz_t acc = xyzz_inf();
+    for (uint32_t t = threadIdx.x; t < count; t += blockDim.x) {
+        uint32_t j = t;
+        if (tg >= 2) j = ((t >> k) << (k + 1)) | (1u << k) | (t & ((1u << k) - 1));
+        acc = xyzz_add(acc, xyzz_load(src + j));
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (uint32_t off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) red[threadIdx.x] = xyzz_add(red[threadIdx.x], red[threadIdx.x + off]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+// ---- host ---------------------------------------------------------------------------
+static zkh::Xyzz to_host(const xyzz_t& d) {
+    zkh::Xyzz h;
+    std::memcpy(h.X.v, d.X.v, 32);
+    std::memcpy(h.Y.v, d.Y.v, 32);
+    std::memcpy(h.ZZ.v, d.ZZ.v, 32);
+    std::memcpy(h.ZZZ.v, d.ZZZ.v, 32);
+    return h;
+}
+
+static zkh::Xyzz host_dbl_n(zkh::Xyzz p, uint32_t times) {
+    for (uint32_t i = 0; i < times; i++) p = zkh::xyzz_dbl(p);
+    return p;
+}
+
+int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
+            uint8_t out_xy[64], int* out_is_inf) {
+    ZK_CHECK_ARG(n < (1ull << 31), "MSM size must be below 2^31 points");
+    ZK_CHECK_ARG(window_bits == 0 || (window_bits >= 4 && window_bits <= 20), "window_bits must be 0 or 4..20");
+    if (n == 0) {
+        std::memset(out_xy, 0, 64);
+        *out_is_inf = 1;
+        return ZK_OK;
+    }
+    const uint32_t cbits = window_bits ? window_bits : msm_auto_window(n);
+    const MsmShape sh = make_shape(cbits);
+    const uint64_t nbuckets = (uint64_t)sh.W * sh.B;
+    const uint64_t max_entries = (uint64_t)n * sh.W;
+    ZK_CHECK_ARG(max_entries < (1ull << 32) - kSegment, "MSM too large for 32-bit CSR offsets");
+
+    // scratch layout
+    uint32_t *digits = nullptr, *row_ptr = nullptr, *cursor = nullptr, *entries = nullptr, *keys = nullptr;
+    xyzz_t *buckets = nullptr, *Yb = nullptr, *Eb = nullptr, *tgt = nullptr;
+    std::vector<void*> allocs;
+    auto alloc = [&](size_t bytes, void** p) -> int {
+        int rc = scratch_alloc(c, bytes, p);
+        if (rc == ZK_OK) allocs.push_back(*p);
+        return rc;
+    };
+    auto release = [&]() {
+        for (void* p : allocs) scratch_free(c, p);
+        allocs.clear();
+    };
+    int rc;
+    if ((rc = alloc(max_entries * 4, (void**)&digits)) != ZK_OK ||
+        (rc = alloc((nbuckets + 1) * 4, (void**)&row_ptr)) != ZK_OK ||
+        (rc = alloc(nbuckets * 4, (void**)&cursor)) != ZK_OK ||
+        (rc = alloc(max_entries * 4, (void**)&entries)) != ZK_OK ||
+        (rc = alloc(max_entries * 4, (void**)&keys)) != ZK_OK ||
+        (rc = alloc(nbuckets * sizeof(xyzz_t), (void**)&buckets)) != ZK_OK ||
+        (rc = alloc((size_t)sh.W * sh.G * sizeof(xyzz_t), (void**)&Yb)) != ZK_OK ||
+        (rc = alloc((size_t)sh.W * sh.G * sizeof(xyzz_t), (void**)&Eb)) != ZK_OK ||
+        (rc = alloc((size_t)sh.W * sh.targets * sizeof(xyzz_t), (void**)&tgt)) != ZK_OK) {
+        release();
+        return rc;
+    }
+    cudaStream_t st = c->stream;
+    ZK_TRY_CUDA(cudaMemsetAsync(row_ptr, 0, (nbuckets + 1) * 4, st));
+    ZK_TRY_CUDA(cudaMemsetAsync(buckets, 0, nbuckets * sizeof(xyzz_t), st));
+
+    const uint32_t nn = (uint32_t)n;
+    msm_digits_kernel<<<(nn + 255) / 256, 256, 0, st>>>(scalars, bases, nn, scalars_mont, sh, digits, row_ptr);
+    ZK_TRY_CUDA(cudaGetLastError());
+    // row_ptr[0..nbuckets) := exclusive scan; row_ptr[nbuckets] := total
+    if ((rc = device_exclusive_scan(c, row_ptr, nbuckets, row_ptr + nbuckets)) != ZK_OK) {
+        release();
+        return rc;
+    }
+    ZK_TRY_CUDA(cudaMemcpyAsync(cursor, row_ptr, nbuckets * 4, cudaMemcpyDeviceToDevice, st));
+    msm_scatter_kernel<<<(nn + 255) / 256, 256, 0, st>>>(digits, nn, sh, cursor, entries, keys);
+    ZK_TRY_CUDA(cudaGetLastError());
+
+    // accumulation rounds
+    const uint32_t* d_total = row_ptr + nbuckets;
+    uint32_t units = (uint32_t)((max_entries + kSegment - 1) / kSegment);
+    uint32_t *slot_keys_a = nullptr, *slot_keys_b = nullptr;
+    xyzz_t *slot_pts_a = nullptr, *slot_pts_b = nullptr;
+    if ((rc = alloc((size_t)2 * units * 4, (void**)&slot_keys_a)) != ZK_OK ||
+        (rc = alloc((size_t)2 * units * sizeof(xyzz_t), (void**)&slot_pts_a)) != ZK_OK ||
+        (rc = alloc((size_t)2 * ((units + kGroup - 1) / kGroup) * 4, (void**)&slot_keys_b)) != ZK_OK ||
+        (rc = alloc((size_t)2 * ((units + kGroup - 1) / kGroup) * sizeof(xyzz_t), (void**)&slot_pts_b)) !=
+            ZK_OK) {
+        release();
+        return rc;
+    }
+    msm_accumulate_kernel<<<(units + 127) / 128, 128, 0, st>>>(entries, keys, d_total, row_ptr, bases, units, buckets,
+                                                                slot_keys_a, slot_pts_a);
+    ZK_TRY_CUDA(cudaGetLastError());
+    uint64_t span = kSegment;
+    uint32_t in_units = units;
+    uint32_t *ik = slot_keys_a, *ok = slot_keys_b;
+    xyzz_t *ip = slot_pts_a, *op = slot_pts_b;
+    while (in_units > 1) {
+        const uint32_t out_units = (in_units + kGroup - 1) / kGroup;
+        span *= kGroup;
+        msm_merge_kernel<<<(out_units + 127) / 128, 128, 0, st>>>(ik, ip, in_units, d_total, row_ptr, span, out_units,
+                                                                   buckets, ok, op);
+        ZK_TRY_CUDA(cudaGetLastError());
+        std::swap(ik, ok);
+        std::swap(ip, op);
+        in_units = out_units;
+    }
+
+    // window reduction
+    const uint32_t nblk = sh.W * sh.G;
+    msm_bucket_blocks_kernel<<<(nblk + 127) / 128, 128, 0, st>>>(buckets, sh, Yb, Eb);
+    ZK_TRY_CUDA(cudaGetLastError());
+    msm_targets_kernel<<<sh.W * sh.targets, kTargetThreads, 0, st>>>(Yb, Eb, sh, tgt);
+    ZK_TRY_CUDA(cudaGetLastError());
+    std::vector<xyzz_t> host_t((size_t)sh.W * sh.targets);
+    ZK_TRY_CUDA(cudaMemcpyAsync(host_t.data(), tgt, host_t.size() * sizeof(xyzz_t), cudaMemcpyDeviceToHost, st));
+    ZK_TRY_CUDA(cudaStreamSynchronize(st));
+    release();
+
+    // host: S_w = T_E + g (T_Y + sum_k 2^k M_k); total = sum_w 2^(c w) S_w
+    uint32_t log_g = 0;
+    while ((1u << log_g) < sh.g) log_g++;
+    zkh::Xyzz total = zkh::xyzz_inf();
+    for (int w = (int)sh.W - 1; w >= 0; w--) {
+        const xyzz_t* T = host_t.data() + (size_t)w * sh.targets;
+        zkh::Xyzz h = zkh::xyzz_inf();
+        for (int k = (int)sh.K - 1; k >= 0; k--) {
+            h = zkh::xyzz_dbl(h);
+            h = zkh::xyzz_add(h, to_host(T[2 + k]));
+        }
+        zkh::Xyzz sw = zkh::xyzz_add(h, to_host(T[1]));
+        sw = host_dbl_n(sw, log_g);
+        sw = zkh::xyzz_add(sw, to_host(T[0]));
+        total = host_dbl_n(total, sh.c);
+        total = zkh::xyzz_add(total, sw);
+    }
+    zkh::F4 x, y;
+    *out_is_inf = zkh::xyzz_to_affine_canonical(total, &x, &y) ? 1 : 0;
+    std::memcpy(out_xy, x.v, 32);
+    std::memcpy(out_xy + 32, y.v, 32);
+    return ZK_OK;
+}
+
+}  // namespace zk

@@ -1,0 +1,364 @@
+// ntt.cu -- Fr NTT / iNTT / coset NTT for sm_103a.
+//
+// Semantics: crypto/poly/ntt.py:103-146 (the transforms behind the ROOTS_* and
+// COSET_* ops, runtime/kernels/cpu/kernels.py:175-250). Natural order in and out.
+//
+// Algorithm: radix-2^k Stockham autosort passes. With n = R_1 R_2 ... R_P and
+// L = R_1 ... R_{p-1} before pass p, pass p computes, for every column
+// c = j L + k (j < n/(R L), k < L) and m, q < R:
+//     y_m = in[c + m n/R] * w_{RL}^(m k),   z_q = sum_m y_m w_R^(m q),
+//     out[j R L + k + q L] = z_q,
+// where w_N = omega^(n/N). Radix 2 with n/2 threads per pass is the reference's
+// Metal v2 (runtime/metal/runtime.py:336-362); here one CTA runs a whole radix-R
+// column group in shared memory (R up to 2^11) so a 2^22 transform makes two HBM
+// round trips instead of 22. Inside the CTA the R-point DFT is a decimation-in-
+// frequency sequence of radix-2 stages in place in shared memory, read back in
+// bit-reversed order. Coset scaling (shift^g) is applied while loading the first
+// pass and the inverse scale (n^-1 shift^-i) while storing the last pass.
+//
+// Shared memory holds each 32-byte element as two 16-byte planes (low/high limbs)
+// so that eight consecutive elements cover all 32 banks; element positions are
+// XOR-swizzled so the bit-reversed read-back does not hit one bank group.
+#include <cstdio>
+#include <cstring>
+
+#include "zk_internal.cuh"
+
+namespace zk {
+
+static constexpr int kNttThreads = 256;
+static constexpr int kMaxLogR = 11;       // 2048 elements * 32 B = 64 KB of shared memory
+static constexpr int kTileLogElems = 11;  // R * T = 2048 elements per CTA
+
+struct NttPassParams {
+    const fe* in;
+    fe* out;
+    const fe* radix_tw;  // w_R^i, i < R/2
+    const fe* tw_lo;
+    const fe* tw_hi;
+    const fe* pre_lo;
+    const fe* pre_hi;
+    const fe* post_lo;
+    const fe* post_hi;
+    uint32_t in_len;  // valid input elements (first pass), <= n
+    uint32_t log_n;
+    uint32_t log_r;
+    uint32_t log_t;
+    uint32_t log_l;
+    uint32_t s_bits;
+};
+
+__device__ __forceinline__ fe lookup2(const fe* lo, const fe* hi, uint32_t e, uint32_t s_bits) {
+    fe a = fe_ldg(lo + (e & ((1u << s_bits) - 1)));
+    uint32_t h = e >> s_bits;
+    if (h == 0) return a;
+    return fe_mul<FrP>(a, fe_ldg(hi + h));
+}
+
+__device__ __forceinline__ uint32_t swz(uint32_t pos, uint32_t log_r) {
+    return log_r >= 6 ? (pos ^ ((pos >> (log_r - 3)) & 7u)) : pos;
+}
+
+__device__ __forceinline__ fe smem_get(const uint4* s_lo, const uint4* s_hi, uint32_t i) {
+    uint4 a = s_lo[i], b = s_hi[i];
+    fe r;
+    r.v[0] = a.x;
+    r.v[1] = a.y;
+    r.v[2] = a.z;
+    r.v[3] = a.w;
+    r.v[4] = b.x;
+    r.v[5] = b.y;
+    r.v[6] = b.z;
+    r.v[7] = b.w;
+    return r;
+}
+
+__device__ __forceinline__ void smem_put(uint4* s_lo, uint4* s_hi, uint32_t i, const fe& v) {
+    s_lo[i] = make_uint4(v.v[0], v.v[1], v.v[2], v.v[3]);
+    s_hi[i] = make_uint4(v.v[4], v.v[5], v.v[6], v.v[7]);
+}
+
+__global__ void __launch_bounds__(kNttThreads, 3) ntt_pass_kernel(NttPassParams P) {
+    extern __shared__ uint4 smem[];
+    const uint32_t log_r = P.log_r, log_t = P.log_t;
+    const uint32_t R = 1u << log_r, T = 1u << log_t, E = R << log_t;
+    uint4* s_lo = smem;
+    uint4* s_hi = smem + E;
+    const uint32_t c0 = blockIdx.x << log_t;
+    const uint32_t stride_log = P.log_n - log_r;
+    const uint32_t l_mask = (1u << P.log_l) - 1;
+    const uint32_t tw_shift = P.log_n - log_r - P.log_l;
+
+    // ---- load (+ coset scale on the first pass, + inter-pass twiddle) ----
+    for (uint32_t idx = threadIdx.x; idx < E; idx += blockDim.x) {
+        const uint32_t m = idx >> log_t, t = idx & (T - 1);
+        const uint32_t col = c0 + t;
+        const uint32_t g = col + (m << stride_log);
+        fe v = g < P.in_len ? fe_ldg(P.in + g) : fe_zero();
+        if (P.pre_lo != nullptr && g < P.in_len) v = fe_mul<FrP>(v, lookup2(P.pre_lo, P.pre_hi, g, P.s_bits));
+        if (P.log_l != 0) {
+            const uint32_t e = (m * (col & l_mask)) << tw_shift;
+            if (e != 0) v = fe_mul<FrP>(v, lookup2(P.tw_lo, P.tw_hi, e, P.s_bits));
+        }
+        smem_put(s_lo, s_hi, (swz(m, log_r) << log_t) + t, v);
+    }
+    __syncthreads();
+
+    // ---- R-point DFT per column: radix-2 DIF stages in shared memory ----
+    for (uint32_t st = 0; st < log_r; st++) {
+        const uint32_t log_h = log_r - st - 1;
+        const uint32_t h = 1u << log_h;
+        for (uint32_t bi = threadIdx.x; bi < (E >> 1); bi += blockDim.x) {
+            const uint32_t t = bi & (T - 1), b = bi >> log_t;
+            const uint32_t j = b & (h - 1);
+            const uint32_t i0 = ((b >> log_h) << (log_h + 1)) + j;
+            const uint32_t a0 = (swz(i0, log_r) << log_t) + t;
+            const uint32_t a1 = (swz(i0 + h, log_r) << log_t) + t;
+            fe u = smem_get(s_lo, s_hi, a0);
+            fe v = smem_get(s_lo, s_hi, a1);
+            fe sum = fe_add<FrP>(u, v);
+            fe diff = fe_sub<FrP>(u, v);
+            if (j != 0) diff = fe_mul<FrP>(diff, fe_ldg(P.radix_tw + (j << st)));
+            smem_put(s_lo, s_hi, a0, sum);
+            smem_put(s_lo, s_hi, a1, diff);
+        }
+        __syncthreads();
+    }
+
+    // ---- store z_q (at bit-reversed position), + final scale on the last pass ----
+    for (uint32_t idx = threadIdx.x; idx < E; idx += blockDim.x) {
+        uint32_t q, t;
+        if (P.log_l == 0) {  // output of the tile is one contiguous block: walk q fastest
+            q = idx & (R - 1);
+            t = idx >> log_r;
+        } else {  // runs of T consecutive columns: walk t fastest
+            q = idx >> log_t;
+            t = idx & (T - 1);
+        }
+        const uint32_t col = c0 + t;
+        const uint32_t pos = log_r ? (__brev(q) >> (32 - log_r)) : 0;
+        fe val = smem_get(s_lo, s_hi, (swz(pos, log_r) << log_t) + t);
+        const uint32_t o = ((col >> P.log_l) << (log_r + P.log_l)) + (col & l_mask) + (q << P.log_l);
+        if (P.post_lo != nullptr) {
+            fe s = P.post_hi != nullptr ? lookup2(P.post_lo, P.post_hi, o, P.s_bits) : fe_ldg(P.post_lo);
+            val = fe_mul<FrP>(val, s);
+        }
+        fe_store(P.out + o, val);
+    }
+}
+
+// ------------------------------------------------------------------------------
+// host side: plans and launches
+// ------------------------------------------------------------------------------
+static zkh::F4 load_canon(const uint8_t b[32]) {
+    zkh::F4 r;
+    std::memcpy(r.v, b, 32);
+    return r;
+}
+
+static int upload_table(Ctx* c, NttPlan* plan, const std::vector<zkh::F4>& v, fe** out) {
+    void* p = nullptr;
+    ZK_TRY_CUDA(cudaMalloc(&p, v.size() * 32));
+    plan->allocations.push_back(p);
+    ZK_TRY_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * 32, cudaMemcpyHostToDevice, c->stream));
+    *out = static_cast<fe*>(p);
+    return ZK_OK;
+}
+
+// powers base^i for i < count (Montgomery)
+static std::vector<zkh::F4> powers(const zkh::F4& base, size_t count) {
+    const zkh::Field& F = zkh::fr();
+    std::vector<zkh::F4> v(count);
+    zkh::F4 cur = zkh::one(F);
+    for (size_t i = 0; i < count; i++) {
+        v[i] = cur;
+        cur = zkh::mul(F, cur, base);
+    }
+    return v;
+}
+
+static void split_passes(uint32_t log_n, NttPlan* plan) {
+    if (log_n == 0) {
+        plan->npass = 0;
+        return;
+    }
+    int np = (int)((log_n + kMaxLogR - 1) / kMaxLogR);
+    if (np < 1) np = 1;
+    uint32_t base = log_n / np, extra = log_n % np;
+    plan->npass = np;
+    for (int p = 0; p < np; p++) plan->pass_log_r[p] = base + ((uint32_t)p < extra ? 1u : 0u);
+}
+
+static int build_plan(Ctx* c, int mode, uint32_t log_n, const zkh::F4& omega_m, const zkh::F4& shift_m,
+                      NttPlan** out) {
+    const zkh::Field& F = zkh::fr();
+    NttPlan* plan = new NttPlan();
+    plan->log_n = log_n;
+    split_passes(log_n, plan);
+    const bool inverse = (mode == ZK_NTT_COEFFS_FROM_EVALS || mode == ZK_NTT_COSET_COEFFS_FROM_EVALS);
+    const zkh::F4 w = inverse ? zkh::inv(F, omega_m) : omega_m;
+    const uint64_t n = 1ull << log_n;
+    plan->s_bits = (log_n + 1) / 2;
+    const uint64_t lo_count = 1ull << plan->s_bits;
+    const uint64_t hi_count = (n >> plan->s_bits) + 1;
+    int rc;
+    // two-level twiddle table: w^i and w^(i 2^s)
+    {
+        std::vector<zkh::F4> lo = powers(w, lo_count);
+        zkh::F4 ws = zkh::pow_u64(F, w, lo_count);
+        std::vector<zkh::F4> hi = powers(ws, hi_count);
+        if ((rc = upload_table(c, plan, lo, &plan->tw_lo)) != ZK_OK) return rc;
+        if ((rc = upload_table(c, plan, hi, &plan->tw_hi)) != ZK_OK) return rc;
+    }
+    for (int p = 0; p < plan->npass; p++) {
+        const uint32_t lr = plan->pass_log_r[p];
+        const zkh::F4 wr = zkh::pow_u64(F, w, n >> lr);
+        std::vector<zkh::F4> t = powers(wr, std::max<uint64_t>(1, (1ull << lr) / 2));
+        if ((rc = upload_table(c, plan, t, &plan->radix_tw[p])) != ZK_OK) return rc;
+    }
+    if (mode == ZK_NTT_COSET_EVALS_FROM_COEFFS) {
+        std::vector<zkh::F4> lo = powers(shift_m, lo_count);
+        zkh::F4 ss = zkh::pow_u64(F, shift_m, lo_count);
+        std::vector<zkh::F4> hi = powers(ss, hi_count);
+        if ((rc = upload_table(c, plan, lo, &plan->pre_lo)) != ZK_OK) return rc;
+        if ((rc = upload_table(c, plan, hi, &plan->pre_hi)) != ZK_OK) return rc;
+    }
+    if (inverse) {
+        zkh::F4 nn = {{n, 0, 0, 0}};
+        zkh::F4 ninv = zkh::inv(F, zkh::to_mont(F, nn));
+        if (mode == ZK_NTT_COEFFS_FROM_EVALS) {
+            std::vector<zkh::F4> one(1, ninv);
+            if ((rc = upload_table(c, plan, one, &plan->post_lo)) != ZK_OK) return rc;
+        } else {
+            // coefficient i is scaled by n^-1 shift^-i; a zero shift scales every i > 0 by 0
+            zkh::F4 is = zkh::is_zero(shift_m) ? shift_m : zkh::inv(F, shift_m);
+            std::vector<zkh::F4> lo = powers(is, lo_count);
+            for (auto& x : lo) x = zkh::mul(F, x, ninv);
+            zkh::F4 iss = zkh::pow_u64(F, is, lo_count);
+            std::vector<zkh::F4> hi = powers(iss, hi_count);
+            if ((rc = upload_table(c, plan, lo, &plan->post_lo)) != ZK_OK) return rc;
+            if ((rc = upload_table(c, plan, hi, &plan->post_hi)) != ZK_OK) return rc;
+        }
+    }
+    *out = plan;
+    return ZK_OK;
+}
+
+static int get_plan(Ctx* c, int mode, uint32_t log_n, const uint8_t omega[32], const uint8_t shift[32],
+                    NttPlan** out) {
+    std::string key(reinterpret_cast<const char*>(omega), 32);
+    key.append(reinterpret_cast<const char*>(shift), 32);
+    key.push_back((char)mode);
+    key.push_back((char)log_n);
+    auto it = c->ntt_plans.find(key);
+    if (it != c->ntt_plans.end()) {
+        *out = it->second;
+        return ZK_OK;
+    }
+    const zkh::Field& F = zkh::fr();
+    zkh::F4 om = zkh::to_mont(F, load_canon(omega));
+    zkh::F4 sh = zkh::to_mont(F, load_canon(shift));
+    // omega must have order exactly n: omega^(n/2) == -1 (and omega^n == 1 for n == 1 is vacuous)
+    if (log_n >= 1) {
+        zkh::F4 h = zkh::pow_u64(F, om, 1ull << (log_n - 1));
+        zkh::F4 m1 = zkh::neg(F, zkh::one(F));
+        if (!zkh::eq(h, m1)) {
+            set_error("omega is not a primitive n-th root of unity (omega^(n/2) != -1)");
+            return ZK_EINVAL;
+        }
+    }
+    NttPlan* plan = nullptr;
+    int rc = build_plan(c, mode, log_n, om, sh, &plan);
+    if (rc != ZK_OK) return rc;
+    c->ntt_plans[key] = plan;
+    *out = plan;
+    return ZK_OK;
+}
+
+int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log_n, const uint8_t omega[32],
+            const uint8_t shift[32]) {
+    ZK_CHECK_ARG(mode >= 0 && mode <= 3, "invalid NTT mode");
+    ZK_CHECK_ARG(log_n <= 28, "domain too large for BN254 root of unity (log2 n > 28)");
+    const uint64_t n = 1ull << log_n;
+    const bool inverse = (mode == ZK_NTT_COEFFS_FROM_EVALS || mode == ZK_NTT_COSET_COEFFS_FROM_EVALS);
+    ZK_CHECK_ARG(!inverse || in_len == n, "inverse transforms need len(evals) == n (a power of two)");
+    ZK_CHECK_ARG(out != nullptr && (in != nullptr || in_len == 0), "null buffer");
+    NttPlan* plan = nullptr;
+    {
+        std::lock_guard<std::mutex> g(c->mu);
+        int rc = get_plan(c, mode, log_n, omega, shift, &plan);
+        if (rc != ZK_OK) return rc;
+    }
+    const uint32_t valid = (uint32_t)(in_len < n ? in_len : n);
+    if (log_n == 0) {
+        // n == 1: the transform is the identity up to the scale factors
+        NttPassParams P{};
+        P.in = in;
+        P.out = out;
+        P.radix_tw = plan->tw_lo;
+        P.tw_lo = plan->tw_lo;
+        P.tw_hi = plan->tw_hi;
+        P.pre_lo = plan->pre_lo;
+        P.pre_hi = plan->pre_hi;
+        P.post_lo = plan->post_lo;
+        P.post_hi = plan->post_hi;
+        P.in_len = valid;
+        P.log_n = 0;
+        P.log_r = 0;
+        P.log_t = 0;
+        P.log_l = 0;
+        P.s_bits = plan->s_bits;
+        ntt_pass_kernel<<<1, 32, 2 * 16, c->stream>>>(P);
+        ZK_TRY_CUDA(cudaGetLastError());
+        return ZK_OK;
+    }
+    fe* scratch = nullptr;
+    if (plan->npass > 1) {
+        int rc = scratch_alloc(c, n * 32, reinterpret_cast<void**>(&scratch));
+        if (rc != ZK_OK) return rc;
+    }
+    static bool attr_set = false;
+    if (!attr_set) {
+        ZK_TRY_CUDA(cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (2 << kTileLogElems) * 16));
+        attr_set = true;
+    }
+    uint32_t log_l = 0;
+    const fe* src = in;
+    for (int p = 0; p < plan->npass; p++) {
+        const uint32_t lr = plan->pass_log_r[p];
+        // columns per CTA: fill the 2^11-element tile, but not beyond the number of columns
+        uint32_t lt = kTileLogElems > (int)lr ? kTileLogElems - lr : 0;
+        if (lt > log_n - lr) lt = log_n - lr;
+        // the last pass writes `out`; earlier passes alternate so that pass npass-1 lands in out
+        const int remaining = plan->npass - 1 - p;
+        fe* dst = (remaining % 2 == 0) ? out : scratch;
+        NttPassParams P{};
+        P.in = src;
+        P.out = dst;
+        P.radix_tw = plan->radix_tw[p];
+        P.tw_lo = plan->tw_lo;
+        P.tw_hi = plan->tw_hi;
+        P.pre_lo = p == 0 ? plan->pre_lo : nullptr;
+        P.pre_hi = p == 0 ? plan->pre_hi : nullptr;
+        P.post_lo = p == plan->npass - 1 ? plan->post_lo : nullptr;
+        P.post_hi = p == plan->npass - 1 ? plan->post_hi : nullptr;
+        P.in_len = p == 0 ? valid : (uint32_t)n;
+        P.log_n = log_n;
+        P.log_r = lr;
+        P.log_t = lt;
+        P.log_l = log_l;
+        P.s_bits = plan->s_bits;
+        const uint32_t elems = 1u << (lr + lt);
+        const uint32_t threads = elems / 2 < (uint32_t)kNttThreads ? (elems / 2 < 32 ? 32 : elems / 2) : kNttThreads;
+        const uint32_t blocks = (uint32_t)(n >> (lr + lt));
+        ntt_pass_kernel<<<blocks, threads, (size_t)elems * 32, c->stream>>>(P);
+        ZK_TRY_CUDA(cudaGetLastError());
+        src = dst;
+        log_l += lr;
+    }
+    if (scratch) scratch_free(c, scratch);
+    return ZK_OK;
+}
+
+}  // namespace zk

@@ -1,0 +1,170 @@
+// ops.cu -- elementwise Fr/Fq kernels and fixed-base scalar multiplication.
+//
+// to/from Montgomery replace the per-element Python loops of _to_device /
+// _from_device (runtime/kernels/cpu/kernels.py:98-172); fr_mul / fr_sub are the
+// POINTWISE_MUL / POLY_SUB kernels (runtime/metal/runtime.py:204-224).
+#include <cstring>
+#include <vector>
+
+#include "zk_internal.cuh"
+
+namespace zk {
+
+static unsigned grid_for(size_t n, int threads, int num_sms) {
+    size_t blocks = (n + threads - 1) / threads;
+    size_t cap = (size_t)num_sms * 16;
+    if (blocks > cap) blocks = cap;
+    return (unsigned)(blocks ? blocks : 1);
+}
+
+template <class F, int DIR>
+__global__ void convert_kernel(fe* out, const fe* in, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        fe v = fe_ldg(in + i);
+        fe_store(out + i, DIR ? fe_to_mont<F>(v) : fe_from_mont<F>(v));
+    }
+}
+
+__global__ void fr_mul_kernel(fe* out, const fe* a, const fe* b, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        fe_store(out + i, fe_mul<FrP>(fe_ldg(a + i), fe_ldg(b + i)));
+}
+
+__global__ void fr_sub_kernel(fe* out, const fe* a, const fe* b, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        fe_store(out + i, fe_sub<FrP>(fe_ldg(a + i), fe_ldg(b + i)));
+}
+
+template <class F, int DIR>
+int convert(Ctx* c, void* out, const void* in, size_t n) {
+    if (n == 0) return ZK_OK;
+    ZK_CHECK_ARG(out != nullptr && in != nullptr, "null buffer");
+    convert_kernel<F, DIR><<<grid_for(n, 256, c->num_sms), 256, 0, c->stream>>>(static_cast<fe*>(out),
+                                                                                 static_cast<const fe*>(in), n);
+    ZK_TRY_CUDA(cudaGetLastError());
+    return ZK_OK;
+}
+
+template int convert<FrP, 1>(Ctx*, void*, const void*, size_t);
+template int convert<FrP, 0>(Ctx*, void*, const void*, size_t);
+template int convert<FqP, 1>(Ctx*, void*, const void*, size_t);
+template int convert<FqP, 0>(Ctx*, void*, const void*, size_t);
+
+int fr_binary(Ctx* c, int op, void* out, const void* a, const void* b, size_t n) {
+    if (n == 0) return ZK_OK;
+    ZK_CHECK_ARG(out != nullptr && a != nullptr && b != nullptr, "null buffer");
+    if (op == 0)
+        fr_mul_kernel<<<grid_for(n, 256, c->num_sms), 256, 0, c->stream>>>(
+            static_cast<fe*>(out), static_cast<const fe*>(a), static_cast<const fe*>(b), n);
+    else
+        fr_sub_kernel<<<grid_for(n, 256, c->num_sms), 256, 0, c->stream>>>(
+            static_cast<fe*>(out), static_cast<const fe*>(a), static_cast<const fe*>(b), n);
+    ZK_TRY_CUDA(cudaGetLastError());
+    return ZK_OK;
+}
+
+// ---- fixed-base multiplication: out_i = [k_i] P --------------------------------------
+// table[j * 256 + d] = d * 2^(8 j) * P (affine Montgomery, entry d = 0 unused).
+template <class F>
+__device__ fe fe_inverse(const fe& a) {
+    // a^(p - 2) by left-to-right square-and-multiply over the constant exponent
+    uint32_t e[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) e[i] = F::P(i);
+    e[0] -= 2;  // p is odd and > 2: no borrow
+    fe r = fe_one<F>();
+    for (int limb = 7; limb >= 0; limb--) {
+        for (int b = 31; b >= 0; b--) {
+            r = fe_sqr<F>(r);
+            if ((e[limb] >> b) & 1) r = fe_mul<F>(r, a);
+        }
+    }
+    return r;
+}
+
+__global__ void fixed_base_kernel(const affine_t* __restrict__ table, const fe* __restrict__ k, size_t n,
+                                  affine_t* __restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    // reduce k mod r (canonical in) by a Montgomery round trip
+    fe s = fe_from_mont<FrP>(fe_to_mont<FrP>(fe_ldg(k + i)));
+    xyzz_t acc = xyzz_inf();
+    for (int j = 0; j < 32; j++) {
+        const uint32_t d = (s.v[j >> 2] >> (8 * (j & 3))) & 0xffu;
+        if (d) {
+            affine_t p = affine_load(table + j * 256 + d);
+            acc = xyzz_madd(acc, p.x, p.y);
+        }
+    }
+    affine_t r;
+    if (xyzz_is_inf(acc)) {
+        r.x = fe_zero();
+        r.y = fe_zero();
+    } else {
+        fe I = fe_inverse<FqP>(fe_mul<FqP>(acc.ZZ, acc.ZZZ));
+        fe izz = fe_mul<FqP>(acc.ZZZ, I);
+        fe izzz = fe_mul<FqP>(acc.ZZ, I);
+        r.x = fe_from_mont<FqP>(fe_mul<FqP>(acc.X, izz));
+        r.y = fe_from_mont<FqP>(fe_mul<FqP>(acc.Y, izzz));
+    }
+    fe_store(&out[i].x, r.x);
+    fe_store(&out[i].y, r.y);
+}
+
+int fixed_base_mul(Ctx* c, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_dev) {
+    if (n == 0) return ZK_OK;
+    ZK_CHECK_ARG(k_dev != nullptr && out_dev != nullptr, "null buffer");
+    const zkh::Field& F = zkh::fq();
+    zkh::F4 px, py;
+    std::memcpy(px.v, point_xy, 32);
+    std::memcpy(py.v, point_xy + 32, 32);
+    std::vector<affine_t> table(32 * 256);
+    std::memset(table.data(), 0, table.size() * sizeof(affine_t));
+    if (!(zkh::is_zero(px) && zkh::is_zero(py))) {
+        zkh::Xyzz base;
+        base.X = zkh::to_mont(F, px);
+        base.Y = zkh::to_mont(F, py);
+        base.ZZ = zkh::one(F);
+        base.ZZZ = zkh::one(F);
+        std::vector<zkh::Xyzz> pts(32 * 256);
+        for (int j = 0; j < 32; j++) {
+            pts[j * 256] = zkh::xyzz_inf();
+            for (int d = 1; d < 256; d++) pts[j * 256 + d] = zkh::xyzz_add(pts[j * 256 + d - 1], base);
+            for (int b = 0; b < 8; b++) base = zkh::xyzz_dbl(base);
+        }
+        // batch normalisation: one inversion of the product of all ZZ * ZZZ
+        std::vector<zkh::F4> pref(pts.size());
+        zkh::F4 run = zkh::one(F);
+        for (size_t i = 0; i < pts.size(); i++) {
+            pref[i] = run;
+            if (!zkh::is_zero(pts[i].ZZ)) run = zkh::mul(F, run, zkh::mul(F, pts[i].ZZ, pts[i].ZZZ));
+        }
+        zkh::F4 inv = zkh::inv(F, run);
+        for (size_t i = pts.size(); i-- > 0;) {
+            if (zkh::is_zero(pts[i].ZZ)) continue;
+            zkh::F4 zz_zzz = zkh::mul(F, pts[i].ZZ, pts[i].ZZZ);
+            zkh::F4 I = zkh::mul(F, inv, pref[i]);
+            inv = zkh::mul(F, inv, zz_zzz);
+            zkh::F4 izz = zkh::mul(F, pts[i].ZZZ, I);
+            zkh::F4 izzz = zkh::mul(F, pts[i].ZZ, I);
+            zkh::F4 x = zkh::mul(F, pts[i].X, izz);
+            zkh::F4 y = zkh::mul(F, pts[i].Y, izzz);
+            std::memcpy(table[i].x.v, x.v, 32);
+            std::memcpy(table[i].y.v, y.v, 32);
+        }
+    }
+    affine_t* dtab = nullptr;
+    int rc = scratch_alloc(c, table.size() * sizeof(affine_t), reinterpret_cast<void**>(&dtab));
+    if (rc != ZK_OK) return rc;
+    ZK_TRY_CUDA(cudaMemcpyAsync(dtab, table.data(), table.size() * sizeof(affine_t), cudaMemcpyHostToDevice,
+                                c->stream));
+    fixed_base_kernel<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(dtab, static_cast<const fe*>(k_dev), n,
+                                                                           static_cast<affine_t*>(out_dev));
+    ZK_TRY_CUDA(cudaGetLastError());
+    // the host table must outlive the async copy
+    ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
+    scratch_free(c, dtab);
+    return ZK_OK;
+}
+
+}  // namespace zk
