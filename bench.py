@@ -1,0 +1,516 @@
+"""Benchmark of the BN254 prover hot path on GB300: G1 MSM (Mpts/s) and Fr NTT (Melem/s) at 2^20.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+A step of the headline (``value``) is one G1 MSM over n = 2^20 points: bases are
+[k_i]G with k_i uniform in [1, r), resident on the device in Montgomery form;
+scalars uniform in [0, r), resident in Montgomery form (the TO_DEVICE layout).
+L2 is flushed (a 256 MB memset) before every timed step; each step is timed with
+CUDA events on the library's stream and includes the host-side final window
+combination of the MSM. ``e2e`` is the same MSM through the C ABI from pinned host
+buffers: per step the affine bases (64 B/point) and the canonical scalars
+(32 B/point) are copied host->device, converted and summed, and the affine result
+(64 B) returns to the host. The Fr NTT at 2^20 (forward, omega = omega_for_size(n))
+is measured the same way in ``ntt``; a 2^22 forward NTT is reported in ``ntt_2_22``.
+
+Multi-GPU: one process per GPU (torchrun); the MSM does not need a collective, so
+ranks run independent replicas of the step and ``value`` sums their throughput
+over the slowest rank's time ("replicas only").
+
+``--impl reference`` times the reference's algorithms restated in C (oracle/,
+crypto/msm/pippenger.py:10-64 with the window rule of
+runtime/kernels/cpu/kernels.py:559, and crypto/poly/ntt.py:42-100) on all host
+cores, on the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "G1 MSM Mpts/s & Fr NTT Melem/s @2^20; proofs/s + p50/p99 vs plain (bit-exact)"
+LOG_N = 20
+FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--log-n", type=int, default=LOG_N)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", default="all", choices=["all", "msm", "ntt"],
+                    help="msm / ntt: only that kernel family, no e2e (short commands for profiling)")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------ ranks
+class Ranks:
+    def __init__(self, gpus: int) -> None:
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self) -> None:
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.dist is None:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self) -> None:
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int) -> None:
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self) -> None:
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, parts[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------ inputs
+def make_inputs(ctx, log_n: int):
+    from pyzkp_gb300 import synth
+
+    n = 1 << log_n
+    seed = synth.seed_for(2, log_n)
+    k = synth.base_dlogs(seed, n)
+    s = synth.fr_uniform(seed, n)
+    dk = ctx.to_device(k)
+    bases_xy = ctx.alloc(n * 64)
+    ctx.g1_fixed_base_mul((1, 2), dk, n, bases_xy)
+    host_xy = bases_xy.download().view("<u8").reshape(n, 8)
+    return n, seed, k, s, bases_xy, host_xy
+
+
+def ntt_omega(n: int) -> int:
+    from pyzkp_gb300 import synth
+
+    root = 19103219067921713944291392827692070036145651957329286315305642004821462161904  # 2^28-th root
+    return pow(root, 1 << (28 - (n.bit_length() - 1)), synth.FR_MODULUS)
+
+
+# ------------------------------------------------------------------------------ GPU arm
+def run_gpu(args, ranks: Ranks) -> dict:
+    from pyzkp_gb300 import _native as N
+    from pyzkp_gb300 import synth
+
+    ctx = N.Context(ranks.local)
+    L = N.load()
+    if args.only == "ntt":
+        flush = ctx.alloc(FLUSH_BYTES)
+        peaks = load_peaks()
+        return run_gpu_ntt(ctx, args, ranks, args.log_n, flush, ctx.imad_peak(), peaks.get("hbm_gbs") or 6800.0,
+                           brief=True)
+    log_n = args.log_n
+    n, seed, k, s, bases_xy, host_xy = make_inputs(ctx, log_n)
+    bases = ctx.bases_from_device(bases_xy, n)
+    ds = ctx.to_device(s)
+    ctx.fr_to_mont(ds, ds, n)
+    flush = ctx.alloc(FLUSH_BYTES)
+    imad_tops = ctx.imad_peak()
+
+    def msm_step():
+        return ctx.msm_g1(bases, ds, n)
+
+    for _ in range(args.warmup):
+        res = msm_step()
+
+    sampler = ClockSampler(ranks.local)
+    sampler.start()
+    launches0 = ctx.launch_count()
+    ranks.barrier()
+    ctx.sync()
+    times = []
+    for _ in range(args.steps):
+        ctx.memset(flush, 1)
+        ctx.timer_start()
+        msm_step()
+        times.append(ctx.timer_stop())
+    ctx.sync()
+    ranks.barrier()
+    launches = ctx.launch_count() - launches0
+    clocks = sampler.stop()
+    total_ms = ranks.max(sum(times))
+    mpts = n * args.steps * ranks.world / (total_ms * 1e-3) / 1e6
+    stats = ctx.msm_last_stats()
+
+    # per-kernel device times (profiling pass, same workload)
+    ctx.prof_reset()
+    ctx.prof_enable(True)
+    prof_steps = 3
+    for _ in range(prof_steps):
+        ctx.memset(flush, 1)
+        msm_step()
+    ctx.prof_enable(False)
+    table = ctx.prof_table()
+    ctx.prof_reset()
+    acc_launches, acc_ms = table.get("msm_accumulate", (1, 0.0))
+    acc_ms_launch = acc_ms / max(1, acc_launches)
+    entries = stats["entries"]
+    # algorithmic work of one accumulate launch: one XYZZ mixed addition (8M + 2S = 10 Fq
+    # multiplications) per CSR entry; a Montgomery multiplication with 8 limbs is 2*8^2 + 8 = 136
+    # 32x32->64 multiply-accumulates, i.e. 272 IMAD (lo + hi) instructions.
+    acc_imad = entries * 10 * 272
+    acc_tops = acc_imad / (acc_ms_launch * 1e-3) / 1e12
+    # algorithmic bytes: per entry the 4-byte CSR entry + 4-byte key + the 64-byte affine base
+    acc_bytes = entries * 72
+    peaks = load_peaks()
+    hbm_peak = peaks.get("hbm_gbs") or 6800.0
+    roofline = {
+        "kernel": "msm_accumulate",
+        "bound": "imad",
+        "achieved": round(acc_tops, 3),
+        "peak": round(imad_tops, 3),
+        "unit": "T IMAD/s",
+        "frac": round(acc_tops / imad_tops, 4),
+        "peak_source": "measured in this run by zk_imad_peak (no IMAD figure in MEASURED_PEAKS.json)",
+        "launch_ms": round(acc_ms_launch, 4),
+        "share_of_step": round(acc_ms / max(1e-9, sum(v[1] for v in table.values())), 4),
+        "traffic": None,
+        "hbm": {"achieved": round(acc_bytes / (acc_ms_launch * 1e-3) / 1e9, 1), "peak": hbm_peak,
+                "unit": "GB/s", "frac": round(acc_bytes / (acc_ms_launch * 1e-3) / 1e9 / hbm_peak, 4),
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks.get("hbm_gbs") else "fallback 6800"},
+        "algorithmic_work": f"{entries} CSR entries x 10 Fq mults x 272 IMAD; {entries} x 72 B",
+    }
+    kernels = {name: {"launches": la // prof_steps, "ms_per_step": round(ms / prof_steps, 4)}
+               for name, (la, ms) in sorted(table.items())}
+
+    if args.only == "msm":
+        return {"metric": METRIC, "value": round(mpts, 3), "unit": "Mpts/s", "kernels": kernels,
+                "roofline": roofline, "gpu_launches": launches}
+
+    # e2e through the C ABI from pinned host memory
+    pin_xy = ctx.pinned(n * 64)
+    pin_xy.array[:] = host_xy.view(np.uint8).reshape(-1)
+    pin_s = ctx.pinned(n * 32)
+    pin_s.array[:] = s.view(np.uint8).reshape(-1)
+    d_s = ctx.alloc(n * 32)
+    import ctypes
+
+    out = (ctypes.c_uint8 * 64)()
+    inf = ctypes.c_int()
+
+    def e2e_step():
+        h = ctypes.c_void_p()
+        N.check(L.zk_bases_create(ctx.handle, pin_xy.ptr, n, ctypes.byref(h)), "zk_bases_create")
+        N.check(L.zk_h2d(ctx.handle, d_s.ptr, pin_s.ptr, n * 32), "zk_h2d")
+        N.check(L.zk_msm_g1(ctx.handle, h, 0, d_s.ptr, n, 0, 0, out, ctypes.byref(inf)), "zk_msm_g1")
+        L.zk_bases_destroy(h)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    e2e_ok = (int.from_bytes(bytes(out)[:32], "little"), int.from_bytes(bytes(out)[32:], "little")) == res
+    ranks.barrier()
+    e2e_times = []
+    for _ in range(args.steps):
+        ctx.memset(flush, 1)
+        ctx.timer_start()
+        e2e_step()
+        e2e_times.append(ctx.timer_stop())
+    e2e_total = ranks.max(sum(e2e_times))
+    e2e_mpts = n * args.steps * ranks.world / (e2e_total * 1e-3) / 1e6
+
+    ntt = run_gpu_ntt(ctx, args, ranks, 20, flush, imad_tops, hbm_peak)
+    ntt22 = run_gpu_ntt(ctx, args, ranks, 22, flush, imad_tops, hbm_peak, brief=True)
+
+    result = {
+        "metric": METRIC,
+        "value": round(mpts, 3),
+        "unit": "Mpts/s",
+        "n_gpus": ranks.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32 limbs (exact BN254 Fq/Fr Montgomery arithmetic)",
+        "data": "synthetic: seeded PCG64 scalars uniform in [0,r); bases [k_i]G, k_i uniform in [1,r)",
+        "config": {"workload": f"G1 MSM n=2^{log_n} (uniform scalars, resident bases) + Fr NTT n=2^20 / 2^22",
+                   "n": n, "seed": seed, "window_bits": stats["window_bits"], "windows": stats["windows"],
+                   "csr_entries": entries, "l2": "flushed (256 MB memset) before every timed step",
+                   "parallelism": f"replicas x{ranks.world}"},
+        "msm_result": [hex(res[0]), hex(res[1])] if res else None,
+        "e2e": {"value": round(e2e_mpts, 3), "unit": "Mpts/s", "h2d_bytes_per_step": n * 96,
+                "d2h_bytes_per_step": 64 + 4, "result_ok": e2e_ok,
+                "path": "zk_bases_create(pinned host affine) + zk_h2d(pinned scalars) + zk_msm_g1 -> host point"},
+        "gpu_launches": launches,
+        "gpu_launches_per_step": launches // max(1, args.steps),
+        "kernels": kernels,
+        "roofline": roofline,
+        "ntt": ntt,
+        "ntt_2_22": ntt22,
+        "clocks": clocks,
+    }
+    return result
+
+
+def run_gpu_ntt(ctx, args, ranks, log_n, flush, imad_tops, hbm_peak, brief=False) -> dict:
+    from pyzkp_gb300 import _native as N
+    from pyzkp_gb300 import synth
+
+    n = 1 << log_n
+    v = synth.fr_uniform(synth.seed_for(1, log_n), n)
+    om = ntt_omega(n)
+    din = ctx.to_device(v)
+    ctx.fr_to_mont(din, din, n)
+    dout = ctx.alloc(n * 32)
+    for _ in range(args.warmup):
+        ctx.ntt(N.NTT_EVALS_FROM_COEFFS, dout, din, n, log_n, om)
+    ranks.barrier()
+    times = []
+    for _ in range(args.steps):
+        ctx.memset(flush, 1)
+        ctx.timer_start()
+        ctx.ntt(N.NTT_EVALS_FROM_COEFFS, dout, din, n, log_n, om)
+        times.append(ctx.timer_stop())
+    total = ranks.max(sum(times))
+    melem = n * args.steps * ranks.world / (total * 1e-3) / 1e6
+    out = {"metric": f"Fr NTT Melem/s @2^{log_n} (forward)", "value": round(melem, 2), "unit": "Melem/s",
+           "ms_per_step": round(total / args.steps, 4)}
+    # per-pass device time
+    ctx.prof_reset()
+    ctx.prof_enable(True)
+    for _ in range(3):
+        ctx.memset(flush, 1)
+        ctx.ntt(N.NTT_EVALS_FROM_COEFFS, dout, din, n, log_n, om)
+    ctx.prof_enable(False)
+    la, ms = ctx.prof_table().get("ntt_pass", (1, 0.0))
+    ctx.prof_reset()
+    passes = la // 3
+    pass_ms = ms / max(1, la)
+    # per pass: every element read once and written once (64 B); radix-2 work of log2(R) stages,
+    # (n/2) log2(R) butterflies of one Montgomery multiplication (136 wide MACs = 272 IMAD)
+    log_r = log_n / max(1, passes)
+    pass_bytes = 64 * n
+    pass_imad = (n / 2) * log_r * 272
+    gbs = pass_bytes / (pass_ms * 1e-3) / 1e9
+    tops = pass_imad / (pass_ms * 1e-3) / 1e12
+    out["roofline"] = {"kernel": "ntt_pass", "bound": "imad", "achieved": round(tops, 3), "peak": round(imad_tops, 3),
+                       "unit": "T IMAD/s", "frac": round(tops / imad_tops, 4), "passes": passes,
+                       "launch_ms": round(pass_ms, 4), "traffic": None,
+                       "hbm": {"achieved": round(gbs, 1), "peak": hbm_peak, "unit": "GB/s",
+                               "frac": round(gbs / hbm_peak, 4)},
+                       "algorithmic_work": "per pass 64 B/element; (n/2) log2(R) butterflies x 272 IMAD"}
+    if not brief:
+        # e2e: canonical host input -> device, to Montgomery, NTT, back to canonical, device -> host
+        pin_in = ctx.pinned(n * 32)
+        pin_in.array[:] = v.view(np.uint8).reshape(-1)
+        pin_out = ctx.pinned(n * 32)
+        L = N.load()
+
+        def e2e():
+            N.check(L.zk_h2d(ctx.handle, din.ptr, pin_in.ptr, n * 32))
+            ctx.fr_to_mont(din, din, n)
+            ctx.ntt(N.NTT_EVALS_FROM_COEFFS, dout, din, n, log_n, om)
+            ctx.fr_from_mont(dout, dout, n)
+            N.check(L.zk_d2h(ctx.handle, pin_out.ptr, dout.ptr, n * 32))
+
+        for _ in range(args.warmup):
+            e2e()
+        ts = []
+        for _ in range(args.steps):
+            ctx.memset(flush, 1)
+            ctx.timer_start()
+            e2e()
+            ts.append(ctx.timer_stop())
+        tot = ranks.max(sum(ts))
+        out["e2e"] = {"value": round(n * args.steps * ranks.world / (tot * 1e-3) / 1e6, 2), "unit": "Melem/s",
+                      "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 32}
+    return out
+
+
+def load_peaks() -> dict:
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# ------------------------------------------------------------------------------ CPU (oracle port)
+def cpu_msm_sample(log_n: int, budget_s: float = 10.0, full_size: bool = False):
+    """The reference's Pippenger (restated in C, all host threads) on the same workload."""
+    from oracle import oracle as O
+    from pyzkp_gb300 import synth
+
+    n = 1 << log_n
+    seed = synth.seed_for(2, log_n)
+    k = synth.base_dlogs(seed, n)
+    s = synth.fr_uniform(seed, n)
+    bases = O.g1_fixed_base_mul(O.G1_GENERATOR, k)
+    w = O.msm_window_rule(n)
+    runs, t0 = 0, time.perf_counter()
+    while True:
+        O.msm_pippenger(bases, s, w)
+        runs += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or full_size:
+            break
+    return n * runs / el / 1e6, runs, el
+
+
+def cpu_ntt_sample(log_n: int, budget_s: float = 5.0):
+    from oracle import oracle as O
+    from pyzkp_gb300 import synth
+
+    n = 1 << log_n
+    v = synth.fr_uniform(synth.seed_for(1, log_n), n)
+    om = O.omega_for_size(n)
+    runs, t0 = 0, time.perf_counter()
+    while True:
+        O.ntt_op(0, v, n, om)
+        runs += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s:
+            break
+    return n * runs / el / 1e6, runs, el
+
+
+def cpu_baseline(log_n: int, gpu_result) -> dict:
+    """CPU baseline leg (rank 0, N=1): the oracle port timed on a bounded sample; it also
+    checks the GPU arm's MSM result against the known answer [sum k_i s_i]G."""
+    from oracle import oracle as O
+    from pyzkp_gb300 import synth
+
+    n = 1 << log_n
+    seed = synth.seed_for(2, log_n)
+    known = O.affine_to_ints(O.msm_known_answer(synth.base_dlogs(seed, n), synth.fr_uniform(seed, n)))
+    mp, runs, el = cpu_msm_sample(log_n, 10.0)
+    ne, nruns, nel = cpu_ntt_sample(20, 5.0)
+    return {"value": round(mp, 4), "unit": "Mpts/s", "cores": O.num_threads(), "kind": "port",
+            "gpu_result_matches_known_answer": [hex(known[0]), hex(known[1])] == gpu_result,
+            "sample": f"C restatement of crypto/msm/pippenger.py (window rule w={O.msm_window_rule(1 << log_n)}), "
+                      f"full n=2^{log_n} MSM x{runs} in {el:.1f}s on all host threads",
+            "ntt": {"value": round(ne, 3), "unit": "Melem/s",
+                    "sample": f"C restatement of crypto/poly/ntt.py, forward n=2^20 x{nruns} in {nel:.1f}s"}}
+
+
+def run_reference(args, ranks: Ranks) -> dict:
+    from oracle import oracle as O
+    from pyzkp_gb300 import synth
+
+    log_n = args.log_n
+    n = 1 << log_n
+    seed = synth.seed_for(2, log_n)
+    k = synth.base_dlogs(seed, n)
+    s = synth.fr_uniform(seed, n)
+    bases = O.g1_fixed_base_mul(O.G1_GENERATOR, k)
+    w = O.msm_window_rule(n)
+    for _ in range(args.warmup):
+        O.msm_pippenger(bases, s, w)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.msm_pippenger(bases, s, w)
+        ts.append(time.perf_counter() - t0)
+    total = sum(ts)
+    value = n * args.steps / total / 1e6
+    ne, nruns, nel = cpu_ntt_sample(20, 3.0)
+    return {
+        "metric": METRIC, "value": round(value, 4), "unit": "Mpts/s", "impl": "reference", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total / args.steps * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 limbs (exact)",
+        "data": "synthetic (same seeds as the gb300 arm)",
+        "config": {"workload": f"G1 MSM n=2^{log_n} (uniform scalars) + Fr NTT n=2^20", "n": n, "seed": seed,
+                   "window_bits": w},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mpts/s", "cores": O.num_threads(), "kind": "port",
+                         "sample": f"full n=2^{log_n} MSM per step, C restatement of crypto/msm/pippenger.py"},
+        "e2e": {"value": round(value, 4), "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "ntt": {"value": round(ne, 3), "unit": "Melem/s", "sample": f"forward n=2^20 x{nruns} in {nel:.1f}s"},
+    }
+
+
+def main() -> None:
+    args = parse()
+    if args.warmup < 3:
+        args.warmup = 3
+    ranks = Ranks(args.gpus)
+    try:
+        if args.impl == "reference":
+            if ranks.rank == 0:
+                print(json.dumps(run_reference(args, ranks)), flush=True)
+            return
+        res = run_gpu(args, ranks)
+        if ranks.rank == 0:
+            if ranks.world == 1 and not args.no_cpu_baseline:
+                res["cpu_baseline"] = cpu_baseline(args.log_n, res.get("msm_result"))
+            print(json.dumps(res), flush=True)
+    finally:
+        ranks.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -59,6 +59,27 @@ int zk_ctx_stream(zk_ctx *ctx, void **stream_out);
 int zk_ctx_num_sms(zk_ctx *ctx, int *out);
 
 /*
+ * Kernel accounting, for measurement (no counterpart in the reference, whose
+ * Trace only times whole ops, runtime/trace.py:49-101). Every kernel the library
+ * launches is counted; with profiling enabled each launch is also bracketed by
+ * CUDA events on the context stream and its device time accumulated per kernel.
+ */
+int zk_launch_count(zk_ctx *ctx, uint64_t *out);
+int zk_prof_enable(zk_ctx *ctx, int on);
+int zk_prof_reset(zk_ctx *ctx);
+int zk_prof_count(zk_ctx *ctx, int *nkernels);
+int zk_prof_get(zk_ctx *ctx, int idx, char *name_buf, size_t name_len, uint64_t *launches, double *total_ms);
+/* Device time between zk_timer_start and zk_timer_stop, from CUDA events recorded on
+ * the context stream (stop synchronises; host work inside synchronous calls counts). */
+int zk_timer_start(zk_ctx *ctx);
+int zk_timer_stop(zk_ctx *ctx, double *ms);
+/* Shape of the last zk_msm_g1 call: CSR entries (non-zero signed digits), window bits, windows. */
+int zk_msm_last_stats(zk_ctx *ctx, uint64_t *entries, uint32_t *window_bits, uint32_t *windows);
+/* Measured throughput of the 32-bit integer multiply-add pipe (mad.lo/mad.hi carry chains
+ * shaped like the Montgomery inner loop), in 10^12 IMAD instructions per second. */
+int zk_imad_peak(zk_ctx *ctx, double *tera_imad_per_s);
+
+/*
  * Device memory (stream-ordered pool of the context). Replaces
  * MemoryPool.alloc_metal / release_metal (runtime/memory.py:56-91).
  */
@@ -67,6 +88,10 @@ int zk_free(zk_ctx *ctx, void *dptr);
 /* Copies on the context stream; both block until the copy is complete. */
 int zk_h2d(zk_ctx *ctx, void *dst_dev, const void *src_host, size_t bytes);
 int zk_d2h(zk_ctx *ctx, void *dst_host, const void *src_dev, size_t bytes);
+/* Device-to-device copy on the context stream (asynchronous). */
+int zk_d2d(zk_ctx *ctx, void *dst_dev, const void *src_dev, size_t bytes);
+/* Fill bytes of device memory (asynchronous on the context stream). */
+int zk_memset(zk_ctx *ctx, void *dptr, int value, size_t bytes);
 /* Page-locked host memory for fast copies. */
 int zk_host_alloc(size_t bytes, void **out);
 int zk_host_free(void *p);
@@ -87,6 +112,9 @@ int zk_fq_from_mont(zk_ctx *ctx, void *out, const void *in, size_t n);
 int zk_fr_mul(zk_ctx *ctx, void *out, const void *a, const void *b, size_t n);
 /* out[i] = a[i] - b[i]: POLY_SUB on equal lengths, runtime/kernels/metal/kernels.py:122-167. */
 int zk_fr_sub(zk_ctx *ctx, void *out, const void *a, const void *b, size_t n);
+/* *out = 1 + index of the last non-zero element of a[0..n) (0 if all are zero): the
+ * trailing-zero trim of crypto/poly/cpu_ref.py:_trim used by poly_sub (:18-25). Blocks. */
+int zk_fr_trimmed_len(zk_ctx *ctx, const void *a, size_t n, size_t *out);
 
 /*
  * NTT family over Fr, natural order in and out, Montgomery in and out.

@@ -30,7 +30,9 @@ EXPORTED_SYMBOLS = (
     "zk_ctx_num_sms", "zk_alloc", "zk_free", "zk_h2d", "zk_d2h", "zk_host_alloc", "zk_host_free",
     "zk_fr_to_mont", "zk_fr_from_mont", "zk_fq_to_mont", "zk_fq_from_mont", "zk_fr_mul", "zk_fr_sub", "zk_ntt",
     "zk_bases_create", "zk_bases_create_dev", "zk_bases_destroy", "zk_bases_count", "zk_msm_g1",
-    "zk_g1_fixed_base_mul",
+    "zk_g1_fixed_base_mul", "zk_memset", "zk_launch_count", "zk_prof_enable", "zk_prof_reset", "zk_prof_count",
+    "zk_prof_get", "zk_timer_start", "zk_timer_stop", "zk_msm_last_stats", "zk_imad_peak", "zk_d2d",
+    "zk_fr_trimmed_len",
 )
 
 _lib: Optional[ctypes.CDLL] = None
@@ -79,6 +81,20 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_bases_count": ([P, ctypes.POINTER(ctypes.c_size_t)], I),
             "zk_msm_g1": ([P, P, S, P, S, I, U32, P, ctypes.POINTER(ctypes.c_int)], I),
             "zk_g1_fixed_base_mul": ([P, P, P, S, P], I),
+            "zk_memset": ([P, P, I, S], I),
+            "zk_launch_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
+            "zk_prof_enable": ([P, I], I),
+            "zk_prof_reset": ([P], I),
+            "zk_prof_count": ([P, ctypes.POINTER(ctypes.c_int)], I),
+            "zk_prof_get": ([P, I, ctypes.c_char_p, S, ctypes.POINTER(ctypes.c_uint64),
+                             ctypes.POINTER(ctypes.c_double)], I),
+            "zk_timer_start": ([P], I),
+            "zk_timer_stop": ([P, ctypes.POINTER(ctypes.c_double)], I),
+            "zk_msm_last_stats": ([P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint32),
+                                   ctypes.POINTER(ctypes.c_uint32)], I),
+            "zk_imad_peak": ([P, ctypes.POINTER(ctypes.c_double)], I),
+            "zk_d2d": ([P, P, P, S], I),
+            "zk_fr_trimmed_len": ([P, P, S, ctypes.POINTER(ctypes.c_size_t)], I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -123,6 +139,10 @@ class DeviceArray:
         except Exception:
             pass
 
+    def length(self) -> int:
+        """Byte size (the MTLBuffer.length() protocol used by MemoryPool.release_metal)."""
+        return self.nbytes
+
     def upload(self, host: np.ndarray) -> None:
         buf = np.ascontiguousarray(host)
         if buf.nbytes > self.nbytes:
@@ -134,6 +154,29 @@ class DeviceArray:
         out = np.empty(nb, dtype=np.uint8)
         check(load().zk_d2h(self.ctx.handle, out.ctypes.data, self.ptr, nb), "zk_d2h")
         return out
+
+
+class PinnedBuffer:
+    """Page-locked host memory exposed as a numpy uint8 array (``.array``)."""
+
+    def __init__(self, nbytes: int) -> None:
+        p = ctypes.c_void_p()
+        check(load().zk_host_alloc(max(16, int(nbytes)), ctypes.byref(p)), "zk_host_alloc")
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+        self.array = np.ctypeslib.as_array((ctypes.c_uint8 * max(16, self.nbytes)).from_address(self.ptr))[:self.nbytes]
+
+    def free(self) -> None:
+        if self.ptr is not None:
+            self.array = None
+            load().zk_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self) -> None:
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 class Bases:
@@ -179,7 +222,58 @@ class Context:
         check(load().zk_ctx_num_sms(self.handle, ctypes.byref(v)))
         return v.value
 
+    # ---- measurement ----
+    def memset(self, d: DeviceArray, value: int = 0) -> None:
+        check(load().zk_memset(self.handle, d.ptr, int(value), d.nbytes), "zk_memset")
+
+    def launch_count(self) -> int:
+        v = ctypes.c_uint64()
+        check(load().zk_launch_count(self.handle, ctypes.byref(v)))
+        return int(v.value)
+
+    def prof_enable(self, on: bool) -> None:
+        check(load().zk_prof_enable(self.handle, 1 if on else 0), "zk_prof_enable")
+
+    def prof_reset(self) -> None:
+        check(load().zk_prof_reset(self.handle), "zk_prof_reset")
+
+    def prof_table(self) -> dict:
+        """{kernel name: (launches, total device ms)} accumulated since the last reset."""
+        L = load()
+        cnt = ctypes.c_int()
+        check(L.zk_prof_count(self.handle, ctypes.byref(cnt)))
+        out = {}
+        buf = ctypes.create_string_buffer(128)
+        for i in range(cnt.value):
+            la, ms = ctypes.c_uint64(), ctypes.c_double()
+            check(L.zk_prof_get(self.handle, i, buf, 128, ctypes.byref(la), ctypes.byref(ms)))
+            out[buf.value.decode()] = (int(la.value), float(ms.value))
+        return out
+
+    def timer_start(self) -> None:
+        check(load().zk_timer_start(self.handle), "zk_timer_start")
+
+    def timer_stop(self) -> float:
+        """Milliseconds since timer_start, from CUDA events on the context stream."""
+        v = ctypes.c_double()
+        check(load().zk_timer_stop(self.handle, ctypes.byref(v)), "zk_timer_stop")
+        return float(v.value)
+
+    def msm_last_stats(self) -> dict:
+        e, c, w = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint32()
+        check(load().zk_msm_last_stats(self.handle, ctypes.byref(e), ctypes.byref(c), ctypes.byref(w)))
+        return {"entries": int(e.value), "window_bits": int(c.value), "windows": int(w.value)}
+
+    def imad_peak(self) -> float:
+        """Measured 32-bit IMAD throughput, 10^12 instructions/s."""
+        v = ctypes.c_double()
+        check(load().zk_imad_peak(self.handle, ctypes.byref(v)), "zk_imad_peak")
+        return float(v.value)
+
     # ---- memory ----
+    def pinned(self, nbytes: int) -> "PinnedBuffer":
+        return PinnedBuffer(nbytes)
+
     def alloc(self, nbytes: int) -> DeviceArray:
         return DeviceArray(self, nbytes)
 
@@ -195,6 +289,14 @@ class Context:
 
     def fr_from_mont(self, out: DeviceArray, inp: DeviceArray, n: int) -> None:
         check(load().zk_fr_from_mont(self.handle, out.ptr, inp.ptr, n), "zk_fr_from_mont")
+
+    def d2d(self, dst: DeviceArray, src: DeviceArray, nbytes: int) -> None:
+        check(load().zk_d2d(self.handle, dst.ptr, src.ptr, int(nbytes)), "zk_d2d")
+
+    def fr_trimmed_len(self, a: DeviceArray, n: int) -> int:
+        v = ctypes.c_size_t()
+        check(load().zk_fr_trimmed_len(self.handle, a.ptr, int(n), ctypes.byref(v)), "zk_fr_trimmed_len")
+        return int(v.value)
 
     def fr_mul(self, out: DeviceArray, a: DeviceArray, b: DeviceArray, n: int) -> None:
         check(load().zk_fr_mul(self.handle, out.ptr, a.ptr, b.ptr, n), "zk_fr_mul")

@@ -1,5 +1,6 @@
 // capi.cu -- extern "C" entry points declared in include/zkgpu.h.
 #include <cstring>
+#include <iterator>
 #include <string>
 
 #include "zk_internal.cuh"
@@ -25,10 +26,59 @@ void scratch_free(Ctx* c, void* p) {
     if (p) cudaFreeAsync(p, c->stream);
 }
 
+static cudaEvent_t take_event(Ctx* c) {
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+int prof_begin(Ctx* c, const char* name) {
+    c->launches++;
+    if (!c->prof_on) {
+        c->prof[name].launches++;
+        return -1;
+    }
+    ProfPending p;
+    p.name = name;
+    p.start = take_event(c);
+    p.stop = take_event(c);
+    cudaEventRecord(p.start, c->stream);
+    c->prof_pending.push_back(p);
+    return (int)c->prof_pending.size() - 1;
+}
+
+void prof_end(Ctx* c, int token) {
+    if (token < 0) return;
+    cudaEventRecord(c->prof_pending[token].stop, c->stream);
+}
+
+int prof_resolve(Ctx* c) {
+    if (c->prof_pending.empty()) return ZK_OK;
+    ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
+    for (auto& p : c->prof_pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.start, p.stop);
+        ProfEntry& e = c->prof[p.name];
+        e.launches++;
+        e.total_ms += ms;
+        c->event_pool.push_back(p.start);
+        c->event_pool.push_back(p.stop);
+    }
+    c->prof_pending.clear();
+    return ZK_OK;
+}
+
 template <class F, int DIR>
 int convert(Ctx* c, void* out, const void* in, size_t n);
 int fr_binary(Ctx* c, int op, void* out, const void* a, const void* b, size_t n);
 int fixed_base_mul(Ctx* c, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_dev);
+int imad_peak(Ctx* c, double* tera);
+int trimmed_len(Ctx* c, const void* a, size_t n, size_t* out);
 
 }  // namespace zk
 
@@ -88,6 +138,10 @@ int zk_ctx_destroy(zk_ctx* ctx) {
     if (ctx == nullptr) return ZK_OK;
     cudaSetDevice(ctx->impl.device);
     cudaStreamSynchronize(ctx->impl.stream);
+    zk::prof_resolve(&ctx->impl);
+    for (cudaEvent_t e : ctx->impl.event_pool) cudaEventDestroy(e);
+    if (ctx->impl.timer_start) cudaEventDestroy(ctx->impl.timer_start);
+    if (ctx->impl.timer_stop) cudaEventDestroy(ctx->impl.timer_stop);
     for (auto& kv : ctx->impl.ntt_plans) {
         for (void* p : kv.second->allocations) cudaFree(p);
         delete kv.second;
@@ -113,6 +167,110 @@ int zk_ctx_num_sms(zk_ctx* ctx, int* out) {
     CTX_OR_FAIL(ctx);
     *out = ctx->impl.num_sms;
     return ZK_OK;
+}
+
+int zk_d2d(zk_ctx* ctx, void* dst_dev, const void* src_dev, size_t bytes) {
+    CTX_OR_FAIL(ctx);
+    if (bytes == 0) return ZK_OK;
+    ZK_TRY_CUDA(cudaMemcpyAsync(dst_dev, src_dev, bytes, cudaMemcpyDeviceToDevice, ctx->impl.stream));
+    return ZK_OK;
+}
+
+int zk_fr_trimmed_len(zk_ctx* ctx, const void* a, size_t n, size_t* out) {
+    CTX_OR_FAIL(ctx);
+    if (out == nullptr) {
+        zk::set_error("null output pointer");
+        return ZK_EINVAL;
+    }
+    return zk::trimmed_len(&ctx->impl, a, n, out);
+}
+
+int zk_memset(zk_ctx* ctx, void* dptr, int value, size_t bytes) {
+    CTX_OR_FAIL(ctx);
+    if (bytes == 0) return ZK_OK;
+    ZK_TRY_CUDA(cudaMemsetAsync(dptr, value, bytes, ctx->impl.stream));
+    return ZK_OK;
+}
+
+int zk_launch_count(zk_ctx* ctx, uint64_t* out) {
+    CTX_OR_FAIL(ctx);
+    *out = ctx->impl.launches;
+    return ZK_OK;
+}
+
+int zk_prof_enable(zk_ctx* ctx, int on) {
+    CTX_OR_FAIL(ctx);
+    int rc = zk::prof_resolve(&ctx->impl);
+    ctx->impl.prof_on = on != 0;
+    return rc;
+}
+
+int zk_prof_reset(zk_ctx* ctx) {
+    CTX_OR_FAIL(ctx);
+    int rc = zk::prof_resolve(&ctx->impl);
+    ctx->impl.prof.clear();
+    return rc;
+}
+
+int zk_prof_count(zk_ctx* ctx, int* nkernels) {
+    CTX_OR_FAIL(ctx);
+    int rc = zk::prof_resolve(&ctx->impl);
+    *nkernels = (int)ctx->impl.prof.size();
+    return rc;
+}
+
+int zk_prof_get(zk_ctx* ctx, int idx, char* name_buf, size_t name_len, uint64_t* launches, double* total_ms) {
+    CTX_OR_FAIL(ctx);
+    int rc = zk::prof_resolve(&ctx->impl);
+    if (rc != ZK_OK) return rc;
+    if (idx < 0 || idx >= (int)ctx->impl.prof.size() || name_buf == nullptr || name_len == 0) {
+        zk::set_error("profile index out of range");
+        return ZK_EINVAL;
+    }
+    auto it = ctx->impl.prof.begin();
+    std::advance(it, idx);
+    std::strncpy(name_buf, it->first.c_str(), name_len - 1);
+    name_buf[name_len - 1] = 0;
+    *launches = it->second.launches;
+    *total_ms = it->second.total_ms;
+    return ZK_OK;
+}
+
+int zk_timer_start(zk_ctx* ctx) {
+    CTX_OR_FAIL(ctx);
+    zk::Ctx* c = &ctx->impl;
+    if (!c->timer_start) ZK_TRY_CUDA(cudaEventCreate(&c->timer_start));
+    if (!c->timer_stop) ZK_TRY_CUDA(cudaEventCreate(&c->timer_stop));
+    ZK_TRY_CUDA(cudaEventRecord(c->timer_start, c->stream));
+    return ZK_OK;
+}
+
+int zk_timer_stop(zk_ctx* ctx, double* ms) {
+    CTX_OR_FAIL(ctx);
+    zk::Ctx* c = &ctx->impl;
+    if (!c->timer_start || !c->timer_stop) {
+        zk::set_error("zk_timer_stop without zk_timer_start");
+        return ZK_EINVAL;
+    }
+    ZK_TRY_CUDA(cudaEventRecord(c->timer_stop, c->stream));
+    ZK_TRY_CUDA(cudaEventSynchronize(c->timer_stop));
+    float f = 0.f;
+    ZK_TRY_CUDA(cudaEventElapsedTime(&f, c->timer_start, c->timer_stop));
+    *ms = f;
+    return ZK_OK;
+}
+
+int zk_msm_last_stats(zk_ctx* ctx, uint64_t* entries, uint32_t* window_bits, uint32_t* windows) {
+    CTX_OR_FAIL(ctx);
+    *entries = ctx->impl.msm_entries;
+    *window_bits = ctx->impl.msm_window_bits;
+    *windows = ctx->impl.msm_windows;
+    return ZK_OK;
+}
+
+int zk_imad_peak(zk_ctx* ctx, double* tera_imad_per_s) {
+    CTX_OR_FAIL(ctx);
+    return zk::imad_peak(&ctx->impl, tera_imad_per_s);
 }
 
 int zk_alloc(zk_ctx* ctx, size_t bytes, void** dptr) {

@@ -334,7 +334,8 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
     ZK_TRY_CUDA(cudaMemsetAsync(buckets, 0, nbuckets * sizeof(xyzz_t), st));
 
     const uint32_t nn = (uint32_t)n;
-    msm_digits_kernel<<<(nn + 255) / 256, 256, 0, st>>>(scalars, bases, nn, scalars_mont, sh, digits, row_ptr);
+    ZK_LAUNCH(c, "msm_digits", msm_digits_kernel, (nn + 255) / 256, 256, 0, scalars, bases, nn, scalars_mont, sh, digits,
+              row_ptr);
     ZK_TRY_CUDA(cudaGetLastError());
     // row_ptr[0..nbuckets) := exclusive scan; row_ptr[nbuckets] := total
     if ((rc = device_exclusive_scan(c, row_ptr, nbuckets, row_ptr + nbuckets)) != ZK_OK) {
@@ -342,7 +343,7 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
         return rc;
     }
     ZK_TRY_CUDA(cudaMemcpyAsync(cursor, row_ptr, nbuckets * 4, cudaMemcpyDeviceToDevice, st));
-    msm_scatter_kernel<<<(nn + 255) / 256, 256, 0, st>>>(digits, nn, sh, cursor, entries, keys);
+    ZK_LAUNCH(c, "msm_scatter", msm_scatter_kernel, (nn + 255) / 256, 256, 0, digits, nn, sh, cursor, entries, keys);
     ZK_TRY_CUDA(cudaGetLastError());
 
     // accumulation rounds
@@ -358,8 +359,8 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
         release();
         return rc;
     }
-    msm_accumulate_kernel<<<(units + 127) / 128, 128, 0, st>>>(entries, keys, d_total, row_ptr, bases, units, buckets,
-                                                                slot_keys_a, slot_pts_a);
+    ZK_LAUNCH(c, "msm_accumulate", msm_accumulate_kernel, (units + 127) / 128, 128, 0, entries, keys, d_total, row_ptr,
+              bases, units, buckets, slot_keys_a, slot_pts_a);
     ZK_TRY_CUDA(cudaGetLastError());
     uint64_t span = kSegment;
     uint32_t in_units = units;
@@ -368,8 +369,8 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
     while (in_units > 1) {
         const uint32_t out_units = (in_units + kGroup - 1) / kGroup;
         span *= kGroup;
-        msm_merge_kernel<<<(out_units + 127) / 128, 128, 0, st>>>(ik, ip, in_units, d_total, row_ptr, span, out_units,
-                                                                   buckets, ok, op);
+        ZK_LAUNCH(c, "msm_merge", msm_merge_kernel, (out_units + 127) / 128, 128, 0, ik, ip, in_units, d_total, row_ptr,
+                  span, out_units, buckets, ok, op);
         ZK_TRY_CUDA(cudaGetLastError());
         std::swap(ik, ok);
         std::swap(ip, op);
@@ -378,14 +379,19 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
 
     // window reduction
     const uint32_t nblk = sh.W * sh.G;
-    msm_bucket_blocks_kernel<<<(nblk + 127) / 128, 128, 0, st>>>(buckets, sh, Yb, Eb);
+    ZK_LAUNCH(c, "msm_bucket_blocks", msm_bucket_blocks_kernel, (nblk + 127) / 128, 128, 0, buckets, sh, Yb, Eb);
     ZK_TRY_CUDA(cudaGetLastError());
-    msm_targets_kernel<<<sh.W * sh.targets, kTargetThreads, 0, st>>>(Yb, Eb, sh, tgt);
+    ZK_LAUNCH(c, "msm_targets", msm_targets_kernel, sh.W * sh.targets, kTargetThreads, 0, Yb, Eb, sh, tgt);
     ZK_TRY_CUDA(cudaGetLastError());
     std::vector<xyzz_t> host_t((size_t)sh.W * sh.targets);
+    uint32_t total_entries = 0;
     ZK_TRY_CUDA(cudaMemcpyAsync(host_t.data(), tgt, host_t.size() * sizeof(xyzz_t), cudaMemcpyDeviceToHost, st));
+    ZK_TRY_CUDA(cudaMemcpyAsync(&total_entries, d_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     ZK_TRY_CUDA(cudaStreamSynchronize(st));
     release();
+    c->msm_entries = total_entries;
+    c->msm_window_bits = sh.c;
+    c->msm_windows = sh.W;
 
     // host: S_w = T_E + g (T_Y + sum_k 2^k M_k); total = sum_w 2^(c w) S_w
     uint32_t log_g = 0;

@@ -308,7 +308,7 @@ int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log
         P.log_t = 0;
         P.log_l = 0;
         P.s_bits = plan->s_bits;
-        ntt_pass_kernel<<<1, 32, 2 * 16, c->stream>>>(P);
+        ZK_LAUNCH(c, "ntt_pass", ntt_pass_kernel, 1, 32, 2 * 16, P);
         ZK_TRY_CUDA(cudaGetLastError());
         return ZK_OK;
     }
@@ -352,7 +352,7 @@ int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log
         const uint32_t elems = 1u << (lr + lt);
         const uint32_t threads = elems / 2 < (uint32_t)kNttThreads ? (elems / 2 < 32 ? 32 : elems / 2) : kNttThreads;
         const uint32_t blocks = (uint32_t)(n >> (lr + lt));
-        ntt_pass_kernel<<<blocks, threads, (size_t)elems * 32, c->stream>>>(P);
+        ZK_LAUNCH(c, "ntt_pass", ntt_pass_kernel, blocks, threads, (size_t)elems * 32, P);
         ZK_TRY_CUDA(cudaGetLastError());
         src = dst;
         log_l += lr;

@@ -35,12 +35,36 @@ __global__ void fr_sub_kernel(fe* out, const fe* a, const fe* b, size_t n) {
         fe_store(out + i, fe_sub<FrP>(fe_ldg(a + i), fe_ldg(b + i)));
 }
 
+__global__ void last_nonzero_kernel(const fe* a, size_t n, unsigned long long* out) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        if (!fe_is_zero(fe_ldg(a + i))) atomicMax(out, (unsigned long long)(i + 1));
+}
+
+int trimmed_len(Ctx* c, const void* a, size_t n, size_t* out) {
+    *out = 0;
+    if (n == 0) return ZK_OK;
+    ZK_CHECK_ARG(a != nullptr, "null buffer");
+    unsigned long long* d = nullptr;
+    int rc = scratch_alloc(c, sizeof(unsigned long long), reinterpret_cast<void**>(&d));
+    if (rc != ZK_OK) return rc;
+    ZK_TRY_CUDA(cudaMemsetAsync(d, 0, sizeof(unsigned long long), c->stream));
+    ZK_LAUNCH(c, "last_nonzero", last_nonzero_kernel, grid_for(n, 256, c->num_sms), 256, 0,
+              static_cast<const fe*>(a), n, d);
+    ZK_TRY_CUDA(cudaGetLastError());
+    unsigned long long h = 0;
+    ZK_TRY_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
+    scratch_free(c, d);
+    *out = (size_t)h;
+    return ZK_OK;
+}
+
 template <class F, int DIR>
 int convert(Ctx* c, void* out, const void* in, size_t n) {
     if (n == 0) return ZK_OK;
     ZK_CHECK_ARG(out != nullptr && in != nullptr, "null buffer");
-    convert_kernel<F, DIR><<<grid_for(n, 256, c->num_sms), 256, 0, c->stream>>>(static_cast<fe*>(out),
-                                                                                 static_cast<const fe*>(in), n);
+    ZK_LAUNCH(c, DIR ? "to_mont" : "from_mont", (convert_kernel<F, DIR>), grid_for(n, 256, c->num_sms), 256, 0,
+              static_cast<fe*>(out), static_cast<const fe*>(in), n);
     ZK_TRY_CUDA(cudaGetLastError());
     return ZK_OK;
 }
@@ -54,11 +78,11 @@ int fr_binary(Ctx* c, int op, void* out, const void* a, const void* b, size_t n)
     if (n == 0) return ZK_OK;
     ZK_CHECK_ARG(out != nullptr && a != nullptr && b != nullptr, "null buffer");
     if (op == 0)
-        fr_mul_kernel<<<grid_for(n, 256, c->num_sms), 256, 0, c->stream>>>(
-            static_cast<fe*>(out), static_cast<const fe*>(a), static_cast<const fe*>(b), n);
+        ZK_LAUNCH(c, "fr_mul", fr_mul_kernel, grid_for(n, 256, c->num_sms), 256, 0, static_cast<fe*>(out),
+                  static_cast<const fe*>(a), static_cast<const fe*>(b), n);
     else
-        fr_sub_kernel<<<grid_for(n, 256, c->num_sms), 256, 0, c->stream>>>(
-            static_cast<fe*>(out), static_cast<const fe*>(a), static_cast<const fe*>(b), n);
+        ZK_LAUNCH(c, "fr_sub", fr_sub_kernel, grid_for(n, 256, c->num_sms), 256, 0, static_cast<fe*>(out),
+                  static_cast<const fe*>(a), static_cast<const fe*>(b), n);
     ZK_TRY_CUDA(cudaGetLastError());
     return ZK_OK;
 }
@@ -158,12 +182,81 @@ int fixed_base_mul(Ctx* c, const uint8_t point_xy[64], const void* k_dev, size_t
     if (rc != ZK_OK) return rc;
     ZK_TRY_CUDA(cudaMemcpyAsync(dtab, table.data(), table.size() * sizeof(affine_t), cudaMemcpyHostToDevice,
                                 c->stream));
-    fixed_base_kernel<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(dtab, static_cast<const fe*>(k_dev), n,
-                                                                           static_cast<affine_t*>(out_dev));
+    ZK_LAUNCH(c, "fixed_base", fixed_base_kernel, (unsigned)((n + 127) / 128), 128, 0, dtab,
+              static_cast<const fe*>(k_dev), n, static_cast<affine_t*>(out_dev));
     ZK_TRY_CUDA(cudaGetLastError());
     // the host table must outlive the async copy
     ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
     scratch_free(c, dtab);
+    return ZK_OK;
+}
+
+}  // namespace zk
+
+namespace zk {
+
+// ---- IMAD throughput probe: 8 independent carry chains per thread, each step a
+// mad.lo.cc / madc.hi.cc pair per limb like one row of the Montgomery product. ----
+__global__ void imad_probe_kernel(uint32_t iters, uint32_t seed, uint32_t* sink) {
+    uint32_t a[8], x = seed ^ threadIdx.x, y = seed * 2654435761u + blockIdx.x;
+#pragma unroll
+    for (int i = 0; i < 8; i++) a[i] = x + i;
+    for (uint32_t it = 0; it < iters; it++) {
+        asm volatile(
+            "mad.lo.cc.u32  %0, %8, %9, %0;\n\t"
+            "madc.hi.cc.u32 %1, %8, %9, %1;\n\t"
+            "madc.lo.cc.u32 %2, %8, %9, %2;\n\t"
+            "madc.hi.cc.u32 %3, %8, %9, %3;\n\t"
+            "madc.lo.cc.u32 %4, %8, %9, %4;\n\t"
+            "madc.hi.cc.u32 %5, %8, %9, %5;\n\t"
+            "madc.lo.cc.u32 %6, %8, %9, %6;\n\t"
+            "madc.hi.u32    %7, %8, %9, %7;\n\t"
+            : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
+            : "r"(x), "r"(y));
+        asm volatile(
+            "mad.lo.cc.u32  %0, %8, %9, %0;\n\t"
+            "madc.hi.cc.u32 %1, %8, %9, %1;\n\t"
+            "madc.lo.cc.u32 %2, %8, %9, %2;\n\t"
+            "madc.hi.cc.u32 %3, %8, %9, %3;\n\t"
+            "madc.lo.cc.u32 %4, %8, %9, %4;\n\t"
+            "madc.hi.cc.u32 %5, %8, %9, %5;\n\t"
+            "madc.lo.cc.u32 %6, %8, %9, %6;\n\t"
+            "madc.hi.u32    %7, %8, %9, %7;\n\t"
+            : "+r"(a[7]), "+r"(a[6]), "+r"(a[5]), "+r"(a[4]), "+r"(a[3]), "+r"(a[2]), "+r"(a[1]), "+r"(a[0])
+            : "r"(y), "r"(x));
+        x += a[0];
+    }
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) s ^= a[i];
+    if (s == 0x9e3779b9u) sink[0] = s;  // keeps the chains alive
+}
+
+int imad_peak(Ctx* c, double* tera) {
+    uint32_t* sink = nullptr;
+    int rc = scratch_alloc(c, 16, reinterpret_cast<void**>(&sink));
+    if (rc != ZK_OK) return rc;
+    const uint32_t blocks = (uint32_t)c->num_sms * 8, threads = 256, iters = 4096;
+    cudaEvent_t e0, e1;
+    ZK_TRY_CUDA(cudaEventCreate(&e0));
+    ZK_TRY_CUDA(cudaEventCreate(&e1));
+    imad_probe_kernel<<<blocks, threads, 0, c->stream>>>(iters, 1u, sink);  // warm-up
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; rep++) {
+        ZK_TRY_CUDA(cudaEventRecord(e0, c->stream));
+        imad_probe_kernel<<<blocks, threads, 0, c->stream>>>(iters, 2u + rep, sink);
+        ZK_TRY_CUDA(cudaEventRecord(e1, c->stream));
+        ZK_TRY_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        ZK_TRY_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) best = ms;
+    }
+    ZK_TRY_CUDA(cudaGetLastError());
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    scratch_free(c, sink);
+    const double ops = (double)blocks * threads * iters * 16.0;
+    *tera = ops / (best * 1e-3) / 1e12;
     return ZK_OK;
 }
 

@@ -63,13 +63,13 @@ int device_exclusive_scan(Ctx* c, uint32_t* data, size_t n, uint32_t* total) {
     uint32_t* sums = nullptr;
     int rc = scratch_alloc(c, (tiles + 1) * sizeof(uint32_t), reinterpret_cast<void**>(&sums));
     if (rc != ZK_OK) return rc;
-    scan_tiles_kernel<<<(unsigned)tiles, kScanThreads, 0, c->stream>>>(data, n, sums);
+    ZK_LAUNCH(c, "scan_tiles", scan_tiles_kernel, (unsigned)tiles, kScanThreads, 0, data, n, sums);
     ZK_TRY_CUDA(cudaGetLastError());
     if (tiles > 1) {
         // sums[tiles] receives the grand total through the recursive scan's total slot
         rc = device_exclusive_scan(c, sums, tiles, total);
         if (rc != ZK_OK) return rc;
-        scan_add_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(data, n, sums);
+        ZK_LAUNCH(c, "scan_add", scan_add_kernel, (unsigned)((n + 255) / 256), 256, 0, data, n, sums);
         ZK_TRY_CUDA(cudaGetLastError());
     } else if (total != nullptr) {
         ZK_TRY_CUDA(cudaMemcpyAsync(total, sums, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c->stream));

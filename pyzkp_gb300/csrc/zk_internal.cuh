@@ -50,13 +50,45 @@ struct NttPlan {
     std::vector<void*> allocations;
 };
 
+// Per-kernel accounting (zk_prof_*): launches are always counted; with profiling on,
+// each launch is bracketed by events on the context stream and resolved lazily.
+struct ProfEntry {
+    uint64_t launches = 0;
+    double total_ms = 0.0;
+};
+
+struct ProfPending {
+    std::string name;
+    cudaEvent_t start, stop;
+};
+
 struct Ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     std::mutex mu;
     std::map<std::string, NttPlan*> ntt_plans;
+    uint64_t launches = 0;
+    bool prof_on = false;
+    std::map<std::string, ProfEntry> prof;
+    std::vector<ProfPending> prof_pending;
+    std::vector<cudaEvent_t> event_pool;
+    cudaEvent_t timer_start = nullptr, timer_stop = nullptr;
+    uint64_t msm_entries = 0;
+    uint32_t msm_window_bits = 0, msm_windows = 0;
 };
+
+int prof_begin(Ctx* c, const char* name);
+void prof_end(Ctx* c, int token);
+int prof_resolve(Ctx* c);
+
+// Launch `kernel` on the context stream with launch accounting.
+#define ZK_LAUNCH(ctxp, name, kernel, grid, block, smem, ...)                 \
+    do {                                                                      \
+        int _tok = ::zk::prof_begin((ctxp), (name));                          \
+        kernel<<<(grid), (block), (smem), (ctxp)->stream>>>(__VA_ARGS__);     \
+        ::zk::prof_end((ctxp), _tok);                                         \
+    } while (0)
 
 // Stream-ordered scratch allocation on the context stream (pooled by the driver).
 int scratch_alloc(Ctx* c, size_t bytes, void** p);
