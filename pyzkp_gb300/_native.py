@@ -16,7 +16,7 @@ from typing import Optional
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "libzkgpu.so")
+LIB_PATH = os.environ.get("ZKGPU_LIB") or os.path.join(HERE, "_lib", "libzkgpu.so")
 
 ZK_OK, ZK_EINVAL, ZK_ECUDA, ZK_ENOMEM, ZK_ENODEV = 0, 1, 2, 3, 4
 

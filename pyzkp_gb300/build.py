@@ -43,8 +43,8 @@ def _headers_mtime() -> float:
     return max(os.path.getmtime(h) for h in hs)
 
 
-def _compile(src: str, extra: List[str]) -> str:
-    obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
+def _compile(src: str, extra: List[str], obj_dir: str) -> str:
+    obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
     newest = max(os.path.getmtime(src), _headers_mtime())
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest:
         return obj
@@ -58,23 +58,29 @@ def _compile(src: str, extra: List[str]) -> str:
     return obj
 
 
-def build(force: bool = False, verbose_ptxas: bool = False) -> str:
-    os.makedirs(OBJ_DIR, exist_ok=True)
+def build(force: bool = False, verbose_ptxas: bool = False, defines: List[str] = (), lib_path: str = "") -> str:
+    """Compile and link; ``defines`` (e.g. ["ZK_MUL_STYLE=1"]) build a variant into ``lib_path``."""
+    obj_dir, out_path = OBJ_DIR, LIB_PATH
+    if defines or lib_path:
+        tag = "_".join(d.replace("=", "") for d in defines) or "custom"
+        obj_dir = os.path.join(LIB_DIR, "obj_" + tag)
+        out_path = lib_path or os.path.join(LIB_DIR, f"libzkgpu_{tag}.so")
+    os.makedirs(obj_dir, exist_ok=True)
     if force:
-        for f in os.listdir(OBJ_DIR):
-            os.remove(os.path.join(OBJ_DIR, f))
-    extra = ["-Xptxas", "-v"] if verbose_ptxas else []
+        for f in os.listdir(obj_dir):
+            os.remove(os.path.join(obj_dir, f))
+    extra = (["-Xptxas", "-v"] if verbose_ptxas else []) + [f"-D{d}" for d in defines]
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(os.path.getmtime(o) for o in objs):
-        tmp = LIB_PATH + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, extra, obj_dir), srcs))
+    if force or not os.path.exists(out_path) or os.path.getmtime(out_path) < max(os.path.getmtime(o) for o in objs):
+        tmp = out_path + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-        os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+        os.replace(tmp, out_path)
+    return out_path
 
 
 if __name__ == "__main__":

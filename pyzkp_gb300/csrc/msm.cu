@@ -34,8 +34,9 @@ int device_exclusive_scan(Ctx* c, uint32_t* data, size_t n, uint32_t* total);
 
 static constexpr uint32_t kNone = 0xffffffffu;
 static constexpr uint32_t kSegment = 32;   // entries per thread in the first accumulation round
-static constexpr uint32_t kGroup = 32;     // units merged per thread in later rounds
-static constexpr uint32_t kBlockG = 16;    // buckets per block in the window reduction
+static constexpr uint32_t kFirstGroup = 2; // units merged per thread in the first merge round
+static constexpr uint32_t kGroup = 16;     // units merged per thread in later rounds
+static constexpr uint32_t kBlockG = 8;     // buckets per block in the window reduction
 static constexpr int kTargetThreads = 256;
 
 struct MsmShape {
@@ -194,11 +195,13 @@ __global__ void __launch_bounds__(128) msm_accumulate_kernel(const uint32_t* __r
     emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
 }
 
-// Round r >= 2: unit u merges the slots of units [u*kGroup, (u+1)*kGroup) of the previous
-// round, covering entries [u * span, (u+1) * span) with span = kSegment * kGroup^(r-1).
+// Round r >= 2: unit u merges the slots of units [u*group, (u+1)*group) of the previous
+// round, covering entries [u * span, (u+1) * span) (span = kSegment times the product of
+// the group sizes so far). The first merge round uses pairs: most straddling buckets
+// cross exactly one segment boundary, so that round carries nearly all the work.
 __global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restrict__ in_keys,
                                                         const xyzz_t* __restrict__ in_pts, uint32_t in_units,
-                                                        const uint32_t* __restrict__ d_total,
+                                                        uint32_t group, const uint32_t* __restrict__ d_total,
                                                         const uint32_t* __restrict__ row_ptr, uint64_t span,
                                                         uint32_t units, xyzz_t* __restrict__ buckets,
                                                         uint32_t* __restrict__ slot_keys,
@@ -212,8 +215,8 @@ __global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restri
     if (e0l >= M) return;
     const uint32_t e0 = (uint32_t)e0l;
     const uint32_t e1 = (uint32_t)min(e0l + span, M);
-    const uint32_t s0 = 2 * u * kGroup;
-    const uint32_t s1 = min(2 * (u + 1) * kGroup, 2 * in_units);
+    const uint32_t s0 = 2 * u * group;
+    const uint32_t s1 = min(2 * (u + 1) * group, 2 * in_units);
     uint32_t cur = kNone;
     xyzz_t acc = xyzz_inf();
     for (uint32_t s = s0; s < s1; s++) {
@@ -353,8 +356,8 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
     xyzz_t *slot_pts_a = nullptr, *slot_pts_b = nullptr;
     if ((rc = alloc((size_t)2 * units * 4, (void**)&slot_keys_a)) != ZK_OK ||
         (rc = alloc((size_t)2 * units * sizeof(xyzz_t), (void**)&slot_pts_a)) != ZK_OK ||
-        (rc = alloc((size_t)2 * ((units + kGroup - 1) / kGroup) * 4, (void**)&slot_keys_b)) != ZK_OK ||
-        (rc = alloc((size_t)2 * ((units + kGroup - 1) / kGroup) * sizeof(xyzz_t), (void**)&slot_pts_b)) !=
+        (rc = alloc((size_t)2 * ((units + kFirstGroup - 1) / kFirstGroup) * 4, (void**)&slot_keys_b)) != ZK_OK ||
+        (rc = alloc((size_t)2 * ((units + kFirstGroup - 1) / kFirstGroup) * sizeof(xyzz_t), (void**)&slot_pts_b)) !=
             ZK_OK) {
         release();
         return rc;
@@ -366,15 +369,17 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
     uint32_t in_units = units;
     uint32_t *ik = slot_keys_a, *ok = slot_keys_b;
     xyzz_t *ip = slot_pts_a, *op = slot_pts_b;
+    uint32_t group = kFirstGroup;
     while (in_units > 1) {
-        const uint32_t out_units = (in_units + kGroup - 1) / kGroup;
-        span *= kGroup;
-        ZK_LAUNCH(c, "msm_merge", msm_merge_kernel, (out_units + 127) / 128, 128, 0, ik, ip, in_units, d_total, row_ptr,
-                  span, out_units, buckets, ok, op);
+        const uint32_t out_units = (in_units + group - 1) / group;
+        span *= group;
+        ZK_LAUNCH(c, "msm_merge", msm_merge_kernel, (out_units + 127) / 128, 128, 0, ik, ip, in_units, group, d_total,
+                  row_ptr, span, out_units, buckets, ok, op);
         ZK_TRY_CUDA(cudaGetLastError());
         std::swap(ik, ok);
         std::swap(ip, op);
         in_units = out_units;
+        group = kGroup;
     }
 
     // window reduction
