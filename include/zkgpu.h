@@ -140,6 +140,21 @@ int zk_ntt(zk_ctx *ctx, int mode, void *out_dev, const void *in_dev, size_t in_l
            const uint8_t omega[32], const uint8_t shift[32]);
 
 /*
+ * zk_ntt without any device allocation. No counterpart in the reference: it is for
+ * callers that cannot allocate device memory while they transform (a process whose
+ * memory budget was reserved up front by its own pool, or a latency-critical path
+ * that must avoid cudaMalloc's implicit synchronisation). Same arguments and results
+ * as zk_ntt; the intermediate buffer and the twiddle / scale tables live in one
+ * static device array of the library (2 MiB + 128 KiB per device that loads it,
+ * held until exit), so n <= 2^16 (log_n <= 16, larger sizes give ZK_EINVAL). Every
+ * call on a device shares that array: calls that overlap on the GPU race and must be
+ * serialised by the caller. The first call on each device sets up the array's device
+ * address; make that first call before any stream capture.
+ */
+int zk_ntt_noalloc(zk_ctx *ctx, int mode, void *out_dev, const void *in_dev, size_t in_len, uint32_t log_n,
+                   const uint8_t omega[32], const uint8_t shift[32]);
+
+/*
  * Resident G1 bases (affine, converted to Montgomery once on the device).
  * Replaces the per-call packing of _pack_g1_point (runtime/metal/msm.py:13-34,
  * 79-85, 200-204). Input: n affine canonical points, 64 bytes each, (0,0) = infinity,

@@ -32,7 +32,7 @@ EXPORTED_SYMBOLS = (
     "zk_bases_create", "zk_bases_create_dev", "zk_bases_destroy", "zk_bases_count", "zk_msm_g1",
     "zk_g1_fixed_base_mul", "zk_memset", "zk_launch_count", "zk_prof_enable", "zk_prof_reset", "zk_prof_count",
     "zk_prof_get", "zk_timer_start", "zk_timer_stop", "zk_msm_last_stats", "zk_imad_peak", "zk_d2d",
-    "zk_fr_trimmed_len",
+    "zk_fr_trimmed_len", "zk_ntt_noalloc",
 )
 
 _lib: Optional[ctypes.CDLL] = None
@@ -95,6 +95,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_imad_peak": ([P, ctypes.POINTER(ctypes.c_double)], I),
             "zk_d2d": ([P, P, P, S], I),
             "zk_fr_trimmed_len": ([P, P, S, ctypes.POINTER(ctypes.c_size_t)], I),
+            "zk_ntt_noalloc": ([P, I, P, P, S, U32, P, P], I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

@@ -19,6 +19,7 @@
 // Shared memory holds each 32-byte element as two 16-byte planes (low/high limbs)
 // so that eight consecutive elements cover all 32 banks; element positions are
 // XOR-swizzled so the bit-reversed read-back does not hit one bank group.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 
@@ -362,3 +363,214 @@ int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log
 }
 
 }  // namespace zk
+
+// ==============================================================================
+// Allocation-free NTT entry point (zk_ntt_noalloc).
+//
+// Some callers cannot allocate device memory when they transform: a serving process
+// that reserved the whole device up front for its own pool, code that must not pay
+// cudaMalloc's implicit device synchronisation on a latency-critical path, or a
+// library embedded in a host whose allocator owns the GPU. zk_ntt_noalloc runs the
+// same passes as zk_ntt but takes its scratch -- the intermediate pass buffer and the
+// twiddle / scale tables, which zk_ntt allocates and caches -- from one file-scope
+// static device array of fixed size. Limits and rules:
+//   * n <= 2^16 (kNoAllocMaxLogN); larger sizes are rejected with ZK_EINVAL;
+//   * the array is shared by every call on a device and keeps the last call's
+//     contents; nothing in it has to start at zero (each call uploads its tables and
+//     its first pass writes every element the second pass reads), but calls that
+//     overlap on the GPU (different streams, or different contexts of one device)
+//     race on it and must be serialised by the caller;
+//   * the first call on each device does the set-up (cudaGetSymbolAddress of the
+//     array, the kernel's shared-memory attribute), so that first call should come
+//     before any stream capture;
+//   * no cudaMalloc, cudaFree or other allocating routine is called.
+// ==============================================================================
+namespace zk {
+
+static constexpr uint32_t kNoAllocMaxLogN = 16;
+static constexpr size_t kNoAllocDataElems = (size_t)1 << kNoAllocMaxLogN;
+// tables for log_n <= 16: two-level twiddles (<= 256 + 257), radix tables (<= 1024),
+// first-pass scale (<= 513), last-pass scale (<= 513): at most 2563 elements
+static constexpr size_t kNoAllocTableElems = 4096;
+
+static __device__ __align__(256) fe g_ntt_noalloc_scratch[kNoAllocDataElems + kNoAllocTableElems];
+
+static constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static fe* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Once per device, with that device current: device address of the static array.
+static int noalloc_setup(int device, fe** out) {
+    ZK_CHECK_ARG(device >= 0 && device < kNoAllocMaxDevices, "device index out of range for zk_ntt_noalloc");
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (g_noalloc_ptr[device] == nullptr) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_ntt_noalloc_scratch);
+        if (e != cudaSuccess) {
+            set_error(std::string("cudaGetSymbolAddress(g_ntt_noalloc_scratch): ") + cudaGetErrorString(e));
+            return ZK_ECUDA;
+        }
+        ZK_TRY_CUDA(cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (2 << kTileLogElems) * 16));
+        g_noalloc_ptr[device] = static_cast<fe*>(p);
+    }
+    *out = g_noalloc_ptr[device];
+    return ZK_OK;
+}
+
+// Host staging of the tables (fixed size, reused; guarded by g_noalloc_stage_mu).
+static std::mutex g_noalloc_stage_mu;
+static zkh::F4 g_noalloc_stage[kNoAllocTableElems];
+
+static void stage_powers(const zkh::F4& base, size_t count, size_t* pos, const zkh::F4* scale = nullptr) {
+    const zkh::Field& F = zkh::fr();
+    zkh::F4 cur = scale ? *scale : zkh::one(F);
+    for (size_t i = 0; i < count; i++) {
+        g_noalloc_stage[(*pos)++] = cur;
+        cur = zkh::mul(F, cur, base);
+    }
+}
+
+static int ntt_run_noalloc(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log_n,
+                           const uint8_t omega[32], const uint8_t shift[32]) {
+    ZK_CHECK_ARG(mode >= 0 && mode <= 3, "invalid NTT mode");
+    ZK_CHECK_ARG(log_n <= kNoAllocMaxLogN, "zk_ntt_noalloc supports n <= 2^16 (its static scratch size)");
+    const uint64_t n = 1ull << log_n;
+    const bool inverse = (mode == ZK_NTT_COEFFS_FROM_EVALS || mode == ZK_NTT_COSET_COEFFS_FROM_EVALS);
+    ZK_CHECK_ARG(!inverse || in_len == n, "inverse transforms need len(evals) == n (a power of two)");
+    ZK_CHECK_ARG(out != nullptr && (in != nullptr || in_len == 0), "null buffer");
+    fe* base = nullptr;
+    int rc = noalloc_setup(c->device, &base);
+    if (rc != ZK_OK) return rc;
+    fe* data = base;
+    fe* tables = base + kNoAllocDataElems;
+
+    const zkh::Field& F = zkh::fr();
+    const zkh::F4 om = zkh::to_mont(F, load_canon(omega));
+    const zkh::F4 sh = zkh::to_mont(F, load_canon(shift));
+    if (log_n >= 1) {
+        zkh::F4 h = zkh::pow_u64(F, om, 1ull << (log_n - 1));
+        if (!zkh::eq(h, zkh::neg(F, zkh::one(F)))) {
+            set_error("omega is not a primitive n-th root of unity (omega^(n/2) != -1)");
+            return ZK_EINVAL;
+        }
+    }
+    NttPlan plan;  // shape only: every table pointer below points into the static array
+    plan.log_n = log_n;
+    split_passes(log_n, &plan);
+    plan.s_bits = (log_n + 1) / 2;
+    const uint64_t lo_count = 1ull << plan.s_bits;
+    const uint64_t hi_count = (n >> plan.s_bits) + 1;
+    const zkh::F4 w = inverse ? zkh::inv(F, om) : om;
+
+    std::lock_guard<std::mutex> g(g_noalloc_stage_mu);
+    size_t pos = 0;
+    size_t off_lo = pos;
+    stage_powers(w, lo_count, &pos);
+    size_t off_hi = pos;
+    stage_powers(zkh::pow_u64(F, w, lo_count), hi_count, &pos);
+    size_t off_radix[4] = {0, 0, 0, 0};
+    for (int p = 0; p < plan.npass; p++) {
+        off_radix[p] = pos;
+        const uint32_t lr = plan.pass_log_r[p];
+        stage_powers(zkh::pow_u64(F, w, n >> lr), std::max<uint64_t>(1, (1ull << lr) / 2), &pos);
+    }
+    size_t off_pre_lo = 0, off_pre_hi = 0, off_post_lo = 0, off_post_hi = 0;
+    bool has_pre = false, has_post = false, post_const = false;
+    if (mode == ZK_NTT_COSET_EVALS_FROM_COEFFS) {
+        has_pre = true;
+        off_pre_lo = pos;
+        stage_powers(sh, lo_count, &pos);
+        off_pre_hi = pos;
+        stage_powers(zkh::pow_u64(F, sh, lo_count), hi_count, &pos);
+    }
+    if (inverse) {
+        has_post = true;
+        zkh::F4 nn = {{n, 0, 0, 0}};
+        zkh::F4 ninv = zkh::inv(F, zkh::to_mont(F, nn));
+        off_post_lo = pos;
+        if (mode == ZK_NTT_COEFFS_FROM_EVALS) {
+            post_const = true;
+            g_noalloc_stage[pos++] = ninv;
+        } else {
+            zkh::F4 is = zkh::is_zero(sh) ? sh : zkh::inv(F, sh);
+            stage_powers(is, lo_count, &pos, &ninv);
+            off_post_hi = pos;
+            stage_powers(zkh::pow_u64(F, is, lo_count), hi_count, &pos);
+        }
+    }
+    if (pos > kNoAllocTableElems) {
+        set_error("zk_ntt_noalloc: table layout exceeds the static scratch");
+        return ZK_EINVAL;
+    }
+    // pageable source: the copy is staged before cudaMemcpyAsync returns, so the host
+    // staging area may be reused by the next call
+    ZK_TRY_CUDA(cudaMemcpyAsync(tables, g_noalloc_stage, pos * 32, cudaMemcpyHostToDevice, c->stream));
+
+    const uint32_t valid = (uint32_t)(in_len < n ? in_len : n);
+    NttPassParams P{};
+    P.tw_lo = tables + off_lo;
+    P.tw_hi = tables + off_hi;
+    P.s_bits = plan.s_bits;
+    if (log_n == 0) {
+        P.in = in;
+        P.out = out;
+        P.radix_tw = tables + off_lo;
+        P.pre_lo = has_pre ? tables + off_pre_lo : nullptr;
+        P.pre_hi = has_pre ? tables + off_pre_hi : nullptr;
+        P.post_lo = has_post ? tables + off_post_lo : nullptr;
+        P.post_hi = (has_post && !post_const) ? tables + off_post_hi : nullptr;
+        P.in_len = valid;
+        ZK_LAUNCH(c, "ntt_pass", ntt_pass_kernel, 1, 32, 2 * 16, P);
+        ZK_TRY_CUDA(cudaGetLastError());
+        return ZK_OK;
+    }
+    uint32_t log_l = 0;
+    const fe* src = in;
+    for (int p = 0; p < plan.npass; p++) {
+        const uint32_t lr = plan.pass_log_r[p];
+        uint32_t lt = kTileLogElems > (int)lr ? kTileLogElems - lr : 0;
+        if (lt > log_n - lr) lt = log_n - lr;
+        const int remaining = plan.npass - 1 - p;
+        fe* dst = (remaining % 2 == 0) ? out : data;
+        P.in = src;
+        P.out = dst;
+        P.radix_tw = tables + off_radix[p];
+        P.pre_lo = (p == 0 && has_pre) ? tables + off_pre_lo : nullptr;
+        P.pre_hi = (p == 0 && has_pre) ? tables + off_pre_hi : nullptr;
+        const bool last = p == plan.npass - 1;
+        P.post_lo = (last && has_post) ? tables + off_post_lo : nullptr;
+        P.post_hi = (last && has_post && !post_const) ? tables + off_post_hi : nullptr;
+        P.in_len = p == 0 ? valid : (uint32_t)n;
+        P.log_n = log_n;
+        P.log_r = lr;
+        P.log_t = lt;
+        P.log_l = log_l;
+        const uint32_t elems = 1u << (lr + lt);
+        const uint32_t threads = elems / 2 < (uint32_t)kNttThreads ? (elems / 2 < 32 ? 32 : elems / 2) : kNttThreads;
+        const uint32_t blocks = (uint32_t)(n >> (lr + lt));
+        ZK_LAUNCH(c, "ntt_pass", ntt_pass_kernel, blocks, threads, (size_t)elems * 32, P);
+        ZK_TRY_CUDA(cudaGetLastError());
+        src = dst;
+        log_l += lr;
+    }
+    return ZK_OK;
+}
+
+}  // namespace zk
+
+extern "C" int zk_ntt_noalloc(zk_ctx* ctx, int mode, void* out_dev, const void* in_dev, size_t in_len, uint32_t log_n,
+                              const uint8_t omega[32], const uint8_t shift[32]) {
+    if (ctx == nullptr || omega == nullptr) {
+        zk::set_error("null zk_ctx or omega");
+        return ZK_EINVAL;
+    }
+    cudaError_t e = cudaSetDevice(ctx->impl.device);
+    if (e != cudaSuccess) {
+        zk::set_error(cudaGetErrorString(e));
+        return ZK_ECUDA;
+    }
+    static const uint8_t one[32] = {1};
+    return zk::ntt_run_noalloc(&ctx->impl, mode, static_cast<zk::fe*>(out_dev), static_cast<const zk::fe*>(in_dev),
+                               in_len, log_n, omega, shift ? shift : one);
+}
