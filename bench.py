@@ -171,7 +171,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
     if args.only == "ntt":
         flush = ctx.alloc(FLUSH_BYTES)
         peaks = load_peaks()
-        return run_gpu_ntt(ctx, args, ranks, args.log_n, flush, ctx.imad_peak(), peaks.get("hbm_gbs") or 6800.0,
+        return run_gpu_ntt(ctx, args, ranks, args.log_n, flush, imad_peak(ctx)[1], peaks.get("hbm_gbs") or 6800.0,
                            brief=True)
     log_n = args.log_n
     n, seed, k, s, bases_xy, host_xy = make_inputs(ctx, log_n)
@@ -179,16 +179,17 @@ def run_gpu(args, ranks: Ranks) -> dict:
     ds = ctx.to_device(s)
     ctx.fr_to_mont(ds, ds, n)
     flush = ctx.alloc(FLUSH_BYTES)
-    imad_tops = ctx.imad_peak()
+    imad_probes, imad_tops = imad_peak(ctx)
 
     def msm_step():
         return ctx.msm_g1(bases, ds, n)
 
+    # clocks are sampled from the warm-up to the end of the last timed GPU section
+    sampler = ClockSampler(ranks.local)
+    sampler.start()
     for _ in range(args.warmup):
         res = msm_step()
 
-    sampler = ClockSampler(ranks.local)
-    sampler.start()
     launches0 = ctx.launch_count()
     ranks.barrier()
     ctx.sync()
@@ -201,7 +202,6 @@ def run_gpu(args, ranks: Ranks) -> dict:
     ctx.sync()
     ranks.barrier()
     launches = ctx.launch_count() - launches0
-    clocks = sampler.stop()
     total_ms = ranks.max(sum(times))
     mpts = n * args.steps * ranks.world / (total_ms * 1e-3) / 1e6
     stats = ctx.msm_last_stats()
@@ -235,7 +235,10 @@ def run_gpu(args, ranks: Ranks) -> dict:
         "peak": round(imad_tops, 3),
         "unit": "T IMAD/s",
         "frac": round(acc_tops / imad_tops, 4),
-        "peak_source": "measured in this run by zk_imad_peak (no IMAD figure in MEASURED_PEAKS.json)",
+        "peak_source": ("measured in this run (no IMAD figure in MEASURED_PEAKS.json): the fastest rate of "
+                        "32x32->64 multiply-accumulates, as lo+hi pairs (harmonic mean of the mad.lo and mad.hi "
+                        "probes) or as mad.wide, counted as 2 IMAD each like the algorithmic work"),
+        "imad_probes_T_per_s": imad_probes,
         "launch_ms": round(acc_ms_launch, 4),
         "share_of_step": round(acc_ms / max(1e-9, sum(v[1] for v in table.values())), 4),
         "traffic": None,
@@ -249,7 +252,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
 
     if args.only == "msm":
         return {"metric": METRIC, "value": round(mpts, 3), "unit": "Mpts/s", "kernels": kernels,
-                "roofline": roofline, "gpu_launches": launches}
+                "roofline": roofline, "gpu_launches": launches, "clocks": sampler.stop()}
 
     # e2e through the C ABI from pinned host memory
     pin_xy = ctx.pinned(n * 64)
@@ -284,6 +287,9 @@ def run_gpu(args, ranks: Ranks) -> dict:
 
     ntt = run_gpu_ntt(ctx, args, ranks, 20, flush, imad_tops, hbm_peak)
     ntt22 = run_gpu_ntt(ctx, args, ranks, 22, flush, imad_tops, hbm_peak, brief=True)
+    clocks = sampler.stop()
+    sweep = run_gpu_msm_sweep(ctx, args, flush) if ranks.world == 1 else None
+    fixed = run_gpu_fixed_base(ctx, args, flush) if ranks.world == 1 else None
 
     result = {
         "metric": METRIC,
@@ -312,6 +318,8 @@ def run_gpu(args, ranks: Ranks) -> dict:
         "roofline": roofline,
         "ntt": ntt,
         "ntt_2_22": ntt22,
+        "msm_sweep": sweep,
+        "msm_fixed_base_2_20": fixed,
         "clocks": clocks,
     }
     return result
@@ -390,6 +398,80 @@ def run_gpu_ntt(ctx, args, ranks, log_n, flush, imad_tops, hbm_peak, brief=False
         out["e2e"] = {"value": round(n * args.steps * ranks.world / (tot * 1e-3) / 1e6, 2), "unit": "Melem/s",
                       "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 32}
     return out
+
+
+def imad_peak(ctx):
+    """Probe the integer pipe; return (probes, peak) in 10^12 IMAD/s (a wide MAC = 2 IMAD)."""
+    pr = {"carry_chain": ctx.imad_probe(0), "mad_lo": ctx.imad_probe(1), "mad_hi": ctx.imad_probe(2),
+          "mad_wide_as_2": ctx.imad_probe(3)}
+    pair = 1.0 / (1.0 / pr["mad_lo"] + 1.0 / pr["mad_hi"])  # wide MACs/s as lo + hi
+    wide = pr["mad_wide_as_2"] / 2.0  # wide MACs/s as mad.wide
+    peak = 2.0 * max(pair, wide)
+    return {k: round(v, 3) for k, v in pr.items()}, peak
+
+
+def run_gpu_msm_sweep(ctx, args, flush, sizes=(16, 17, 18, 19, 20, 21, 22)) -> dict:
+    """MSM size sweep 2^16..2^22 under uniform and witness-like scalars (resident inputs)."""
+    from pyzkp_gb300 import synth
+
+    out = {}
+    steps = max(3, min(args.steps, 10))
+    for log_n in sizes:
+        n = 1 << log_n
+        seed = synth.seed_for(2, log_n)
+        dk = ctx.to_device(synth.base_dlogs(seed, n))
+        xy = ctx.alloc(n * 64)
+        ctx.g1_fixed_base_mul((1, 2), dk, n, xy)
+        bases = ctx.bases_from_device(xy, n)
+        del dk, xy
+        row = {}
+        for kind, gen in (("uniform", synth.fr_uniform), ("witness_like", synth.fr_witness_like)):
+            ds = ctx.to_device(gen(seed, n))
+            ctx.fr_to_mont(ds, ds, n)
+            for _ in range(2):
+                ctx.msm_g1(bases, ds, n)
+            ts = []
+            for _ in range(steps):
+                ctx.memset(flush, 1)
+                ctx.timer_start()
+                ctx.msm_g1(bases, ds, n)
+                ts.append(ctx.timer_stop())
+            row[kind] = {"Mpts_s": round(n / (statistics.median(ts) * 1e-3) / 1e6, 2),
+                         "ms": round(statistics.median(ts), 4)}
+        out[f"2^{log_n}"] = row
+        bases.free()
+    return out
+
+
+def run_gpu_fixed_base(ctx, args, flush, log_n: int = 20, calls: int = 16) -> dict:
+    """One base set reused across 16 MSMs (fixed-base rows computed on the first call)."""
+    from pyzkp_gb300 import plugin, synth
+
+    n = 1 << log_n
+    seed = synth.seed_for(2, log_n) + 7
+    dk = ctx.to_device(synth.base_dlogs(seed, n))
+    xy = ctx.alloc(n * 64)
+    ctx.g1_fixed_base_mul((1, 2), dk, n, xy)
+    bases = ctx.bases_from_device(xy, n)
+    c = plugin.fixed_base_window(n)
+    scal = [ctx.to_device(synth.fr_uniform(seed + i, n)) for i in range(calls)]
+    for d in scal:
+        ctx.fr_to_mont(d, d, n)
+    ctx.memset(flush, 1)
+    ctx.timer_start()
+    ctx.bases_precompute(bases, c)
+    ctx.msm_g1(bases, scal[0], n)
+    first = ctx.timer_stop()
+    ts = []
+    for i in range(1, calls):
+        ctx.memset(flush, 1)
+        ctx.timer_start()
+        ctx.msm_g1(bases, scal[i], n)
+        ts.append(ctx.timer_stop())
+    steady = statistics.median(ts)
+    return {"n": n, "calls": calls, "window_bits": c, "first_call_ms": round(first, 3),
+            "steady_ms": round(steady, 4), "steady_Mpts_s": round(n / (steady * 1e-3) / 1e6, 2),
+            "note": "first call includes the window-shifted base rows (zk_bases_precompute)"}
 
 
 def load_peaks() -> dict:

@@ -75,8 +75,11 @@ int zk_timer_start(zk_ctx *ctx);
 int zk_timer_stop(zk_ctx *ctx, double *ms);
 /* Shape of the last zk_msm_g1 call: CSR entries (non-zero signed digits), window bits, windows. */
 int zk_msm_last_stats(zk_ctx *ctx, uint64_t *entries, uint32_t *window_bits, uint32_t *windows);
-/* Measured throughput of the 32-bit integer multiply-add pipe (mad.lo/mad.hi carry chains
- * shaped like the Montgomery inner loop), in 10^12 IMAD instructions per second. */
+/* Measured throughput of the 32-bit integer multiply-add pipe, in 10^12 IMAD instructions
+ * per second: probe mode 0 = carry chains shaped like a Montgomery row (mad.lo.cc /
+ * madc.hi.cc), 1 = independent mad.lo.u32, 2 = independent mad.hi.u32; zk_imad_peak is
+ * the largest of the three (the roofline denominator of the IMAD-bound kernels). */
+int zk_imad_probe(zk_ctx *ctx, int mode, double *tera_imad_per_s);
 int zk_imad_peak(zk_ctx *ctx, double *tera_imad_per_s);
 
 /*
@@ -163,6 +166,16 @@ int zk_ntt_noalloc(zk_ctx *ctx, int mode, void *out_dev, const void *in_dev, siz
 int zk_bases_create(zk_ctx *ctx, const void *xy_canonical_host, size_t n, zk_bases **out);
 int zk_bases_create_dev(zk_ctx *ctx, const void *xy_canonical_dev, size_t n, zk_bases **out);
 int zk_bases_destroy(zk_bases *b);
+/*
+ * Fixed-base precomputation for a base set used by many MSMs (the reference's
+ * fixed_base_precompute / msm_fixed_base, crypto/msm/pippenger.py:217-295, and the
+ * fixed_base attrs of runtime/kernels/cpu/kernels.py:560-569). Instead of the
+ * reference's per-point table d*P_i (d < 2^w; 17 GB at n = 2^20, w = 8) the library
+ * stores the window-shifted rows [2^(c j)] P_i for j < ceil(255/c) (W*n*64 bytes); every
+ * later zk_msm_g1 on these bases (with window_bits 0 or c) then sums all windows in one
+ * bucket set: no per-window bucket reduction and no doubling chain. Same result.
+ */
+int zk_bases_precompute(zk_ctx *ctx, zk_bases *b, uint32_t window_bits);
 int zk_bases_count(const zk_bases *b, size_t *n);
 
 /*

@@ -32,7 +32,7 @@ EXPORTED_SYMBOLS = (
     "zk_bases_create", "zk_bases_create_dev", "zk_bases_destroy", "zk_bases_count", "zk_msm_g1",
     "zk_g1_fixed_base_mul", "zk_memset", "zk_launch_count", "zk_prof_enable", "zk_prof_reset", "zk_prof_count",
     "zk_prof_get", "zk_timer_start", "zk_timer_stop", "zk_msm_last_stats", "zk_imad_peak", "zk_d2d",
-    "zk_fr_trimmed_len", "zk_ntt_noalloc",
+    "zk_fr_trimmed_len", "zk_ntt_noalloc", "zk_imad_probe", "zk_bases_precompute",
 )
 
 _lib: Optional[ctypes.CDLL] = None
@@ -96,6 +96,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_d2d": ([P, P, P, S], I),
             "zk_fr_trimmed_len": ([P, P, S, ctypes.POINTER(ctypes.c_size_t)], I),
             "zk_ntt_noalloc": ([P, I, P, P, S, U32, P, P], I),
+            "zk_imad_probe": ([P, I, ctypes.POINTER(ctypes.c_double)], I),
+            "zk_bases_precompute": ([P, P, U32], I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -265,6 +267,11 @@ class Context:
         check(load().zk_msm_last_stats(self.handle, ctypes.byref(e), ctypes.byref(c), ctypes.byref(w)))
         return {"entries": int(e.value), "window_bits": int(c.value), "windows": int(w.value)}
 
+    def imad_probe(self, mode: int) -> float:
+        v = ctypes.c_double()
+        check(load().zk_imad_probe(self.handle, int(mode), ctypes.byref(v)), "zk_imad_probe")
+        return float(v.value)
+
     def imad_peak(self) -> float:
         """Measured 32-bit IMAD throughput, 10^12 instructions/s."""
         v = ctypes.c_double()
@@ -318,6 +325,10 @@ class Context:
         h = ctypes.c_void_p()
         check(load().zk_bases_create(self.handle, a.ctypes.data, a.shape[0], ctypes.byref(h)), "zk_bases_create")
         return Bases(self, h.value, a.shape[0])
+
+    def bases_precompute(self, bases: "Bases", window_bits: int) -> None:
+        """Window-shifted rows for fixed-base MSMs on ``bases`` (zk_bases_precompute)."""
+        check(load().zk_bases_precompute(self.handle, bases.handle, int(window_bits)), "zk_bases_precompute")
 
     def bases_from_device(self, xy: DeviceArray, n: int) -> Bases:
         h = ctypes.c_void_p()

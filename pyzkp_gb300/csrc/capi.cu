@@ -52,6 +52,13 @@ int prof_begin(Ctx* c, const char* name) {
     return (int)c->prof_pending.size() - 1;
 }
 
+void prof_host(Ctx* c, const char* name, double ms) {
+    if (!c->prof_on) return;
+    ProfEntry& e = c->prof[name];
+    e.launches++;
+    e.total_ms += ms;
+}
+
 void prof_end(Ctx* c, int token) {
     if (token < 0) return;
     cudaEventRecord(c->prof_pending[token].stop, c->stream);
@@ -78,6 +85,7 @@ int convert(Ctx* c, void* out, const void* in, size_t n);
 int fr_binary(Ctx* c, int op, void* out, const void* a, const void* b, size_t n);
 int fixed_base_mul(Ctx* c, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_dev);
 int imad_peak(Ctx* c, double* tera);
+int imad_probe(Ctx* c, int mode, double* tera);
 int trimmed_len(Ctx* c, const void* a, size_t n, size_t* out);
 
 }  // namespace zk
@@ -273,6 +281,11 @@ int zk_imad_peak(zk_ctx* ctx, double* tera_imad_per_s) {
     return zk::imad_peak(&ctx->impl, tera_imad_per_s);
 }
 
+int zk_imad_probe(zk_ctx* ctx, int mode, double* tera_imad_per_s) {
+    CTX_OR_FAIL(ctx);
+    return zk::imad_probe(&ctx->impl, mode, tera_imad_per_s);
+}
+
 int zk_alloc(zk_ctx* ctx, size_t bytes, void** dptr) {
     CTX_OR_FAIL(ctx);
     if (dptr == nullptr) {
@@ -404,9 +417,29 @@ int zk_bases_create_dev(zk_ctx* ctx, const void* xy_canonical_dev, size_t n, zk_
     return rc;
 }
 
+int zk_bases_precompute(zk_ctx* ctx, zk_bases* b, uint32_t window_bits) {
+    CTX_OR_FAIL(ctx);
+    if (b == nullptr) {
+        zk::set_error("null bases");
+        return ZK_EINVAL;
+    }
+    if (b->shifted && b->shifted_c == window_bits) return ZK_OK;
+    zk::affine_t* rows = nullptr;
+    uint32_t windows = 0;
+    int rc = zk::shift_bases(&ctx->impl, b->dev, b->n, window_bits, &rows, &windows);
+    if (rc != ZK_OK) return rc;
+    if (b->shifted) zk::scratch_free(&ctx->impl, b->shifted);
+    b->shifted = rows;
+    b->shifted_c = window_bits;
+    b->shifted_windows = windows;
+    ZK_TRY_CUDA(cudaStreamSynchronize(ctx->impl.stream));
+    return ZK_OK;
+}
+
 int zk_bases_destroy(zk_bases* b) {
     if (b == nullptr) return ZK_OK;
     cudaSetDevice(b->ctx->impl.device);
+    if (b->shifted) zk::scratch_free(&b->ctx->impl, b->shifted);
     zk::scratch_free(&b->ctx->impl, b->dev);
     delete b;
     return ZK_OK;
@@ -433,7 +466,8 @@ int zk_msm_g1(zk_ctx* ctx, const zk_bases* bases, size_t offset, const void* sca
         return ZK_EINVAL;
     }
     return zk::msm_run(&ctx->impl, bases->dev + offset, static_cast<const zk::fe*>(scalars_dev), n, scalars_mont,
-                       window_bits, out_xy, out_is_inf);
+                       window_bits, out_xy, out_is_inf, bases->shifted ? bases->shifted + offset : nullptr,
+                       bases->shifted_c, bases->n);
 }
 
 int zk_g1_fixed_base_mul(zk_ctx* ctx, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_xy_dev) {

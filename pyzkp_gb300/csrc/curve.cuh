@@ -46,37 +46,40 @@ __device__ __forceinline__ xyzz_t xyzz_neg(const xyzz_t& p) {
     return r;
 }
 
+// The formulas below issue their multiplications in independent pairs (fe_mul2), so the
+// two carry-chain sequences of a pair overlap.
+
 // 2 * (x, y) for an affine point that is not infinity (y != 0 on this curve).
 __device__ __forceinline__ xyzz_t xyzz_dbl_affine(const fe& x, const fe& y) {
     using F = FqP;
-    fe U = fe_dbl<F>(y);
-    fe V = fe_sqr<F>(U);
-    fe W = fe_mul<F>(U, V);
-    fe S = fe_mul<F>(x, V);
-    fe x2 = fe_sqr<F>(x);
-    fe M = fe_add<F>(fe_dbl<F>(x2), x2);
+    const fe U = fe_dbl<F>(y);
+    const fe2 vx = fe_mul2<F>(U, U, x, x);  // V = U^2, x^2
+    const fe2 ws = fe_mul2<F>(U, vx.x, x, vx.x);  // W = U V, S = x V
+    const fe M = fe_add<F>(fe_dbl<F>(vx.y), vx.y);
+    const fe MM = fe_sqr<F>(M);
     xyzz_t r;
-    r.X = fe_sub<F>(fe_sqr<F>(M), fe_dbl<F>(S));
-    r.Y = fe_sub<F>(fe_mul<F>(M, fe_sub<F>(S, r.X)), fe_mul<F>(W, y));
-    r.ZZ = V;
-    r.ZZZ = W;
+    r.X = fe_sub<F>(MM, fe_dbl<F>(ws.y));
+    const fe2 t = fe_mul2<F>(M, fe_sub<F>(ws.y, r.X), ws.x, y);
+    r.Y = fe_sub<F>(t.x, t.y);
+    r.ZZ = vx.x;
+    r.ZZZ = ws.x;
     return r;
 }
 
 __device__ __forceinline__ xyzz_t xyzz_dbl(const xyzz_t& p) {
     using F = FqP;
     if (xyzz_is_inf(p)) return p;
-    fe U = fe_dbl<F>(p.Y);
-    fe V = fe_sqr<F>(U);
-    fe W = fe_mul<F>(U, V);
-    fe S = fe_mul<F>(p.X, V);
-    fe x2 = fe_sqr<F>(p.X);
-    fe M = fe_add<F>(fe_dbl<F>(x2), x2);
+    const fe U = fe_dbl<F>(p.Y);
+    const fe2 vx = fe_mul2<F>(U, U, p.X, p.X);    // V = U^2, X^2
+    const fe2 ws = fe_mul2<F>(U, vx.x, p.X, vx.x);  // W = U V, S = X V
+    const fe M = fe_add<F>(fe_dbl<F>(vx.y), vx.y);
+    const fe2 mz = fe_mul2<F>(M, M, vx.x, p.ZZ);  // M^2, ZZ3 = V ZZ
     xyzz_t r;
-    r.X = fe_sub<F>(fe_sqr<F>(M), fe_dbl<F>(S));
-    r.Y = fe_sub<F>(fe_mul<F>(M, fe_sub<F>(S, r.X)), fe_mul<F>(W, p.Y));
-    r.ZZ = fe_mul<F>(V, p.ZZ);
-    r.ZZZ = fe_mul<F>(W, p.ZZZ);
+    r.X = fe_sub<F>(mz.x, fe_dbl<F>(ws.y));
+    const fe2 t = fe_mul2<F>(M, fe_sub<F>(ws.y, r.X), ws.x, p.Y);
+    r.Y = fe_sub<F>(t.x, t.y);
+    r.ZZ = mz.y;
+    r.ZZZ = fe_mul<F>(ws.x, p.ZZZ);
     return r;
 }
 
@@ -91,22 +94,22 @@ __device__ __forceinline__ xyzz_t xyzz_madd(const xyzz_t& acc, const fe& x, cons
         r.ZZZ = fe_one<F>();
         return r;
     }
-    fe U2 = fe_mul<F>(x, acc.ZZ);
-    fe S2 = fe_mul<F>(y, acc.ZZZ);
-    fe P = fe_sub<F>(U2, acc.X);
-    fe R = fe_sub<F>(S2, acc.Y);
+    const fe2 us = fe_mul2<F>(x, acc.ZZ, y, acc.ZZZ);  // U2, S2
+    const fe P = fe_sub<F>(us.x, acc.X);
+    const fe R = fe_sub<F>(us.y, acc.Y);
     if (fe_is_zero(P)) {
         if (fe_is_zero(R)) return xyzz_dbl_affine(x, y);
         return xyzz_inf();
     }
-    fe PP = fe_sqr<F>(P);
-    fe PPP = fe_mul<F>(P, PP);
-    fe Q = fe_mul<F>(acc.X, PP);
+    const fe2 pr = fe_mul2<F>(P, P, R, R);          // PP, R^2
+    const fe2 pq = fe_mul2<F>(P, pr.x, acc.X, pr.x);  // PPP, Q
     xyzz_t r;
-    r.X = fe_sub<F>(fe_sub<F>(fe_sqr<F>(R), PPP), fe_dbl<F>(Q));
-    r.Y = fe_sub<F>(fe_mul<F>(R, fe_sub<F>(Q, r.X)), fe_mul<F>(acc.Y, PPP));
-    r.ZZ = fe_mul<F>(acc.ZZ, PP);
-    r.ZZZ = fe_mul<F>(acc.ZZZ, PPP);
+    r.X = fe_sub<F>(fe_sub<F>(pr.y, pq.x), fe_dbl<F>(pq.y));
+    const fe2 zz = fe_mul2<F>(acc.ZZ, pr.x, acc.ZZZ, pq.x);
+    const fe2 t = fe_mul2<F>(R, fe_sub<F>(pq.y, r.X), acc.Y, pq.x);
+    r.Y = fe_sub<F>(t.x, t.y);
+    r.ZZ = zz.x;
+    r.ZZZ = zz.y;
     return r;
 }
 
@@ -114,24 +117,24 @@ __device__ __forceinline__ xyzz_t xyzz_add(const xyzz_t& p, const xyzz_t& q) {
     using F = FqP;
     if (xyzz_is_inf(p)) return q;
     if (xyzz_is_inf(q)) return p;
-    fe U1 = fe_mul<F>(p.X, q.ZZ);
-    fe U2 = fe_mul<F>(q.X, p.ZZ);
-    fe S1 = fe_mul<F>(p.Y, q.ZZZ);
-    fe S2 = fe_mul<F>(q.Y, p.ZZZ);
-    fe P = fe_sub<F>(U2, U1);
-    fe R = fe_sub<F>(S2, S1);
+    const fe2 u = fe_mul2<F>(p.X, q.ZZ, q.X, p.ZZ);    // U1, U2
+    const fe2 s = fe_mul2<F>(p.Y, q.ZZZ, q.Y, p.ZZZ);  // S1, S2
+    const fe P = fe_sub<F>(u.y, u.x);
+    const fe R = fe_sub<F>(s.y, s.x);
     if (fe_is_zero(P)) {
         if (fe_is_zero(R)) return xyzz_dbl(p);
         return xyzz_inf();
     }
-    fe PP = fe_sqr<F>(P);
-    fe PPP = fe_mul<F>(P, PP);
-    fe Q = fe_mul<F>(U1, PP);
+    const fe2 pr = fe_mul2<F>(P, P, R, R);           // PP, R^2
+    const fe2 pq = fe_mul2<F>(P, pr.x, u.x, pr.x);   // PPP, Q
+    const fe2 zz = fe_mul2<F>(p.ZZ, q.ZZ, p.ZZZ, q.ZZZ);
     xyzz_t r;
-    r.X = fe_sub<F>(fe_sub<F>(fe_sqr<F>(R), PPP), fe_dbl<F>(Q));
-    r.Y = fe_sub<F>(fe_mul<F>(R, fe_sub<F>(Q, r.X)), fe_mul<F>(S1, PPP));
-    r.ZZ = fe_mul<F>(fe_mul<F>(p.ZZ, q.ZZ), PP);
-    r.ZZZ = fe_mul<F>(fe_mul<F>(p.ZZZ, q.ZZZ), PPP);
+    r.X = fe_sub<F>(fe_sub<F>(pr.y, pq.x), fe_dbl<F>(pq.y));
+    const fe2 z3 = fe_mul2<F>(zz.x, pr.x, zz.y, pq.x);
+    const fe2 t = fe_mul2<F>(R, fe_sub<F>(pq.y, r.X), s.x, pq.x);
+    r.Y = fe_sub<F>(t.x, t.y);
+    r.ZZ = z3.x;
+    r.ZZZ = z3.y;
     return r;
 }
 

@@ -23,7 +23,7 @@ namespace zk {
 struct FrP {
     __host__ __device__ static constexpr uint32_t P(int i) { return i == 0 ? 0xf0000001u : i == 1 ? 0x43e1f593u : i == 2 ? 0x79b97091u : i == 3 ? 0x2833e848u : i == 4 ? 0x8181585du : i == 5 ? 0xb85045b6u : i == 6 ? 0xe131a029u : 0x30644e72u; }
     static constexpr uint32_t INV = 0xefffffffu  /* -r^-1 mod 2^32 */;
-    static constexpr int MUL_STYLE = 0;
+    static constexpr int MUL_STYLE = 4;
     __host__ __device__ static constexpr uint32_t ONE(int i) { return i == 0 ? 0x4ffffffbu : i == 1 ? 0xac96341cu : i == 2 ? 0x9f60cd29u : i == 3 ? 0x36fc7695u : i == 4 ? 0x7879462eu : i == 5 ? 0x666ea36fu : i == 6 ? 0x9a07df2fu : 0x0e0a77c1u; }
     __host__ __device__ static constexpr uint32_t R2(int i) { return i == 0 ? 0xae216da7u : i == 1 ? 0x1bb8e645u : i == 2 ? 0xe35c59e3u : i == 3 ? 0x53fe3ab1u : i == 4 ? 0x53bb8085u : i == 5 ? 0x8c49833du : i == 6 ? 0x7f4e44a5u : 0x0216d0b1u; }
 };
@@ -31,7 +31,7 @@ struct FrP {
 struct FqP {
     __host__ __device__ static constexpr uint32_t P(int i) { return i == 0 ? 0xd87cfd47u : i == 1 ? 0x3c208c16u : i == 2 ? 0x6871ca8du : i == 3 ? 0x97816a91u : i == 4 ? 0x8181585du : i == 5 ? 0xb85045b6u : i == 6 ? 0xe131a029u : 0x30644e72u; }
     static constexpr uint32_t INV = 0xe4866389u  /* -q^-1 mod 2^32 */;
-    static constexpr int MUL_STYLE = 1;
+    static constexpr int MUL_STYLE = 3;
     __host__ __device__ static constexpr uint32_t ONE(int i) { return i == 0 ? 0xc58f0d9du : i == 1 ? 0xd35d438du : i == 2 ? 0xf5c70b3du : i == 3 ? 0x0a78eb28u : i == 4 ? 0x7879462cu : i == 5 ? 0x666ea36fu : i == 6 ? 0x9a07df2fu : 0x0e0a77c1u; }
     __host__ __device__ static constexpr uint32_t R2(int i) { return i == 0 ? 0x538afa89u : i == 1 ? 0xf32cfc5bu : i == 2 ? 0xd44501fbu : i == 3 ? 0xb5e71911u : i == 4 ? 0x0a417ff6u : i == 5 ? 0x47ab1effu : i == 6 ? 0xcab8351fu : 0x06d89f71u; }
 };
@@ -220,11 +220,14 @@ __device__ __forceinline__ fe fe_dbl(const fe& a) {
 // both at compile time for measurements):
 //   0: the 8 rows fully unrolled and inlined at every call site (largest code);
 //   1: one non-inlined copy of the unrolled body, called from every site;
-//   2: inlined, but the row loop kept rolled (b's limbs rotate through one register).
+//   2: inlined, but the row loop kept rolled (b's limbs rotate through one register);
+//   3: like 1 on full-width products (fe_mul_wide_unrolled: mul.wide + add chains);
+//   4: like 0 on full-width products.
 // The curve formulas hold 10-14 multiplications per loop body, so inlining them all
 // overflows the instruction cache (the MSM accumulation stalled on "no instruction");
-// measured on GB300 at n = 2^20: MSM 125 / 160 / 147 Mpts/s and 2^22 NTT 3013 / 2966 /
-// 2643 Melem/s for styles 0 / 1 / 2. Fq (curve) uses 1, Fr (NTT butterflies) uses 0.
+// measured on GB300 at n = 2^20: MSM 125 / 160 / 147 / 179 / 143 Mpts/s and 2^22 NTT
+// 3013 / 2966 / 2643 / 3098 / 3136 Melem/s for styles 0 / 1 / 2 / 3 / 4.
+// Fq (curve) uses 3, Fr (NTT butterflies) uses 4.
 
 template <class F>
 __device__ __forceinline__ fe fe_mul_unrolled(const fe& a, const fe& b) {
@@ -271,9 +274,167 @@ __device__ __forceinline__ fe fe_mul_rolled(const fe& a, const fe& b) {
     return fe_reduce_once<F>(t);
 }
 
+// CIOS on full-width products: mul.wide.u32 (IMAD.WIDE) yields lo and hi of a_j * b_i
+// in one instruction -- measured on GB300 at twice the rate of a mad.lo + mad.hi pair,
+// whose hi half issues at half rate -- and two add-with-carry chains fold the halves
+// into t (lo(P_j) into t_j, hi(P_j) into t_{j+1}). Same bounds as ZK_MUL_ROW.
+#define ZK_ADD_LO_CHAIN(p0, p1, p2, p3, p4, p5, p6, p7)                                                         \
+    asm("add.cc.u32  %0, %0, %9;\n\t"                                                                          \
+        "addc.cc.u32 %1, %1, %10;\n\t"                                                                         \
+        "addc.cc.u32 %2, %2, %11;\n\t"                                                                         \
+        "addc.cc.u32 %3, %3, %12;\n\t"                                                                         \
+        "addc.cc.u32 %4, %4, %13;\n\t"                                                                         \
+        "addc.cc.u32 %5, %5, %14;\n\t"                                                                         \
+        "addc.cc.u32 %6, %6, %15;\n\t"                                                                         \
+        "addc.cc.u32 %7, %7, %16;\n\t"                                                                         \
+        "addc.u32    %8, %8, 0;"                                                                               \
+        : "+r"(t0), "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8)            \
+        : "r"((uint32_t)(p0)), "r"((uint32_t)(p1)), "r"((uint32_t)(p2)), "r"((uint32_t)(p3)),                 \
+          "r"((uint32_t)(p4)), "r"((uint32_t)(p5)), "r"((uint32_t)(p6)), "r"((uint32_t)(p7)))
+#define ZK_ADD_HI_CHAIN(p0, p1, p2, p3, p4, p5, p6, p7)                                                         \
+    asm("add.cc.u32  %0, %0, %8;\n\t"                                                                          \
+        "addc.cc.u32 %1, %1, %9;\n\t"                                                                          \
+        "addc.cc.u32 %2, %2, %10;\n\t"                                                                         \
+        "addc.cc.u32 %3, %3, %11;\n\t"                                                                         \
+        "addc.cc.u32 %4, %4, %12;\n\t"                                                                         \
+        "addc.cc.u32 %5, %5, %13;\n\t"                                                                         \
+        "addc.cc.u32 %6, %6, %14;\n\t"                                                                         \
+        "addc.u32    %7, %7, %15;"                                                                             \
+        : "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8)                       \
+        : "r"((uint32_t)((p0) >> 32)), "r"((uint32_t)((p1) >> 32)), "r"((uint32_t)((p2) >> 32)),              \
+          "r"((uint32_t)((p3) >> 32)), "r"((uint32_t)((p4) >> 32)), "r"((uint32_t)((p5) >> 32)),              \
+          "r"((uint32_t)((p6) >> 32)), "r"((uint32_t)((p7) >> 32)))
+
+template <class F>
+__device__ __forceinline__ fe fe_mul_wide_unrolled(const fe& a, const fe& b) {
+    uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0, t8 = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const uint32_t bi = b.v[i];
+        const uint64_t p0 = (uint64_t)a.v[0] * bi, p1 = (uint64_t)a.v[1] * bi, p2 = (uint64_t)a.v[2] * bi,
+                       p3 = (uint64_t)a.v[3] * bi, p4 = (uint64_t)a.v[4] * bi, p5 = (uint64_t)a.v[5] * bi,
+                       p6 = (uint64_t)a.v[6] * bi, p7 = (uint64_t)a.v[7] * bi;
+        ZK_ADD_LO_CHAIN(p0, p1, p2, p3, p4, p5, p6, p7);
+        ZK_ADD_HI_CHAIN(p0, p1, p2, p3, p4, p5, p6, p7);
+        const uint32_t m = t0 * F::INV;
+        const uint64_t q0 = (uint64_t)m * F::P(0), q1 = (uint64_t)m * F::P(1), q2 = (uint64_t)m * F::P(2),
+                       q3 = (uint64_t)m * F::P(3), q4 = (uint64_t)m * F::P(4), q5 = (uint64_t)m * F::P(5),
+                       q6 = (uint64_t)m * F::P(6), q7 = (uint64_t)m * F::P(7);
+        ZK_ADD_LO_CHAIN(q0, q1, q2, q3, q4, q5, q6, q7);
+        ZK_ADD_HI_CHAIN(q0, q1, q2, q3, q4, q5, q6, q7);
+        t0 = t1;
+        t1 = t2;
+        t2 = t3;
+        t3 = t4;
+        t4 = t5;
+        t5 = t6;
+        t6 = t7;
+        t7 = t8;
+        t8 = 0;
+    }
+    fe t;
+    t.v[0] = t0;
+    t.v[1] = t1;
+    t.v[2] = t2;
+    t.v[3] = t3;
+    t.v[4] = t4;
+    t.v[5] = t5;
+    t.v[6] = t6;
+    t.v[7] = t7;
+    return fe_reduce_once<F>(t);
+}
+
+// Two independent products a*b and c*d with their rows interleaved: the carry chains of
+// one product fill the latency of the other's (a thread's carry flag serialises each chain).
+#define ZK_LO_CHAIN_R(r0, r1, r2, r3, r4, r5, r6, r7, r8, p0, p1, p2, p3, p4, p5, p6, p7)                     \
+    asm("add.cc.u32  %0, %0, %9;\n\t"                                                                          \
+        "addc.cc.u32 %1, %1, %10;\n\t"                                                                         \
+        "addc.cc.u32 %2, %2, %11;\n\t"                                                                         \
+        "addc.cc.u32 %3, %3, %12;\n\t"                                                                         \
+        "addc.cc.u32 %4, %4, %13;\n\t"                                                                         \
+        "addc.cc.u32 %5, %5, %14;\n\t"                                                                         \
+        "addc.cc.u32 %6, %6, %15;\n\t"                                                                         \
+        "addc.cc.u32 %7, %7, %16;\n\t"                                                                         \
+        "addc.u32    %8, %8, 0;"                                                                               \
+        : "+r"(r0), "+r"(r1), "+r"(r2), "+r"(r3), "+r"(r4), "+r"(r5), "+r"(r6), "+r"(r7), "+r"(r8)            \
+        : "r"((uint32_t)(p0)), "r"((uint32_t)(p1)), "r"((uint32_t)(p2)), "r"((uint32_t)(p3)),                 \
+          "r"((uint32_t)(p4)), "r"((uint32_t)(p5)), "r"((uint32_t)(p6)), "r"((uint32_t)(p7)))
+#define ZK_HI_CHAIN_R(r1, r2, r3, r4, r5, r6, r7, r8, p0, p1, p2, p3, p4, p5, p6, p7)                         \
+    asm("add.cc.u32  %0, %0, %8;\n\t"                                                                          \
+        "addc.cc.u32 %1, %1, %9;\n\t"                                                                          \
+        "addc.cc.u32 %2, %2, %10;\n\t"                                                                         \
+        "addc.cc.u32 %3, %3, %11;\n\t"                                                                         \
+        "addc.cc.u32 %4, %4, %12;\n\t"                                                                         \
+        "addc.cc.u32 %5, %5, %13;\n\t"                                                                         \
+        "addc.cc.u32 %6, %6, %14;\n\t"                                                                         \
+        "addc.u32    %7, %7, %15;"                                                                             \
+        : "+r"(r1), "+r"(r2), "+r"(r3), "+r"(r4), "+r"(r5), "+r"(r6), "+r"(r7), "+r"(r8)                       \
+        : "r"((uint32_t)((p0) >> 32)), "r"((uint32_t)((p1) >> 32)), "r"((uint32_t)((p2) >> 32)),              \
+          "r"((uint32_t)((p3) >> 32)), "r"((uint32_t)((p4) >> 32)), "r"((uint32_t)((p5) >> 32)),              \
+          "r"((uint32_t)((p6) >> 32)), "r"((uint32_t)((p7) >> 32)))
+
+struct fe2 {
+    fe x, y;
+};
+
+template <class F>
+__device__ __forceinline__ fe2 fe_mul2_wide_unrolled(const fe& a, const fe& b, const fe& c, const fe& d) {
+    uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0, t8 = 0;
+    uint32_t u0 = 0, u1 = 0, u2 = 0, u3 = 0, u4 = 0, u5 = 0, u6 = 0, u7 = 0, u8 = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const uint32_t bi = b.v[i], di = d.v[i];
+        const uint64_t p0 = (uint64_t)a.v[0] * bi, p1 = (uint64_t)a.v[1] * bi, p2 = (uint64_t)a.v[2] * bi,
+                       p3 = (uint64_t)a.v[3] * bi, p4 = (uint64_t)a.v[4] * bi, p5 = (uint64_t)a.v[5] * bi,
+                       p6 = (uint64_t)a.v[6] * bi, p7 = (uint64_t)a.v[7] * bi;
+        const uint64_t r0 = (uint64_t)c.v[0] * di, r1 = (uint64_t)c.v[1] * di, r2 = (uint64_t)c.v[2] * di,
+                       r3 = (uint64_t)c.v[3] * di, r4 = (uint64_t)c.v[4] * di, r5 = (uint64_t)c.v[5] * di,
+                       r6 = (uint64_t)c.v[6] * di, r7 = (uint64_t)c.v[7] * di;
+        ZK_LO_CHAIN_R(t0, t1, t2, t3, t4, t5, t6, t7, t8, p0, p1, p2, p3, p4, p5, p6, p7);
+        ZK_LO_CHAIN_R(u0, u1, u2, u3, u4, u5, u6, u7, u8, r0, r1, r2, r3, r4, r5, r6, r7);
+        ZK_HI_CHAIN_R(t1, t2, t3, t4, t5, t6, t7, t8, p0, p1, p2, p3, p4, p5, p6, p7);
+        ZK_HI_CHAIN_R(u1, u2, u3, u4, u5, u6, u7, u8, r0, r1, r2, r3, r4, r5, r6, r7);
+        const uint32_t m = t0 * F::INV, mu = u0 * F::INV;
+        const uint64_t q0 = (uint64_t)m * F::P(0), q1 = (uint64_t)m * F::P(1), q2 = (uint64_t)m * F::P(2),
+                       q3 = (uint64_t)m * F::P(3), q4 = (uint64_t)m * F::P(4), q5 = (uint64_t)m * F::P(5),
+                       q6 = (uint64_t)m * F::P(6), q7 = (uint64_t)m * F::P(7);
+        const uint64_t s0 = (uint64_t)mu * F::P(0), s1 = (uint64_t)mu * F::P(1), s2 = (uint64_t)mu * F::P(2),
+                       s3 = (uint64_t)mu * F::P(3), s4 = (uint64_t)mu * F::P(4), s5 = (uint64_t)mu * F::P(5),
+                       s6 = (uint64_t)mu * F::P(6), s7 = (uint64_t)mu * F::P(7);
+        ZK_LO_CHAIN_R(t0, t1, t2, t3, t4, t5, t6, t7, t8, q0, q1, q2, q3, q4, q5, q6, q7);
+        ZK_LO_CHAIN_R(u0, u1, u2, u3, u4, u5, u6, u7, u8, s0, s1, s2, s3, s4, s5, s6, s7);
+        ZK_HI_CHAIN_R(t1, t2, t3, t4, t5, t6, t7, t8, q0, q1, q2, q3, q4, q5, q6, q7);
+        ZK_HI_CHAIN_R(u1, u2, u3, u4, u5, u6, u7, u8, s0, s1, s2, s3, s4, s5, s6, s7);
+        t0 = t1, t1 = t2, t2 = t3, t3 = t4, t4 = t5, t5 = t6, t6 = t7, t7 = t8, t8 = 0;
+        u0 = u1, u1 = u2, u2 = u3, u3 = u4, u4 = u5, u5 = u6, u6 = u7, u7 = u8, u8 = 0;
+    }
+    fe x, y;
+    x.v[0] = t0, x.v[1] = t1, x.v[2] = t2, x.v[3] = t3, x.v[4] = t4, x.v[5] = t5, x.v[6] = t6, x.v[7] = t7;
+    y.v[0] = u0, y.v[1] = u1, y.v[2] = u2, y.v[3] = u3, y.v[4] = u4, y.v[5] = u5, y.v[6] = u6, y.v[7] = u7;
+    fe2 r;
+    r.x = fe_reduce_once<F>(x);
+    r.y = fe_reduce_once<F>(y);
+    return r;
+}
+
+template <class F>
+__device__ __noinline__ fe2 fe_mul2_call(const fe a, const fe b, const fe c, const fe d) {
+    return fe_mul2_wide_unrolled<F>(a, b, c, d);
+}
+
+// (a*b, c*d): two calls of fe_mul, or (with ZK_USE_MUL2 and style 3) one call of the
+// interleaved product.
+template <class F>
+__device__ __forceinline__ fe2 fe_mul2(const fe& a, const fe& b, const fe& c, const fe& d);
+
 template <class F>
 __device__ __noinline__ fe fe_mul_call(const fe a, const fe b) {
     return fe_mul_unrolled<F>(a, b);
+}
+
+template <class F>
+__device__ __noinline__ fe fe_mul_wide_call(const fe a, const fe b) {
+    return fe_mul_wide_unrolled<F>(a, b);
 }
 
 // r = a * b * 2^-256 mod p (CIOS, see the file header).
@@ -288,9 +449,30 @@ __device__ __forceinline__ fe fe_mul(const fe& a, const fe& b) {
         return fe_mul_unrolled<F>(a, b);
     } else if constexpr (style == 1) {
         return fe_mul_call<F>(a, b);
+    } else if constexpr (style == 3) {
+        return fe_mul_wide_call<F>(a, b);
+    } else if constexpr (style == 4) {
+        return fe_mul_wide_unrolled<F>(a, b);
     } else {
         return fe_mul_rolled<F>(a, b);
     }
+}
+
+template <class F>
+__device__ __forceinline__ fe2 fe_mul2(const fe& a, const fe& b, const fe& c, const fe& d) {
+#ifdef ZK_MUL_STYLE
+    constexpr int style = ZK_MUL_STYLE;
+#else
+    constexpr int style = F::MUL_STYLE;
+#endif
+#ifdef ZK_USE_MUL2
+    // measured on GB300 (MSM 2^20): 179 Mpts/s with the interleaved pair, 180 without
+    if constexpr (style == 3) return fe_mul2_call<F>(a, b, c, d);
+#endif
+    fe2 r;
+    r.x = fe_mul<F>(a, b);
+    r.y = fe_mul<F>(c, d);
+    return r;
 }
 
 template <class F>

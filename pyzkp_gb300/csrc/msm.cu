@@ -23,6 +23,7 @@
 //                         whose index has bit k set: plain sums, reduced by CTA trees.
 //  7. host: per window S_w = T_E + g (T_Y + sum_k 2^k M_k), then Horner over windows.
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <vector>
 
@@ -33,20 +34,32 @@ namespace zk {
 int device_exclusive_scan(Ctx* c, uint32_t* data, size_t n, uint32_t* total);
 
 static constexpr uint32_t kNone = 0xffffffffu;
-static constexpr uint32_t kSegment = 32;   // entries per thread in the first accumulation round
-static constexpr uint32_t kFirstGroup = 2; // units merged per thread in the first merge round
-static constexpr uint32_t kGroup = 16;     // units merged per thread in later rounds
-static constexpr uint32_t kBlockG = 8;     // buckets per block in the window reduction
+#ifndef ZK_MSM_SEGMENT
+#define ZK_MSM_SEGMENT 32
+#endif
+#ifndef ZK_MSM_BLOCKG
+#define ZK_MSM_BLOCKG 8
+#endif
+static constexpr uint32_t kSegment = ZK_MSM_SEGMENT;  // entries per thread in the first accumulation round
+static constexpr uint32_t kFirstGroup = 2;            // units merged per thread in the first merge round
+static constexpr uint32_t kGroup = 16;                // units merged per thread in later rounds
+static constexpr uint32_t kBlockG = ZK_MSM_BLOCKG;    // buckets per block in the window reduction
 static constexpr int kTargetThreads = 256;
 
 struct MsmShape {
     uint32_t c;        // window bits
     uint32_t W;        // windows
     uint32_t B;        // buckets per window (|digit| in 1..B)
-    uint32_t g;        // block size of the window reduction (<= B)
-    uint32_t G;        // blocks per window
-    uint32_t K;        // log2(G)
-    uint32_t targets;  // 2 + K
+    uint32_t g;        // level-1 block size of the window reduction (<= B)
+    uint32_t G;        // level-1 blocks per window
+    uint32_t g2;       // level-2 block size (1: no second level)
+    uint32_t G2;       // level-2 blocks per window (G / g2)
+    uint32_t K;        // log2(G2)
+    uint32_t plain;    // plain-sum targets: 2 (one level) or 3 (two levels)
+    uint32_t targets;  // plain + K
+    uint32_t shared;   // 1: fixed-base mode, all windows share one bucket set (window-shifted bases)
+    uint32_t Wr;       // bucket sets to reduce: W, or 1 in fixed-base mode
+    uint32_t stride;   // fixed-base mode: row stride of the shifted-bases array
 };
 
 static MsmShape make_shape(uint32_t c) {
@@ -56,9 +69,15 @@ static MsmShape make_shape(uint32_t c) {
     s.B = 1u << (c - 1);
     s.g = std::min<uint32_t>(kBlockG, s.B);
     s.G = s.B / s.g;
+    s.g2 = s.G >= 16 ? kBlockG : 1;
+    s.G2 = s.G / s.g2;
     s.K = 0;
-    while ((1u << s.K) < s.G) s.K++;
-    s.targets = 2 + s.K;
+    while ((1u << s.K) < s.G2) s.K++;
+    s.plain = s.g2 > 1 ? 3 : 2;
+    s.targets = s.plain + s.K;
+    s.shared = 0;
+    s.Wr = s.W;
+    s.stride = 0;
     return s;
 }
 
@@ -115,7 +134,7 @@ __global__ void msm_digits_kernel(const fe* __restrict__ scalars, const affine_t
         }
         const bool nz = valid && mag != 0;
         if (valid) digits[(size_t)w * n + i] = nz ? (mag | (neg << 31)) : 0u;
-        warp_aggregated_inc(counts, w * sh.B + (mag - 1), nz);
+        warp_aggregated_inc(counts, (sh.shared ? 0u : w * sh.B) + (mag - 1), nz);
     }
 }
 
@@ -128,7 +147,8 @@ __global__ void msm_scatter_kernel(const uint32_t* __restrict__ digits, uint32_t
     for (uint32_t w = 0; w < sh.W; w++) {
         const uint32_t d = valid ? digits[(size_t)w * n + i] : 0u;
         const bool nz = d != 0;
-        const uint32_t key = w * sh.B + (d & 0x7fffffffu) - 1;
+        const uint32_t key = (sh.shared ? 0u : w * sh.B) + (d & 0x7fffffffu) - 1;
+        const uint32_t point = sh.shared ? w * sh.stride + i : i;  // fixed-base: row w of the shifted bases
         const uint32_t live = __ballot_sync(0xffffffffu, nz);
         if (nz) {
             const uint32_t peers = __match_any_sync(live, key);
@@ -138,7 +158,7 @@ __global__ void msm_scatter_kernel(const uint32_t* __restrict__ digits, uint32_t
             if (lane == leader) base = atomicAdd(cursor + key, (uint32_t)__popc(peers));
             base = __shfl_sync(peers, base, leader);
             const uint32_t rank = __popc(peers & ((1u << lane) - 1));
-            entries[base + rank] = i | (d & 0x80000000u);
+            entries[base + rank] = point | (d & 0x80000000u);
             keys[base + rank] = key;
         }
     }
@@ -232,13 +252,17 @@ __global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restri
     if (cur != kNone) emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
 }
 
-// ---- 5. window reduction, level 1 -------------------------------------------------
-// Block j of window w holds buckets b = j*g + 1 .. j*g + g (stored at index b - 1).
-// Y_j = sum of the block, E_j = -(s_1 + ... + s_{g-1}) with s_u the prefix sums.
+// ---- 5. window reduction ----------------------------------------------------------------
+// For points X_1..X_N with weights, WS(X) = sum_b b X_b. Blocks of g: X_{(j-1)g+u}, u = 1..g:
+// WS(X) = sum_j E_j + g WS(Y), Y_j = block sum, E_j = -(s_1 + ... + s_{g-1}) with s_u the
+// prefix sums inside the block (because sum_u u X_u = g Y_j - sum_{u<g} s_u). Applied
+// twice (buckets -> Y1, E1 -> Y2, E2, F2 = block sums of E1), then WS(Y2) by plain sums:
+// WS(Y2) = sum_j Y2_j + sum_k 2^k M_k, M_k = sum of Y2_j with bit k of (j - 1) set.
+// Level 1: block j of window w holds buckets b = j*g + 1 .. j*g + g (stored at index b - 1).
 __global__ void __launch_bounds__(128) msm_bucket_blocks_kernel(const xyzz_t* __restrict__ buckets, MsmShape sh,
                                                                 xyzz_t* __restrict__ Y, xyzz_t* __restrict__ E) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= sh.W * sh.G) return;
+    if (t >= sh.Wr * sh.G) return;
     const xyzz_t* b = buckets + (size_t)t * sh.g;
     xyzz_t s = xyzz_inf();
     xyzz_t e = xyzz_inf();
@@ -250,21 +274,47 @@ __global__ void __launch_bounds__(128) msm_bucket_blocks_kernel(const xyzz_t* __
     xyzz_store(E + t, xyzz_neg(e));
 }
 
+// Level 2 over (Y1, E1): Y2, E2 as above on Y1, and F2 = plain block sums of E1.
+__global__ void __launch_bounds__(128) msm_bucket_blocks2_kernel(const xyzz_t* __restrict__ Y1,
+                                                                 const xyzz_t* __restrict__ E1, MsmShape sh,
+                                                                 xyzz_t* __restrict__ Y2, xyzz_t* __restrict__ E2,
+                                                                 xyzz_t* __restrict__ F2) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= sh.Wr * sh.G2) return;
+    const size_t base = (size_t)t * sh.g2;
+    xyzz_t s = xyzz_inf();
+    xyzz_t e = xyzz_inf();
+    xyzz_t f = xyzz_inf();
+    for (uint32_t u = 0; u < sh.g2; u++) {
+        s = xyzz_add(s, xyzz_load(Y1 + base + u));
+        if (u + 1 < sh.g2) e = xyzz_add(e, s);
+        f = xyzz_add(f, xyzz_load(E1 + base + u));
+    }
+    xyzz_store(Y2 + t, s);
+    xyzz_store(E2 + t, xyzz_neg(e));
+    xyzz_store(F2 + t, f);
+}
+
 // ---- 6. plain sums per (window, target) ---------------------------------------------
-// target 0: sum_j E_j; target 1: sum_j Y_j; target 2 + k: sum of Y_j over j with bit k set.
-__global__ void __launch_bounds__(kTargetThreads) msm_targets_kernel(const xyzz_t* __restrict__ Y,
-                                                                     const xyzz_t* __restrict__ E, MsmShape sh,
+// targets 0 .. plain-1: full sums of P0, P1 (, P2) over G2 entries per window;
+// target plain + k: sum of Ylast_j over j with bit k set.
+__global__ void __launch_bounds__(kTargetThreads) msm_targets_kernel(const xyzz_t* __restrict__ P0,
+                                                                     const xyzz_t* __restrict__ P1,
+                                                                     const xyzz_t* __restrict__ P2,
+                                                                     const xyzz_t* __restrict__ Ylast, MsmShape sh,
                                                                      xyzz_t* __restrict__ out) {
     __shared__ xyzz_t red[kTargetThreads];
     const uint32_t w = blockIdx.x / sh.targets;
     const uint32_t tg = blockIdx.x % sh.targets;
-    const xyzz_t* src = (tg == 0 ? E : Y) + (size_t)w * sh.G;
-    const uint32_t count = tg >= 2 ? sh.G / 2 : sh.G;
-    const uint32_t k = tg >= 2 ? tg - 2 : 0;
+    const bool bits = tg >= sh.plain;
+    const xyzz_t* src = bits ? Ylast : (tg == 0 ? P0 : (tg == 1 ? P1 : P2));
+    src += (size_t)w * sh.G2;
+    const uint32_t count = bits ? sh.G2 / 2 : sh.G2;
+    const uint32_t k = bits ? tg - sh.plain : 0;
     xyzz_t acc = xyzz_inf();
     for (uint32_t t = threadIdx.x; t < count; t += blockDim.x) {
         uint32_t j = t;
-        if (tg >= 2) j = ((t >> k) << (k + 1)) | (1u << k) | (t & ((1u << k) - 1));
+        if (bits) j = ((t >> k) << (k + 1)) | (1u << k) | (t & ((1u << k) - 1));
         acc = xyzz_add(acc, xyzz_load(src + j));
     }
     red[threadIdx.x] = acc;
@@ -274,6 +324,88 @@ __global__ void __launch_bounds__(kTargetThreads) msm_targets_kernel(const xyzz_
         __syncthreads();
     }
     if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+// ---- fixed-base precomputation ----------------------------------------------------------
+// Row j of the output holds [2^(c j)] P_i in affine Montgomery form (row 0 = P_i). Per point
+// the W - 1 shifted points are built by c doublings each in XYZZ, then normalised with one
+// field inversion (Montgomery's trick over the point's own rows). Infinity stays (0, 0);
+// no shifted point of a finite point is infinity (2^(c j) is invertible mod r).
+template <class F>
+__device__ fe fe_inverse_fermat(const fe& a) {
+    fe r = fe_one<F>();
+    for (int limb = 7; limb >= 0; limb--) {
+        const uint32_t e = limb == 0 ? F::P(0) - 2u : F::P(limb);
+        for (int b = 31; b >= 0; b--) {
+            r = fe_sqr<F>(r);
+            if ((e >> b) & 1) r = fe_mul<F>(r, a);
+        }
+    }
+    return r;
+}
+
+__global__ void __launch_bounds__(128) msm_shift_bases_kernel(const affine_t* __restrict__ bases, uint32_t n,
+                                                              uint32_t c, uint32_t W, affine_t* __restrict__ out,
+                                                              xyzz_t* __restrict__ tmp, fe* __restrict__ pref) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const affine_t p = affine_load(bases + i);
+    fe_store(&out[i].x, p.x);
+    fe_store(&out[i].y, p.y);
+    if (affine_is_inf(p)) {
+        for (uint32_t j = 1; j < W; j++) {
+            fe_store(&out[(size_t)j * n + i].x, fe_zero());
+            fe_store(&out[(size_t)j * n + i].y, fe_zero());
+        }
+        return;
+    }
+    xyzz_t q;
+    q.X = p.x;
+    q.Y = p.y;
+    q.ZZ = fe_one<FqP>();
+    q.ZZZ = fe_one<FqP>();
+    fe run = fe_one<FqP>();
+    for (uint32_t j = 1; j < W; j++) {
+        for (uint32_t d = 0; d < c; d++) q = xyzz_dbl(q);
+        xyzz_store(tmp + (size_t)j * n + i, q);
+        fe_store(pref + (size_t)j * n + i, run);
+        run = fe_mul<FqP>(run, fe_mul<FqP>(q.ZZ, q.ZZZ));
+    }
+    fe inv = fe_inverse_fermat<FqP>(run);
+    for (uint32_t j = W - 1; j >= 1; j--) {
+        const xyzz_t t = xyzz_load(tmp + (size_t)j * n + i);
+        const fe zz_zzz = fe_mul<FqP>(t.ZZ, t.ZZZ);
+        const fe I = fe_mul<FqP>(inv, fe_load(pref + (size_t)j * n + i));
+        inv = fe_mul<FqP>(inv, zz_zzz);
+        fe_store(&out[(size_t)j * n + i].x, fe_mul<FqP>(t.X, fe_mul<FqP>(t.ZZZ, I)));
+        fe_store(&out[(size_t)j * n + i].y, fe_mul<FqP>(t.Y, fe_mul<FqP>(t.ZZ, I)));
+    }
+}
+
+int shift_bases(Ctx* c, const affine_t* bases, size_t n, uint32_t window_bits, affine_t** out, uint32_t* windows) {
+    ZK_CHECK_ARG(window_bits >= 4 && window_bits <= 20, "fixed-base window_bits must be 4..20");
+    ZK_CHECK_ARG(n > 0 && n < (1ull << 31), "fixed-base precomputation needs 0 < n < 2^31");
+    const MsmShape sh = make_shape(window_bits);
+    ZK_CHECK_ARG((uint64_t)sh.W * n < (1ull << 31), "fixed-base rows exceed 31-bit entry indices");
+    affine_t* rows = nullptr;
+    xyzz_t* tmp = nullptr;
+    fe* pref = nullptr;
+    int rc = scratch_alloc(c, (size_t)sh.W * n * sizeof(affine_t), reinterpret_cast<void**>(&rows));
+    if (rc != ZK_OK) return rc;
+    if ((rc = scratch_alloc(c, (size_t)sh.W * n * sizeof(xyzz_t), reinterpret_cast<void**>(&tmp))) != ZK_OK ||
+        (rc = scratch_alloc(c, (size_t)sh.W * n * sizeof(fe), reinterpret_cast<void**>(&pref))) != ZK_OK) {
+        scratch_free(c, rows);
+        scratch_free(c, tmp);
+        return rc;
+    }
+    ZK_LAUNCH(c, "msm_shift_bases", msm_shift_bases_kernel, (unsigned)((n + 127) / 128), 128, 0, bases, (uint32_t)n,
+              window_bits, sh.W, rows, tmp, pref);
+    ZK_TRY_CUDA(cudaGetLastError());
+    scratch_free(c, tmp);
+    scratch_free(c, pref);
+    *out = rows;
+    *windows = sh.W;
+    return ZK_OK;
 }
 
 // ---- host ---------------------------------------------------------------------------
@@ -292,7 +424,7 @@ static zkh::Xyzz host_dbl_n(zkh::Xyzz p, uint32_t times) {
 }
 
 int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
-            uint8_t out_xy[64], int* out_is_inf) {
+            uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted, uint32_t shifted_c, uint64_t stride) {
     ZK_CHECK_ARG(n < (1ull << 31), "MSM size must be below 2^31 points");
     ZK_CHECK_ARG(window_bits == 0 || (window_bits >= 4 && window_bits <= 20), "window_bits must be 0 or 4..20");
     if (n == 0) {
@@ -300,15 +432,25 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
         *out_is_inf = 1;
         return ZK_OK;
     }
-    const uint32_t cbits = window_bits ? window_bits : msm_auto_window(n);
-    const MsmShape sh = make_shape(cbits);
-    const uint64_t nbuckets = (uint64_t)sh.W * sh.B;
+    // fixed-base mode: the bases carry window-shifted rows [2^(c j)] P_i (zk_bases_precompute)
+    const bool fixed = shifted != nullptr && (window_bits == 0 || window_bits == shifted_c);
+    const uint32_t cbits = fixed ? shifted_c : (window_bits ? window_bits : msm_auto_window(n));
+    MsmShape sh = make_shape(cbits);
+    if (fixed) {
+        sh.shared = 1;
+        sh.Wr = 1;
+        sh.stride = (uint32_t)stride;
+        ZK_CHECK_ARG((uint64_t)sh.W * stride < (1ull << 31), "fixed-base rows exceed 31-bit entry indices");
+    }
+    const affine_t* acc_bases = fixed ? shifted : bases;
+    const uint64_t nbuckets = (uint64_t)sh.Wr * sh.B;
     const uint64_t max_entries = (uint64_t)n * sh.W;
     ZK_CHECK_ARG(max_entries < (1ull << 32) - kSegment, "MSM too large for 32-bit CSR offsets");
 
     // scratch layout
     uint32_t *digits = nullptr, *row_ptr = nullptr, *cursor = nullptr, *entries = nullptr, *keys = nullptr;
-    xyzz_t *buckets = nullptr, *Yb = nullptr, *Eb = nullptr, *tgt = nullptr;
+    xyzz_t *buckets = nullptr, *Yb = nullptr, *Eb = nullptr, *Y2 = nullptr, *E2 = nullptr, *F2 = nullptr,
+           *tgt = nullptr;
     std::vector<void*> allocs;
     auto alloc = [&](size_t bytes, void** p) -> int {
         int rc = scratch_alloc(c, bytes, p);
@@ -326,9 +468,12 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
         (rc = alloc(max_entries * 4, (void**)&entries)) != ZK_OK ||
         (rc = alloc(max_entries * 4, (void**)&keys)) != ZK_OK ||
         (rc = alloc(nbuckets * sizeof(xyzz_t), (void**)&buckets)) != ZK_OK ||
-        (rc = alloc((size_t)sh.W * sh.G * sizeof(xyzz_t), (void**)&Yb)) != ZK_OK ||
-        (rc = alloc((size_t)sh.W * sh.G * sizeof(xyzz_t), (void**)&Eb)) != ZK_OK ||
-        (rc = alloc((size_t)sh.W * sh.targets * sizeof(xyzz_t), (void**)&tgt)) != ZK_OK) {
+        (rc = alloc((size_t)sh.Wr * sh.G * sizeof(xyzz_t), (void**)&Yb)) != ZK_OK ||
+        (rc = alloc((size_t)sh.Wr * sh.G * sizeof(xyzz_t), (void**)&Eb)) != ZK_OK ||
+        (rc = alloc((size_t)sh.Wr * sh.G2 * sizeof(xyzz_t), (void**)&Y2)) != ZK_OK ||
+        (rc = alloc((size_t)sh.Wr * sh.G2 * sizeof(xyzz_t), (void**)&E2)) != ZK_OK ||
+        (rc = alloc((size_t)sh.Wr * sh.G2 * sizeof(xyzz_t), (void**)&F2)) != ZK_OK ||
+        (rc = alloc((size_t)sh.Wr * sh.targets * sizeof(xyzz_t), (void**)&tgt)) != ZK_OK) {
         release();
         return rc;
     }
@@ -363,7 +508,7 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
         return rc;
     }
     ZK_LAUNCH(c, "msm_accumulate", msm_accumulate_kernel, (units + 127) / 128, 128, 0, entries, keys, d_total, row_ptr,
-              bases, units, buckets, slot_keys_a, slot_pts_a);
+              acc_bases, units, buckets, slot_keys_a, slot_pts_a);
     ZK_TRY_CUDA(cudaGetLastError());
     uint64_t span = kSegment;
     uint32_t in_units = units;
@@ -373,8 +518,8 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
     while (in_units > 1) {
         const uint32_t out_units = (in_units + group - 1) / group;
         span *= group;
-        ZK_LAUNCH(c, "msm_merge", msm_merge_kernel, (out_units + 127) / 128, 128, 0, ik, ip, in_units, group, d_total,
-                  row_ptr, span, out_units, buckets, ok, op);
+        ZK_LAUNCH(c, group == kFirstGroup ? "msm_merge_pairs" : "msm_merge", msm_merge_kernel, (out_units + 127) / 128,
+                  128, 0, ik, ip, in_units, group, d_total, row_ptr, span, out_units, buckets, ok, op);
         ZK_TRY_CUDA(cudaGetLastError());
         std::swap(ik, ok);
         std::swap(ip, op);
@@ -383,12 +528,20 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
     }
 
     // window reduction
-    const uint32_t nblk = sh.W * sh.G;
+    const uint32_t nblk = sh.Wr * sh.G;
     ZK_LAUNCH(c, "msm_bucket_blocks", msm_bucket_blocks_kernel, (nblk + 127) / 128, 128, 0, buckets, sh, Yb, Eb);
     ZK_TRY_CUDA(cudaGetLastError());
-    ZK_LAUNCH(c, "msm_targets", msm_targets_kernel, sh.W * sh.targets, kTargetThreads, 0, Yb, Eb, sh, tgt);
+    if (sh.g2 > 1) {
+        const uint32_t nblk2 = sh.Wr * sh.G2;
+        ZK_LAUNCH(c, "msm_bucket_blocks2", msm_bucket_blocks2_kernel, (nblk2 + 127) / 128, 128, 0, Yb, Eb, sh, Y2, E2,
+                  F2);
+        ZK_TRY_CUDA(cudaGetLastError());
+        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel, sh.Wr * sh.targets, kTargetThreads, 0, F2, E2, Y2, Y2, sh, tgt);
+    } else {
+        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel, sh.Wr * sh.targets, kTargetThreads, 0, Eb, Yb, Yb, Yb, sh, tgt);
+    }
     ZK_TRY_CUDA(cudaGetLastError());
-    std::vector<xyzz_t> host_t((size_t)sh.W * sh.targets);
+    std::vector<xyzz_t> host_t((size_t)sh.Wr * sh.targets);
     uint32_t total_entries = 0;
     ZK_TRY_CUDA(cudaMemcpyAsync(host_t.data(), tgt, host_t.size() * sizeof(xyzz_t), cudaMemcpyDeviceToHost, st));
     ZK_TRY_CUDA(cudaMemcpyAsync(&total_entries, d_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -398,23 +551,33 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
     c->msm_window_bits = sh.c;
     c->msm_windows = sh.W;
 
-    // host: S_w = T_E + g (T_Y + sum_k 2^k M_k); total = sum_w 2^(c w) S_w
-    uint32_t log_g = 0;
+    // host: one level   S_w = T0 + g (T1 + H)            (T0 = sum E1, T1 = sum Y1)
+    //       two levels  S_w = T0 + g (T1 + g2 (T2 + H))  (T0 = sum F2 = sum E1, T1 = sum E2, T2 = sum Y2)
+    // with H = sum_k 2^k M_k (Horner); then total = sum_w 2^(c w) S_w (Horner over windows).
+    const auto t_host0 = std::chrono::steady_clock::now();
+    uint32_t log_g = 0, log_g2 = 0;
     while ((1u << log_g) < sh.g) log_g++;
+    while ((1u << log_g2) < sh.g2) log_g2++;
     zkh::Xyzz total = zkh::xyzz_inf();
-    for (int w = (int)sh.W - 1; w >= 0; w--) {
+    for (int w = (int)sh.Wr - 1; w >= 0; w--) {
         const xyzz_t* T = host_t.data() + (size_t)w * sh.targets;
         zkh::Xyzz h = zkh::xyzz_inf();
         for (int k = (int)sh.K - 1; k >= 0; k--) {
             h = zkh::xyzz_dbl(h);
-            h = zkh::xyzz_add(h, to_host(T[2 + k]));
+            h = zkh::xyzz_add(h, to_host(T[sh.plain + k]));
         }
-        zkh::Xyzz sw = zkh::xyzz_add(h, to_host(T[1]));
+        zkh::Xyzz sw = zkh::xyzz_add(h, to_host(T[sh.plain - 1]));
+        if (sh.plain == 3) {
+            sw = host_dbl_n(sw, log_g2);
+            sw = zkh::xyzz_add(sw, to_host(T[1]));
+        }
         sw = host_dbl_n(sw, log_g);
         sw = zkh::xyzz_add(sw, to_host(T[0]));
         total = host_dbl_n(total, sh.c);
         total = zkh::xyzz_add(total, sw);
     }
+    prof_host(c, "msm_host_combine",
+              std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_host0).count());
     zkh::F4 x, y;
     *out_is_inf = zkh::xyzz_to_affine_canonical(total, &x, &y) ? 1 : 0;
     std::memcpy(out_xy, x.v, 32);

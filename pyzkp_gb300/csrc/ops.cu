@@ -195,36 +195,92 @@ int fixed_base_mul(Ctx* c, const uint8_t point_xy[64], const void* k_dev, size_t
 
 namespace zk {
 
-// ---- IMAD throughput probe: 8 independent carry chains per thread, each step a
-// mad.lo.cc / madc.hi.cc pair per limb like one row of the Montgomery product. ----
+// ---- IMAD throughput probes (roofline denominator) ------------------------------------
+// MODE 0: carry chains shaped like one Montgomery row (mad.lo.cc / madc.hi.cc, each
+//         chain serial through the carry flag);
+// MODE 1: 8 independent mad.lo.u32 accumulators per thread (raw IMAD issue rate);
+// MODE 2: 8 independent mad.hi.u32 accumulators per thread;
+// MODE 3: 8 independent mad.wide.u32 (32x32 -> 64-bit) accumulators per thread, counted
+//         as 2 IMAD each (one full-width product replaces a lo + hi pair).
+template <int MODE>
 __global__ void imad_probe_kernel(uint32_t iters, uint32_t seed, uint32_t* sink) {
     uint32_t a[8], x = seed ^ threadIdx.x, y = seed * 2654435761u + blockIdx.x;
 #pragma unroll
     for (int i = 0; i < 8; i++) a[i] = x + i;
     for (uint32_t it = 0; it < iters; it++) {
-        asm volatile(
-            "mad.lo.cc.u32  %0, %8, %9, %0;\n\t"
-            "madc.hi.cc.u32 %1, %8, %9, %1;\n\t"
-            "madc.lo.cc.u32 %2, %8, %9, %2;\n\t"
-            "madc.hi.cc.u32 %3, %8, %9, %3;\n\t"
-            "madc.lo.cc.u32 %4, %8, %9, %4;\n\t"
-            "madc.hi.cc.u32 %5, %8, %9, %5;\n\t"
-            "madc.lo.cc.u32 %6, %8, %9, %6;\n\t"
-            "madc.hi.u32    %7, %8, %9, %7;\n\t"
-            : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
-            : "r"(x), "r"(y));
-        asm volatile(
-            "mad.lo.cc.u32  %0, %8, %9, %0;\n\t"
-            "madc.hi.cc.u32 %1, %8, %9, %1;\n\t"
-            "madc.lo.cc.u32 %2, %8, %9, %2;\n\t"
-            "madc.hi.cc.u32 %3, %8, %9, %3;\n\t"
-            "madc.lo.cc.u32 %4, %8, %9, %4;\n\t"
-            "madc.hi.cc.u32 %5, %8, %9, %5;\n\t"
-            "madc.lo.cc.u32 %6, %8, %9, %6;\n\t"
-            "madc.hi.u32    %7, %8, %9, %7;\n\t"
-            : "+r"(a[7]), "+r"(a[6]), "+r"(a[5]), "+r"(a[4]), "+r"(a[3]), "+r"(a[2]), "+r"(a[1]), "+r"(a[0])
-            : "r"(y), "r"(x));
-        x += a[0];
+        if constexpr (MODE == 0) {
+            asm volatile(
+                "mad.lo.cc.u32  %0, %8, %9, %0;\n\t"
+                "madc.hi.cc.u32 %1, %8, %9, %1;\n\t"
+                "madc.lo.cc.u32 %2, %8, %9, %2;\n\t"
+                "madc.hi.cc.u32 %3, %8, %9, %3;\n\t"
+                "madc.lo.cc.u32 %4, %8, %9, %4;\n\t"
+                "madc.hi.cc.u32 %5, %8, %9, %5;\n\t"
+                "madc.lo.cc.u32 %6, %8, %9, %6;\n\t"
+                "madc.hi.u32    %7, %8, %9, %7;\n\t"
+                : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7])
+                : "r"(x), "r"(y));
+            asm volatile(
+                "mad.lo.cc.u32  %0, %8, %9, %0;\n\t"
+                "madc.hi.cc.u32 %1, %8, %9, %1;\n\t"
+                "madc.lo.cc.u32 %2, %8, %9, %2;\n\t"
+                "madc.hi.cc.u32 %3, %8, %9, %3;\n\t"
+                "madc.lo.cc.u32 %4, %8, %9, %4;\n\t"
+                "madc.hi.cc.u32 %5, %8, %9, %5;\n\t"
+                "madc.lo.cc.u32 %6, %8, %9, %6;\n\t"
+                "madc.hi.u32    %7, %8, %9, %7;\n\t"
+                : "+r"(a[7]), "+r"(a[6]), "+r"(a[5]), "+r"(a[4]), "+r"(a[3]), "+r"(a[2]), "+r"(a[1]), "+r"(a[0])
+                : "r"(y), "r"(x));
+            x += a[0];
+        } else {
+#pragma unroll
+            for (int rep = 0; rep < 2; rep++) {
+                if constexpr (MODE == 3) {
+                    uint64_t w0 = a[0], w1 = a[1], w2 = a[2], w3 = a[3];
+                    asm volatile(
+                        "mad.wide.u32 %0, %4, %5, %0;\n\t"
+                        "mad.wide.u32 %1, %4, %5, %1;\n\t"
+                        "mad.wide.u32 %2, %4, %5, %2;\n\t"
+                        "mad.wide.u32 %3, %4, %5, %3;\n\t"
+                        "mad.wide.u32 %0, %5, %4, %0;\n\t"
+                        "mad.wide.u32 %1, %5, %4, %1;\n\t"
+                        "mad.wide.u32 %2, %5, %4, %2;\n\t"
+                        "mad.wide.u32 %3, %5, %4, %3;\n\t"
+                        : "+l"(w0), "+l"(w1), "+l"(w2), "+l"(w3)
+                        : "r"(x), "r"(y));
+                    a[0] = (uint32_t)w0 ^ (uint32_t)(w0 >> 32);
+                    a[1] = (uint32_t)w1 ^ (uint32_t)(w1 >> 32);
+                    a[2] = (uint32_t)w2 ^ (uint32_t)(w2 >> 32);
+                    a[3] = (uint32_t)w3 ^ (uint32_t)(w3 >> 32);
+                } else if constexpr (MODE == 1) {
+                    asm volatile(
+                        "mad.lo.u32 %0, %0, %8, %9;\n\t"
+                        "mad.lo.u32 %1, %1, %8, %9;\n\t"
+                        "mad.lo.u32 %2, %2, %8, %9;\n\t"
+                        "mad.lo.u32 %3, %3, %8, %9;\n\t"
+                        "mad.lo.u32 %4, %4, %8, %9;\n\t"
+                        "mad.lo.u32 %5, %5, %8, %9;\n\t"
+                        "mad.lo.u32 %6, %6, %8, %9;\n\t"
+                        "mad.lo.u32 %7, %7, %8, %9;\n\t"
+                        : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]),
+                          "+r"(a[7])
+                        : "r"(x), "r"(y));
+                } else {
+                    asm volatile(
+                        "mad.hi.u32 %0, %0, %8, %9;\n\t"
+                        "mad.hi.u32 %1, %1, %8, %9;\n\t"
+                        "mad.hi.u32 %2, %2, %8, %9;\n\t"
+                        "mad.hi.u32 %3, %3, %8, %9;\n\t"
+                        "mad.hi.u32 %4, %4, %8, %9;\n\t"
+                        "mad.hi.u32 %5, %5, %8, %9;\n\t"
+                        "mad.hi.u32 %6, %6, %8, %9;\n\t"
+                        "mad.hi.u32 %7, %7, %8, %9;\n\t"
+                        : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]),
+                          "+r"(a[7])
+                        : "r"(x), "r"(y));
+                }
+            }
+        }
     }
     uint32_t s = 0;
 #pragma unroll
@@ -232,19 +288,17 @@ __global__ void imad_probe_kernel(uint32_t iters, uint32_t seed, uint32_t* sink)
     if (s == 0x9e3779b9u) sink[0] = s;  // keeps the chains alive
 }
 
-int imad_peak(Ctx* c, double* tera) {
-    uint32_t* sink = nullptr;
-    int rc = scratch_alloc(c, 16, reinterpret_cast<void**>(&sink));
-    if (rc != ZK_OK) return rc;
+template <int MODE>
+static int imad_probe_run(Ctx* c, uint32_t* sink, double* tera) {
     const uint32_t blocks = (uint32_t)c->num_sms * 8, threads = 256, iters = 4096;
     cudaEvent_t e0, e1;
     ZK_TRY_CUDA(cudaEventCreate(&e0));
     ZK_TRY_CUDA(cudaEventCreate(&e1));
-    imad_probe_kernel<<<blocks, threads, 0, c->stream>>>(iters, 1u, sink);  // warm-up
+    imad_probe_kernel<MODE><<<blocks, threads, 0, c->stream>>>(iters, 1u, sink);  // warm-up
     float best = 1e30f;
     for (int rep = 0; rep < 5; rep++) {
         ZK_TRY_CUDA(cudaEventRecord(e0, c->stream));
-        imad_probe_kernel<<<blocks, threads, 0, c->stream>>>(iters, 2u + rep, sink);
+        imad_probe_kernel<MODE><<<blocks, threads, 0, c->stream>>>(iters, 2u + rep, sink);
         ZK_TRY_CUDA(cudaEventRecord(e1, c->stream));
         ZK_TRY_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -254,9 +308,37 @@ int imad_peak(Ctx* c, double* tera) {
     ZK_TRY_CUDA(cudaGetLastError());
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    scratch_free(c, sink);
-    const double ops = (double)blocks * threads * iters * 16.0;
+    const double ops = (double)blocks * threads * iters * 16.0 * (MODE == 3 ? 2.0 : 1.0);
     *tera = ops / (best * 1e-3) / 1e12;
+    return ZK_OK;
+}
+
+int imad_probe(Ctx* c, int mode, double* tera) {
+    ZK_CHECK_ARG(mode >= 0 && mode <= 3, "IMAD probe mode must be 0..3");
+    uint32_t* sink = nullptr;
+    int rc = scratch_alloc(c, 16, reinterpret_cast<void**>(&sink));
+    if (rc != ZK_OK) return rc;
+    if (mode == 0)
+        rc = imad_probe_run<0>(c, sink, tera);
+    else if (mode == 1)
+        rc = imad_probe_run<1>(c, sink, tera);
+    else if (mode == 2)
+        rc = imad_probe_run<2>(c, sink, tera);
+    else
+        rc = imad_probe_run<3>(c, sink, tera);
+    scratch_free(c, sink);
+    return rc;
+}
+
+int imad_peak(Ctx* c, double* tera) {
+    double best = 0.0;
+    for (int mode = 0; mode < 4; mode++) {
+        double t = 0.0;
+        int rc = imad_probe(c, mode, &t);
+        if (rc != ZK_OK) return rc;
+        if (t > best) best = t;
+    }
+    *tera = best;
     return ZK_OK;
 }
 

@@ -81,6 +81,9 @@ struct Ctx {
 int prof_begin(Ctx* c, const char* name);
 void prof_end(Ctx* c, int token);
 int prof_resolve(Ctx* c);
+// Host-side work inside a library call, recorded in the same table when profiling is on
+// (not counted as a kernel launch).
+void prof_host(Ctx* c, const char* name, double ms);
 
 // Launch `kernel` on the context stream with launch accounting.
 #define ZK_LAUNCH(ctxp, name, kernel, grid, block, smem, ...)                 \
@@ -98,7 +101,9 @@ void scratch_free(Ctx* c, void* p);
 int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log_n, const uint8_t omega[32],
             const uint8_t shift[32]);
 int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
-            uint8_t out_xy[64], int* out_is_inf);
+            uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted = nullptr, uint32_t shifted_c = 0,
+            uint64_t stride = 0);
+int shift_bases(Ctx* c, const affine_t* bases, size_t n, uint32_t window_bits, affine_t** out, uint32_t* windows);
 
 }  // namespace zk
 
@@ -110,4 +115,7 @@ struct zk_bases {
     zk_ctx* ctx;
     zk::affine_t* dev;  // Montgomery affine, (0, 0) = infinity
     size_t n;
+    zk::affine_t* shifted = nullptr;  // fixed-base rows [2^(c j)] P_i, j < shifted_windows, row stride n
+    uint32_t shifted_c = 0;
+    uint32_t shifted_windows = 0;
 };

@@ -113,6 +113,13 @@ class GpuRuntime:
         return b
 
 
+def fixed_base_window(n: int) -> int:
+    """Window of the fixed-base mode: its bucket reduction runs once, not once per window,
+    so a wider window (fewer CSR entries) pays off: c = clamp(log2(n) - 1, 8, 20)."""
+    lg = max(1, int(n)).bit_length() - 1
+    return max(8, min(20, lg - 1))
+
+
 def _fingerprint(points) -> int:
     n = len(points)
     idx = sorted(set([0, n - 1] + [i * n // 16 for i in range(16)])) if n else []
@@ -382,6 +389,17 @@ def register_gb300_kernels(registry, *, ir: Any = None) -> None:
         w = int(attrs.get("window_bits", 0) or 0)
         return w if 4 <= w <= 20 else 0  # any valid window yields the same point
 
+    def _fixed_base(rt: GpuRuntime, bases: N.Bases, num: int, attrs) -> None:
+        """Fixed-base mode when the op asks for it (attrs fixed_base True, or the policy "on",
+        runtime/kernels/cpu/kernels.py:560-569 / runtime/warmup.py:125-150): window-shifted rows
+        of the resident bases, computed once per base set. The point is the same either way."""
+        if not (attrs.get("fixed_base") is True or attrs.get("fixed_base_policy") == "on"):
+            return
+        c = fixed_base_window(bases.n)
+        if getattr(bases, "fixed_c", None) != c:
+            rt.zk.bases_precompute(bases, c)
+            bases.fixed_c = c
+
     def msm_g1(ctx):
         node = ctx["node"]
         points, scalars = ctx["inputs"][0], ctx["inputs"][1]
@@ -397,6 +415,7 @@ def register_gb300_kernels(registry, *, ir: Any = None) -> None:
             pt = _g1_point(None)
         else:
             bases = rt.bases_for(points.data)
+            _fixed_base(rt, bases, num, ctx["attrs"])
             pt = _g1_point(rt.zk.msm_g1(bases, gs.mtl_buffer, num, window_bits=_window_hint(ctx["attrs"])))
         return {"outputs": {out_id: Buffer(id=out_id, device=Device.CPU, dtype=DType.G1, data=pt)}}
 

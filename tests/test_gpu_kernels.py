@@ -251,3 +251,28 @@ def test_msm_empty_and_errors(gpu_ctx):
         gpu_ctx.msm_g1(bases, ds, 5)
     with pytest.raises(ValueError):
         gpu_ctx.msm_g1(bases, ds, 4, window_bits=3)
+
+
+@pytest.mark.parametrize("kind", ["uniform", "witness"])
+def test_msm_fixed_base_precompute_matches_oracle(gpu_ctx, kind):
+    """Window-shifted fixed-base rows (zk_bases_precompute) give the same point as plain Pippenger."""
+    n = 1 << 14
+    seed = synth.seed_for(2, 14) + 5
+    k = synth.base_dlogs(seed, n)
+    k[3] = 0  # an infinity base
+    s = synth.fr_uniform(seed, n) if kind == "uniform" else synth.fr_witness_like(seed, n)
+    bases_xy = O.g1_fixed_base_mul(O.G1_GENERATOR, k)
+    exp = O.affine_to_ints(O.msm_known_answer(k, s))
+    b = gpu_ctx.bases_from_host(bases_xy)
+    ds = gpu_ctx.to_device(s)
+    gpu_ctx.fr_to_mont(ds, ds, n)
+    assert gpu_ctx.msm_g1(b, ds, n) == exp
+    for c in (5, 8, 13, 16, 20):
+        gpu_ctx.bases_precompute(b, c)
+        assert gpu_ctx.msm_g1(b, ds, n) == exp, c
+        assert gpu_ctx.msm_g1(b, ds, n, window_bits=c) == exp, c
+        # a different explicit window falls back to the plain path
+        assert gpu_ctx.msm_g1(b, ds, n, window_bits=12 if c != 12 else 11) == exp
+        # prefix with offset over the shifted rows
+        m = 777
+        assert gpu_ctx.msm_g1(b, ds, m, offset=100) == O.affine_to_ints(O.msm_known_answer(k[100:100 + m], s[:m]))
