@@ -26,6 +26,7 @@ cores, on the same workload.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -52,7 +53,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--log-n", type=int, default=LOG_N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "msm", "ntt"],
+    ap.add_argument("--only", default="all", choices=["all", "msm", "ntt", "batch"],
                     help="msm / ntt: only that kernel family, no e2e (short commands for profiling)")
     return ap.parse_args()
 
@@ -168,6 +169,9 @@ def run_gpu(args, ranks: Ranks) -> dict:
 
     ctx = N.Context(ranks.local)
     L = N.load()
+    if args.only == "batch":
+        flush = ctx.alloc(FLUSH_BYTES)
+        return {"batch": run_gpu_batch(ctx, args, flush)}
     if args.only == "ntt":
         flush = ctx.alloc(FLUSH_BYTES)
         peaks = load_peaks()
@@ -290,6 +294,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
     clocks = sampler.stop()
     sweep = run_gpu_msm_sweep(ctx, args, flush) if ranks.world == 1 else None
     fixed = run_gpu_fixed_base(ctx, args, flush) if ranks.world == 1 else None
+    batch = run_gpu_batch(ctx, args, flush) if ranks.world == 1 else None
 
     result = {
         "metric": METRIC,
@@ -320,6 +325,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
         "ntt_2_22": ntt22,
         "msm_sweep": sweep,
         "msm_fixed_base_2_20": fixed,
+        "batch_64": batch,
         "clocks": clocks,
     }
     return result
@@ -472,6 +478,145 @@ def run_gpu_fixed_base(ctx, args, flush, log_n: int = 20, calls: int = 16) -> di
     return {"n": n, "calls": calls, "window_bits": c, "first_call_ms": round(first, 3),
             "steady_ms": round(steady, 4), "steady_Mpts_s": round(n / (steady * 1e-3) / 1e6, 2),
             "note": "first call includes the window-shifted base rows (zk_bases_precompute)"}
+
+
+def run_gpu_batch(ctx, args, flush, count: int = 64, lo: int = 10, hi: int = 20) -> dict:
+    """64 MSMs + 64 NTTs with sizes 2^U, U ~ Uniform[lo, hi] (MSM n = round(2^U), NTT n =
+    2^round(U)): plain per-instance calls against the batched engine (direct, then as a
+    CUDA-graph plan, then with autotuned windows / radix splits). Results must agree bit
+    for bit with the per-instance calls."""
+    from pyzkp_gb300 import _native as N
+    from pyzkp_gb300 import synth
+
+    seed = synth.seed_for(3, hi)
+    rng = np.random.default_rng(seed)
+    msm_sizes = [int(round(2 ** u)) for u in rng.uniform(lo, hi, size=count)]
+    ntt_logs = [int(round(u)) for u in rng.uniform(lo, hi, size=count)]
+    nmax = 1 << hi
+    dk = ctx.to_device(synth.base_dlogs(seed, nmax))
+    xy = ctx.alloc(nmax * 64)
+    ctx.g1_fixed_base_mul((1, 2), dk, nmax, xy)
+    bases = ctx.bases_from_device(xy, nmax)
+    del dk, xy
+    total = sum(msm_sizes)
+    flat = ctx.to_device(synth.fr_uniform(seed + 1, total))
+    ctx.fr_to_mont(flat, flat, total)
+    ptrs, off = [], 0
+    for m in msm_sizes:
+        ptrs.append(flat.ptr + 32 * off)
+        off += m
+    reps = max(3, min(args.steps, 5))
+
+    def timed(fn):
+        fn()  # warm-up: pools, tables, plans
+        ts = []
+        for _ in range(reps):
+            ctx.memset(flush, 1)
+            ctx.timer_start()
+            fn()
+            ts.append(ctx.timer_stop())
+        return statistics.median(ts)
+
+    def plain_msm():
+        return [ctx.msm_g1(bases, N.DeviceArray(ctx, m * 32, ptr=p, owned=False), m)
+                for m, p in zip(msm_sizes, ptrs)]
+
+    ref = plain_msm()
+    out = {"instances": count, "msm_sizes_log2_range": [lo, hi], "msm_points": total,
+           "ntt_sizes": {f"2^{k}": ntt_logs.count(k) for k in sorted(set(ntt_logs))}}
+    t_plain = timed(plain_msm)
+    got = ctx.msm_g1_batch(bases, ptrs, msm_sizes)
+    t_batch = timed(lambda: ctx.msm_g1_batch(bases, ptrs, msm_sizes))
+    plan = ctx.msm_plan(bases, msm_sizes, use_graph=True)
+    for j, m in enumerate(msm_sizes):
+        ctx.d2d(plan.slot(j), N.DeviceArray(ctx, m * 32, ptr=ptrs[j], owned=False), m * 32)
+    got_plan = plan.run()
+    t_plan = timed(plan.run)
+    plan_launches = plan.launches()
+    plan.free()
+    # autotuned windows for every size class of the batch (best of c in rule +- 2)
+    t0 = time.perf_counter()
+    tuned = {}
+    for lg in sorted(set(max(1, m - 1).bit_length() for m in msm_sizes)):
+        lg = min(lg, hi)
+        c, _ = ctx.autotune_msm(bases, flat, lg, reps=1)
+        tuned[lg] = c
+    tune_s = time.perf_counter() - t0
+    plan = ctx.msm_plan(bases, msm_sizes, use_graph=True)
+    for j, m in enumerate(msm_sizes):
+        ctx.d2d(plan.slot(j), N.DeviceArray(ctx, m * 32, ptr=ptrs[j], owned=False), m * 32)
+    got_tuned = plan.run()
+    t_tuned = timed(plan.run)
+    plan.free()
+    out["msm"] = {
+        "plain_ms": round(t_plain, 3), "batch_ms": round(t_batch, 3), "plan_graph_ms": round(t_plan, 3),
+        "plan_graph_tuned_ms": round(t_tuned, 3),
+        "plain_Mpts_s": round(total / (t_plain * 1e-3) / 1e6, 2),
+        "batch_Mpts_s": round(total / (t_batch * 1e-3) / 1e6, 2),
+        "plan_graph_Mpts_s": round(total / (t_plan * 1e-3) / 1e6, 2),
+        "plan_graph_tuned_Mpts_s": round(total / (t_tuned * 1e-3) / 1e6, 2),
+        "graph_kernels": plan_launches, "tuned_windows": {f"2^{k}": v for k, v in tuned.items()},
+        "autotune_s": round(tune_s, 2),
+        "bit_exact_vs_plain": got == ref and got_plan == ref and got_tuned == ref,
+    }
+    for lg in tuned:
+        ctx.tune_set_msm_window(lg, 0)
+    del flat
+
+    # NTTs: coset forward (shift 5) of uniform inputs, out of place
+    bufs = []
+    for j, lg in enumerate(ntt_logs):
+        n = 1 << lg
+        a = ctx.to_device(synth.fr_uniform(seed + 100 + j, n))
+        ctx.fr_to_mont(a, a, n)
+        bufs.append((a, ctx.alloc(n * 32)))
+    jobs = [(2, o, a, 1 << lg, lg, ntt_omega(1 << lg), 5) for (a, o), lg in zip(bufs, ntt_logs)]
+    elems = sum(1 << lg for lg in ntt_logs)
+
+    def plain_ntt():
+        for (mode, o, a, ln, lg, om, sh) in jobs:
+            ctx.ntt(mode, o, a, ln, lg, om, sh)
+
+    def snapshot():
+        ctx.sync()
+        return [hashlib.sha256(o.download((1 << lg) * 32).tobytes()).hexdigest() for (_, o, _, _, lg, _, _) in jobs]
+
+    plain_ntt()
+    ref_n = snapshot()
+    t_nplain = timed(plain_ntt)
+    t_nbatch = timed(lambda: ctx.ntt_batch(jobs))
+    ok_batch = snapshot() == ref_n
+    nplan = ctx.ntt_plan(jobs, use_graph=True)
+    t_nplan = timed(nplan.run)
+    ok_plan = snapshot() == ref_n
+    nplan_launches = nplan.launches()
+    nplan.free()
+    t0 = time.perf_counter()
+    splits = {}
+    scratch = ctx.alloc((1 << hi) * 32)
+    for lg in sorted(set(ntt_logs)):
+        splits[lg], _ = ctx.autotune_ntt(scratch, lg, reps=3)
+    del scratch
+    ntune_s = time.perf_counter() - t0
+    nplan = ctx.ntt_plan(jobs, use_graph=True)
+    t_ntuned = timed(nplan.run)
+    ok_tuned = snapshot() == ref_n
+    nplan.free()
+    for lg in splits:
+        ctx.tune_set_ntt_split(lg, [])
+    out["ntt"] = {
+        "mode": "coset forward, shift 5", "elements": elems,
+        "plain_ms": round(t_nplain, 3), "batch_ms": round(t_nbatch, 3), "plan_graph_ms": round(t_nplan, 3),
+        "plan_graph_tuned_ms": round(t_ntuned, 3),
+        "plain_Melem_s": round(elems / (t_nplain * 1e-3) / 1e6, 1),
+        "batch_Melem_s": round(elems / (t_nbatch * 1e-3) / 1e6, 1),
+        "plan_graph_Melem_s": round(elems / (t_nplan * 1e-3) / 1e6, 1),
+        "plan_graph_tuned_Melem_s": round(elems / (t_ntuned * 1e-3) / 1e6, 1),
+        "graph_kernels": nplan_launches, "tuned_splits": {f"2^{k}": v for k, v in splits.items()},
+        "autotune_s": round(ntune_s, 2), "bit_exact_vs_plain": ok_batch and ok_plan and ok_tuned,
+    }
+    bases.free()
+    return out
 
 
 def load_peaks() -> dict:

@@ -133,7 +133,8 @@ int zk_fr_trimmed_len(zk_ctx *ctx, const void *a, size_t n, size_t *out);
  * omega and shift are 32-byte canonical little-endian values. omega must be a
  * primitive n-th root of unity (omega^(n/2) == -1 for n >= 2), else ZK_EINVAL.
  * n = 2^log_n, log_n <= 28 (2-adicity of r, crypto/poly/ntt.py:9,21-22).
- * out holds n elements and must not overlap in.
+ * out holds n elements; it may be the same buffer as in (in place) but must not
+ * overlap it otherwise.
  */
 #define ZK_NTT_EVALS_FROM_COEFFS 0
 #define ZK_NTT_COEFFS_FROM_EVALS 1
@@ -141,6 +142,52 @@ int zk_fr_trimmed_len(zk_ctx *ctx, const void *a, size_t n, size_t *out);
 #define ZK_NTT_COSET_COEFFS_FROM_EVALS 3
 int zk_ntt(zk_ctx *ctx, int mode, void *out_dev, const void *in_dev, size_t in_len, uint32_t log_n,
            const uint8_t omega[32], const uint8_t shift[32]);
+
+/*
+ * Batched NTTs: transform k is zk_ntt(modes[k], outs[k], ins[k], in_lens[k], log_ns[k],
+ * omegas + 32k, shifts + 32k) (shifts may be NULL: all 1), with the same semantics and
+ * errors. All transforms of the batch run their first pass in one launch, their second
+ * pass in the next, and so on (at most three launches up to n = 2^28), each CTA looking
+ * up its transform and tile in a prefix table. Asynchronous on the context stream like
+ * zk_ntt. No reference counterpart (the reference runs one op at a time).
+ */
+int zk_ntt_batch(zk_ctx *ctx, size_t count, const int *modes, void *const *outs, const void *const *ins,
+                 const uint64_t *in_lens, const uint32_t *log_ns, const uint8_t *omegas, const uint8_t *shifts);
+
+/*
+ * NTT batch plan: the descriptors and scratch of a zk_ntt_batch with fixed buffers,
+ * prepared once; with use_graph = 1 a run is one CUDA graph launch. zk_ntt_plan_run
+ * is asynchronous on the context stream; the buffers must outlive the plan.
+ */
+typedef struct zk_ntt_plan zk_ntt_plan;
+int zk_ntt_plan_create(zk_ctx *ctx, size_t count, const int *modes, void *const *outs, const void *const *ins,
+                       const uint64_t *in_lens, const uint32_t *log_ns, const uint8_t *omegas, const uint8_t *shifts,
+                       int use_graph, zk_ntt_plan **out);
+int zk_ntt_plan_run(zk_ntt_plan *plan);
+int zk_ntt_plan_launches(zk_ntt_plan *plan, uint64_t *kernels);
+int zk_ntt_plan_destroy(zk_ntt_plan *plan);
+
+/*
+ * Tuning tables of a context (0 = the built-in rule). MSM: window bits for MSMs whose
+ * ceil(log2 n) is log_n (the reference's fixed rule is max(4, min(16, bitlen(n) - 2)),
+ * runtime/kernels/cpu/kernels.py:553-571; this library's default is clamp(log2 n - 3,
+ * 4, 16)). NTT: radix bits of each pass for 2^log_n (1..4 passes of 1..11 bits summing
+ * to log_n; default: the fewest passes, as equal as possible). zk_tune_get_* report the
+ * effective choice. zk_autotune_msm / zk_autotune_ntt time the candidates on the device
+ * and keep the fastest (best_ms: its time); zk_autotune_save / _load write and read the
+ * tables as JSON ({"msm_window": {"20": 17}, "ntt_split": {"20": [10, 10]}}). Tuning
+ * changes timings only, never results. No reference counterpart.
+ */
+int zk_tune_set_msm_window(zk_ctx *ctx, uint32_t log_n, uint32_t window_bits);
+int zk_tune_get_msm_window(zk_ctx *ctx, uint64_t n, uint32_t *window_bits);
+int zk_tune_set_ntt_split(zk_ctx *ctx, uint32_t log_n, uint32_t npass, const uint32_t *bits);
+int zk_tune_get_ntt_split(zk_ctx *ctx, uint32_t log_n, uint32_t *npass, uint32_t bits[4]);
+int zk_autotune_msm(zk_ctx *ctx, const zk_bases *bases, const void *scalars_dev, uint32_t log_n, int reps,
+                    uint32_t *best_window, double *best_ms);
+int zk_autotune_ntt(zk_ctx *ctx, void *data_dev, uint32_t log_n, int reps, uint32_t *npass, uint32_t bits[4],
+                    double *best_ms);
+int zk_autotune_save(zk_ctx *ctx, const char *path);
+int zk_autotune_load(zk_ctx *ctx, const char *path);
 
 /*
  * zk_ntt without any device allocation. No counterpart in the reference: it is for
@@ -190,6 +237,59 @@ int zk_bases_count(const zk_bases *b, size_t *n);
  */
 int zk_msm_g1(zk_ctx *ctx, const zk_bases *bases, size_t offset, const void *scalars_dev, size_t n,
               int scalars_mont, uint32_t window_bits, uint8_t out_xy[64], int *out_is_inf);
+
+/*
+ * Batched G1 MSM: out[k] = sum_i scalars[k][i] * bases[k][offsets[k] + i] for i < sizes[k],
+ * k < count. Replaces the per-instance loops of MSM_G1_BATCH and KZG_BATCH_COMMIT
+ * (_msm_g1_batch / _kzg_batch_commit, runtime/kernels/cpu/kernels.py:441-496, which call
+ * msm_pippenger_batch, crypto/msm/pippenger.py:124-214, on the prefix points[:len(s)];
+ * Metal: runtime/kernels/metal/kernels.py:22-82). Instances with the same window size
+ * share one pipeline (one launch per stage for all of them); instances of size 0 give
+ * infinity. bases[k] may repeat one handle; offsets may be NULL (all 0). Results as in
+ * zk_msm_g1: out_xy holds count * 64 bytes, out_is_inf count flags. window_bits: 0 =
+ * tuned or automatic per instance, else 4..20 for all.
+ */
+int zk_msm_g1_batch(zk_ctx *ctx, size_t count, const zk_bases *const *bases, const uint64_t *offsets,
+                    const void *const *scalars_dev, const uint64_t *sizes, int scalars_mont, uint32_t window_bits,
+                    uint8_t *out_xy, int32_t *out_is_inf);
+
+/*
+ * G2 (the sextic twist over Fq2 = Fq[u]/(u^2 + 1)): MSM_G2, computed by the reference on
+ * the CPU only (_msm_g2 / _msm_g2_impl, runtime/kernels/cpu/kernels.py:338-348,574-582;
+ * Groth16's b_query_g2 * w, protocols/groth16/prove.py:76-77). Bases are affine canonical
+ * (x.c0, x.c1, y.c0, y.c1), 128 bytes each, element c0 + c1 u as py_ecc's FQ2([c0, c1]);
+ * all-zero is infinity. The handle is freed by zk_bases_destroy and is accepted only by
+ * the G2 calls. Results are 128 bytes in the same layout (all zero and *out_is_inf = 1 for
+ * infinity). Same pipeline as G1 with Fq2 coordinates; no fixed-base mode.
+ */
+int zk_bases_g2_create(zk_ctx *ctx, const void *xy_canonical_host, size_t n, zk_bases **out);
+/* out[i] = [k_i] P on G2 (P host canonical, 128 bytes; k and out as zk_g1_fixed_base_mul). */
+int zk_g2_fixed_base_mul(zk_ctx *ctx, const uint8_t point_xy[128], const void *k_dev, size_t n, void *out_xy_dev);
+int zk_msm_g2(zk_ctx *ctx, const zk_bases *bases, size_t offset, const void *scalars_dev, size_t n,
+              int scalars_mont, uint32_t window_bits, uint8_t out_xy[128], int *out_is_inf);
+int zk_msm_g2_batch(zk_ctx *ctx, size_t count, const zk_bases *const *bases, const uint64_t *offsets,
+                    const void *const *scalars_dev, const uint64_t *sizes, int scalars_mont, uint32_t window_bits,
+                    uint8_t *out_xy, int32_t *out_is_inf);
+
+/*
+ * Batch plan: a zk_msm_g1_batch with fixed shapes, prepared once and run many times
+ * (serving, repeated commitments). The plan owns one scalar slot per instance
+ * (zk_msm_plan_scalars: device address of sizes[k] elements, filled by the caller by
+ * zk_h2d or by a kernel such as zk_ntt writing into it), all scratch and pinned result
+ * buffers, so a run allocates nothing. With use_graph = 1 the device work of a run is
+ * captured once as a CUDA graph and each run is one graph launch. The bases handles
+ * must outlive the plan. No reference counterpart (the reference rebuilds its batch per
+ * call).
+ */
+typedef struct zk_msm_plan zk_msm_plan;
+int zk_msm_plan_create(zk_ctx *ctx, size_t count, const zk_bases *const *bases, const uint64_t *offsets,
+                       const uint64_t *sizes, int scalars_mont, uint32_t window_bits, int use_graph,
+                       zk_msm_plan **out);
+int zk_msm_plan_scalars(zk_msm_plan *plan, size_t index, void **scalars_dev);
+int zk_msm_plan_run(zk_msm_plan *plan, uint8_t *out_xy, int32_t *out_is_inf);
+/* Kernel launches one run makes (the nodes of its graph). */
+int zk_msm_plan_launches(zk_msm_plan *plan, uint64_t *kernels);
+int zk_msm_plan_destroy(zk_msm_plan *plan);
 
 /*
  * out[i] = [k_i] P for one affine point P (host, canonical) and n scalars k_i

@@ -21,10 +21,14 @@
  *     sparse "dict" path with gap multiplications, Horner acc = acc*2^w + sum.
  *   - the G1 group law of py_ecc.optimized_bn128 (crypto/ecc/bn254.py:9-28) in
  *     Jacobian coordinates, complete w.r.t. infinity / P == Q / P == -Q.
+ *   - the G2 group law (crypto/ecc/bn254.py g2_add / g2_mul over py_ecc's FQ2 with
+ *     u^2 = -1) in Jacobian coordinates over Fq2, and MSM_G2 as the plain sum of
+ *     scalar multiples (_msm_g2_impl, runtime/kernels/cpu/kernels.py:574-582).
  *
  * Layout at the ABI: field elements are 4 little-endian uint64 limbs of the
  * canonical value; affine G1 points are 8 limbs (x then y), the point at
- * infinity is (0, 0) (not on y^2 = x^3 + 3).
+ * infinity is (0, 0) (not on y^2 = x^3 + 3). Affine G2 points are 16 limbs
+ * (x.c0, x.c1, y.c0, y.c1 for x = x.c0 + x.c1 u), infinity all zero.
  *
  * Portable C11 + pthreads + unsigned __int128 (gcc on x86_64 and aarch64).
  */
@@ -853,3 +857,280 @@ int orc_to_from_mont(int which, int dir, const uint64_t *in, uint64_t *out, size
 }
 
 int orc_num_threads(void) { return resolve_threads(0); }
+
+/* ------------------------------------------------------------------------- */
+/* G2 over Fq2 = Fq[u] / (u^2 + 1), Jacobian coordinates (Montgomery)          */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    uint64_t a[4], b[4]; /* a + b u */
+} fq2_t;
+
+typedef struct {
+    fq2_t X, Y, Z;
+} jac2;
+
+static void f2add(fq2_t *r, const fq2_t *x, const fq2_t *y) {
+    fadd(&FQ, r->a, x->a, y->a);
+    fadd(&FQ, r->b, x->b, y->b);
+}
+
+static void f2sub(fq2_t *r, const fq2_t *x, const fq2_t *y) {
+    fsub(&FQ, r->a, x->a, y->a);
+    fsub(&FQ, r->b, x->b, y->b);
+}
+
+/* (xa + xb u)(ya + yb u) = (xa ya - xb yb) + (xa yb + xb ya) u (schoolbook, 4 products) */
+static void f2mul(fq2_t *r, const fq2_t *x, const fq2_t *y) {
+    uint64_t t0[4], t1[4], t2[4], t3[4];
+    fmul(&FQ, t0, x->a, y->a);
+    fmul(&FQ, t1, x->b, y->b);
+    fmul(&FQ, t2, x->a, y->b);
+    fmul(&FQ, t3, x->b, y->a);
+    fsub(&FQ, r->a, t0, t1);
+    fadd(&FQ, r->b, t2, t3);
+}
+
+static int f2is_zero(const fq2_t *x) { return is_zero4(x->a) && is_zero4(x->b); }
+
+/* 1 / (a + b u) = (a - b u) / (a^2 + b^2) */
+static void f2inv(fq2_t *r, const fq2_t *x) {
+    uint64_t t0[4], t1[4], z[4] = {0, 0, 0, 0};
+    fmul(&FQ, t0, x->a, x->a);
+    fmul(&FQ, t1, x->b, x->b);
+    fadd(&FQ, t0, t0, t1);
+    finv(&FQ, t1, t0);
+    fmul(&FQ, r->a, x->a, t1);
+    fmul(&FQ, t0, x->b, t1);
+    fsub(&FQ, r->b, z, t0);
+}
+
+static void jac2_set_inf(jac2 *p) {
+    memcpy(p->X.a, FQ.one, 32);
+    memset(p->X.b, 0, 32);
+    memcpy(p->Y.a, FQ.one, 32);
+    memset(p->Y.b, 0, 32);
+    memset(&p->Z, 0, sizeof(fq2_t));
+}
+
+static int jac2_is_inf(const jac2 *p) { return f2is_zero(&p->Z); }
+
+static void jac2_dbl(jac2 *r, const jac2 *p) {
+    if (jac2_is_inf(p)) {
+        *r = *p;
+        return;
+    }
+    fq2_t A, B, C, S, M, t, X3, Y3, Z3;
+    f2mul(&A, &p->X, &p->X);
+    f2mul(&B, &p->Y, &p->Y);
+    f2mul(&C, &B, &B);
+    f2mul(&S, &p->X, &B);
+    f2add(&S, &S, &S);
+    f2add(&S, &S, &S); /* 4 X B */
+    f2add(&M, &A, &A);
+    f2add(&M, &M, &A); /* 3 A */
+    f2mul(&X3, &M, &M);
+    f2sub(&X3, &X3, &S);
+    f2sub(&X3, &X3, &S);
+    f2sub(&t, &S, &X3);
+    f2mul(&Y3, &M, &t);
+    f2add(&C, &C, &C);
+    f2add(&C, &C, &C);
+    f2add(&C, &C, &C); /* 8 C */
+    f2sub(&Y3, &Y3, &C);
+    f2mul(&Z3, &p->Y, &p->Z);
+    f2add(&Z3, &Z3, &Z3);
+    r->X = X3;
+    r->Y = Y3;
+    r->Z = Z3;
+}
+
+static void jac2_add(jac2 *r, const jac2 *p, const jac2 *q) {
+    if (jac2_is_inf(p)) {
+        *r = *q;
+        return;
+    }
+    if (jac2_is_inf(q)) {
+        *r = *p;
+        return;
+    }
+    fq2_t Z1Z1, Z2Z2, U1, U2, S1, S2, H, R, t;
+    f2mul(&Z1Z1, &p->Z, &p->Z);
+    f2mul(&Z2Z2, &q->Z, &q->Z);
+    f2mul(&U1, &p->X, &Z2Z2);
+    f2mul(&U2, &q->X, &Z1Z1);
+    f2mul(&t, &q->Z, &Z2Z2);
+    f2mul(&S1, &p->Y, &t);
+    f2mul(&t, &p->Z, &Z1Z1);
+    f2mul(&S2, &q->Y, &t);
+    f2sub(&H, &U2, &U1);
+    f2sub(&R, &S2, &S1);
+    if (f2is_zero(&H)) {
+        if (f2is_zero(&R)) {
+            jac2_dbl(r, p);
+        } else {
+            jac2_set_inf(r);
+        }
+        return;
+    }
+    fq2_t HH, HHH, V, X3, Y3, Z3;
+    f2mul(&HH, &H, &H);
+    f2mul(&HHH, &H, &HH);
+    f2mul(&V, &U1, &HH);
+    f2mul(&X3, &R, &R);
+    f2sub(&X3, &X3, &HHH);
+    f2sub(&X3, &X3, &V);
+    f2sub(&X3, &X3, &V);
+    f2sub(&t, &V, &X3);
+    f2mul(&Y3, &R, &t);
+    f2mul(&t, &S1, &HHH);
+    f2sub(&Y3, &Y3, &t);
+    f2mul(&Z3, &p->Z, &q->Z);
+    f2mul(&Z3, &Z3, &H);
+    r->X = X3;
+    r->Y = Y3;
+    r->Z = Z3;
+}
+
+static void jac2_from_affine(jac2 *r, const uint64_t P[16]) {
+    if (is_zero4(P) && is_zero4(P + 4) && is_zero4(P + 8) && is_zero4(P + 12)) {
+        jac2_set_inf(r);
+        return;
+    }
+    to_mont(&FQ, r->X.a, P);
+    to_mont(&FQ, r->X.b, P + 4);
+    to_mont(&FQ, r->Y.a, P + 8);
+    to_mont(&FQ, r->Y.b, P + 12);
+    memcpy(r->Z.a, FQ.one, 32);
+    memset(r->Z.b, 0, 32);
+}
+
+static void jac2_to_affine(uint64_t out[16], const jac2 *p) {
+    if (jac2_is_inf(p)) {
+        memset(out, 0, 128);
+        return;
+    }
+    fq2_t zi, zi2, zi3, x, y;
+    f2inv(&zi, &p->Z);
+    f2mul(&zi2, &zi, &zi);
+    f2mul(&zi3, &zi2, &zi);
+    f2mul(&x, &p->X, &zi2);
+    f2mul(&y, &p->Y, &zi3);
+    from_mont(&FQ, out, x.a);
+    from_mont(&FQ, out + 4, x.b);
+    from_mont(&FQ, out + 8, y.a);
+    from_mont(&FQ, out + 12, y.b);
+}
+
+static void jac2_mul(jac2 *r, const jac2 *p, const uint64_t k[4]) {
+    uint64_t kk[4];
+    memcpy(kk, k, 32);
+    while (geq(kk, FR.p)) sub4(kk, kk, FR.p);
+    jac2 acc;
+    jac2_set_inf(&acc);
+    for (int i = 255; i >= 0; i--) {
+        jac2_dbl(&acc, &acc);
+        if ((kk[i >> 6] >> (i & 63)) & 1) jac2_add(&acc, &acc, p);
+    }
+    *r = acc;
+}
+
+/* out = [k] P on affine canonical G2 points (k reduced mod r). */
+int orc_g2_mul(const uint64_t P[16], const uint64_t k[4], uint64_t out[16]) {
+    init_once();
+    jac2 base, acc;
+    jac2_from_affine(&base, P);
+    jac2_mul(&acc, &base, k);
+    jac2_to_affine(out, &acc);
+    return 0;
+}
+
+/* out = P + Q on affine canonical G2 points */
+int orc_g2_add(const uint64_t P[16], const uint64_t Q[16], uint64_t out[16]) {
+    init_once();
+    jac2 a, b;
+    jac2_from_affine(&a, P);
+    jac2_from_affine(&b, Q);
+    jac2_add(&a, &a, &b);
+    jac2_to_affine(out, &a);
+    return 0;
+}
+
+typedef struct {
+    const uint64_t *bases; /* msm: n affine canonical G2 points (16 limbs each) */
+    const uint64_t *k;     /* n scalars */
+    uint64_t *out;         /* fixed-base: n affine canonical results */
+    const jac2 *table;     /* fixed-base: table[j * 16 + d] = d * 2^(4 j) * P, j < 64 */
+    jac2 *total;           /* msm: running sum of the per-thread partial sums */
+    pthread_mutex_t mu;
+} g2_ctx;
+
+static void g2_fb_range(void *c, size_t lo, size_t hi) {
+    g2_ctx *x = (g2_ctx *)c;
+    for (size_t i = lo; i < hi; i++) {
+        uint64_t kk[4];
+        memcpy(kk, x->k + 4 * i, 32);
+        while (geq(kk, FR.p)) sub4(kk, kk, FR.p);
+        jac2 a;
+        jac2_set_inf(&a);
+        for (int j = 0; j < 64; j++) {
+            uint32_t d = (uint32_t)((kk[j >> 4] >> (4 * (j & 15))) & 0xf);
+            if (d) jac2_add(&a, &a, &x->table[j * 16 + d]);
+        }
+        jac2_to_affine(x->out + 16 * i, &a);
+    }
+}
+
+/* out[i] = [k_i] P (affine canonical G2), from a table of 4-bit windows. */
+int orc_g2_fixed_base_mul(const uint64_t P[16], const uint64_t *k, size_t n, uint64_t *out, int nthreads) {
+    init_once();
+    jac2 *table = (jac2 *)malloc(sizeof(jac2) * 64 * 16);
+    if (!table) return -3;
+    jac2 base;
+    jac2_from_affine(&base, P);
+    for (int j = 0; j < 64; j++) {
+        jac2_set_inf(&table[j * 16]);
+        for (int d = 1; d < 16; d++) jac2_add(&table[j * 16 + d], &table[j * 16 + d - 1], &base);
+        for (int b = 0; b < 4; b++) jac2_dbl(&base, &base);
+    }
+    g2_ctx x;
+    memset(&x, 0, sizeof(x));
+    x.k = k;
+    x.out = out;
+    x.table = table;
+    parallel_for(n, nthreads, g2_fb_range, &x);
+    free(table);
+    return 0;
+}
+
+static void g2_msm_range(void *c, size_t lo, size_t hi) {
+    g2_ctx *x = (g2_ctx *)c;
+    jac2 acc;
+    jac2_set_inf(&acc);
+    for (size_t i = lo; i < hi; i++) {
+        jac2 p, t;
+        jac2_from_affine(&p, x->bases + 16 * i);
+        jac2_mul(&t, &p, x->k + 4 * i);
+        jac2_add(&acc, &acc, &t);
+    }
+    pthread_mutex_lock(&x->mu);
+    jac2_add(x->total, x->total, &acc);
+    pthread_mutex_unlock(&x->mu);
+}
+
+/* MSM_G2 as sum_i [s_i] P_i (runtime/kernels/cpu/kernels.py:574-582; every result is the
+ * same unique point whatever the method). bases: n affine canonical G2 points. */
+int orc_g2_msm(const uint64_t *bases, const uint64_t *scalars, size_t n, uint64_t out[16], int nthreads) {
+    init_once();
+    g2_ctx x;
+    jac2 total;
+    memset(&x, 0, sizeof(x));
+    jac2_set_inf(&total);
+    x.bases = bases;
+    x.k = scalars;
+    x.total = &total;
+    pthread_mutex_init(&x.mu, NULL);
+    parallel_for(n, nthreads, g2_msm_range, &x);
+    pthread_mutex_destroy(&x.mu);
+    jac2_to_affine(out, &total);
+    return 0;
+}

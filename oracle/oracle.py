@@ -59,8 +59,13 @@ def lib() -> ctypes.CDLL:
         L.orc_g1_add.argtypes = [P, P, P]
         L.orc_fr_dot.argtypes = [P, P, ctypes.c_size_t, P]
         L.orc_to_from_mont.argtypes = [ctypes.c_int, ctypes.c_int, P, P, ctypes.c_size_t, ctypes.c_int]
+        L.orc_g2_mul.argtypes = [P, P, P]
+        L.orc_g2_add.argtypes = [P, P, P]
+        L.orc_g2_fixed_base_mul.argtypes = [P, P, ctypes.c_size_t, P, ctypes.c_int]
+        L.orc_g2_msm.argtypes = [P, P, ctypes.c_size_t, P, ctypes.c_int]
         for f in (L.orc_ntt_op, L.orc_msm_pippenger, L.orc_g1_fixed_base_mul, L.orc_g1_mul, L.orc_g1_add,
-                  L.orc_fr_dot, L.orc_to_from_mont, L.orc_num_threads):
+                  L.orc_fr_dot, L.orc_to_from_mont, L.orc_num_threads, L.orc_g2_mul, L.orc_g2_add,
+                  L.orc_g2_fixed_base_mul, L.orc_g2_msm):
             f.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -177,6 +182,68 @@ G1_GENERATOR = np.array([1, 0, 0, 0, 2, 0, 0, 0], dtype=np.uint64)
 def msm_known_answer(dlogs: np.ndarray, scalars: np.ndarray) -> np.ndarray:
     """Independent exact check for bases P_i = [k_i]G: MSM(P, s) = [sum k_i s_i mod r] G."""
     return g1_mul(G1_GENERATOR, fr_dot(dlogs, scalars))
+
+
+# G2 generator (crypto/ecc/bn254.py G2_GENERATOR = py_ecc G2; the EIP-197 constants):
+# x = x0 + x1 u, y = y0 + y1 u as 16 limbs (x0, x1, y0, y1)
+G2_GENERATOR = np.concatenate([_limbs(v) for v in (
+    10857046999023057135944570762232829481370756359578518086990519993285655852781,
+    11559732032986387107991004021392285783925812861821192530917403151452391805634,
+    8495653923123431417604973247489272438418190587263600148770280649306958101930,
+    4082367875863433681332203403145435568316851327593401208105741076214120093531)])
+
+
+def g2_mul(point: np.ndarray, k: int) -> np.ndarray:
+    """[k] P on G2 (affine canonical 16 limbs; all zero = infinity)."""
+    p = np.ascontiguousarray(point, dtype=np.uint64).reshape(16)
+    kk = _limbs(k % FR_MODULUS)
+    out = np.zeros(16, dtype=np.uint64)
+    lib().orc_g2_mul(_ptr(p), _ptr(kk), _ptr(out))
+    return out
+
+
+def g2_add(p: np.ndarray, q: np.ndarray) -> np.ndarray:
+    a = np.ascontiguousarray(p, dtype=np.uint64).reshape(16)
+    b = np.ascontiguousarray(q, dtype=np.uint64).reshape(16)
+    out = np.zeros(16, dtype=np.uint64)
+    lib().orc_g2_add(_ptr(a), _ptr(b), _ptr(out))
+    return out
+
+
+def g2_fixed_base_mul(point: np.ndarray, k: np.ndarray, nthreads: int = 0) -> np.ndarray:
+    """[k_i] P on G2 for many k_i (synthetic G2 bases [k_i]G2)."""
+    p = np.ascontiguousarray(point, dtype=np.uint64).reshape(16)
+    kk = np.ascontiguousarray(k, dtype=np.uint64).reshape(-1, 4)
+    out = np.zeros((kk.shape[0], 16), dtype=np.uint64)
+    rc = lib().orc_g2_fixed_base_mul(_ptr(p), _ptr(kk), kk.shape[0], _ptr(out), int(nthreads))
+    if rc != 0:
+        raise ValueError(f"orc_g2_fixed_base_mul failed ({rc})")
+    return out
+
+
+def g2_msm(bases: np.ndarray, scalars: np.ndarray, nthreads: int = 0) -> np.ndarray:
+    """MSM_G2 (runtime/kernels/cpu/kernels.py:574-582) as the plain sum of [s_i] P_i."""
+    b = np.ascontiguousarray(bases, dtype=np.uint64).reshape(-1, 16)
+    s = np.ascontiguousarray(scalars, dtype=np.uint64).reshape(-1, 4)
+    if b.shape[0] != s.shape[0]:
+        raise ValueError("points and scalars length mismatch")
+    out = np.zeros(16, dtype=np.uint64)
+    rc = lib().orc_g2_msm(_ptr(b), _ptr(s), b.shape[0], _ptr(out), int(nthreads))
+    if rc != 0:
+        raise ValueError(f"orc_g2_msm failed ({rc})")
+    return out
+
+
+def g2_msm_known_answer(dlogs: np.ndarray, scalars: np.ndarray) -> np.ndarray:
+    """For G2 bases [k_i]G2: MSM = [sum k_i s_i mod r] G2."""
+    return g2_mul(G2_GENERATOR, fr_dot(dlogs, scalars))
+
+
+def g2_to_ints(p: np.ndarray):
+    """16 limbs -> ((x0, x1), (y0, y1)) canonical ints."""
+    b = np.ascontiguousarray(p, dtype="<u8").tobytes()
+    v = [int.from_bytes(b[32 * i:32 * i + 32], "little") for i in range(4)]
+    return (v[0], v[1]), (v[2], v[3])
 
 
 def affine_to_ints(p: np.ndarray):

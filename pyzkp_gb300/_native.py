@@ -32,7 +32,12 @@ EXPORTED_SYMBOLS = (
     "zk_bases_create", "zk_bases_create_dev", "zk_bases_destroy", "zk_bases_count", "zk_msm_g1",
     "zk_g1_fixed_base_mul", "zk_memset", "zk_launch_count", "zk_prof_enable", "zk_prof_reset", "zk_prof_count",
     "zk_prof_get", "zk_timer_start", "zk_timer_stop", "zk_msm_last_stats", "zk_imad_peak", "zk_d2d",
-    "zk_fr_trimmed_len", "zk_ntt_noalloc", "zk_imad_probe", "zk_bases_precompute",
+    "zk_fr_trimmed_len", "zk_ntt_noalloc", "zk_imad_probe", "zk_bases_precompute", "zk_msm_g1_batch",
+    "zk_msm_plan_create", "zk_msm_plan_scalars", "zk_msm_plan_run", "zk_msm_plan_launches", "zk_msm_plan_destroy",
+    "zk_ntt_batch", "zk_ntt_plan_create", "zk_ntt_plan_run", "zk_ntt_plan_launches", "zk_ntt_plan_destroy",
+    "zk_tune_set_msm_window", "zk_tune_get_msm_window", "zk_tune_set_ntt_split", "zk_tune_get_ntt_split",
+    "zk_autotune_msm", "zk_autotune_ntt", "zk_autotune_save", "zk_autotune_load", "zk_bases_g2_create",
+    "zk_msm_g2", "zk_msm_g2_batch", "zk_g2_fixed_base_mul",
 )
 
 _lib: Optional[ctypes.CDLL] = None
@@ -98,6 +103,29 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_ntt_noalloc": ([P, I, P, P, S, U32, P, P], I),
             "zk_imad_probe": ([P, I, ctypes.POINTER(ctypes.c_double)], I),
             "zk_bases_precompute": ([P, P, U32], I),
+            "zk_msm_g1_batch": ([P, S, PP, P, PP, P, I, U32, P, P], I),
+            "zk_msm_plan_create": ([P, S, PP, P, P, I, U32, I, PP], I),
+            "zk_msm_plan_scalars": ([P, S, PP], I),
+            "zk_msm_plan_run": ([P, P, P], I),
+            "zk_msm_plan_launches": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
+            "zk_msm_plan_destroy": ([P], I),
+            "zk_ntt_batch": ([P, S, P, PP, PP, P, P, P, P], I),
+            "zk_ntt_plan_create": ([P, S, P, PP, PP, P, P, P, P, I, PP], I),
+            "zk_ntt_plan_run": ([P], I),
+            "zk_ntt_plan_launches": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
+            "zk_ntt_plan_destroy": ([P], I),
+            "zk_tune_set_msm_window": ([P, U32, U32], I),
+            "zk_tune_get_msm_window": ([P, ctypes.c_uint64, ctypes.POINTER(U32)], I),
+            "zk_tune_set_ntt_split": ([P, U32, U32, P], I),
+            "zk_tune_get_ntt_split": ([P, U32, ctypes.POINTER(U32), P], I),
+            "zk_autotune_msm": ([P, P, P, U32, I, ctypes.POINTER(U32), ctypes.POINTER(ctypes.c_double)], I),
+            "zk_autotune_ntt": ([P, P, U32, I, ctypes.POINTER(U32), P, ctypes.POINTER(ctypes.c_double)], I),
+            "zk_autotune_save": ([P, ctypes.c_char_p], I),
+            "zk_autotune_load": ([P, ctypes.c_char_p], I),
+            "zk_bases_g2_create": ([P, P, S, PP], I),
+            "zk_msm_g2": ([P, P, S, P, S, I, U32, P, ctypes.POINTER(ctypes.c_int)], I),
+            "zk_msm_g2_batch": ([P, S, PP, P, PP, P, I, U32, P, P], I),
+            "zk_g2_fixed_base_mul": ([P, P, P, S, P], I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -122,17 +150,23 @@ def check(rc: int, what: str = "") -> None:
 class DeviceArray:
     """An owned device allocation of ``nbytes`` (freed with the context's pool)."""
 
-    __slots__ = ("ctx", "ptr", "nbytes", "__weakref__")
+    __slots__ = ("ctx", "ptr", "nbytes", "owned", "__weakref__")
 
-    def __init__(self, ctx: "Context", nbytes: int) -> None:
+    def __init__(self, ctx: "Context", nbytes: int, ptr: Optional[int] = None, owned: bool = True) -> None:
+        """Allocate ``nbytes``; or, with ``ptr`` given and ``owned=False``, view memory that
+        something else owns (a plan's scalar slot), which free() leaves alone."""
         self.ctx = ctx
         self.nbytes = int(nbytes)
+        self.owned = owned
+        if ptr is not None:
+            self.ptr = ptr
+            return
         p = ctypes.c_void_p()
         check(load().zk_alloc(ctx.handle, max(16, self.nbytes), ctypes.byref(p)), "zk_alloc")
         self.ptr = p.value
 
     def free(self) -> None:
-        if self.ptr is not None and self.ctx.handle is not None:
+        if self.owned and self.ptr is not None and self.ctx.handle is not None:
             load().zk_free(self.ctx.handle, self.ptr)
         self.ptr = None
 
@@ -193,6 +227,93 @@ class Bases:
     def free(self) -> None:
         if self.handle is not None:
             load().zk_bases_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self) -> None:
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _points_from(out: np.ndarray, inf: np.ndarray):
+    res = []
+    for k in range(out.shape[0]):
+        if inf[k]:
+            res.append(None)
+        else:
+            b = out[k].tobytes()
+            res.append((int.from_bytes(b[:32], "little"), int.from_bytes(b[32:], "little")))
+    return res
+
+
+def _g2_from(b: bytes):
+    v = [int.from_bytes(b[32 * i:32 * i + 32], "little") for i in range(4)]
+    return (v[0], v[1]), (v[2], v[3])
+
+
+def _fr_bytes(v: int) -> bytes:
+    return (int(v) % (1 << 256)).to_bytes(32, "little")
+
+
+class NttPlan:
+    """A prepared NTT batch (zk_ntt_plan_*); run() is asynchronous on the context stream."""
+
+    def __init__(self, ctx: "Context", handle: int, buffers) -> None:
+        self.ctx = ctx
+        self.handle = handle
+        self._buffers = buffers  # keep the device buffers alive as long as the plan
+
+    def run(self) -> None:
+        check(load().zk_ntt_plan_run(self.handle), "zk_ntt_plan_run")
+
+    def launches(self) -> int:
+        v = ctypes.c_uint64()
+        check(load().zk_ntt_plan_launches(self.handle, ctypes.byref(v)), "zk_ntt_plan_launches")
+        return int(v.value)
+
+    def free(self) -> None:
+        if self.handle is not None:
+            load().zk_ntt_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self) -> None:
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class MsmPlan:
+    """A prepared MSM batch (zk_msm_plan_*): plan-owned scalar slots, optional CUDA graph."""
+
+    def __init__(self, ctx: "Context", handle: int, sizes, bases) -> None:
+        self.ctx = ctx
+        self.handle = handle
+        self.sizes = sizes
+        self._bases = bases  # keep the bases alive as long as the plan
+
+    def slot(self, index: int) -> DeviceArray:
+        """Device view of instance ``index``'s scalar slot (sizes[index] elements)."""
+        p = ctypes.c_void_p()
+        check(load().zk_msm_plan_scalars(self.handle, int(index), ctypes.byref(p)), "zk_msm_plan_scalars")
+        return DeviceArray(self.ctx, self.sizes[index] * 32, ptr=p.value or 0, owned=False)
+
+    def run(self):
+        count = len(self.sizes)
+        out = np.zeros((max(count, 1), 64), dtype=np.uint8)
+        inf = np.zeros(max(count, 1), dtype=np.int32)
+        check(load().zk_msm_plan_run(self.handle, out.ctypes.data, inf.ctypes.data), "zk_msm_plan_run")
+        return _points_from(out[:count], inf[:count])
+
+    def launches(self) -> int:
+        v = ctypes.c_uint64()
+        check(load().zk_msm_plan_launches(self.handle, ctypes.byref(v)), "zk_msm_plan_launches")
+        return int(v.value)
+
+    def free(self) -> None:
+        if self.handle is not None:
+            load().zk_msm_plan_destroy(self.handle)
             self.handle = None
 
     def __del__(self) -> None:
@@ -326,6 +447,39 @@ class Context:
         check(load().zk_bases_create(self.handle, a.ctypes.data, a.shape[0], ctypes.byref(h)), "zk_bases_create")
         return Bases(self, h.value, a.shape[0])
 
+    def bases_g2_from_host(self, xy: np.ndarray) -> Bases:
+        """G2 bases: rows of 16 uint64 limbs (x.c0, x.c1, y.c0, y.c1 canonical; zero = infinity)."""
+        a = np.ascontiguousarray(xy, dtype=np.uint64).reshape(-1, 16)
+        h = ctypes.c_void_p()
+        check(load().zk_bases_g2_create(self.handle, a.ctypes.data, a.shape[0], ctypes.byref(h)),
+              "zk_bases_g2_create")
+        return Bases(self, h.value, a.shape[0])
+
+    def msm_g2(self, bases: Bases, scalars: DeviceArray, n: int, *, offset: int = 0, scalars_mont: bool = True,
+               window_bits: int = 0):
+        """Returns ((x0, x1), (y0, y1)) canonical ints, or None for the point at infinity."""
+        out = (ctypes.c_uint8 * 128)()
+        inf = ctypes.c_int()
+        check(load().zk_msm_g2(self.handle, bases.handle, int(offset), scalars.ptr, int(n), 1 if scalars_mont else 0,
+                               int(window_bits), out, ctypes.byref(inf)), "zk_msm_g2")
+        return None if inf.value else _g2_from(bytes(out))
+
+    def msm_g2_batch(self, bases, scalars, sizes, *, offsets=None, scalars_mont: bool = True,
+                     window_bits: int = 0):
+        count = len(sizes)
+        if isinstance(bases, Bases):
+            bases = [bases] * count
+        bh = (ctypes.c_void_p * count)(*[b.handle for b in bases])
+        sp = (ctypes.c_void_p * count)(*[getattr(s, "ptr", s) for s in scalars])
+        sz = np.ascontiguousarray(sizes, dtype=np.uint64)
+        off = None if offsets is None else np.ascontiguousarray(offsets, dtype=np.uint64)
+        out = np.zeros((max(count, 1), 128), dtype=np.uint8)
+        inf = np.zeros(max(count, 1), dtype=np.int32)
+        check(load().zk_msm_g2_batch(self.handle, count, bh, None if off is None else off.ctypes.data, sp,
+                                     sz.ctypes.data, 1 if scalars_mont else 0, int(window_bits), out.ctypes.data,
+                                     inf.ctypes.data), "zk_msm_g2_batch")
+        return [None if inf[k] else _g2_from(out[k].tobytes()) for k in range(count)]
+
     def bases_precompute(self, bases: "Bases", window_bits: int) -> None:
         """Window-shifted rows for fixed-base MSMs on ``bases`` (zk_bases_precompute)."""
         check(load().zk_bases_precompute(self.handle, bases.handle, int(window_bits)), "zk_bases_precompute")
@@ -346,6 +500,115 @@ class Context:
             return None
         b = bytes(out)
         return int.from_bytes(b[:32], "little"), int.from_bytes(b[32:], "little")
+
+    def msm_g1_batch(self, bases, scalars, sizes, *, offsets=None, scalars_mont: bool = True,
+                     window_bits: int = 0):
+        """Batched MSM (zk_msm_g1_batch). ``bases``: one Bases or a list (one per instance);
+        ``scalars``: list of DeviceArray (or device pointers); ``sizes``: list of lengths.
+        Returns a list of (x, y) canonical ints or None (infinity)."""
+        count = len(sizes)
+        if isinstance(bases, Bases):
+            bases = [bases] * count
+        bh = (ctypes.c_void_p * count)(*[b.handle for b in bases])
+        sp = (ctypes.c_void_p * count)(*[getattr(s, "ptr", s) for s in scalars])
+        sz = np.ascontiguousarray(sizes, dtype=np.uint64)
+        off = None if offsets is None else np.ascontiguousarray(offsets, dtype=np.uint64)
+        out = np.zeros((max(count, 1), 64), dtype=np.uint8)
+        inf = np.zeros(max(count, 1), dtype=np.int32)
+        check(load().zk_msm_g1_batch(self.handle, count, bh, None if off is None else off.ctypes.data, sp,
+                                     sz.ctypes.data, 1 if scalars_mont else 0, int(window_bits), out.ctypes.data,
+                                     inf.ctypes.data), "zk_msm_g1_batch")
+        return _points_from(out[:count], inf[:count])
+
+    def msm_plan(self, bases, sizes, *, offsets=None, scalars_mont: bool = True, window_bits: int = 0,
+                 use_graph: bool = True) -> "MsmPlan":
+        count = len(sizes)
+        if isinstance(bases, Bases):
+            bases = [bases] * count
+        bh = (ctypes.c_void_p * count)(*[b.handle for b in bases])
+        sz = np.ascontiguousarray(sizes, dtype=np.uint64)
+        off = None if offsets is None else np.ascontiguousarray(offsets, dtype=np.uint64)
+        h = ctypes.c_void_p()
+        check(load().zk_msm_plan_create(self.handle, count, bh, None if off is None else off.ctypes.data,
+                                        sz.ctypes.data, 1 if scalars_mont else 0, int(window_bits),
+                                        1 if use_graph else 0, ctypes.byref(h)), "zk_msm_plan_create")
+        return MsmPlan(self, h.value, [int(x) for x in sizes], list(bases))
+
+    @staticmethod
+    def _ntt_args(jobs):
+        """jobs: (mode, out, inp, in_len, log_n, omega, shift) tuples -> ctypes arrays."""
+        count = len(jobs)
+        modes = np.array([j[0] for j in jobs], dtype=np.int32)
+        outs = (ctypes.c_void_p * count)(*[getattr(j[1], "ptr", j[1]) for j in jobs])
+        ins = (ctypes.c_void_p * count)(*[getattr(j[2], "ptr", j[2]) for j in jobs])
+        lens = np.array([j[3] for j in jobs], dtype=np.uint64)
+        logs = np.array([j[4] for j in jobs], dtype=np.uint32)
+        om = np.frombuffer(b"".join(_fr_bytes(j[5]) for j in jobs) or b"\0", dtype=np.uint8).copy()
+        sh = np.frombuffer(b"".join(_fr_bytes(j[6] if len(j) > 6 else 1) for j in jobs) or b"\0",
+                           dtype=np.uint8).copy()
+        return count, modes, outs, ins, lens, logs, om, sh
+
+    def ntt_batch(self, jobs) -> None:
+        """Many transforms, one launch per pass level (zk_ntt_batch); asynchronous like ntt()."""
+        count, modes, outs, ins, lens, logs, om, sh = self._ntt_args(jobs)
+        check(load().zk_ntt_batch(self.handle, count, modes.ctypes.data, outs, ins, lens.ctypes.data,
+                                  logs.ctypes.data, om.ctypes.data, sh.ctypes.data), "zk_ntt_batch")
+
+    def ntt_plan(self, jobs, *, use_graph: bool = True) -> "NttPlan":
+        count, modes, outs, ins, lens, logs, om, sh = self._ntt_args(jobs)
+        h = ctypes.c_void_p()
+        check(load().zk_ntt_plan_create(self.handle, count, modes.ctypes.data, outs, ins, lens.ctypes.data,
+                                        logs.ctypes.data, om.ctypes.data, sh.ctypes.data, 1 if use_graph else 0,
+                                        ctypes.byref(h)), "zk_ntt_plan_create")
+        return NttPlan(self, h.value, [j[1] for j in jobs] + [j[2] for j in jobs])
+
+    # ---- tuning
+    def tune_set_msm_window(self, log_n: int, window_bits: int) -> None:
+        check(load().zk_tune_set_msm_window(self.handle, int(log_n), int(window_bits)), "zk_tune_set_msm_window")
+
+    def tune_msm_window(self, n: int) -> int:
+        v = ctypes.c_uint32()
+        check(load().zk_tune_get_msm_window(self.handle, int(n), ctypes.byref(v)), "zk_tune_get_msm_window")
+        return int(v.value)
+
+    def tune_set_ntt_split(self, log_n: int, bits) -> None:
+        arr = np.ascontiguousarray(list(bits) or [0], dtype=np.uint32)
+        check(load().zk_tune_set_ntt_split(self.handle, int(log_n), len(bits), arr.ctypes.data),
+              "zk_tune_set_ntt_split")
+
+    def tune_ntt_split(self, log_n: int):
+        np_ = ctypes.c_uint32()
+        bits = np.zeros(4, dtype=np.uint32)
+        check(load().zk_tune_get_ntt_split(self.handle, int(log_n), ctypes.byref(np_), bits.ctypes.data),
+              "zk_tune_get_ntt_split")
+        return [int(b) for b in bits[: np_.value]]
+
+    def autotune_msm(self, bases: "Bases", scalars: DeviceArray, log_n: int, reps: int = 2):
+        c = ctypes.c_uint32()
+        ms = ctypes.c_double()
+        check(load().zk_autotune_msm(self.handle, bases.handle, scalars.ptr, int(log_n), int(reps), ctypes.byref(c),
+                                     ctypes.byref(ms)), "zk_autotune_msm")
+        return int(c.value), float(ms.value)
+
+    def autotune_ntt(self, data: DeviceArray, log_n: int, reps: int = 3):
+        np_ = ctypes.c_uint32()
+        bits = np.zeros(4, dtype=np.uint32)
+        ms = ctypes.c_double()
+        check(load().zk_autotune_ntt(self.handle, data.ptr, int(log_n), int(reps), ctypes.byref(np_),
+                                     bits.ctypes.data, ctypes.byref(ms)), "zk_autotune_ntt")
+        return [int(b) for b in bits[: np_.value]], float(ms.value)
+
+    def autotune_save(self, path: str) -> None:
+        check(load().zk_autotune_save(self.handle, os.fsencode(path)), "zk_autotune_save")
+
+    def autotune_load(self, path: str) -> None:
+        check(load().zk_autotune_load(self.handle, os.fsencode(path)), "zk_autotune_load")
+
+    def g2_fixed_base_mul(self, point, k: DeviceArray, n: int, out: DeviceArray) -> None:
+        """out[i] = [k_i] P on G2; point = ((x0, x1), (y0, y1)) canonical."""
+        (x0, x1), (y0, y1) = point
+        pb = b"".join(int(v).to_bytes(32, "little") for v in (x0, x1, y0, y1))
+        check(load().zk_g2_fixed_base_mul(self.handle, pb, k.ptr, int(n), out.ptr), "zk_g2_fixed_base_mul")
 
     def g1_fixed_base_mul(self, point_xy, k: DeviceArray, n: int, out: DeviceArray) -> None:
         x, y = point_xy

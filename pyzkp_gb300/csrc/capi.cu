@@ -2,6 +2,7 @@
 #include <cstring>
 #include <iterator>
 #include <string>
+#include <vector>
 
 #include "zk_internal.cuh"
 
@@ -84,6 +85,7 @@ template <class F, int DIR>
 int convert(Ctx* c, void* out, const void* in, size_t n);
 int fr_binary(Ctx* c, int op, void* out, const void* a, const void* b, size_t n);
 int fixed_base_mul(Ctx* c, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_dev);
+int fixed_base_mul_g2(Ctx* c, const uint8_t point_xy[128], const void* k_dev, size_t n, void* out_dev);
 int imad_peak(Ctx* c, double* tera);
 int imad_probe(Ctx* c, int mode, double* tera);
 int trimmed_len(Ctx* c, const void* a, size_t n, size_t* out);
@@ -419,8 +421,8 @@ int zk_bases_create_dev(zk_ctx* ctx, const void* xy_canonical_dev, size_t n, zk_
 
 int zk_bases_precompute(zk_ctx* ctx, zk_bases* b, uint32_t window_bits) {
     CTX_OR_FAIL(ctx);
-    if (b == nullptr) {
-        zk::set_error("null bases");
+    if (b == nullptr || b->dev == nullptr) {
+        zk::set_error("zk_bases_precompute needs G1 bases");
         return ZK_EINVAL;
     }
     if (b->shifted && b->shifted_c == window_bits) return ZK_OK;
@@ -440,7 +442,8 @@ int zk_bases_destroy(zk_bases* b) {
     if (b == nullptr) return ZK_OK;
     cudaSetDevice(b->ctx->impl.device);
     if (b->shifted) zk::scratch_free(&b->ctx->impl, b->shifted);
-    zk::scratch_free(&b->ctx->impl, b->dev);
+    if (b->dev) zk::scratch_free(&b->ctx->impl, b->dev);
+    if (b->dev2) zk::scratch_free(&b->ctx->impl, b->dev2);
     delete b;
     return ZK_OK;
 }
@@ -461,6 +464,10 @@ int zk_msm_g1(zk_ctx* ctx, const zk_bases* bases, size_t offset, const void* sca
         zk::set_error("null pointer");
         return ZK_EINVAL;
     }
+    if (bases->dev == nullptr) {
+        zk::set_error("zk_msm_g1 needs G1 bases (this handle holds G2 points)");
+        return ZK_EINVAL;
+    }
     if (offset > bases->n || n > bases->n - offset) {
         zk::set_error("scalars length exceeds points length");
         return ZK_EINVAL;
@@ -477,6 +484,272 @@ int zk_g1_fixed_base_mul(zk_ctx* ctx, const uint8_t point_xy[64], const void* k_
         return ZK_EINVAL;
     }
     return zk::fixed_base_mul(&ctx->impl, point_xy, k_dev, n, out_xy_dev);
+}
+
+// ---- batched MSM ------------------------------------------------------------------------
+static int make_jobs(size_t count, const zk_bases* const* bases, const uint64_t* offsets,
+                     const void* const* scalars_dev, const uint64_t* sizes, std::vector<zk::MsmJob>* jobs,
+                     bool g2 = false) {
+    if (count && (bases == nullptr || sizes == nullptr)) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    jobs->resize(count);
+    for (size_t k = 0; k < count; k++) {
+        const zk_bases* b = bases[k];
+        const uint64_t off = offsets ? offsets[k] : 0;
+        if (b == nullptr) {
+            zk::set_error("null bases handle in batch");
+            return ZK_EINVAL;
+        }
+        if ((g2 ? (const void*)b->dev2 : (const void*)b->dev) == nullptr) {
+            zk::set_error(g2 ? "G2 MSM needs G2 bases" : "G1 MSM needs G1 bases");
+            return ZK_EINVAL;
+        }
+        if (off > b->n || sizes[k] > b->n - off) {
+            zk::set_error("scalars length exceeds points length");
+            return ZK_EINVAL;
+        }
+        zk::MsmJob& j = (*jobs)[k];
+        j.scalars = scalars_dev ? static_cast<const zk::fe*>(scalars_dev[k]) : nullptr;
+        if (scalars_dev && sizes[k] && j.scalars == nullptr) {
+            zk::set_error("null scalars in batch");
+            return ZK_EINVAL;
+        }
+        j.n = sizes[k];
+        if (g2) {
+            j.bases = b->dev2 + off;
+        } else {
+            j.bases = b->dev + off;
+            j.shifted = b->shifted ? b->shifted + off : nullptr;
+        }
+        j.shifted_c = b->shifted_c;
+        j.stride = b->n;
+    }
+    return ZK_OK;
+}
+
+int zk_msm_g1_batch(zk_ctx* ctx, size_t count, const zk_bases* const* bases, const uint64_t* offsets,
+                    const void* const* scalars_dev, const uint64_t* sizes, int scalars_mont, uint32_t window_bits,
+                    uint8_t* out_xy, int32_t* out_is_inf) {
+    CTX_OR_FAIL(ctx);
+    if (count && (scalars_dev == nullptr || out_xy == nullptr || out_is_inf == nullptr)) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    std::vector<zk::MsmJob> jobs;
+    int rc = make_jobs(count, bases, offsets, scalars_dev, sizes, &jobs);
+    if (rc != ZK_OK) return rc;
+    return zk::msm_batch_run(&ctx->impl, jobs.data(), count, scalars_mont, window_bits, out_xy, out_is_inf);
+}
+
+int zk_msm_plan_create(zk_ctx* ctx, size_t count, const zk_bases* const* bases, const uint64_t* offsets,
+                       const uint64_t* sizes, int scalars_mont, uint32_t window_bits, int use_graph,
+                       zk_msm_plan** out) {
+    CTX_OR_FAIL(ctx);
+    if (out == nullptr) {
+        zk::set_error("null output pointer");
+        return ZK_EINVAL;
+    }
+    *out = nullptr;
+    std::vector<zk::MsmJob> jobs;
+    int rc = make_jobs(count, bases, offsets, nullptr, sizes, &jobs);
+    if (rc != ZK_OK) return rc;
+    zk::MsmPlan* impl = nullptr;
+    rc = zk::msm_plan_create(&ctx->impl, jobs.data(), count, scalars_mont, window_bits, use_graph != 0, &impl);
+    if (rc != ZK_OK) return rc;
+    *out = new zk_msm_plan{ctx, impl};
+    return ZK_OK;
+}
+
+int zk_msm_plan_scalars(zk_msm_plan* plan, size_t index, void** scalars_dev) {
+    if (plan == nullptr || scalars_dev == nullptr) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    return zk::msm_plan_slot(plan->impl, index, scalars_dev);
+}
+
+int zk_msm_plan_run(zk_msm_plan* plan, uint8_t* out_xy, int32_t* out_is_inf) {
+    if (plan == nullptr || out_xy == nullptr || out_is_inf == nullptr) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    CTX_OR_FAIL(plan->ctx);
+    return zk::msm_plan_run(&plan->ctx->impl, plan->impl, out_xy, out_is_inf);
+}
+
+int zk_msm_plan_launches(zk_msm_plan* plan, uint64_t* kernels) {
+    if (plan == nullptr || kernels == nullptr) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    *kernels = zk::msm_plan_kernels(plan->impl);
+    return ZK_OK;
+}
+
+int zk_msm_plan_destroy(zk_msm_plan* plan) {
+    if (plan == nullptr) return ZK_OK;
+    cudaSetDevice(plan->ctx->impl.device);
+    zk::msm_plan_destroy(&plan->ctx->impl, plan->impl);
+    delete plan;
+    return ZK_OK;
+}
+
+// ---- G2 -------------------------------------------------------------------------------------
+int zk_g2_fixed_base_mul(zk_ctx* ctx, const uint8_t point_xy[128], const void* k_dev, size_t n, void* out_xy_dev) {
+    CTX_OR_FAIL(ctx);
+    if (point_xy == nullptr) {
+        zk::set_error("null point");
+        return ZK_EINVAL;
+    }
+    return zk::fixed_base_mul_g2(&ctx->impl, point_xy, k_dev, n, out_xy_dev);
+}
+
+int zk_bases_g2_create(zk_ctx* ctx, const void* xy_canonical_host, size_t n, zk_bases** out) {
+    CTX_OR_FAIL(ctx);
+    if (out == nullptr || (n && xy_canonical_host == nullptr)) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    zk_bases* b = new zk_bases();
+    b->ctx = ctx;
+    b->n = n;
+    b->dev = nullptr;
+    int rc = zk::scratch_alloc(&ctx->impl, n * sizeof(zk::affine2_t), reinterpret_cast<void**>(&b->dev2));
+    if (rc != ZK_OK) {
+        delete b;
+        return rc;
+    }
+    if (n) {
+        cudaError_t e = cudaMemcpyAsync(b->dev2, xy_canonical_host, n * sizeof(zk::affine2_t), cudaMemcpyHostToDevice,
+                                        ctx->impl.stream);
+        // (x.c0, x.c1, y.c0, y.c1) canonical -> Montgomery, as 4n base-field elements in place
+        if (e == cudaSuccess) rc = zk::convert<zk::FqP, 1>(&ctx->impl, b->dev2, b->dev2, 4 * n);
+        else {
+            zk::set_error(std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
+            rc = ZK_ECUDA;
+        }
+        if (rc == ZK_OK && (e = cudaStreamSynchronize(ctx->impl.stream)) != cudaSuccess) {
+            zk::set_error(std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
+            rc = ZK_ECUDA;
+        }
+    }
+    if (rc != ZK_OK) {
+        zk::scratch_free(&ctx->impl, b->dev2);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return ZK_OK;
+}
+
+int zk_msm_g2(zk_ctx* ctx, const zk_bases* bases, size_t offset, const void* scalars_dev, size_t n, int scalars_mont,
+              uint32_t window_bits, uint8_t out_xy[128], int* out_is_inf) {
+    CTX_OR_FAIL(ctx);
+    if (bases == nullptr || out_xy == nullptr || out_is_inf == nullptr) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    const uint64_t off = offset, size = n;
+    std::vector<zk::MsmJob> jobs;
+    int rc = make_jobs(1, &bases, &off, &scalars_dev, &size, &jobs, true);
+    if (rc != ZK_OK) return rc;
+    int32_t inf = 0;
+    rc = zk::msm_g2_batch_run(&ctx->impl, jobs.data(), 1, scalars_mont, window_bits, out_xy, &inf);
+    *out_is_inf = inf;
+    return rc;
+}
+
+int zk_msm_g2_batch(zk_ctx* ctx, size_t count, const zk_bases* const* bases, const uint64_t* offsets,
+                    const void* const* scalars_dev, const uint64_t* sizes, int scalars_mont, uint32_t window_bits,
+                    uint8_t* out_xy, int32_t* out_is_inf) {
+    CTX_OR_FAIL(ctx);
+    if (count && (scalars_dev == nullptr || out_xy == nullptr || out_is_inf == nullptr)) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    std::vector<zk::MsmJob> jobs;
+    int rc = make_jobs(count, bases, offsets, scalars_dev, sizes, &jobs, true);
+    if (rc != ZK_OK) return rc;
+    return zk::msm_g2_batch_run(&ctx->impl, jobs.data(), count, scalars_mont, window_bits, out_xy, out_is_inf);
+}
+
+// ---- batched NTT ------------------------------------------------------------------------
+static int make_ntt_jobs(size_t count, const int* modes, void* const* outs, const void* const* ins,
+                         const uint64_t* in_lens, const uint32_t* log_ns, const uint8_t* omegas,
+                         const uint8_t* shifts, std::vector<zk::NttJob>* jobs) {
+    if (count && (modes == nullptr || outs == nullptr || ins == nullptr || in_lens == nullptr || log_ns == nullptr ||
+                  omegas == nullptr)) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    jobs->resize(count);
+    for (size_t k = 0; k < count; k++) {
+        zk::NttJob& j = (*jobs)[k];
+        j.mode = modes[k];
+        j.out = static_cast<zk::fe*>(outs[k]);
+        j.in = static_cast<const zk::fe*>(ins[k]);
+        j.in_len = in_lens[k];
+        j.log_n = log_ns[k];
+        j.omega = omegas + 32 * k;
+        j.shift = shifts ? shifts + 32 * k : nullptr;
+    }
+    return ZK_OK;
+}
+
+int zk_ntt_batch(zk_ctx* ctx, size_t count, const int* modes, void* const* outs, const void* const* ins,
+                 const uint64_t* in_lens, const uint32_t* log_ns, const uint8_t* omegas, const uint8_t* shifts) {
+    CTX_OR_FAIL(ctx);
+    std::vector<zk::NttJob> jobs;
+    int rc = make_ntt_jobs(count, modes, outs, ins, in_lens, log_ns, omegas, shifts, &jobs);
+    if (rc != ZK_OK) return rc;
+    return zk::ntt_batch_run(&ctx->impl, jobs.data(), count);
+}
+
+int zk_ntt_plan_create(zk_ctx* ctx, size_t count, const int* modes, void* const* outs, const void* const* ins,
+                       const uint64_t* in_lens, const uint32_t* log_ns, const uint8_t* omegas, const uint8_t* shifts,
+                       int use_graph, zk_ntt_plan** out) {
+    CTX_OR_FAIL(ctx);
+    if (out == nullptr) {
+        zk::set_error("null output pointer");
+        return ZK_EINVAL;
+    }
+    *out = nullptr;
+    std::vector<zk::NttJob> jobs;
+    int rc = make_ntt_jobs(count, modes, outs, ins, in_lens, log_ns, omegas, shifts, &jobs);
+    if (rc != ZK_OK) return rc;
+    zk::NttBatchPlan* impl = nullptr;
+    rc = zk::ntt_plan_create(&ctx->impl, jobs.data(), count, use_graph != 0, &impl);
+    if (rc != ZK_OK) return rc;
+    *out = new zk_ntt_plan{ctx, impl};
+    return ZK_OK;
+}
+
+int zk_ntt_plan_run(zk_ntt_plan* plan) {
+    if (plan == nullptr) {
+        zk::set_error("null plan");
+        return ZK_EINVAL;
+    }
+    CTX_OR_FAIL(plan->ctx);
+    return zk::ntt_plan_run(&plan->ctx->impl, plan->impl);
+}
+
+int zk_ntt_plan_launches(zk_ntt_plan* plan, uint64_t* kernels) {
+    if (plan == nullptr || kernels == nullptr) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    *kernels = zk::ntt_plan_kernels(plan->impl);
+    return ZK_OK;
+}
+
+int zk_ntt_plan_destroy(zk_ntt_plan* plan) {
+    if (plan == nullptr) return ZK_OK;
+    cudaSetDevice(plan->ctx->impl.device);
+    zk::ntt_plan_destroy(&plan->ctx->impl, plan->impl);
+    delete plan;
+    return ZK_OK;
 }
 
 }  // extern "C"

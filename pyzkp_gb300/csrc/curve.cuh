@@ -1,164 +1,261 @@
-// curve.cuh -- BN254 G1 (y^2 = x^3 + 3 over Fq) point arithmetic for the MSM kernels.
+// curve.cuh -- BN254 point arithmetic for the MSM kernels: G1 (y^2 = x^3 + 3 over Fq)
+// and G2 (the sextic twist y^2 = x^3 + 3/(9 + u) over Fq2 = Fq[u]/(u^2 + 1)).
 //
-// Bases are affine (x, y) in Montgomery form, 64 bytes; the point at infinity is
-// stored as (0, 0), which is not on the curve. Bucket accumulators use XYZZ
-// coordinates (x = X/ZZ, y = Y/ZZZ, ZZ^3 = ZZZ^2), infinity is ZZ == 0. The formulas
-// are the published short-Weierstrass a = 0 XYZZ formulas (madd-2008-s, add-2008-s,
-// dbl-2008-s-1, mdbl-2008-s-1 of the Explicit-Formulas Database), made complete here
-// by handling infinity, P == Q (doubling) and P == -Q (infinity) explicitly -- the
-// same cases the reference's Jacobian code handles (runtime/metal/ecc_source.py:206-293).
+// Bases are affine (x, y) in Montgomery form (64 bytes for G1, 128 for G2); the point at
+// infinity is stored as all-zero coordinates, which is on neither curve. Bucket
+// accumulators use XYZZ coordinates (x = X/ZZ, y = Y/ZZZ, ZZ^3 = ZZZ^2), infinity is
+// ZZ == 0. The formulas are the published short-Weierstrass a = 0 XYZZ formulas
+// (madd-2008-s, add-2008-s, dbl-2008-s-1, mdbl-2008-s-1 of the Explicit-Formulas
+// Database); they do not involve b, so one generic version serves both groups. They are
+// made complete by handling infinity, P == Q (doubling) and P == -Q (infinity)
+// explicitly -- the same cases the reference's Jacobian code handles
+// (runtime/metal/ecc_source.py:206-293; G2 in crypto/ecc/bn254.py via py_ecc).
 #pragma once
 #include "field.cuh"
 
 namespace zk {
 
-struct __align__(16) affine_t {
-    fe x, y;
+// ---- Fq2 = Fq[u] / (u^2 + 1) ------------------------------------------------------------
+struct __align__(16) fq2 {
+    fe c0, c1;  // c0 + c1 u
 };
 
-struct __align__(16) xyzz_t {
-    fe X, Y, ZZ, ZZZ;
+// ---- coordinate operations, overloaded for Fq (fe) and Fq2 (fq2) ------------------------
+__device__ __forceinline__ fe c_add(const fe& a, const fe& b) { return fe_add<FqP>(a, b); }
+__device__ __forceinline__ fe c_sub(const fe& a, const fe& b) { return fe_sub<FqP>(a, b); }
+__device__ __forceinline__ fe c_dbl(const fe& a) { return fe_dbl<FqP>(a); }
+__device__ __forceinline__ fe c_neg(const fe& a) { return fe_neg<FqP>(a); }
+__device__ __forceinline__ fe c_mul(const fe& a, const fe& b) { return fe_mul<FqP>(a, b); }
+__device__ __forceinline__ fe c_sqr(const fe& a) { return fe_sqr<FqP>(a); }
+__device__ __forceinline__ bool c_is_zero(const fe& a) { return fe_is_zero(a); }
+__device__ __forceinline__ void c_set_zero(fe& a) { a = fe_zero(); }
+__device__ __forceinline__ void c_set_one(fe& a) { a = fe_one<FqP>(); }
+__device__ __forceinline__ fe c_ldg(const fe* p) { return fe_ldg(p); }
+__device__ __forceinline__ fe c_load(const fe* p) { return fe_load(p); }
+__device__ __forceinline__ void c_store(fe* p, const fe& a) { fe_store(p, a); }
+
+template <class T>
+struct c_pair {
+    T x, y;
 };
 
-__device__ __forceinline__ bool affine_is_inf(const affine_t& p) { return fe_is_zero(p.x) && fe_is_zero(p.y); }
+// Two independent products; for Fq they go through fe_mul2 (one interleaved pair when
+// ZK_USE_MUL2 is set).
+__device__ __forceinline__ c_pair<fe> c_mul2(const fe& a, const fe& b, const fe& c, const fe& d) {
+    const fe2 r = fe_mul2<FqP>(a, b, c, d);
+    return {r.x, r.y};
+}
 
-__device__ __forceinline__ xyzz_t xyzz_inf() {
-    xyzz_t r;
-    r.X = fe_zero();
-    r.Y = fe_zero();
-    r.ZZ = fe_zero();
-    r.ZZZ = fe_zero();
+__device__ __forceinline__ fq2 c_add(const fq2& a, const fq2& b) { return {c_add(a.c0, b.c0), c_add(a.c1, b.c1)}; }
+__device__ __forceinline__ fq2 c_sub(const fq2& a, const fq2& b) { return {c_sub(a.c0, b.c0), c_sub(a.c1, b.c1)}; }
+__device__ __forceinline__ fq2 c_dbl(const fq2& a) { return {c_dbl(a.c0), c_dbl(a.c1)}; }
+__device__ __forceinline__ fq2 c_neg(const fq2& a) { return {c_neg(a.c0), c_neg(a.c1)}; }
+// (a0 + a1 u)(b0 + b1 u) = (a0 b0 - a1 b1) + ((a0 + a1)(b0 + b1) - a0 b0 - a1 b1) u: 3 products
+__device__ __forceinline__ fq2 c_mul(const fq2& a, const fq2& b) {
+    const fe t0 = c_mul(a.c0, b.c0);
+    const fe t1 = c_mul(a.c1, b.c1);
+    const fe t2 = c_mul(c_add(a.c0, a.c1), c_add(b.c0, b.c1));
+    return {c_sub(t0, t1), c_sub(c_sub(t2, t0), t1)};
+}
+// (a0 + a1 u)^2 = (a0 + a1)(a0 - a1) + 2 a0 a1 u: 2 products
+__device__ __forceinline__ fq2 c_sqr(const fq2& a) {
+    const fe t0 = c_mul(c_add(a.c0, a.c1), c_sub(a.c0, a.c1));
+    const fe t1 = c_mul(a.c0, a.c1);
+    return {t0, c_dbl(t1)};
+}
+__device__ __forceinline__ bool c_is_zero(const fq2& a) { return fe_is_zero(a.c0) && fe_is_zero(a.c1); }
+__device__ __forceinline__ void c_set_zero(fq2& a) {
+    a.c0 = fe_zero();
+    a.c1 = fe_zero();
+}
+__device__ __forceinline__ void c_set_one(fq2& a) {
+    a.c0 = fe_one<FqP>();
+    a.c1 = fe_zero();
+}
+__device__ __forceinline__ fq2 c_ldg(const fq2* p) { return {fe_ldg(&p->c0), fe_ldg(&p->c1)}; }
+__device__ __forceinline__ fq2 c_load(const fq2* p) { return {fe_load(&p->c0), fe_load(&p->c1)}; }
+__device__ __forceinline__ void c_store(fq2* p, const fq2& a) {
+    fe_store(&p->c0, a.c0);
+    fe_store(&p->c1, a.c1);
+}
+__device__ __forceinline__ c_pair<fq2> c_mul2(const fq2& a, const fq2& b, const fq2& c, const fq2& d) {
+    return {c_mul(a, b), c_mul(c, d)};
+}
+
+// ---- points -------------------------------------------------------------------------------
+template <class T>
+struct __align__(16) AffineT {
+    T x, y;
+};
+
+template <class T>
+struct __align__(16) XyzzT {
+    T X, Y, ZZ, ZZZ;
+};
+
+using affine_t = AffineT<fe>;
+using xyzz_t = XyzzT<fe>;
+using affine2_t = AffineT<fq2>;
+using xyzz2_t = XyzzT<fq2>;
+
+template <class T>
+__device__ __forceinline__ bool affine_is_inf(const AffineT<T>& p) {
+    return c_is_zero(p.x) && c_is_zero(p.y);
+}
+
+template <class T = fe>
+__device__ __forceinline__ XyzzT<T> xyzz_inf() {
+    XyzzT<T> r;
+    c_set_zero(r.X);
+    c_set_zero(r.Y);
+    c_set_zero(r.ZZ);
+    c_set_zero(r.ZZZ);
     return r;
 }
 
-__device__ __forceinline__ bool xyzz_is_inf(const xyzz_t& p) { return fe_is_zero(p.ZZ); }
+template <class T>
+__device__ __forceinline__ bool xyzz_is_inf(const XyzzT<T>& p) {
+    return c_is_zero(p.ZZ);
+}
 
-__device__ __forceinline__ affine_t affine_neg(const affine_t& p) {
-    affine_t r;
-    r.x = p.x;
-    r.y = fe_neg<FqP>(p.y);
+template <class T>
+__device__ __forceinline__ XyzzT<T> xyzz_neg(const XyzzT<T>& p) {
+    XyzzT<T> r = p;
+    r.Y = c_neg(p.Y);
     return r;
 }
 
-__device__ __forceinline__ xyzz_t xyzz_neg(const xyzz_t& p) {
-    xyzz_t r = p;
-    r.Y = fe_neg<FqP>(p.Y);
-    return r;
-}
+// The formulas below issue their multiplications in independent pairs (c_mul2), so the
+// two carry-chain sequences of a pair can overlap.
 
-// The formulas below issue their multiplications in independent pairs (fe_mul2), so the
-// two carry-chain sequences of a pair overlap.
-
-// 2 * (x, y) for an affine point that is not infinity (y != 0 on this curve).
-__device__ __forceinline__ xyzz_t xyzz_dbl_affine(const fe& x, const fe& y) {
-    using F = FqP;
-    const fe U = fe_dbl<F>(y);
-    const fe2 vx = fe_mul2<F>(U, U, x, x);  // V = U^2, x^2
-    const fe2 ws = fe_mul2<F>(U, vx.x, x, vx.x);  // W = U V, S = x V
-    const fe M = fe_add<F>(fe_dbl<F>(vx.y), vx.y);
-    const fe MM = fe_sqr<F>(M);
-    xyzz_t r;
-    r.X = fe_sub<F>(MM, fe_dbl<F>(ws.y));
-    const fe2 t = fe_mul2<F>(M, fe_sub<F>(ws.y, r.X), ws.x, y);
-    r.Y = fe_sub<F>(t.x, t.y);
+// 2 * (x, y) for an affine point that is not infinity (y != 0 on these curves).
+template <class T>
+__device__ __forceinline__ XyzzT<T> xyzz_dbl_affine(const T& x, const T& y) {
+    const T U = c_dbl(y);
+    const c_pair<T> vx = c_mul2(U, U, x, x);        // V = U^2, x^2
+    const c_pair<T> ws = c_mul2(U, vx.x, x, vx.x);  // W = U V, S = x V
+    const T M = c_add(c_dbl(vx.y), vx.y);
+    const T MM = c_sqr(M);
+    XyzzT<T> r;
+    r.X = c_sub(MM, c_dbl(ws.y));
+    const c_pair<T> t = c_mul2(M, c_sub(ws.y, r.X), ws.x, y);
+    r.Y = c_sub(t.x, t.y);
     r.ZZ = vx.x;
     r.ZZZ = ws.x;
     return r;
 }
 
-__device__ __forceinline__ xyzz_t xyzz_dbl(const xyzz_t& p) {
-    using F = FqP;
+template <class T>
+__device__ __forceinline__ XyzzT<T> xyzz_dbl(const XyzzT<T>& p) {
     if (xyzz_is_inf(p)) return p;
-    const fe U = fe_dbl<F>(p.Y);
-    const fe2 vx = fe_mul2<F>(U, U, p.X, p.X);    // V = U^2, X^2
-    const fe2 ws = fe_mul2<F>(U, vx.x, p.X, vx.x);  // W = U V, S = X V
-    const fe M = fe_add<F>(fe_dbl<F>(vx.y), vx.y);
-    const fe2 mz = fe_mul2<F>(M, M, vx.x, p.ZZ);  // M^2, ZZ3 = V ZZ
-    xyzz_t r;
-    r.X = fe_sub<F>(mz.x, fe_dbl<F>(ws.y));
-    const fe2 t = fe_mul2<F>(M, fe_sub<F>(ws.y, r.X), ws.x, p.Y);
-    r.Y = fe_sub<F>(t.x, t.y);
+    const T U = c_dbl(p.Y);
+    const c_pair<T> vx = c_mul2(U, U, p.X, p.X);      // V = U^2, X^2
+    const c_pair<T> ws = c_mul2(U, vx.x, p.X, vx.x);  // W = U V, S = X V
+    const T M = c_add(c_dbl(vx.y), vx.y);
+    const c_pair<T> mz = c_mul2(M, M, vx.x, p.ZZ);  // M^2, ZZ3 = V ZZ
+    XyzzT<T> r;
+    r.X = c_sub(mz.x, c_dbl(ws.y));
+    const c_pair<T> t = c_mul2(M, c_sub(ws.y, r.X), ws.x, p.Y);
+    r.Y = c_sub(t.x, t.y);
     r.ZZ = mz.y;
-    r.ZZZ = fe_mul<F>(ws.x, p.ZZZ);
+    r.ZZZ = c_mul(ws.x, p.ZZZ);
     return r;
 }
 
 // acc + (x, y), (x, y) affine and not infinity.
-__device__ __forceinline__ xyzz_t xyzz_madd(const xyzz_t& acc, const fe& x, const fe& y) {
-    using F = FqP;
+template <class T>
+__device__ __forceinline__ XyzzT<T> xyzz_madd(const XyzzT<T>& acc, const T& x, const T& y) {
     if (xyzz_is_inf(acc)) {
-        xyzz_t r;
+        XyzzT<T> r;
         r.X = x;
         r.Y = y;
-        r.ZZ = fe_one<F>();
-        r.ZZZ = fe_one<F>();
+        c_set_one(r.ZZ);
+        c_set_one(r.ZZZ);
         return r;
     }
-    const fe2 us = fe_mul2<F>(x, acc.ZZ, y, acc.ZZZ);  // U2, S2
-    const fe P = fe_sub<F>(us.x, acc.X);
-    const fe R = fe_sub<F>(us.y, acc.Y);
-    if (fe_is_zero(P)) {
-        if (fe_is_zero(R)) return xyzz_dbl_affine(x, y);
-        return xyzz_inf();
+    const c_pair<T> us = c_mul2(x, acc.ZZ, y, acc.ZZZ);  // U2, S2
+    const T P = c_sub(us.x, acc.X);
+    const T R = c_sub(us.y, acc.Y);
+    if (c_is_zero(P)) {
+        if (c_is_zero(R)) return xyzz_dbl_affine(x, y);
+        return xyzz_inf<T>();
     }
-    const fe2 pr = fe_mul2<F>(P, P, R, R);          // PP, R^2
-    const fe2 pq = fe_mul2<F>(P, pr.x, acc.X, pr.x);  // PPP, Q
-    xyzz_t r;
-    r.X = fe_sub<F>(fe_sub<F>(pr.y, pq.x), fe_dbl<F>(pq.y));
-    const fe2 zz = fe_mul2<F>(acc.ZZ, pr.x, acc.ZZZ, pq.x);
-    const fe2 t = fe_mul2<F>(R, fe_sub<F>(pq.y, r.X), acc.Y, pq.x);
-    r.Y = fe_sub<F>(t.x, t.y);
+    const c_pair<T> pr = c_mul2(P, P, R, R);            // PP, R^2
+    const c_pair<T> pq = c_mul2(P, pr.x, acc.X, pr.x);  // PPP, Q
+    XyzzT<T> r;
+    r.X = c_sub(c_sub(pr.y, pq.x), c_dbl(pq.y));
+    const c_pair<T> zz = c_mul2(acc.ZZ, pr.x, acc.ZZZ, pq.x);
+    const c_pair<T> t = c_mul2(R, c_sub(pq.y, r.X), acc.Y, pq.x);
+    r.Y = c_sub(t.x, t.y);
     r.ZZ = zz.x;
     r.ZZZ = zz.y;
     return r;
 }
 
-__device__ __forceinline__ xyzz_t xyzz_add(const xyzz_t& p, const xyzz_t& q) {
-    using F = FqP;
+template <class T>
+__device__ __forceinline__ XyzzT<T> xyzz_add(const XyzzT<T>& p, const XyzzT<T>& q) {
     if (xyzz_is_inf(p)) return q;
     if (xyzz_is_inf(q)) return p;
-    const fe2 u = fe_mul2<F>(p.X, q.ZZ, q.X, p.ZZ);    // U1, U2
-    const fe2 s = fe_mul2<F>(p.Y, q.ZZZ, q.Y, p.ZZZ);  // S1, S2
-    const fe P = fe_sub<F>(u.y, u.x);
-    const fe R = fe_sub<F>(s.y, s.x);
-    if (fe_is_zero(P)) {
-        if (fe_is_zero(R)) return xyzz_dbl(p);
-        return xyzz_inf();
+    const c_pair<T> u = c_mul2(p.X, q.ZZ, q.X, p.ZZ);    // U1, U2
+    const c_pair<T> s = c_mul2(p.Y, q.ZZZ, q.Y, p.ZZZ);  // S1, S2
+    const T P = c_sub(u.y, u.x);
+    const T R = c_sub(s.y, s.x);
+    if (c_is_zero(P)) {
+        if (c_is_zero(R)) return xyzz_dbl(p);
+        return xyzz_inf<T>();
     }
-    const fe2 pr = fe_mul2<F>(P, P, R, R);           // PP, R^2
-    const fe2 pq = fe_mul2<F>(P, pr.x, u.x, pr.x);   // PPP, Q
-    const fe2 zz = fe_mul2<F>(p.ZZ, q.ZZ, p.ZZZ, q.ZZZ);
-    xyzz_t r;
-    r.X = fe_sub<F>(fe_sub<F>(pr.y, pq.x), fe_dbl<F>(pq.y));
-    const fe2 z3 = fe_mul2<F>(zz.x, pr.x, zz.y, pq.x);
-    const fe2 t = fe_mul2<F>(R, fe_sub<F>(pq.y, r.X), s.x, pq.x);
-    r.Y = fe_sub<F>(t.x, t.y);
+    const c_pair<T> pr = c_mul2(P, P, R, R);          // PP, R^2
+    const c_pair<T> pq = c_mul2(P, pr.x, u.x, pr.x);  // PPP, Q
+    const c_pair<T> zz = c_mul2(p.ZZ, q.ZZ, p.ZZZ, q.ZZZ);
+    XyzzT<T> r;
+    r.X = c_sub(c_sub(pr.y, pq.x), c_dbl(pq.y));
+    const c_pair<T> z3 = c_mul2(zz.x, pr.x, zz.y, pq.x);
+    const c_pair<T> t = c_mul2(R, c_sub(pq.y, r.X), s.x, pq.x);
+    r.Y = c_sub(t.x, t.y);
     r.ZZ = z3.x;
     r.ZZZ = z3.y;
     return r;
 }
 
-__device__ __forceinline__ affine_t affine_load(const affine_t* p) {
-    affine_t r;
-    r.x = fe_ldg(&p->x);
-    r.y = fe_ldg(&p->y);
+template <class T>
+__device__ __forceinline__ AffineT<T> affine_load(const AffineT<T>* p) {
+    AffineT<T> r;
+    r.x = c_ldg(&p->x);
+    r.y = c_ldg(&p->y);
     return r;
 }
 
-__device__ __forceinline__ xyzz_t xyzz_load(const xyzz_t* p) {
-    xyzz_t r;
-    r.X = fe_load(&p->X);
-    r.Y = fe_load(&p->Y);
-    r.ZZ = fe_load(&p->ZZ);
-    r.ZZZ = fe_load(&p->ZZZ);
+template <class T>
+__device__ __forceinline__ XyzzT<T> xyzz_load(const XyzzT<T>* p) {
+    XyzzT<T> r;
+    r.X = c_load(&p->X);
+    r.Y = c_load(&p->Y);
+    r.ZZ = c_load(&p->ZZ);
+    r.ZZZ = c_load(&p->ZZZ);
     return r;
 }
 
-__device__ __forceinline__ void xyzz_store(xyzz_t* p, const xyzz_t& a) {
-    fe_store(&p->X, a.X);
-    fe_store(&p->Y, a.Y);
-    fe_store(&p->ZZ, a.ZZ);
-    fe_store(&p->ZZZ, a.ZZZ);
+template <class T>
+__device__ __forceinline__ void xyzz_store(XyzzT<T>* p, const XyzzT<T>& a) {
+    c_store(&p->X, a.X);
+    c_store(&p->Y, a.Y);
+    c_store(&p->ZZ, a.ZZ);
+    c_store(&p->ZZZ, a.ZZZ);
 }
+
+// The two groups as template arguments of the MSM kernels.
+struct CurveG1 {
+    using T = fe;
+    using A = affine_t;
+    using P = xyzz_t;
+    static constexpr int kTargetThreads = 256;
+};
+
+struct CurveG2 {
+    using T = fq2;
+    using A = affine2_t;
+    using P = xyzz2_t;
+    static constexpr int kTargetThreads = 128;  // 128 x 256-byte points of shared memory
+};
 
 }  // namespace zk

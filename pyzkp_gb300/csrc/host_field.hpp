@@ -1,4 +1,4 @@
-// host_field.hpp -- host-side BN254 field and G1 arithmetic used by the library's
+// host_field.hpp -- host-side BN254 field, G1 and G2 arithmetic used by the library's
 // host code: NTT twiddle/scale tables, omega checks, and the final combination of
 // MSM window sums into one affine point. 4 x 64-bit limbs, Montgomery R = 2^256
 // (byte-identical to the device's 8 x 32-bit form). Portable C++ (unsigned __int128).
@@ -170,71 +170,114 @@ inline F4 inv(const Field& F, const F4& a) {
     return pow(F, a, e);
 }
 
-// ---- G1 over Fq (Montgomery) ----------------------------------------------
-struct Xyzz {
-    F4 X, Y, ZZ, ZZZ;  // infinity: ZZ == 0
+// ---- coordinate fields of G1 (Fq) and G2 (Fq2 = Fq[u] / (u^2 + 1)), Montgomery ---------
+struct F2 {
+    F4 c0, c1;  // c0 + c1 u
 };
 
-inline Xyzz xyzz_inf() {
-    Xyzz r;
+inline F4 cadd(const F4& a, const F4& b) { return add(fq(), a, b); }
+inline F4 csub(const F4& a, const F4& b) { return sub(fq(), a, b); }
+inline F4 cmul(const F4& a, const F4& b) { return mul(fq(), a, b); }
+inline bool cis_zero(const F4& a) { return is_zero(a); }
+inline F4 cinv(const F4& a) { return inv(fq(), a); }
+inline F4 cfrom_mont(const F4& a) { return from_mont(fq(), a); }
+inline F4 cto_mont(const F4& a) { return to_mont(fq(), a); }
+
+inline F2 cadd(const F2& a, const F2& b) { return {cadd(a.c0, b.c0), cadd(a.c1, b.c1)}; }
+inline F2 csub(const F2& a, const F2& b) { return {csub(a.c0, b.c0), csub(a.c1, b.c1)}; }
+inline F2 cmul(const F2& a, const F2& b) {
+    const F4 t0 = cmul(a.c0, b.c0), t1 = cmul(a.c1, b.c1);
+    const F4 t2 = cmul(cadd(a.c0, a.c1), cadd(b.c0, b.c1));
+    return {csub(t0, t1), csub(csub(t2, t0), t1)};
+}
+inline bool cis_zero(const F2& a) { return is_zero(a.c0) && is_zero(a.c1); }
+// 1 / (a0 + a1 u) = (a0 - a1 u) / (a0^2 + a1^2)
+inline F2 cinv(const F2& a) {
+    const F4 t = inv(fq(), cadd(cmul(a.c0, a.c0), cmul(a.c1, a.c1)));
+    return {cmul(a.c0, t), csub(F4{{0, 0, 0, 0}}, cmul(a.c1, t))};
+}
+inline F2 cfrom_mont(const F2& a) { return {cfrom_mont(a.c0), cfrom_mont(a.c1)}; }
+inline F2 cto_mont(const F2& a) { return {cto_mont(a.c0), cto_mont(a.c1)}; }
+
+// Montgomery one of a coordinate field
+template <class T>
+inline T cone();
+template <>
+inline F4 cone<F4>() {
+    return one(fq());
+}
+template <>
+inline F2 cone<F2>() {
+    return {one(fq()), F4{{0, 0, 0, 0}}};
+}
+
+// ---- XYZZ points over either coordinate field --------------------------------------------
+template <class T>
+struct XyzzT {
+    T X, Y, ZZ, ZZZ;  // infinity: ZZ == 0
+};
+using Xyzz = XyzzT<F4>;
+using Xyzz2 = XyzzT<F2>;
+
+template <class T = F4>
+inline XyzzT<T> xyzz_inf() {
+    XyzzT<T> r;
     std::memset(&r, 0, sizeof(r));
     return r;
 }
 
-inline Xyzz xyzz_dbl(const Xyzz& p) {
-    const Field& F = fq();
-    if (is_zero(p.ZZ)) return p;
-    F4 U = add(F, p.Y, p.Y);
-    F4 V = mul(F, U, U);
-    F4 W = mul(F, U, V);
-    F4 S = mul(F, p.X, V);
-    F4 x2 = mul(F, p.X, p.X);
-    F4 M = add(F, add(F, x2, x2), x2);
-    Xyzz r;
-    r.X = sub(F, mul(F, M, M), add(F, S, S));
-    r.Y = sub(F, mul(F, M, sub(F, S, r.X)), mul(F, W, p.Y));
-    r.ZZ = mul(F, V, p.ZZ);
-    r.ZZZ = mul(F, W, p.ZZZ);
+template <class T>
+inline XyzzT<T> xyzz_dbl(const XyzzT<T>& p) {
+    if (cis_zero(p.ZZ)) return p;
+    T U = cadd(p.Y, p.Y);
+    T V = cmul(U, U);
+    T W = cmul(U, V);
+    T S = cmul(p.X, V);
+    T x2 = cmul(p.X, p.X);
+    T M = cadd(cadd(x2, x2), x2);
+    XyzzT<T> r;
+    r.X = csub(cmul(M, M), cadd(S, S));
+    r.Y = csub(cmul(M, csub(S, r.X)), cmul(W, p.Y));
+    r.ZZ = cmul(V, p.ZZ);
+    r.ZZZ = cmul(W, p.ZZZ);
     return r;
 }
 
-inline Xyzz xyzz_add(const Xyzz& p, const Xyzz& q) {
-    const Field& F = fq();
-    if (is_zero(p.ZZ)) return q;
-    if (is_zero(q.ZZ)) return p;
-    F4 U1 = mul(F, p.X, q.ZZ);
-    F4 U2 = mul(F, q.X, p.ZZ);
-    F4 S1 = mul(F, p.Y, q.ZZZ);
-    F4 S2 = mul(F, q.Y, p.ZZZ);
-    F4 P = sub(F, U2, U1);
-    F4 R = sub(F, S2, S1);
-    if (is_zero(P)) {
-        if (is_zero(R)) return xyzz_dbl(p);
-        return xyzz_inf();
+template <class T>
+inline XyzzT<T> xyzz_add(const XyzzT<T>& p, const XyzzT<T>& q) {
+    if (cis_zero(p.ZZ)) return q;
+    if (cis_zero(q.ZZ)) return p;
+    T U1 = cmul(p.X, q.ZZ);
+    T U2 = cmul(q.X, p.ZZ);
+    T S1 = cmul(p.Y, q.ZZZ);
+    T S2 = cmul(q.Y, p.ZZZ);
+    T P = csub(U2, U1);
+    T R = csub(S2, S1);
+    if (cis_zero(P)) {
+        if (cis_zero(R)) return xyzz_dbl(p);
+        return xyzz_inf<T>();
     }
-    F4 PP = mul(F, P, P);
-    F4 PPP = mul(F, P, PP);
-    F4 Q = mul(F, U1, PP);
-    Xyzz r;
-    r.X = sub(F, sub(F, mul(F, R, R), PPP), add(F, Q, Q));
-    r.Y = sub(F, mul(F, R, sub(F, Q, r.X)), mul(F, S1, PPP));
-    r.ZZ = mul(F, mul(F, p.ZZ, q.ZZ), PP);
-    r.ZZZ = mul(F, mul(F, p.ZZZ, q.ZZZ), PPP);
+    T PP = cmul(P, P);
+    T PPP = cmul(P, PP);
+    T Q = cmul(U1, PP);
+    XyzzT<T> r;
+    r.X = csub(csub(cmul(R, R), PPP), cadd(Q, Q));
+    r.Y = csub(cmul(R, csub(Q, r.X)), cmul(S1, PPP));
+    r.ZZ = cmul(cmul(p.ZZ, q.ZZ), PP);
+    r.ZZZ = cmul(cmul(p.ZZZ, q.ZZZ), PPP);
     return r;
 }
 
-// affine canonical (x, y); infinity -> (0, 0) and returns true
-inline bool xyzz_to_affine_canonical(const Xyzz& p, F4* x, F4* y) {
-    const Field& F = fq();
-    if (is_zero(p.ZZ)) {
-        std::memset(x, 0, sizeof(F4));
-        std::memset(y, 0, sizeof(F4));
+// affine canonical (x, y); infinity -> all zero and returns true
+template <class T>
+inline bool xyzz_to_affine_canonical(const XyzzT<T>& p, T* x, T* y) {
+    if (cis_zero(p.ZZ)) {
+        std::memset(x, 0, sizeof(T));
+        std::memset(y, 0, sizeof(T));
         return true;
     }
-    F4 izz = inv(F, p.ZZ);
-    F4 izzz = inv(F, p.ZZZ);
-    *x = from_mont(F, mul(F, p.X, izz));
-    *y = from_mont(F, mul(F, p.Y, izzz));
+    *x = cfrom_mont(cmul(p.X, cinv(p.ZZ)));
+    *y = cfrom_mont(cmul(p.Y, cinv(p.ZZZ)));
     return false;
 }
 

@@ -15,23 +15,28 @@
 //  4. msm_accumulate_*    equal-size segments of S entries per thread (load balanced
 //                         even when one bucket holds 5% of all points); buckets wholly
 //                         inside a segment are final; a bucket that straddles segment
-//                         boundaries leaves partial sums that tree rounds over groups
-//                         of 32 units merge, deciding "straddles" from the row pointers.
+//                         boundaries leaves partial sums that tree rounds (pairs, then
+//                         groups of 4 units) merge, deciding "straddles" from the row pointers.
 //  5. msm_bucket_blocks   per window, blocks of g buckets: sum_b b*B_b = sum_j E_j + g*WS(Y)
 //                         with Y_j the block sums and E_j = -(sum of the g-1 prefix sums).
 //  6. msm_targets_kernel  WS(Y) = sum_j Y_j + sum_k 2^k M_k with M_k the sum of the Y_j
 //                         whose index has bit k set: plain sums, reduced by CTA trees.
 //  7. host: per window S_w = T_E + g (T_Y + sum_k 2^k M_k), then Horner over windows.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstring>
+#include <map>
+#include <memory>
+#include <thread>
 #include <vector>
 
 #include "zk_internal.cuh"
 
 namespace zk {
 
-int device_exclusive_scan(Ctx* c, uint32_t* data, size_t n, uint32_t* total);
+int device_exclusive_scan(Ctx* c, uint32_t* data, size_t n, uint32_t* total, uint32_t* scratch);
+size_t scan_scratch_elems(size_t n);
 
 static constexpr uint32_t kNone = 0xffffffffu;
 #ifndef ZK_MSM_SEGMENT
@@ -40,11 +45,13 @@ static constexpr uint32_t kNone = 0xffffffffu;
 #ifndef ZK_MSM_BLOCKG
 #define ZK_MSM_BLOCKG 8
 #endif
+#ifndef ZK_MSM_GROUP
+#define ZK_MSM_GROUP 4  // measured at 2^20 / 2^22: merge 0.73 / 1.36 ms with 16, 0.48 / 1.02 ms with 4
+#endif
 static constexpr uint32_t kSegment = ZK_MSM_SEGMENT;  // entries per thread in the first accumulation round
 static constexpr uint32_t kFirstGroup = 2;            // units merged per thread in the first merge round
-static constexpr uint32_t kGroup = 16;                // units merged per thread in later rounds
+static constexpr uint32_t kGroup = ZK_MSM_GROUP;      // units merged per thread in later rounds
 static constexpr uint32_t kBlockG = ZK_MSM_BLOCKG;    // buckets per block in the window reduction
-static constexpr int kTargetThreads = 256;
 
 struct MsmShape {
     uint32_t c;        // window bits
@@ -58,8 +65,19 @@ struct MsmShape {
     uint32_t plain;    // plain-sum targets: 2 (one level) or 3 (two levels)
     uint32_t targets;  // plain + K
     uint32_t shared;   // 1: fixed-base mode, all windows share one bucket set (window-shifted bases)
-    uint32_t Wr;       // bucket sets to reduce: W, or 1 in fixed-base mode
-    uint32_t stride;   // fixed-base mode: row stride of the shifted-bases array
+    uint32_t Wr;       // bucket sets per instance: W, or 1 in fixed-base mode
+    uint32_t inst;     // MSM instances in the pipeline
+    uint32_t sets;     // bucket sets to reduce: inst * Wr
+};
+
+// One MSM of a pipeline: sum_{i < n} scalars[i] * bases[i] (fixed-base mode: bases holds the
+// window-shifted rows, row j at bases + j * stride). Instance k owns the global scalar
+// indices [off_k, off_k + n) and the bucket sets [k Wr, (k + 1) Wr).
+struct MsmInst {
+    const fe* scalars;
+    const void* bases;  // C::A points of the pipeline's curve
+    uint32_t n;
+    uint32_t stride;
 };
 
 static MsmShape make_shape(uint32_t c) {
@@ -77,7 +95,8 @@ static MsmShape make_shape(uint32_t c) {
     s.targets = s.plain + s.K;
     s.shared = 0;
     s.Wr = s.W;
-    s.stride = 0;
+    s.inst = 1;
+    s.sets = s.W;
     return s;
 }
 
@@ -107,16 +126,33 @@ __device__ __forceinline__ void warp_aggregated_inc(uint32_t* counters, uint32_t
     if ((int)(threadIdx.x & 31) == leader) atomicAdd(counters + key, (uint32_t)__popc(peers));
 }
 
-__global__ void msm_digits_kernel(const fe* __restrict__ scalars, const affine_t* __restrict__ bases, uint32_t n,
+// Instance of global scalar index j: the largest k with offs[k] <= j (offs[inst] = total;
+// empty instances repeat an offset and are skipped by taking the largest k).
+__device__ __forceinline__ uint32_t find_inst(const uint32_t* __restrict__ offs, uint32_t ninst, uint32_t j) {
+    uint32_t lo = 0, hi = ninst;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(offs + mid) <= j) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <class C>
+__global__ void msm_digits_kernel(const MsmInst* __restrict__ insts, const uint32_t* __restrict__ offs, uint32_t N,
                                   int scalars_mont, MsmShape sh, uint32_t* __restrict__ digits,
                                   uint32_t* __restrict__ counts) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < n;
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = j < N;
     fe s = fe_zero();
+    uint32_t set0 = 0;
     if (valid) {
-        s = fe_ldg(scalars + i);
+        const uint32_t k = find_inst(offs, sh.inst, j);
+        const uint32_t i = j - __ldg(offs + k);
+        s = fe_ldg(insts[k].scalars + i);
         s = scalars_mont ? fe_from_mont<FrP>(s) : fe_from_mont<FrP>(fe_to_mont<FrP>(s));
-        if (affine_is_inf(affine_load(bases + i))) s = fe_zero();
+        if (affine_is_inf(affine_load(static_cast<const typename C::A*>(insts[k].bases) + i))) s = fe_zero();
+        set0 = k * sh.Wr;
     }
     uint32_t carry = 0;
     const uint32_t half = 1u << (sh.c - 1);
@@ -133,22 +169,30 @@ __global__ void msm_digits_kernel(const fe* __restrict__ scalars, const affine_t
             carry = 0;
         }
         const bool nz = valid && mag != 0;
-        if (valid) digits[(size_t)w * n + i] = nz ? (mag | (neg << 31)) : 0u;
-        warp_aggregated_inc(counts, (sh.shared ? 0u : w * sh.B) + (mag - 1), nz);
+        if (valid) digits[(size_t)w * N + j] = nz ? (mag | (neg << 31)) : 0u;
+        warp_aggregated_inc(counts, (set0 + (sh.shared ? 0u : w)) * sh.B + (mag - 1), nz);
     }
 }
 
 // ---- 3. scatter into CSR ------------------------------------------------------
-__global__ void msm_scatter_kernel(const uint32_t* __restrict__ digits, uint32_t n, MsmShape sh,
+__global__ void msm_scatter_kernel(const uint32_t* __restrict__ digits, const MsmInst* __restrict__ insts,
+                                   const uint32_t* __restrict__ offs, uint32_t N, MsmShape sh,
                                    uint32_t* __restrict__ cursor, uint32_t* __restrict__ entries,
                                    uint32_t* __restrict__ keys) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < n;
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = j < N;
+    uint32_t set0 = 0, i = 0, stride = 0;
+    if (valid) {
+        const uint32_t k = find_inst(offs, sh.inst, j);
+        i = j - __ldg(offs + k);
+        set0 = k * sh.Wr;
+        stride = insts[k].stride;
+    }
     for (uint32_t w = 0; w < sh.W; w++) {
-        const uint32_t d = valid ? digits[(size_t)w * n + i] : 0u;
+        const uint32_t d = valid ? digits[(size_t)w * N + j] : 0u;
         const bool nz = d != 0;
-        const uint32_t key = (sh.shared ? 0u : w * sh.B) + (d & 0x7fffffffu) - 1;
-        const uint32_t point = sh.shared ? w * sh.stride + i : i;  // fixed-base: row w of the shifted bases
+        const uint32_t key = (set0 + (sh.shared ? 0u : w)) * sh.B + (d & 0x7fffffffu) - 1;
+        const uint32_t point = sh.shared ? w * stride + i : i;  // fixed-base: row w of the shifted bases
         const uint32_t live = __ballot_sync(0xffffffffu, nz);
         if (nz) {
             const uint32_t peers = __match_any_sync(live, key);
@@ -168,9 +212,10 @@ __global__ void msm_scatter_kernel(const uint32_t* __restrict__ digits, uint32_t
 // Emit the accumulated sum of `key` over entry range [e0, e1): final if the bucket
 // lies inside the range, else into the unit's first (bucket began earlier) or last
 // (bucket continues later) slot.
-__device__ __forceinline__ void emit_piece(uint32_t key, const xyzz_t& acc, uint32_t e0, uint32_t e1,
-                                           const uint32_t* __restrict__ row_ptr, xyzz_t* __restrict__ buckets,
-                                           uint32_t* slot_keys, xyzz_t* slot_pts, uint32_t unit) {
+template <class P>
+__device__ __forceinline__ void emit_piece(uint32_t key, const P& acc, uint32_t e0, uint32_t e1,
+                                           const uint32_t* __restrict__ row_ptr, P* __restrict__ buckets,
+                                           uint32_t* slot_keys, P* slot_pts, uint32_t unit) {
     if (row_ptr[key] < e0) {
         slot_keys[2 * unit] = key;
         xyzz_store(slot_pts + 2 * unit, acc);
@@ -182,14 +227,24 @@ __device__ __forceinline__ void emit_piece(uint32_t key, const xyzz_t& acc, uint
     }
 }
 
+// Bases of the instance that owns bucket `key` (sets of B buckets, Wr sets per instance).
+template <class C>
+__device__ __forceinline__ const typename C::A* key_bases(const MsmInst* __restrict__ insts, const MsmShape& sh,
+                                                          uint32_t key) {
+    return static_cast<const typename C::A*>(insts[sh.inst == 1 ? 0u : key / (sh.Wr * sh.B)].bases);
+}
+
+template <class C>
 __global__ void __launch_bounds__(128) msm_accumulate_kernel(const uint32_t* __restrict__ entries,
                                                              const uint32_t* __restrict__ keys,
                                                              const uint32_t* __restrict__ d_total,
                                                              const uint32_t* __restrict__ row_ptr,
-                                                             const affine_t* __restrict__ bases, uint32_t units,
-                                                             xyzz_t* __restrict__ buckets,
+                                                             const MsmInst* __restrict__ insts, MsmShape sh,
+                                                             uint32_t units, typename C::P* __restrict__ buckets,
                                                              uint32_t* __restrict__ slot_keys,
-                                                             xyzz_t* __restrict__ slot_pts) {
+                                                             typename C::P* __restrict__ slot_pts) {
+    using P = typename C::P;
+    using A = typename C::A;
     const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= units) return;
     slot_keys[2 * u] = kNone;
@@ -199,17 +254,19 @@ __global__ void __launch_bounds__(128) msm_accumulate_kernel(const uint32_t* __r
     if (e0 >= M) return;
     const uint32_t e1 = min(e0 + kSegment, M);
     uint32_t cur = keys[e0];
-    xyzz_t acc = xyzz_inf();
+    const A* bases = key_bases<C>(insts, sh, cur);
+    P acc = xyzz_inf<typename C::T>();
     for (uint32_t e = e0; e < e1; e++) {
         const uint32_t k = keys[e];
         if (k != cur) {
             emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
             cur = k;
-            acc = xyzz_inf();
+            bases = key_bases<C>(insts, sh, cur);
+            acc = xyzz_inf<typename C::T>();
         }
         const uint32_t ent = entries[e];
-        affine_t p = affine_load(bases + (ent & 0x7fffffffu));
-        if (ent >> 31) p.y = fe_neg<FqP>(p.y);
+        A p = affine_load(bases + (ent & 0x7fffffffu));
+        if (ent >> 31) p.y = c_neg(p.y);
         acc = xyzz_madd(acc, p.x, p.y);
     }
     emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
@@ -219,13 +276,14 @@ __global__ void __launch_bounds__(128) msm_accumulate_kernel(const uint32_t* __r
 // round, covering entries [u * span, (u+1) * span) (span = kSegment times the product of
 // the group sizes so far). The first merge round uses pairs: most straddling buckets
 // cross exactly one segment boundary, so that round carries nearly all the work.
+template <class C>
 __global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restrict__ in_keys,
-                                                        const xyzz_t* __restrict__ in_pts, uint32_t in_units,
+                                                        const typename C::P* __restrict__ in_pts, uint32_t in_units,
                                                         uint32_t group, const uint32_t* __restrict__ d_total,
                                                         const uint32_t* __restrict__ row_ptr, uint64_t span,
-                                                        uint32_t units, xyzz_t* __restrict__ buckets,
+                                                        uint32_t units, typename C::P* __restrict__ buckets,
                                                         uint32_t* __restrict__ slot_keys,
-                                                        xyzz_t* __restrict__ slot_pts) {
+                                                        typename C::P* __restrict__ slot_pts) {
     const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= units) return;
     slot_keys[2 * u] = kNone;
@@ -238,14 +296,14 @@ __global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restri
     const uint32_t s0 = 2 * u * group;
     const uint32_t s1 = min(2 * (u + 1) * group, 2 * in_units);
     uint32_t cur = kNone;
-    xyzz_t acc = xyzz_inf();
+    typename C::P acc = xyzz_inf<typename C::T>();
     for (uint32_t s = s0; s < s1; s++) {
         const uint32_t k = in_keys[s];
         if (k == kNone) continue;
         if (k != cur) {
             if (cur != kNone) emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
             cur = k;
-            acc = xyzz_inf();
+            acc = xyzz_inf<typename C::T>();
         }
         acc = xyzz_add(acc, xyzz_load(in_pts + s));
     }
@@ -259,13 +317,16 @@ __global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restri
 // twice (buckets -> Y1, E1 -> Y2, E2, F2 = block sums of E1), then WS(Y2) by plain sums:
 // WS(Y2) = sum_j Y2_j + sum_k 2^k M_k, M_k = sum of Y2_j with bit k of (j - 1) set.
 // Level 1: block j of window w holds buckets b = j*g + 1 .. j*g + g (stored at index b - 1).
-__global__ void __launch_bounds__(128) msm_bucket_blocks_kernel(const xyzz_t* __restrict__ buckets, MsmShape sh,
-                                                                xyzz_t* __restrict__ Y, xyzz_t* __restrict__ E) {
+template <class C>
+__global__ void __launch_bounds__(128) msm_bucket_blocks_kernel(const typename C::P* __restrict__ buckets,
+                                                                MsmShape sh, typename C::P* __restrict__ Y,
+                                                                typename C::P* __restrict__ E) {
+    using P = typename C::P;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= sh.Wr * sh.G) return;
-    const xyzz_t* b = buckets + (size_t)t * sh.g;
-    xyzz_t s = xyzz_inf();
-    xyzz_t e = xyzz_inf();
+    if (t >= sh.sets * sh.G) return;
+    const P* b = buckets + (size_t)t * sh.g;
+    P s = xyzz_inf<typename C::T>();
+    P e = xyzz_inf<typename C::T>();
     for (uint32_t u = 0; u < sh.g; u++) {
         s = xyzz_add(s, xyzz_load(b + u));
         if (u + 1 < sh.g) e = xyzz_add(e, s);
@@ -275,16 +336,19 @@ __global__ void __launch_bounds__(128) msm_bucket_blocks_kernel(const xyzz_t* __
 }
 
 // Level 2 over (Y1, E1): Y2, E2 as above on Y1, and F2 = plain block sums of E1.
-__global__ void __launch_bounds__(128) msm_bucket_blocks2_kernel(const xyzz_t* __restrict__ Y1,
-                                                                 const xyzz_t* __restrict__ E1, MsmShape sh,
-                                                                 xyzz_t* __restrict__ Y2, xyzz_t* __restrict__ E2,
-                                                                 xyzz_t* __restrict__ F2) {
+template <class C>
+__global__ void __launch_bounds__(128) msm_bucket_blocks2_kernel(const typename C::P* __restrict__ Y1,
+                                                                 const typename C::P* __restrict__ E1, MsmShape sh,
+                                                                 typename C::P* __restrict__ Y2,
+                                                                 typename C::P* __restrict__ E2,
+                                                                 typename C::P* __restrict__ F2) {
+    using P = typename C::P;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= sh.Wr * sh.G2) return;
+    if (t >= sh.sets * sh.G2) return;
     const size_t base = (size_t)t * sh.g2;
-    xyzz_t s = xyzz_inf();
-    xyzz_t e = xyzz_inf();
-    xyzz_t f = xyzz_inf();
+    P s = xyzz_inf<typename C::T>();
+    P e = xyzz_inf<typename C::T>();
+    P f = xyzz_inf<typename C::T>();
     for (uint32_t u = 0; u < sh.g2; u++) {
         s = xyzz_add(s, xyzz_load(Y1 + base + u));
         if (u + 1 < sh.g2) e = xyzz_add(e, s);
@@ -298,20 +362,22 @@ __global__ void __launch_bounds__(128) msm_bucket_blocks2_kernel(const xyzz_t* _
 // ---- 6. plain sums per (window, target) ---------------------------------------------
 // targets 0 .. plain-1: full sums of P0, P1 (, P2) over G2 entries per window;
 // target plain + k: sum of Ylast_j over j with bit k set.
-__global__ void __launch_bounds__(kTargetThreads) msm_targets_kernel(const xyzz_t* __restrict__ P0,
-                                                                     const xyzz_t* __restrict__ P1,
-                                                                     const xyzz_t* __restrict__ P2,
-                                                                     const xyzz_t* __restrict__ Ylast, MsmShape sh,
-                                                                     xyzz_t* __restrict__ out) {
-    __shared__ xyzz_t red[kTargetThreads];
+template <class C>
+__global__ void __launch_bounds__(C::kTargetThreads) msm_targets_kernel(const typename C::P* __restrict__ P0,
+                                                                        const typename C::P* __restrict__ P1,
+                                                                        const typename C::P* __restrict__ P2,
+                                                                        const typename C::P* __restrict__ Ylast,
+                                                                        MsmShape sh, typename C::P* __restrict__ out) {
+    using P = typename C::P;
+    __shared__ P red[C::kTargetThreads];
     const uint32_t w = blockIdx.x / sh.targets;
     const uint32_t tg = blockIdx.x % sh.targets;
     const bool bits = tg >= sh.plain;
-    const xyzz_t* src = bits ? Ylast : (tg == 0 ? P0 : (tg == 1 ? P1 : P2));
+    const P* src = bits ? Ylast : (tg == 0 ? P0 : (tg == 1 ? P1 : P2));
     src += (size_t)w * sh.G2;
     const uint32_t count = bits ? sh.G2 / 2 : sh.G2;
     const uint32_t k = bits ? tg - sh.plain : 0;
-    xyzz_t acc = xyzz_inf();
+    P acc = xyzz_inf<typename C::T>();
     for (uint32_t t = threadIdx.x; t < count; t += blockDim.x) {
         uint32_t j = t;
         if (bits) j = ((t >> k) << (k + 1)) | (1u << k) | (t & ((1u << k) - 1));
@@ -409,117 +475,164 @@ int shift_bases(Ctx* c, const affine_t* bases, size_t n, uint32_t window_bits, a
 }
 
 // ---- host ---------------------------------------------------------------------------
-static zkh::Xyzz to_host(const xyzz_t& d) {
-    zkh::Xyzz h;
-    std::memcpy(h.X.v, d.X.v, 32);
-    std::memcpy(h.Y.v, d.Y.v, 32);
-    std::memcpy(h.ZZ.v, d.ZZ.v, 32);
-    std::memcpy(h.ZZZ.v, d.ZZZ.v, 32);
+template <class C>
+static zkh::XyzzT<typename HostOf<C>::T> to_host(const typename C::P& d) {
+    static_assert(sizeof(typename C::P) == sizeof(zkh::XyzzT<typename HostOf<C>::T>), "layout");
+    zkh::XyzzT<typename HostOf<C>::T> h;
+    std::memcpy(&h, &d, sizeof(h));
     return h;
 }
 
-static zkh::Xyzz host_dbl_n(zkh::Xyzz p, uint32_t times) {
+template <class H>
+static zkh::XyzzT<H> host_dbl_n(zkh::XyzzT<H> p, uint32_t times) {
     for (uint32_t i = 0; i < times; i++) p = zkh::xyzz_dbl(p);
     return p;
 }
 
-int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
-            uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted, uint32_t shifted_c, uint64_t stride) {
-    ZK_CHECK_ARG(n < (1ull << 31), "MSM size must be below 2^31 points");
-    ZK_CHECK_ARG(window_bits == 0 || (window_bits >= 4 && window_bits <= 20), "window_bits must be 0 or 4..20");
-    if (n == 0) {
-        std::memset(out_xy, 0, 64);
-        *out_is_inf = 1;
-        return ZK_OK;
-    }
-    // fixed-base mode: the bases carry window-shifted rows [2^(c j)] P_i (zk_bases_precompute)
-    const bool fixed = shifted != nullptr && (window_bits == 0 || window_bits == shifted_c);
-    const uint32_t cbits = fixed ? shifted_c : (window_bits ? window_bits : msm_auto_window(n));
-    MsmShape sh = make_shape(cbits);
+uint32_t msm_window_for(const Ctx* c, size_t n) {
+    uint32_t lg = 0;
+    while ((1ull << lg) < n) lg++;
+    if (lg < sizeof(c->tune_msm_window) && c->tune_msm_window[lg] != 0) return c->tune_msm_window[lg];
+    return msm_auto_window(n);
+}
+
+// One pipeline: MSM instances with the same window size and mode, sharing every launch.
+// Instance k's scalars are the global indices [offs[k], offs[k+1]); its bucket sets are
+// [k Wr, (k + 1) Wr). All device scratch lives in one arena carved by pipe_layout.
+template <class C>
+struct MsmPipeT {
+    using P = typename C::P;
+    MsmShape sh{};
+    uint64_t N = 0;            // scalars over all instances
+    uint64_t max_entries = 0;  // N * W
+    uint64_t nbuckets = 0;     // sets * B
+    uint32_t units = 0;        // first-round accumulation units
+    std::vector<MsmInst> inst;
+    std::vector<uint32_t> offs;     // inst + 1 prefix offsets
+    std::vector<size_t> out_index;  // result slot of each instance
+    MsmInst* d_inst = nullptr;
+    uint32_t* d_offs = nullptr;
+    uint32_t *digits = nullptr, *row_ptr = nullptr, *cursor = nullptr, *entries = nullptr, *keys = nullptr,
+             *scan_tmp = nullptr;
+    uint32_t *slot_keys_a = nullptr, *slot_keys_b = nullptr;
+    P *slot_pts_a = nullptr, *slot_pts_b = nullptr;
+    P *buckets = nullptr, *Yb = nullptr, *Eb = nullptr, *Y2 = nullptr, *E2 = nullptr, *F2 = nullptr, *tgt = nullptr;
+    P* h_tgt = nullptr;  // host copy of the per-set targets (sets * targets)
+    uint32_t* h_total = nullptr;
+    size_t host_elems() const { return (size_t)sh.sets * sh.targets; }
+};
+
+// Shape and limits of a pipeline over `jobs` (all with window c, fixed-base mode or not).
+template <class C>
+static int pipe_init(MsmPipeT<C>& p, uint32_t c, bool fixed, const std::vector<MsmInst>& jobs,
+                     const std::vector<size_t>& out_index) {
+    p.sh = make_shape(c);
     if (fixed) {
-        sh.shared = 1;
-        sh.Wr = 1;
-        sh.stride = (uint32_t)stride;
-        ZK_CHECK_ARG((uint64_t)sh.W * stride < (1ull << 31), "fixed-base rows exceed 31-bit entry indices");
+        p.sh.shared = 1;
+        p.sh.Wr = 1;
     }
-    const affine_t* acc_bases = fixed ? shifted : bases;
-    const uint64_t nbuckets = (uint64_t)sh.Wr * sh.B;
-    const uint64_t max_entries = (uint64_t)n * sh.W;
-    ZK_CHECK_ARG(max_entries < (1ull << 32) - kSegment, "MSM too large for 32-bit CSR offsets");
+    p.sh.inst = (uint32_t)jobs.size();
+    p.sh.sets = p.sh.inst * p.sh.Wr;
+    p.inst = jobs;
+    p.out_index = out_index;
+    p.offs.assign(jobs.size() + 1, 0);
+    uint64_t N = 0;
+    for (size_t k = 0; k < jobs.size(); k++) {
+        p.offs[k] = (uint32_t)N;
+        N += jobs[k].n;
+        if (fixed) ZK_CHECK_ARG((uint64_t)p.sh.W * jobs[k].stride < (1ull << 31),
+                                "fixed-base rows exceed 31-bit entry indices");
+    }
+    ZK_CHECK_ARG(N < (1ull << 31), "MSM batch too large: total points must be below 2^31");
+    p.offs[jobs.size()] = (uint32_t)N;
+    p.N = N;
+    p.max_entries = N * p.sh.W;
+    ZK_CHECK_ARG(p.max_entries < (1ull << 32) - kSegment, "MSM too large for 32-bit CSR offsets");
+    p.nbuckets = (uint64_t)p.sh.sets * p.sh.B;
+    ZK_CHECK_ARG(p.nbuckets < (1ull << 32) - 1, "MSM batch has too many buckets for 32-bit keys");
+    p.units = (uint32_t)((p.max_entries + kSegment - 1) / kSegment);
+    return ZK_OK;
+}
 
-    // scratch layout
-    uint32_t *digits = nullptr, *row_ptr = nullptr, *cursor = nullptr, *entries = nullptr, *keys = nullptr;
-    xyzz_t *buckets = nullptr, *Yb = nullptr, *Eb = nullptr, *Y2 = nullptr, *E2 = nullptr, *F2 = nullptr,
-           *tgt = nullptr;
-    std::vector<void*> allocs;
-    auto alloc = [&](size_t bytes, void** p) -> int {
-        int rc = scratch_alloc(c, bytes, p);
-        if (rc == ZK_OK) allocs.push_back(*p);
-        return rc;
+// Assign the device scratch of `p` inside an arena at `base` (null: measure only);
+// returns the arena bytes needed.
+template <class C>
+static size_t pipe_layout(MsmPipeT<C>& p, char* base) {
+    using P = typename C::P;
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> char* {
+        off = (off + 255) & ~(size_t)255;
+        char* r = base ? base + off : nullptr;
+        off += bytes ? bytes : 16;
+        return r;
     };
-    auto release = [&]() {
-        for (void* p : allocs) scratch_free(c, p);
-        allocs.clear();
-    };
-    int rc;
-    if ((rc = alloc(max_entries * 4, (void**)&digits)) != ZK_OK ||
-        (rc = alloc((nbuckets + 1) * 4, (void**)&row_ptr)) != ZK_OK ||
-        (rc = alloc(nbuckets * 4, (void**)&cursor)) != ZK_OK ||
-        (rc = alloc(max_entries * 4, (void**)&entries)) != ZK_OK ||
-        (rc = alloc(max_entries * 4, (void**)&keys)) != ZK_OK ||
-        (rc = alloc(nbuckets * sizeof(xyzz_t), (void**)&buckets)) != ZK_OK ||
-        (rc = alloc((size_t)sh.Wr * sh.G * sizeof(xyzz_t), (void**)&Yb)) != ZK_OK ||
-        (rc = alloc((size_t)sh.Wr * sh.G * sizeof(xyzz_t), (void**)&Eb)) != ZK_OK ||
-        (rc = alloc((size_t)sh.Wr * sh.G2 * sizeof(xyzz_t), (void**)&Y2)) != ZK_OK ||
-        (rc = alloc((size_t)sh.Wr * sh.G2 * sizeof(xyzz_t), (void**)&E2)) != ZK_OK ||
-        (rc = alloc((size_t)sh.Wr * sh.G2 * sizeof(xyzz_t), (void**)&F2)) != ZK_OK ||
-        (rc = alloc((size_t)sh.Wr * sh.targets * sizeof(xyzz_t), (void**)&tgt)) != ZK_OK) {
-        release();
-        return rc;
-    }
+    const MsmShape& sh = p.sh;
+    const size_t first_out = (p.units + kFirstGroup - 1) / kFirstGroup;
+    p.d_inst = reinterpret_cast<MsmInst*>(take(p.inst.size() * sizeof(MsmInst)));
+    p.d_offs = reinterpret_cast<uint32_t*>(take(p.offs.size() * 4));
+    p.digits = reinterpret_cast<uint32_t*>(take(p.max_entries * 4));
+    p.row_ptr = reinterpret_cast<uint32_t*>(take((p.nbuckets + 1) * 4));
+    p.cursor = reinterpret_cast<uint32_t*>(take(p.nbuckets * 4));
+    p.entries = reinterpret_cast<uint32_t*>(take(p.max_entries * 4));
+    p.keys = reinterpret_cast<uint32_t*>(take(p.max_entries * 4));
+    p.scan_tmp = reinterpret_cast<uint32_t*>(take(scan_scratch_elems(p.nbuckets) * 4));
+    p.slot_keys_a = reinterpret_cast<uint32_t*>(take((size_t)2 * p.units * 4));
+    p.slot_pts_a = reinterpret_cast<P*>(take((size_t)2 * p.units * sizeof(P)));
+    p.slot_keys_b = reinterpret_cast<uint32_t*>(take(2 * first_out * 4));
+    p.slot_pts_b = reinterpret_cast<P*>(take(2 * first_out * sizeof(P)));
+    p.buckets = reinterpret_cast<P*>(take(p.nbuckets * sizeof(P)));
+    p.Yb = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G * sizeof(P)));
+    p.Eb = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G * sizeof(P)));
+    p.Y2 = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G2 * sizeof(P)));
+    p.E2 = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G2 * sizeof(P)));
+    p.F2 = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G2 * sizeof(P)));
+    p.tgt = reinterpret_cast<P*>(take(p.host_elems() * sizeof(P)));
+    return off;
+}
+
+// Enqueue the device part of a pipeline on the context stream, ending with the copies of
+// the targets and the entry count to p.h_tgt / p.h_total. Allocates nothing, so it can be
+// captured into a CUDA graph (the instance descriptors are uploaded only if `upload`).
+template <class C>
+static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
+    using P = typename C::P;
     cudaStream_t st = c->stream;
-    ZK_TRY_CUDA(cudaMemsetAsync(row_ptr, 0, (nbuckets + 1) * 4, st));
-    ZK_TRY_CUDA(cudaMemsetAsync(buckets, 0, nbuckets * sizeof(xyzz_t), st));
-
-    const uint32_t nn = (uint32_t)n;
-    ZK_LAUNCH(c, "msm_digits", msm_digits_kernel, (nn + 255) / 256, 256, 0, scalars, bases, nn, scalars_mont, sh, digits,
-              row_ptr);
+    const MsmShape& sh = p.sh;
+    if (upload) {
+        ZK_TRY_CUDA(cudaMemcpyAsync(p.d_inst, p.inst.data(), p.inst.size() * sizeof(MsmInst),
+                                    cudaMemcpyHostToDevice, st));
+        ZK_TRY_CUDA(cudaMemcpyAsync(p.d_offs, p.offs.data(), p.offs.size() * 4, cudaMemcpyHostToDevice, st));
+    }
+    ZK_TRY_CUDA(cudaMemsetAsync(p.row_ptr, 0, (p.nbuckets + 1) * 4, st));
+    ZK_TRY_CUDA(cudaMemsetAsync(p.buckets, 0, p.nbuckets * sizeof(P), st));
+    const uint32_t N = (uint32_t)p.N;
+    const unsigned nblk = (unsigned)((p.N + 255) / 256);
+    ZK_LAUNCH(c, "msm_digits", msm_digits_kernel<C>, nblk, 256, 0, p.d_inst, p.d_offs, N, scalars_mont, sh, p.digits,
+              p.row_ptr);
     ZK_TRY_CUDA(cudaGetLastError());
     // row_ptr[0..nbuckets) := exclusive scan; row_ptr[nbuckets] := total
-    if ((rc = device_exclusive_scan(c, row_ptr, nbuckets, row_ptr + nbuckets)) != ZK_OK) {
-        release();
-        return rc;
-    }
-    ZK_TRY_CUDA(cudaMemcpyAsync(cursor, row_ptr, nbuckets * 4, cudaMemcpyDeviceToDevice, st));
-    ZK_LAUNCH(c, "msm_scatter", msm_scatter_kernel, (nn + 255) / 256, 256, 0, digits, nn, sh, cursor, entries, keys);
+    int rc = device_exclusive_scan(c, p.row_ptr, p.nbuckets, p.row_ptr + p.nbuckets, p.scan_tmp);
+    if (rc != ZK_OK) return rc;
+    ZK_TRY_CUDA(cudaMemcpyAsync(p.cursor, p.row_ptr, p.nbuckets * 4, cudaMemcpyDeviceToDevice, st));
+    ZK_LAUNCH(c, "msm_scatter", msm_scatter_kernel, nblk, 256, 0, p.digits, p.d_inst, p.d_offs, N, sh, p.cursor,
+              p.entries, p.keys);
     ZK_TRY_CUDA(cudaGetLastError());
 
     // accumulation rounds
-    const uint32_t* d_total = row_ptr + nbuckets;
-    uint32_t units = (uint32_t)((max_entries + kSegment - 1) / kSegment);
-    uint32_t *slot_keys_a = nullptr, *slot_keys_b = nullptr;
-    xyzz_t *slot_pts_a = nullptr, *slot_pts_b = nullptr;
-    if ((rc = alloc((size_t)2 * units * 4, (void**)&slot_keys_a)) != ZK_OK ||
-        (rc = alloc((size_t)2 * units * sizeof(xyzz_t), (void**)&slot_pts_a)) != ZK_OK ||
-        (rc = alloc((size_t)2 * ((units + kFirstGroup - 1) / kFirstGroup) * 4, (void**)&slot_keys_b)) != ZK_OK ||
-        (rc = alloc((size_t)2 * ((units + kFirstGroup - 1) / kFirstGroup) * sizeof(xyzz_t), (void**)&slot_pts_b)) !=
-            ZK_OK) {
-        release();
-        return rc;
-    }
-    ZK_LAUNCH(c, "msm_accumulate", msm_accumulate_kernel, (units + 127) / 128, 128, 0, entries, keys, d_total, row_ptr,
-              acc_bases, units, buckets, slot_keys_a, slot_pts_a);
+    const uint32_t* d_total = p.row_ptr + p.nbuckets;
+    ZK_LAUNCH(c, "msm_accumulate", msm_accumulate_kernel<C>, (p.units + 127) / 128, 128, 0, p.entries, p.keys, d_total,
+              p.row_ptr, p.d_inst, sh, p.units, p.buckets, p.slot_keys_a, p.slot_pts_a);
     ZK_TRY_CUDA(cudaGetLastError());
     uint64_t span = kSegment;
-    uint32_t in_units = units;
-    uint32_t *ik = slot_keys_a, *ok = slot_keys_b;
-    xyzz_t *ip = slot_pts_a, *op = slot_pts_b;
+    uint32_t in_units = p.units;
+    uint32_t *ik = p.slot_keys_a, *ok = p.slot_keys_b;
+    typename C::P *ip = p.slot_pts_a, *op = p.slot_pts_b;
     uint32_t group = kFirstGroup;
     while (in_units > 1) {
         const uint32_t out_units = (in_units + group - 1) / group;
         span *= group;
-        ZK_LAUNCH(c, group == kFirstGroup ? "msm_merge_pairs" : "msm_merge", msm_merge_kernel, (out_units + 127) / 128,
-                  128, 0, ik, ip, in_units, group, d_total, row_ptr, span, out_units, buckets, ok, op);
+        ZK_LAUNCH(c, group == kFirstGroup ? "msm_merge_pairs" : "msm_merge", msm_merge_kernel<C>, (out_units + 127) / 128,
+                  128, 0, ik, ip, in_units, group, d_total, p.row_ptr, span, out_units, p.buckets, ok, op);
         ZK_TRY_CUDA(cudaGetLastError());
         std::swap(ik, ok);
         std::swap(ip, op);
@@ -528,61 +641,374 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
     }
 
     // window reduction
-    const uint32_t nblk = sh.Wr * sh.G;
-    ZK_LAUNCH(c, "msm_bucket_blocks", msm_bucket_blocks_kernel, (nblk + 127) / 128, 128, 0, buckets, sh, Yb, Eb);
+    const uint32_t nb1 = sh.sets * sh.G;
+    ZK_LAUNCH(c, "msm_bucket_blocks", msm_bucket_blocks_kernel<C>, (nb1 + 127) / 128, 128, 0, p.buckets, sh, p.Yb, p.Eb);
     ZK_TRY_CUDA(cudaGetLastError());
     if (sh.g2 > 1) {
-        const uint32_t nblk2 = sh.Wr * sh.G2;
-        ZK_LAUNCH(c, "msm_bucket_blocks2", msm_bucket_blocks2_kernel, (nblk2 + 127) / 128, 128, 0, Yb, Eb, sh, Y2, E2,
-                  F2);
+        const uint32_t nb2 = sh.sets * sh.G2;
+        ZK_LAUNCH(c, "msm_bucket_blocks2", msm_bucket_blocks2_kernel<C>, (nb2 + 127) / 128, 128, 0, p.Yb, p.Eb, sh, p.Y2,
+                  p.E2, p.F2);
         ZK_TRY_CUDA(cudaGetLastError());
-        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel, sh.Wr * sh.targets, kTargetThreads, 0, F2, E2, Y2, Y2, sh, tgt);
+        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel<C>, sh.sets * sh.targets, C::kTargetThreads, 0, p.F2, p.E2, p.Y2,
+                  p.Y2, sh, p.tgt);
     } else {
-        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel, sh.Wr * sh.targets, kTargetThreads, 0, Eb, Yb, Yb, Yb, sh, tgt);
+        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel<C>, sh.sets * sh.targets, C::kTargetThreads, 0, p.Eb, p.Yb, p.Yb,
+                  p.Yb, sh, p.tgt);
     }
     ZK_TRY_CUDA(cudaGetLastError());
-    std::vector<xyzz_t> host_t((size_t)sh.Wr * sh.targets);
-    uint32_t total_entries = 0;
-    ZK_TRY_CUDA(cudaMemcpyAsync(host_t.data(), tgt, host_t.size() * sizeof(xyzz_t), cudaMemcpyDeviceToHost, st));
-    ZK_TRY_CUDA(cudaMemcpyAsync(&total_entries, d_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    ZK_TRY_CUDA(cudaStreamSynchronize(st));
-    release();
-    c->msm_entries = total_entries;
-    c->msm_window_bits = sh.c;
-    c->msm_windows = sh.W;
+    ZK_TRY_CUDA(cudaMemcpyAsync(p.h_tgt, p.tgt, p.host_elems() * sizeof(P), cudaMemcpyDeviceToHost, st));
+    ZK_TRY_CUDA(cudaMemcpyAsync(p.h_total, d_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    return ZK_OK;
+}
 
-    // host: one level   S_w = T0 + g (T1 + H)            (T0 = sum E1, T1 = sum Y1)
-    //       two levels  S_w = T0 + g (T1 + g2 (T2 + H))  (T0 = sum F2 = sum E1, T1 = sum E2, T2 = sum Y2)
-    // with H = sum_k 2^k M_k (Horner); then total = sum_w 2^(c w) S_w (Horner over windows).
-    const auto t_host0 = std::chrono::steady_clock::now();
+// Host: instance k of pipeline p from its per-set targets.
+//   one level   S_w = T0 + g (T1 + H)            (T0 = sum E1, T1 = sum Y1)
+//   two levels  S_w = T0 + g (T1 + g2 (T2 + H))  (T0 = sum F2 = sum E1, T1 = sum E2, T2 = sum Y2)
+// with H = sum_k 2^k M_k (Horner); then total = sum_w 2^(c w) S_w (Horner over windows; one
+// set in fixed-base mode, where the window shifts are already in the bases).
+template <class C>
+static void pipe_combine(const MsmPipeT<C>& p, uint32_t k, uint8_t* out_xy, int32_t* out_is_inf) {
+    using H = typename HostOf<C>::T;
+    const MsmShape& sh = p.sh;
     uint32_t log_g = 0, log_g2 = 0;
     while ((1u << log_g) < sh.g) log_g++;
     while ((1u << log_g2) < sh.g2) log_g2++;
-    zkh::Xyzz total = zkh::xyzz_inf();
+    zkh::XyzzT<H> total = zkh::xyzz_inf<H>();
     for (int w = (int)sh.Wr - 1; w >= 0; w--) {
-        const xyzz_t* T = host_t.data() + (size_t)w * sh.targets;
-        zkh::Xyzz h = zkh::xyzz_inf();
-        for (int k = (int)sh.K - 1; k >= 0; k--) {
+        const typename C::P* T = p.h_tgt + ((size_t)k * sh.Wr + (size_t)w) * sh.targets;
+        zkh::XyzzT<H> h = zkh::xyzz_inf<H>();
+        for (int b = (int)sh.K - 1; b >= 0; b--) {
             h = zkh::xyzz_dbl(h);
-            h = zkh::xyzz_add(h, to_host(T[sh.plain + k]));
+            h = zkh::xyzz_add(h, to_host<C>(T[sh.plain + b]));
         }
-        zkh::Xyzz sw = zkh::xyzz_add(h, to_host(T[sh.plain - 1]));
+        zkh::XyzzT<H> sw = zkh::xyzz_add(h, to_host<C>(T[sh.plain - 1]));
         if (sh.plain == 3) {
             sw = host_dbl_n(sw, log_g2);
-            sw = zkh::xyzz_add(sw, to_host(T[1]));
+            sw = zkh::xyzz_add(sw, to_host<C>(T[1]));
         }
         sw = host_dbl_n(sw, log_g);
-        sw = zkh::xyzz_add(sw, to_host(T[0]));
+        sw = zkh::xyzz_add(sw, to_host<C>(T[0]));
         total = host_dbl_n(total, sh.c);
         total = zkh::xyzz_add(total, sw);
     }
-    prof_host(c, "msm_host_combine",
-              std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_host0).count());
-    zkh::F4 x, y;
+    H x, y;
     *out_is_inf = zkh::xyzz_to_affine_canonical(total, &x, &y) ? 1 : 0;
-    std::memcpy(out_xy, x.v, 32);
-    std::memcpy(out_xy + 32, y.v, 32);
+    std::memcpy(out_xy, &x, sizeof(H));
+    std::memcpy(out_xy + sizeof(H), &y, sizeof(H));
+}
+
+// Combine every instance of `pipes` (in parallel host threads when there are several).
+template <class C>
+static void combine_all(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, uint8_t* out_xy, int32_t* out_is_inf) {
+    constexpr size_t kOut = 2 * sizeof(typename HostOf<C>::T);  // bytes of one affine result
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::pair<uint32_t, uint32_t>> tasks;
+    uint64_t entries = 0;
+    for (uint32_t q = 0; q < pipes.size(); q++) {
+        entries += *pipes[q].h_total;
+        for (uint32_t k = 0; k < pipes[q].sh.inst; k++) tasks.emplace_back(q, k);
+    }
+    auto run = [&](size_t t) {
+        const MsmPipeT<C>& p = pipes[tasks[t].first];
+        const size_t o = p.out_index[tasks[t].second];
+        pipe_combine(p, tasks[t].second, out_xy + kOut * o, out_is_inf + o);
+    };
+    const size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
+    const size_t nthreads = std::min<size_t>({tasks.size(), hw, 16});
+    if (nthreads <= 1) {
+        for (size_t t = 0; t < tasks.size(); t++) run(t);
+    } else {
+        std::atomic<size_t> next{0};
+        std::vector<std::thread> th;
+        for (size_t i = 0; i < nthreads; i++)
+            th.emplace_back([&]() {
+                for (size_t t; (t = next.fetch_add(1)) < tasks.size();) run(t);
+            });
+        for (auto& t : th) t.join();
+    }
+    prof_host(c, "msm_host_combine",
+              std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+    c->msm_entries = entries;
+    if (!pipes.empty()) {
+        c->msm_window_bits = pipes.back().sh.c;
+        c->msm_windows = pipes.back().sh.W;
+    }
+}
+
+// Group jobs into pipelines: one per (window bits, fixed-base mode), split where a group
+// would exceed the 31-bit point / 32-bit entry limits.
+template <class C>
+static int build_pipes(Ctx* c, const MsmJob* jobs, size_t count, uint32_t window_bits,
+                       std::vector<MsmPipeT<C>>* out, std::vector<size_t>* empty) {
+    ZK_CHECK_ARG(window_bits == 0 || (window_bits >= 4 && window_bits <= 20), "window_bits must be 0 or 4..20");
+    std::map<std::pair<uint32_t, bool>, std::vector<size_t>> groups;
+    for (size_t j = 0; j < count; j++) {
+        const MsmJob& b = jobs[j];
+        ZK_CHECK_ARG(b.n < (1ull << 31), "MSM size must be below 2^31 points");
+        if (b.n == 0) {
+            empty->push_back(j);
+            continue;
+        }
+        const bool fixed = b.shifted != nullptr && (window_bits == 0 || window_bits == b.shifted_c);
+        const uint32_t cb = fixed ? b.shifted_c : (window_bits ? window_bits : msm_window_for(c, b.n));
+        groups[{cb, fixed}].push_back(j);
+    }
+    for (auto& kv : groups) {
+        const uint32_t cb = kv.first.first;
+        const bool fixed = kv.first.second;
+        const uint64_t W = make_shape(cb).W;
+        std::vector<MsmInst> part;
+        std::vector<size_t> idx;
+        uint64_t N = 0;
+        auto flush = [&]() -> int {
+            if (part.empty()) return ZK_OK;
+            out->emplace_back();
+            int rc = pipe_init<C>(out->back(), cb, fixed, part, idx);
+            part.clear();
+            idx.clear();
+            N = 0;
+            return rc;
+        };
+        for (size_t j : kv.second) {
+            const MsmJob& b = jobs[j];
+            if (!part.empty() && ((N + b.n) >= (1ull << 31) || (N + b.n) * W >= (1ull << 32) - kSegment)) {
+                int rc = flush();
+                if (rc != ZK_OK) return rc;
+            }
+            MsmInst mi;
+            mi.scalars = b.scalars;
+            mi.bases = fixed ? b.shifted : b.bases;
+            mi.n = (uint32_t)b.n;
+            mi.stride = fixed ? (uint32_t)b.stride : 0u;
+            part.push_back(mi);
+            idx.push_back(j);
+            N += b.n;
+        }
+        int rc = flush();
+        if (rc != ZK_OK) return rc;
+    }
     return ZK_OK;
+}
+
+static void set_infinity(uint8_t* out_xy, int32_t* out_is_inf, const std::vector<size_t>& which,
+                         size_t out_bytes = 64) {
+    for (size_t j : which) {
+        std::memset(out_xy + out_bytes * j, 0, out_bytes);
+        out_is_inf[j] = 1;
+    }
+}
+
+template <class C>
+static int batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, uint8_t* out_xy,
+                     int32_t* out_is_inf) {
+    std::vector<MsmPipeT<C>> pipes;
+    std::vector<size_t> empty;
+    int rc = build_pipes<C>(c, jobs, count, window_bits, &pipes, &empty);
+    if (rc != ZK_OK) return rc;
+    set_infinity(out_xy, out_is_inf, empty, 2 * sizeof(typename HostOf<C>::T));
+    if (pipes.empty()) return ZK_OK;
+    size_t bytes = 0, host_elems = 0;
+    std::vector<size_t> at(pipes.size());
+    for (size_t q = 0; q < pipes.size(); q++) {
+        at[q] = bytes;
+        bytes += (pipe_layout(pipes[q], nullptr) + 255) & ~(size_t)255;
+        host_elems += pipes[q].host_elems();
+    }
+    char* arena = nullptr;
+    if ((rc = scratch_alloc(c, bytes, reinterpret_cast<void**>(&arena))) != ZK_OK) return rc;
+    std::vector<typename C::P> host_t(host_elems);
+    std::vector<uint32_t> host_total(pipes.size());
+    size_t h = 0;
+    for (size_t q = 0; q < pipes.size(); q++) {
+        pipe_layout(pipes[q], arena + at[q]);
+        pipes[q].h_tgt = host_t.data() + h;
+        pipes[q].h_total = &host_total[q];
+        h += pipes[q].host_elems();
+        if ((rc = pipe_enqueue<C>(c, pipes[q], scalars_mont, true)) != ZK_OK) {
+            cudaStreamSynchronize(c->stream);
+            scratch_free(c, arena);
+            return rc;
+        }
+    }
+    scratch_free(c, arena);
+    ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
+    combine_all<C>(c, pipes, out_xy, out_is_inf);
+    return ZK_OK;
+}
+
+int msm_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, uint8_t* out_xy,
+                  int32_t* out_is_inf) {
+    return batch_run<CurveG1>(c, jobs, count, scalars_mont, window_bits, out_xy, out_is_inf);
+}
+
+int msm_g2_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits,
+                     uint8_t* out_xy, int32_t* out_is_inf) {
+    for (size_t j = 0; j < count; j++) ZK_CHECK_ARG(jobs[j].shifted == nullptr, "G2 MSMs have no fixed-base mode");
+    return batch_run<CurveG2>(c, jobs, count, scalars_mont, window_bits, out_xy, out_is_inf);
+}
+
+int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
+            uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted, uint32_t shifted_c, uint64_t stride) {
+    MsmJob job;
+    job.scalars = scalars;
+    job.n = n;
+    job.bases = bases;
+    job.shifted = shifted;
+    job.shifted_c = shifted_c;
+    job.stride = stride;
+    int32_t inf = 0;
+    int rc = msm_batch_run(c, &job, 1, scalars_mont, window_bits, out_xy, &inf);
+    *out_is_inf = inf;
+    return rc;
+}
+
+// ---- batch plans: pipelines with plan-owned scalar slots and scratch, optionally replayed
+// as one CUDA graph ------------------------------------------------------------------------
+struct MsmPlan {
+    std::vector<MsmPipeT<CurveG1>> pipes;
+    std::vector<size_t> empty;
+    std::vector<fe*> slots;  // device scalar slot of each job (null for empty jobs)
+    size_t count = 0;
+    int scalars_mont = 1;
+    char* arena = nullptr;
+    void* host = nullptr;  // pinned: targets and totals of every pipeline
+    cudaGraphExec_t exec = nullptr;
+    uint64_t kernels = 0;  // kernel launches per run
+};
+
+int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, bool graph,
+                    MsmPlan** out) {
+    std::unique_ptr<MsmPlan> plan(new MsmPlan());
+    plan->count = count;
+    plan->scalars_mont = scalars_mont;
+    int rc = build_pipes<CurveG1>(c, jobs, count, window_bits, &plan->pipes, &plan->empty);
+    if (rc != ZK_OK) return rc;
+    // arena: scalar slots, then every pipeline's scratch
+    std::vector<size_t> slot_at(count, 0);
+    size_t bytes = 0;
+    for (size_t j = 0; j < count; j++) {
+        slot_at[j] = bytes;
+        bytes += ((size_t)jobs[j].n * sizeof(fe) + 255) & ~(size_t)255;
+    }
+    std::vector<size_t> at(plan->pipes.size());
+    size_t host_bytes = 0;
+    for (size_t q = 0; q < plan->pipes.size(); q++) {
+        at[q] = bytes;
+        bytes += (pipe_layout(plan->pipes[q], nullptr) + 255) & ~(size_t)255;
+        host_bytes += plan->pipes[q].host_elems() * sizeof(xyzz_t) + 16;
+    }
+    ZK_TRY_CUDA(cudaMalloc(reinterpret_cast<void**>(&plan->arena), bytes ? bytes : 16));
+    cudaError_t he = cudaMallocHost(&plan->host, host_bytes ? host_bytes : 16);
+    if (he != cudaSuccess) {
+        cudaFree(plan->arena);
+        set_error(std::string("cudaMallocHost: ") + cudaGetErrorString(he));
+        return ZK_ENOMEM;
+    }
+    auto fail = [&](int code) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(plan->arena);
+        cudaFreeHost(plan->host);
+        return code;
+    };
+    plan->slots.assign(count, nullptr);
+    for (size_t j = 0; j < count; j++)
+        if (jobs[j].n) plan->slots[j] = reinterpret_cast<fe*>(plan->arena + slot_at[j]);
+    char* hp = static_cast<char*>(plan->host);
+    for (size_t q = 0; q < plan->pipes.size(); q++) {
+        MsmPipeT<CurveG1>& p = plan->pipes[q];
+        for (size_t k = 0; k < p.inst.size(); k++) p.inst[k].scalars = plan->slots[p.out_index[k]];
+        pipe_layout(p, plan->arena + at[q]);
+        p.h_tgt = reinterpret_cast<xyzz_t*>(hp);
+        hp += p.host_elems() * sizeof(xyzz_t);
+        p.h_total = reinterpret_cast<uint32_t*>(hp);
+        hp += 16;
+        cudaError_t e1 = cudaMemcpyAsync(p.d_inst, p.inst.data(), p.inst.size() * sizeof(MsmInst),
+                                         cudaMemcpyHostToDevice, c->stream);
+        cudaError_t e2 = cudaMemcpyAsync(p.d_offs, p.offs.data(), p.offs.size() * 4, cudaMemcpyHostToDevice, c->stream);
+        if (e1 != cudaSuccess || e2 != cudaSuccess) {
+            set_error(std::string("plan descriptor upload: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+            return fail(ZK_ECUDA);
+        }
+    }
+    cudaError_t se = cudaStreamSynchronize(c->stream);
+    if (se != cudaSuccess) {
+        set_error(std::string("plan set-up: ") + cudaGetErrorString(se));
+        return fail(ZK_ECUDA);
+    }
+    // kernels per run: counted from one enqueue (captured, or counted at run time)
+    if (graph && !plan->pipes.empty()) {
+        const bool prof_was = c->prof_on;
+        const uint64_t launches_was = c->launches;
+        const auto prof_was_map = c->prof;
+        c->prof_on = false;
+        cudaError_t be = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+        if (be != cudaSuccess) {
+            c->prof_on = prof_was;
+            set_error(std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(be));
+            return fail(ZK_ECUDA);
+        }
+        int erc = ZK_OK;
+        for (auto& p : plan->pipes)
+            if ((erc = pipe_enqueue<CurveG1>(c, p, scalars_mont, false)) != ZK_OK) break;
+        cudaGraph_t g = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+        plan->kernels = c->launches - launches_was;
+        c->launches = launches_was;
+        c->prof = prof_was_map;
+        c->prof_on = prof_was;
+        if (erc != ZK_OK || ee != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            if (erc == ZK_OK) set_error(std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ee));
+            return fail(erc != ZK_OK ? erc : ZK_ECUDA);
+        }
+        cudaError_t ie = cudaGraphInstantiate(&plan->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+            return fail(ZK_ECUDA);
+        }
+    }
+    *out = plan.release();
+    return ZK_OK;
+}
+
+int msm_plan_slot(MsmPlan* plan, size_t index, void** dev) {
+    ZK_CHECK_ARG(index < plan->count, "plan instance index out of range");
+    *dev = plan->slots[index];
+    return ZK_OK;
+}
+
+uint64_t msm_plan_kernels(const MsmPlan* plan) { return plan->kernels; }
+
+int msm_plan_run(Ctx* c, MsmPlan* plan, uint8_t* out_xy, int32_t* out_is_inf) {
+    set_infinity(out_xy, out_is_inf, plan->empty);
+    if (plan->pipes.empty()) return ZK_OK;
+    if (plan->exec) {
+        const int tok = prof_begin(c, "msm_plan_graph");
+        ZK_TRY_CUDA(cudaGraphLaunch(plan->exec, c->stream));
+        prof_end(c, tok);
+        c->launches += plan->kernels - 1;  // prof_begin counted the graph launch as one
+    } else {
+        for (auto& p : plan->pipes) {
+            int rc = pipe_enqueue<CurveG1>(c, p, plan->scalars_mont, false);
+            if (rc != ZK_OK) {
+                cudaStreamSynchronize(c->stream);
+                return rc;
+            }
+        }
+    }
+    ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
+    combine_all<CurveG1>(c, plan->pipes, out_xy, out_is_inf);
+    return ZK_OK;
+}
+
+void msm_plan_destroy(Ctx* c, MsmPlan* plan) {
+    if (plan == nullptr) return;
+    cudaStreamSynchronize(c->stream);
+    if (plan->exec) cudaGraphExecDestroy(plan->exec);
+    cudaFree(plan->arena);
+    cudaFreeHost(plan->host);
+    delete plan;
 }
 
 }  // namespace zk

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 
 #include "zk_internal.cuh"
 
@@ -79,13 +80,13 @@ __device__ __forceinline__ void smem_put(uint4* s_lo, uint4* s_hi, uint32_t i, c
     s_hi[i] = make_uint4(v.v[4], v.v[5], v.v[6], v.v[7]);
 }
 
-__global__ void __launch_bounds__(kNttThreads, 3) ntt_pass_kernel(NttPassParams P) {
-    extern __shared__ uint4 smem[];
+// One CTA's tile `tile` of one pass (shared by the single-transform and the batch kernel).
+__device__ __forceinline__ void ntt_pass_body(const NttPassParams& P, uint32_t tile, uint4* smem) {
     const uint32_t log_r = P.log_r, log_t = P.log_t;
     const uint32_t R = 1u << log_r, T = 1u << log_t, E = R << log_t;
     uint4* s_lo = smem;
     uint4* s_hi = smem + E;
-    const uint32_t c0 = blockIdx.x << log_t;
+    const uint32_t c0 = tile << log_t;
     const uint32_t stride_log = P.log_n - log_r;
     const uint32_t l_mask = (1u << P.log_l) - 1;
     const uint32_t tw_shift = P.log_n - log_r - P.log_l;
@@ -148,6 +149,34 @@ __global__ void __launch_bounds__(kNttThreads, 3) ntt_pass_kernel(NttPassParams 
     }
 }
 
+__global__ void __launch_bounds__(kNttThreads, 3) ntt_pass_kernel(NttPassParams P) {
+    extern __shared__ uint4 smem[];
+    ntt_pass_body(P, blockIdx.x, smem);
+}
+
+// Batch: one launch runs the same pass level of many transforms. CTA b runs tile
+// b - first_tile[i] of item i, the largest i with first_tile[i] <= b; the item's
+// parameters are staged in shared memory once per CTA.
+__global__ void __launch_bounds__(kNttThreads, 3) ntt_pass_batch_kernel(const NttPassParams* __restrict__ items,
+                                                                       const uint32_t* __restrict__ first_tile,
+                                                                       uint32_t nitems) {
+    extern __shared__ uint4 smem[];
+    __shared__ NttPassParams sP;
+    __shared__ uint32_t s_tile;
+    if (threadIdx.x == 0) {
+        uint32_t lo = 0, hi = nitems;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (first_tile[mid] <= blockIdx.x) lo = mid;
+            else hi = mid;
+        }
+        sP = items[lo];
+        s_tile = blockIdx.x - first_tile[lo];
+    }
+    __syncthreads();
+    ntt_pass_body(sP, s_tile, smem);
+}
+
 // ------------------------------------------------------------------------------
 // host side: plans and launches
 // ------------------------------------------------------------------------------
@@ -178,9 +207,17 @@ static std::vector<zkh::F4> powers(const zkh::F4& base, size_t count) {
     return v;
 }
 
-static void split_passes(uint32_t log_n, NttPlan* plan) {
+// Radix bits per pass: the tuned split for log_n when one is set (bits summing to log_n,
+// each 1..11), else the fewest passes of at most 11 bits, as equal as possible.
+static void split_passes(uint32_t log_n, NttPlan* plan, const uint8_t* tuned = nullptr) {
     if (log_n == 0) {
         plan->npass = 0;
+        return;
+    }
+    if (tuned != nullptr && tuned[0] != 0) {
+        int np = 0;
+        for (int p = 0; p < 4 && tuned[p] != 0; p++) plan->pass_log_r[np++] = tuned[p];
+        plan->npass = np;
         return;
     }
     int np = (int)((log_n + kMaxLogR - 1) / kMaxLogR);
@@ -195,7 +232,7 @@ static int build_plan(Ctx* c, int mode, uint32_t log_n, const zkh::F4& omega_m, 
     const zkh::Field& F = zkh::fr();
     NttPlan* plan = new NttPlan();
     plan->log_n = log_n;
-    split_passes(log_n, plan);
+    split_passes(log_n, plan, c->tune_ntt_split[log_n]);
     const bool inverse = (mode == ZK_NTT_COEFFS_FROM_EVALS || mode == ZK_NTT_COSET_COEFFS_FROM_EVALS);
     const zkh::F4 w = inverse ? zkh::inv(F, omega_m) : omega_m;
     const uint64_t n = 1ull << log_n;
@@ -251,6 +288,7 @@ static int get_plan(Ctx* c, int mode, uint32_t log_n, const uint8_t omega[32], c
     key.append(reinterpret_cast<const char*>(shift), 32);
     key.push_back((char)mode);
     key.push_back((char)log_n);
+    key.append(reinterpret_cast<const char*>(c->tune_ntt_split[log_n]), 4);
     auto it = c->ntt_plans.find(key);
     if (it != c->ntt_plans.end()) {
         *out = it->second;
@@ -276,54 +314,61 @@ static int get_plan(Ctx* c, int mode, uint32_t log_n, const uint8_t omega[32], c
     return ZK_OK;
 }
 
-int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log_n, const uint8_t omega[32],
-            const uint8_t shift[32]) {
-    ZK_CHECK_ARG(mode >= 0 && mode <= 3, "invalid NTT mode");
-    ZK_CHECK_ARG(log_n <= 28, "domain too large for BN254 root of unity (log2 n > 28)");
-    const uint64_t n = 1ull << log_n;
-    const bool inverse = (mode == ZK_NTT_COEFFS_FROM_EVALS || mode == ZK_NTT_COSET_COEFFS_FROM_EVALS);
-    ZK_CHECK_ARG(!inverse || in_len == n, "inverse transforms need len(evals) == n (a power of two)");
-    ZK_CHECK_ARG(out != nullptr && (in != nullptr || in_len == 0), "null buffer");
-    NttPlan* plan = nullptr;
-    {
-        std::lock_guard<std::mutex> g(c->mu);
-        int rc = get_plan(c, mode, log_n, omega, shift, &plan);
-        if (rc != ZK_OK) return rc;
+// Dynamic shared memory of the pass kernels (set once per device).
+static int set_smem_attr(int device) {
+    static std::mutex mu;
+    static bool done[64] = {};
+    ZK_CHECK_ARG(device >= 0 && device < 64, "device index out of range");
+    std::lock_guard<std::mutex> g(mu);
+    if (!done[device]) {
+        ZK_TRY_CUDA(cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (2 << kTileLogElems) * 16));
+        ZK_TRY_CUDA(cudaFuncSetAttribute(ntt_pass_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (2 << kTileLogElems) * 16));
+        done[device] = true;
     }
-    const uint32_t valid = (uint32_t)(in_len < n ? in_len : n);
-    if (log_n == 0) {
-        // n == 1: the transform is the identity up to the scale factors
-        NttPassParams P{};
+    return ZK_OK;
+}
+
+// One launch of one pass.
+struct PassLaunch {
+    NttPassParams P;
+    uint32_t blocks, threads, smem;
+};
+
+// Scratch elements a transform needs for its intermediate passes.
+static size_t pass_scratch_elems(const NttPlan* plan, const fe* out, const fe* in) {
+    const size_t n = (size_t)1 << plan->log_n;
+    if (plan->npass <= 1) return 0;
+    if (plan->npass == 2 || in != out) return n;
+    return 2 * n;  // in place with 3+ passes: two scratch buffers, `out` only for the last pass
+}
+
+// The passes of one transform: pass p reads the previous pass's output. Intermediate
+// passes go to scratch (and, out of place with 3+ passes, alternate with `out` so that
+// one scratch buffer suffices); the last pass writes `out`.
+static void make_passes(const NttPlan* plan, fe* out, const fe* in, uint32_t valid, fe* scratch,
+                        std::vector<PassLaunch>* launches) {
+    const uint32_t log_n = plan->log_n;
+    const uint64_t n = 1ull << log_n;
+    launches->clear();
+    NttPassParams P{};
+    P.tw_lo = plan->tw_lo;
+    P.tw_hi = plan->tw_hi;
+    P.s_bits = plan->s_bits;
+    if (log_n == 0) {  // n == 1: the transform is the identity up to the scale factors
         P.in = in;
         P.out = out;
         P.radix_tw = plan->tw_lo;
-        P.tw_lo = plan->tw_lo;
-        P.tw_hi = plan->tw_hi;
         P.pre_lo = plan->pre_lo;
         P.pre_hi = plan->pre_hi;
         P.post_lo = plan->post_lo;
         P.post_hi = plan->post_hi;
         P.in_len = valid;
-        P.log_n = 0;
-        P.log_r = 0;
-        P.log_t = 0;
-        P.log_l = 0;
-        P.s_bits = plan->s_bits;
-        ZK_LAUNCH(c, "ntt_pass", ntt_pass_kernel, 1, 32, 2 * 16, P);
-        ZK_TRY_CUDA(cudaGetLastError());
-        return ZK_OK;
+        launches->push_back({P, 1, 32, 2 * 16});
+        return;
     }
-    fe* scratch = nullptr;
-    if (plan->npass > 1) {
-        int rc = scratch_alloc(c, n * 32, reinterpret_cast<void**>(&scratch));
-        if (rc != ZK_OK) return rc;
-    }
-    static bool attr_set = false;
-    if (!attr_set) {
-        ZK_TRY_CUDA(cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (2 << kTileLogElems) * 16));
-        attr_set = true;
-    }
+    const bool two_scratch = plan->npass >= 3 && in == out;
     uint32_t log_l = 0;
     const fe* src = in;
     for (int p = 0; p < plan->npass; p++) {
@@ -331,35 +376,269 @@ int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log
         // columns per CTA: fill the 2^11-element tile, but not beyond the number of columns
         uint32_t lt = kTileLogElems > (int)lr ? kTileLogElems - lr : 0;
         if (lt > log_n - lr) lt = log_n - lr;
-        // the last pass writes `out`; earlier passes alternate so that pass npass-1 lands in out
         const int remaining = plan->npass - 1 - p;
-        fe* dst = (remaining % 2 == 0) ? out : scratch;
-        NttPassParams P{};
+        fe* dst;
+        if (remaining == 0) dst = out;
+        else if (two_scratch) dst = scratch + (size_t)(p & 1) * n;
+        else dst = (remaining % 2 == 0) ? out : scratch;
         P.in = src;
         P.out = dst;
         P.radix_tw = plan->radix_tw[p];
-        P.tw_lo = plan->tw_lo;
-        P.tw_hi = plan->tw_hi;
         P.pre_lo = p == 0 ? plan->pre_lo : nullptr;
         P.pre_hi = p == 0 ? plan->pre_hi : nullptr;
-        P.post_lo = p == plan->npass - 1 ? plan->post_lo : nullptr;
-        P.post_hi = p == plan->npass - 1 ? plan->post_hi : nullptr;
+        P.post_lo = remaining == 0 ? plan->post_lo : nullptr;
+        P.post_hi = remaining == 0 ? plan->post_hi : nullptr;
         P.in_len = p == 0 ? valid : (uint32_t)n;
         P.log_n = log_n;
         P.log_r = lr;
         P.log_t = lt;
         P.log_l = log_l;
-        P.s_bits = plan->s_bits;
         const uint32_t elems = 1u << (lr + lt);
         const uint32_t threads = elems / 2 < (uint32_t)kNttThreads ? (elems / 2 < 32 ? 32 : elems / 2) : kNttThreads;
-        const uint32_t blocks = (uint32_t)(n >> (lr + lt));
-        ZK_LAUNCH(c, "ntt_pass", ntt_pass_kernel, blocks, threads, (size_t)elems * 32, P);
-        ZK_TRY_CUDA(cudaGetLastError());
+        launches->push_back({P, (uint32_t)(n >> (lr + lt)), threads, elems * 32});
         src = dst;
         log_l += lr;
     }
+}
+
+static int check_job(int mode, const fe* out, const fe* in, size_t in_len, uint32_t log_n) {
+    ZK_CHECK_ARG(mode >= 0 && mode <= 3, "invalid NTT mode");
+    ZK_CHECK_ARG(log_n <= 28, "domain too large for BN254 root of unity (log2 n > 28)");
+    const uint64_t n = 1ull << log_n;
+    const bool inverse = (mode == ZK_NTT_COEFFS_FROM_EVALS || mode == ZK_NTT_COSET_COEFFS_FROM_EVALS);
+    ZK_CHECK_ARG(!inverse || in_len == n, "inverse transforms need len(evals) == n (a power of two)");
+    ZK_CHECK_ARG(out != nullptr && (in != nullptr || in_len == 0), "null buffer");
+    return ZK_OK;
+}
+
+int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log_n, const uint8_t omega[32],
+            const uint8_t shift[32]) {
+    int rc = check_job(mode, out, in, in_len, log_n);
+    if (rc != ZK_OK) return rc;
+    const uint64_t n = 1ull << log_n;
+    NttPlan* plan = nullptr;
+    {
+        std::lock_guard<std::mutex> g(c->mu);
+        if ((rc = get_plan(c, mode, log_n, omega, shift, &plan)) != ZK_OK) return rc;
+    }
+    if ((rc = set_smem_attr(c->device)) != ZK_OK) return rc;
+    const uint32_t valid = (uint32_t)(in_len < n ? in_len : n);
+    fe* scratch = nullptr;
+    const size_t se = pass_scratch_elems(plan, out, in);
+    if (se && (rc = scratch_alloc(c, se * 32, reinterpret_cast<void**>(&scratch))) != ZK_OK) return rc;
+    std::vector<PassLaunch> launches;
+    make_passes(plan, out, in, valid, scratch, &launches);
+    for (const PassLaunch& L : launches) {
+        ZK_LAUNCH(c, "ntt_pass", ntt_pass_kernel, L.blocks, L.threads, L.smem, L.P);
+        ZK_TRY_CUDA(cudaGetLastError());
+    }
     if (scratch) scratch_free(c, scratch);
     return ZK_OK;
+}
+
+// ---- batches: one launch per pass level over every transform of the batch ----------------
+struct NttBatch {
+    std::vector<std::vector<PassLaunch>> jobs;  // passes of each transform
+    std::vector<size_t> scratch_at;             // element offset of each job's scratch
+    size_t scratch_elems = 0;
+    // per level: items and their first tiles, uploaded to `desc`
+    std::vector<std::vector<NttPassParams>> items;
+    std::vector<std::vector<uint32_t>> first;
+    std::vector<uint32_t> blocks, threads, smem;
+    size_t desc_bytes = 0;
+    std::vector<size_t> items_at, first_at;  // byte offsets inside desc
+    char* desc = nullptr;
+    fe* scratch = nullptr;
+};
+
+static int batch_prepare(Ctx* c, const NttJob* jobs, size_t count, NttBatch* b) {
+    b->jobs.assign(count, {});
+    b->scratch_at.assign(count, 0);
+    std::vector<NttPlan*> plans(count, nullptr);
+    for (size_t j = 0; j < count; j++) {
+        const NttJob& J = jobs[j];
+        int rc = check_job(J.mode, J.out, J.in, J.in_len, J.log_n);
+        if (rc != ZK_OK) return rc;
+        ZK_CHECK_ARG(J.omega != nullptr, "null omega");
+        std::lock_guard<std::mutex> g(c->mu);
+        static const uint8_t one[32] = {1};
+        if ((rc = get_plan(c, J.mode, J.log_n, J.omega, J.shift ? J.shift : one, &plans[j])) != ZK_OK) return rc;
+        b->scratch_at[j] = b->scratch_elems;
+        b->scratch_elems += pass_scratch_elems(plans[j], J.out, J.in);
+    }
+    size_t levels = 0;
+    for (size_t j = 0; j < count; j++) levels = std::max<size_t>(levels, std::max(plans[j]->npass, 1));
+    b->items.assign(levels, {});
+    b->first.assign(levels, {});
+    b->blocks.assign(levels, 0);
+    b->threads.assign(levels, 32);
+    b->smem.assign(levels, 32);
+    return ZK_OK;
+}
+
+// Pass parameters once the scratch address is known, grouped by level, and the
+// descriptor layout (items then first tiles, per level).
+static int batch_layout(const NttJob* jobs, size_t count, NttBatch* b, Ctx* c) {
+    for (auto& v : b->items) v.clear();
+    for (auto& v : b->first) v.clear();
+    std::fill(b->blocks.begin(), b->blocks.end(), 0);
+    for (size_t j = 0; j < count; j++) {
+        const NttJob& J = jobs[j];
+        NttPlan* plan = nullptr;
+        {
+            std::lock_guard<std::mutex> g(c->mu);
+            static const uint8_t one[32] = {1};
+            int rc = get_plan(c, J.mode, J.log_n, J.omega, J.shift ? J.shift : one, &plan);
+            if (rc != ZK_OK) return rc;
+        }
+        const uint64_t n = 1ull << J.log_n;
+        const uint32_t valid = (uint32_t)(J.in_len < n ? J.in_len : n);
+        make_passes(plan, J.out, J.in, valid, b->scratch ? b->scratch + b->scratch_at[j] : nullptr, &b->jobs[j]);
+        for (size_t L = 0; L < b->jobs[j].size(); L++) {
+            const PassLaunch& pl = b->jobs[j][L];
+            b->first[L].push_back(b->blocks[L]);
+            b->items[L].push_back(pl.P);
+            b->blocks[L] += pl.blocks;
+            b->threads[L] = std::max(b->threads[L], pl.threads);
+            b->smem[L] = std::max(b->smem[L], pl.smem);
+        }
+    }
+    size_t off = 0;
+    b->items_at.assign(b->items.size(), 0);
+    b->first_at.assign(b->items.size(), 0);
+    for (size_t L = 0; L < b->items.size(); L++) {
+        off = (off + 255) & ~(size_t)255;
+        b->items_at[L] = off;
+        off += b->items[L].size() * sizeof(NttPassParams);
+        off = (off + 255) & ~(size_t)255;
+        b->first_at[L] = off;
+        off += b->first[L].size() * 4;
+    }
+    b->desc_bytes = off ? off : 16;
+    return ZK_OK;
+}
+
+static int batch_upload(Ctx* c, NttBatch* b) {
+    for (size_t L = 0; L < b->items.size(); L++) {
+        ZK_TRY_CUDA(cudaMemcpyAsync(b->desc + b->items_at[L], b->items[L].data(),
+                                    b->items[L].size() * sizeof(NttPassParams), cudaMemcpyHostToDevice, c->stream));
+        ZK_TRY_CUDA(cudaMemcpyAsync(b->desc + b->first_at[L], b->first[L].data(), b->first[L].size() * 4,
+                                    cudaMemcpyHostToDevice, c->stream));
+    }
+    return ZK_OK;
+}
+
+static int batch_enqueue(Ctx* c, const NttBatch* b) {
+    for (size_t L = 0; L < b->items.size(); L++) {
+        if (b->blocks[L] == 0) continue;
+        ZK_LAUNCH(c, "ntt_pass_batch", ntt_pass_batch_kernel, b->blocks[L], b->threads[L], b->smem[L],
+                  reinterpret_cast<const NttPassParams*>(b->desc + b->items_at[L]),
+                  reinterpret_cast<const uint32_t*>(b->desc + b->first_at[L]), (uint32_t)b->items[L].size());
+        ZK_TRY_CUDA(cudaGetLastError());
+    }
+    return ZK_OK;
+}
+
+int ntt_batch_run(Ctx* c, const NttJob* jobs, size_t count) {
+    if (count == 0) return ZK_OK;
+    NttBatch b;
+    int rc = batch_prepare(c, jobs, count, &b);
+    if (rc != ZK_OK) return rc;
+    if ((rc = set_smem_attr(c->device)) != ZK_OK) return rc;
+    if ((rc = batch_layout(jobs, count, &b, c)) != ZK_OK) return rc;  // sizes only
+    char* arena = nullptr;
+    const size_t scratch_bytes = ((b.scratch_elems * 32) + 255) & ~(size_t)255;
+    if ((rc = scratch_alloc(c, scratch_bytes + b.desc_bytes, reinterpret_cast<void**>(&arena))) != ZK_OK) return rc;
+    b.scratch = reinterpret_cast<fe*>(arena);
+    b.desc = arena + scratch_bytes;
+    if ((rc = batch_layout(jobs, count, &b, c)) == ZK_OK && (rc = batch_upload(c, &b)) == ZK_OK)
+        rc = batch_enqueue(c, &b);
+    scratch_free(c, arena);
+    return rc;
+}
+
+struct NttBatchPlan {
+    NttBatch b;
+    char* arena = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t kernels = 0;
+};
+
+int ntt_plan_create(Ctx* c, const NttJob* jobs, size_t count, bool graph, NttBatchPlan** out) {
+    std::unique_ptr<NttBatchPlan> plan(new NttBatchPlan());
+    NttBatch& b = plan->b;
+    int rc = batch_prepare(c, jobs, count, &b);
+    if (rc != ZK_OK) return rc;
+    if ((rc = set_smem_attr(c->device)) != ZK_OK) return rc;
+    if ((rc = batch_layout(jobs, count, &b, c)) != ZK_OK) return rc;
+    const size_t scratch_bytes = ((b.scratch_elems * 32) + 255) & ~(size_t)255;
+    ZK_TRY_CUDA(cudaMalloc(reinterpret_cast<void**>(&plan->arena), scratch_bytes + b.desc_bytes));
+    b.scratch = reinterpret_cast<fe*>(plan->arena);
+    b.desc = plan->arena + scratch_bytes;
+    auto fail = [&](int code) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(plan->arena);
+        return code;
+    };
+    if ((rc = batch_layout(jobs, count, &b, c)) != ZK_OK || (rc = batch_upload(c, &b)) != ZK_OK) return fail(rc);
+    cudaError_t se = cudaStreamSynchronize(c->stream);
+    if (se != cudaSuccess) {
+        set_error(std::string("NTT plan set-up: ") + cudaGetErrorString(se));
+        return fail(ZK_ECUDA);
+    }
+    if (graph && count) {
+        const bool prof_was = c->prof_on;
+        const uint64_t launches_was = c->launches;
+        const auto prof_was_map = c->prof;
+        c->prof_on = false;
+        cudaError_t be = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+        if (be != cudaSuccess) {
+            c->prof_on = prof_was;
+            set_error(std::string("cudaStreamBeginCapture: ") + cudaGetErrorString(be));
+            return fail(ZK_ECUDA);
+        }
+        const int erc = batch_enqueue(c, &b);
+        cudaGraph_t g = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+        plan->kernels = c->launches - launches_was;
+        c->launches = launches_was;
+        c->prof = prof_was_map;
+        c->prof_on = prof_was;
+        if (erc != ZK_OK || ee != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            if (erc == ZK_OK) set_error(std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ee));
+            return fail(erc != ZK_OK ? erc : ZK_ECUDA);
+        }
+        cudaError_t ie = cudaGraphInstantiate(&plan->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+            return fail(ZK_ECUDA);
+        }
+    }
+    *out = plan.release();
+    return ZK_OK;
+}
+
+int ntt_plan_run(Ctx* c, NttBatchPlan* plan) {
+    if (plan->exec) {
+        const int tok = prof_begin(c, "ntt_plan_graph");
+        ZK_TRY_CUDA(cudaGraphLaunch(plan->exec, c->stream));
+        prof_end(c, tok);
+        c->launches += plan->kernels - 1;  // prof_begin counted the graph launch as one
+        return ZK_OK;
+    }
+    return batch_enqueue(c, &plan->b);
+}
+
+uint64_t ntt_plan_kernels(const NttBatchPlan* plan) { return plan->kernels; }
+
+void ntt_plan_destroy(Ctx* c, NttBatchPlan* plan) {
+    if (plan == nullptr) return;
+    cudaStreamSynchronize(c->stream);
+    if (plan->exec) cudaGraphExecDestroy(plan->exec);
+    cudaFree(plan->arena);
+    delete plan;
 }
 
 }  // namespace zk
@@ -410,8 +689,8 @@ static int noalloc_setup(int device, fe** out) {
             set_error(std::string("cudaGetSymbolAddress(g_ntt_noalloc_scratch): ") + cudaGetErrorString(e));
             return ZK_ECUDA;
         }
-        ZK_TRY_CUDA(cudaFuncSetAttribute(ntt_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (2 << kTileLogElems) * 16));
+        int rc = set_smem_attr(device);
+        if (rc != ZK_OK) return rc;
         g_noalloc_ptr[device] = static_cast<fe*>(p);
     }
     *out = g_noalloc_ptr[device];

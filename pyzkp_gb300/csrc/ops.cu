@@ -106,89 +106,111 @@ __device__ fe fe_inverse(const fe& a) {
     return r;
 }
 
-__global__ void fixed_base_kernel(const affine_t* __restrict__ table, const fe* __restrict__ k, size_t n,
-                                  affine_t* __restrict__ out) {
+__device__ __forceinline__ fe c_inv_dev(const fe& a) { return fe_inverse<FqP>(a); }
+// 1 / (a0 + a1 u) = (a0 - a1 u) / (a0^2 + a1^2)
+__device__ __forceinline__ fq2 c_inv_dev(const fq2& a) {
+    const fe t = fe_inverse<FqP>(c_add(c_mul(a.c0, a.c0), c_mul(a.c1, a.c1)));
+    return {c_mul(a.c0, t), c_neg(c_mul(a.c1, t))};
+}
+__device__ __forceinline__ fe c_from_mont_dev(const fe& a) { return fe_from_mont<FqP>(a); }
+__device__ __forceinline__ fq2 c_from_mont_dev(const fq2& a) {
+    return {fe_from_mont<FqP>(a.c0), fe_from_mont<FqP>(a.c1)};
+}
+
+// out[i] = [k_i] P from a table of the 8-bit windows of P: table[j * 256 + d] = [d 2^(8 j)] P.
+template <class C>
+__global__ void fixed_base_kernel(const typename C::A* __restrict__ table, const fe* __restrict__ k, size_t n,
+                                  typename C::A* __restrict__ out) {
+    using T = typename C::T;
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     // reduce k mod r (canonical in) by a Montgomery round trip
     fe s = fe_from_mont<FrP>(fe_to_mont<FrP>(fe_ldg(k + i)));
-    xyzz_t acc = xyzz_inf();
+    XyzzT<T> acc = xyzz_inf<T>();
     for (int j = 0; j < 32; j++) {
         const uint32_t d = (s.v[j >> 2] >> (8 * (j & 3))) & 0xffu;
         if (d) {
-            affine_t p = affine_load(table + j * 256 + d);
+            const typename C::A p = affine_load(table + j * 256 + d);
             acc = xyzz_madd(acc, p.x, p.y);
         }
     }
-    affine_t r;
+    typename C::A r;
     if (xyzz_is_inf(acc)) {
-        r.x = fe_zero();
-        r.y = fe_zero();
+        c_set_zero(r.x);
+        c_set_zero(r.y);
     } else {
-        fe I = fe_inverse<FqP>(fe_mul<FqP>(acc.ZZ, acc.ZZZ));
-        fe izz = fe_mul<FqP>(acc.ZZZ, I);
-        fe izzz = fe_mul<FqP>(acc.ZZ, I);
-        r.x = fe_from_mont<FqP>(fe_mul<FqP>(acc.X, izz));
-        r.y = fe_from_mont<FqP>(fe_mul<FqP>(acc.Y, izzz));
+        const T I = c_inv_dev(c_mul(acc.ZZ, acc.ZZZ));
+        const T izz = c_mul(acc.ZZZ, I);
+        const T izzz = c_mul(acc.ZZ, I);
+        r.x = c_from_mont_dev(c_mul(acc.X, izz));
+        r.y = c_from_mont_dev(c_mul(acc.Y, izzz));
     }
-    fe_store(&out[i].x, r.x);
-    fe_store(&out[i].y, r.y);
+    c_store(&out[i].x, r.x);
+    c_store(&out[i].y, r.y);
 }
 
-int fixed_base_mul(Ctx* c, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_dev) {
+template <class C>
+static int fixed_base_mul_t(Ctx* c, const uint8_t* point_xy, const void* k_dev, size_t n, void* out_dev) {
+    using H = typename HostOf<C>::T;
+    using A = typename C::A;
+    static_assert(sizeof(A) == 2 * sizeof(H), "layout");
     if (n == 0) return ZK_OK;
     ZK_CHECK_ARG(k_dev != nullptr && out_dev != nullptr, "null buffer");
-    const zkh::Field& F = zkh::fq();
-    zkh::F4 px, py;
-    std::memcpy(px.v, point_xy, 32);
-    std::memcpy(py.v, point_xy + 32, 32);
-    std::vector<affine_t> table(32 * 256);
-    std::memset(table.data(), 0, table.size() * sizeof(affine_t));
-    if (!(zkh::is_zero(px) && zkh::is_zero(py))) {
-        zkh::Xyzz base;
-        base.X = zkh::to_mont(F, px);
-        base.Y = zkh::to_mont(F, py);
-        base.ZZ = zkh::one(F);
-        base.ZZZ = zkh::one(F);
-        std::vector<zkh::Xyzz> pts(32 * 256);
+    H px, py;
+    std::memcpy(&px, point_xy, sizeof(H));
+    std::memcpy(&py, point_xy + sizeof(H), sizeof(H));
+    std::vector<A> table(32 * 256);
+    std::memset(table.data(), 0, table.size() * sizeof(A));
+    if (!(zkh::cis_zero(px) && zkh::cis_zero(py))) {
+        zkh::XyzzT<H> base;
+        base.X = zkh::cto_mont(px);
+        base.Y = zkh::cto_mont(py);
+        base.ZZ = zkh::cone<H>();
+        base.ZZZ = zkh::cone<H>();
+        std::vector<zkh::XyzzT<H>> pts(32 * 256);
         for (int j = 0; j < 32; j++) {
-            pts[j * 256] = zkh::xyzz_inf();
+            pts[j * 256] = zkh::xyzz_inf<H>();
             for (int d = 1; d < 256; d++) pts[j * 256 + d] = zkh::xyzz_add(pts[j * 256 + d - 1], base);
             for (int b = 0; b < 8; b++) base = zkh::xyzz_dbl(base);
         }
         // batch normalisation: one inversion of the product of all ZZ * ZZZ
-        std::vector<zkh::F4> pref(pts.size());
-        zkh::F4 run = zkh::one(F);
+        std::vector<H> pref(pts.size());
+        H run = zkh::cone<H>();
         for (size_t i = 0; i < pts.size(); i++) {
             pref[i] = run;
-            if (!zkh::is_zero(pts[i].ZZ)) run = zkh::mul(F, run, zkh::mul(F, pts[i].ZZ, pts[i].ZZZ));
+            if (!zkh::cis_zero(pts[i].ZZ)) run = zkh::cmul(run, zkh::cmul(pts[i].ZZ, pts[i].ZZZ));
         }
-        zkh::F4 inv = zkh::inv(F, run);
+        H inv = zkh::cinv(run);
         for (size_t i = pts.size(); i-- > 0;) {
-            if (zkh::is_zero(pts[i].ZZ)) continue;
-            zkh::F4 zz_zzz = zkh::mul(F, pts[i].ZZ, pts[i].ZZZ);
-            zkh::F4 I = zkh::mul(F, inv, pref[i]);
-            inv = zkh::mul(F, inv, zz_zzz);
-            zkh::F4 izz = zkh::mul(F, pts[i].ZZZ, I);
-            zkh::F4 izzz = zkh::mul(F, pts[i].ZZ, I);
-            zkh::F4 x = zkh::mul(F, pts[i].X, izz);
-            zkh::F4 y = zkh::mul(F, pts[i].Y, izzz);
-            std::memcpy(table[i].x.v, x.v, 32);
-            std::memcpy(table[i].y.v, y.v, 32);
+            if (zkh::cis_zero(pts[i].ZZ)) continue;
+            const H zz_zzz = zkh::cmul(pts[i].ZZ, pts[i].ZZZ);
+            const H I = zkh::cmul(inv, pref[i]);
+            inv = zkh::cmul(inv, zz_zzz);
+            const H x = zkh::cmul(pts[i].X, zkh::cmul(pts[i].ZZZ, I));
+            const H y = zkh::cmul(pts[i].Y, zkh::cmul(pts[i].ZZ, I));
+            std::memcpy(&table[i].x, &x, sizeof(H));
+            std::memcpy(&table[i].y, &y, sizeof(H));
         }
     }
-    affine_t* dtab = nullptr;
-    int rc = scratch_alloc(c, table.size() * sizeof(affine_t), reinterpret_cast<void**>(&dtab));
+    A* dtab = nullptr;
+    int rc = scratch_alloc(c, table.size() * sizeof(A), reinterpret_cast<void**>(&dtab));
     if (rc != ZK_OK) return rc;
-    ZK_TRY_CUDA(cudaMemcpyAsync(dtab, table.data(), table.size() * sizeof(affine_t), cudaMemcpyHostToDevice,
-                                c->stream));
-    ZK_LAUNCH(c, "fixed_base", fixed_base_kernel, (unsigned)((n + 127) / 128), 128, 0, dtab,
-              static_cast<const fe*>(k_dev), n, static_cast<affine_t*>(out_dev));
+    ZK_TRY_CUDA(cudaMemcpyAsync(dtab, table.data(), table.size() * sizeof(A), cudaMemcpyHostToDevice, c->stream));
+    ZK_LAUNCH(c, sizeof(H) == 32 ? "fixed_base" : "fixed_base_g2", fixed_base_kernel<C>,
+              (unsigned)((n + 127) / 128), 128, 0, dtab, static_cast<const fe*>(k_dev), n, static_cast<A*>(out_dev));
     ZK_TRY_CUDA(cudaGetLastError());
     // the host table must outlive the async copy
     ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
     scratch_free(c, dtab);
     return ZK_OK;
+}
+
+int fixed_base_mul(Ctx* c, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_dev) {
+    return fixed_base_mul_t<CurveG1>(c, point_xy, k_dev, n, out_dev);
+}
+
+int fixed_base_mul_g2(Ctx* c, const uint8_t point_xy[128], const void* k_dev, size_t n, void* out_dev) {
+    return fixed_base_mul_t<CurveG2>(c, point_xy, k_dev, n, out_dev);
 }
 
 }  // namespace zk

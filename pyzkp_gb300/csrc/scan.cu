@@ -56,25 +56,41 @@ __global__ void scan_add_kernel(uint32_t* data, size_t n, const uint32_t* offs) 
     if (i < n) data[i] += offs[i / kScanTile];
 }
 
+// Scratch elements device_exclusive_scan needs for n counters (tile sums of every level).
+size_t scan_scratch_elems(size_t n) {
+    size_t total = 0;
+    while (n > 0) {
+        const size_t tiles = (n + kScanTile - 1) / kScanTile;
+        total += tiles + 1;
+        if (tiles <= 1) break;
+        n = tiles;
+    }
+    return total;
+}
+
 // data[0..n) -> exclusive prefix sums; if total != nullptr, *total (device) = sum of the inputs.
-int device_exclusive_scan(Ctx* c, uint32_t* data, size_t n, uint32_t* total) {
+// `scratch` (scan_scratch_elems(n) elements) may be given by the caller, for example by a
+// pipeline that is captured into a CUDA graph; else it is allocated on the stream.
+int device_exclusive_scan(Ctx* c, uint32_t* data, size_t n, uint32_t* total, uint32_t* scratch) {
     if (n == 0) return ZK_OK;
     const size_t tiles = (n + kScanTile - 1) / kScanTile;
-    uint32_t* sums = nullptr;
-    int rc = scratch_alloc(c, (tiles + 1) * sizeof(uint32_t), reinterpret_cast<void**>(&sums));
-    if (rc != ZK_OK) return rc;
+    uint32_t* sums = scratch;
+    if (sums == nullptr) {
+        int rc = scratch_alloc(c, (tiles + 1) * sizeof(uint32_t), reinterpret_cast<void**>(&sums));
+        if (rc != ZK_OK) return rc;
+    }
     ZK_LAUNCH(c, "scan_tiles", scan_tiles_kernel, (unsigned)tiles, kScanThreads, 0, data, n, sums);
     ZK_TRY_CUDA(cudaGetLastError());
     if (tiles > 1) {
         // sums[tiles] receives the grand total through the recursive scan's total slot
-        rc = device_exclusive_scan(c, sums, tiles, total);
+        int rc = device_exclusive_scan(c, sums, tiles, total, scratch ? scratch + tiles + 1 : nullptr);
         if (rc != ZK_OK) return rc;
         ZK_LAUNCH(c, "scan_add", scan_add_kernel, (unsigned)((n + 255) / 256), 256, 0, data, n, sums);
         ZK_TRY_CUDA(cudaGetLastError());
     } else if (total != nullptr) {
         ZK_TRY_CUDA(cudaMemcpyAsync(total, sums, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c->stream));
     }
-    scratch_free(c, sums);
+    if (scratch == nullptr) scratch_free(c, sums);
     return ZK_OK;
 }
 

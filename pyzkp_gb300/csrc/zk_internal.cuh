@@ -17,6 +17,18 @@ namespace zk {
 
 void set_error(const std::string& msg);
 
+// Host coordinate type of each curve (the same bytes as the device type).
+template <class C>
+struct HostOf;
+template <>
+struct HostOf<CurveG1> {
+    using T = zkh::F4;
+};
+template <>
+struct HostOf<CurveG2> {
+    using T = zkh::F2;
+};
+
 #define ZK_TRY_CUDA(call)                                                                     \
     do {                                                                                      \
         cudaError_t _e = (call);                                                              \
@@ -76,6 +88,9 @@ struct Ctx {
     cudaEvent_t timer_start = nullptr, timer_stop = nullptr;
     uint64_t msm_entries = 0;
     uint32_t msm_window_bits = 0, msm_windows = 0;
+    // tuning tables (zk_tune_*, zk_autotune_*): 0 means the built-in rule
+    uint8_t tune_msm_window[32] = {};    // MSM window bits by ceil(log2 n)
+    uint8_t tune_ntt_split[29][4] = {};  // NTT radix bits per pass by log2 n
 };
 
 int prof_begin(Ctx* c, const char* name);
@@ -103,7 +118,49 @@ int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log
 int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
             uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted = nullptr, uint32_t shifted_c = 0,
             uint64_t stride = 0);
+
+// One MSM of a batch: sum_{i < n} scalars[i] * bases[i]; `shifted` (optional) holds the
+// window-shifted rows [2^(c j)] bases[i] with row stride `stride` for fixed-base mode.
+struct MsmJob {
+    const fe* scalars = nullptr;
+    uint64_t n = 0;
+    const void* bases = nullptr;  // affine_t (G1) or affine2_t (G2) points
+    const affine_t* shifted = nullptr;
+    uint32_t shifted_c = 0;
+    uint64_t stride = 0;
+};
+struct MsmPlan;
+uint32_t msm_auto_window(size_t n);
+uint32_t msm_window_for(const Ctx* c, size_t n);
+int msm_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, uint8_t* out_xy,
+                  int32_t* out_is_inf);
+// G2: out_xy holds 128 bytes per instance (x.c0, x.c1, y.c0, y.c1); no fixed-base mode
+int msm_g2_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits,
+                     uint8_t* out_xy, int32_t* out_is_inf);
+int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, bool graph,
+                    MsmPlan** out);
+int msm_plan_slot(MsmPlan* plan, size_t index, void** dev);
+uint64_t msm_plan_kernels(const MsmPlan* plan);
+int msm_plan_run(Ctx* c, MsmPlan* plan, uint8_t* out_xy, int32_t* out_is_inf);
+void msm_plan_destroy(Ctx* c, MsmPlan* plan);
 int shift_bases(Ctx* c, const affine_t* bases, size_t n, uint32_t window_bits, affine_t** out, uint32_t* windows);
+
+// One transform of an NTT batch (the arguments of ntt_run).
+struct NttJob {
+    int mode = 0;
+    fe* out = nullptr;
+    const fe* in = nullptr;
+    size_t in_len = 0;
+    uint32_t log_n = 0;
+    const uint8_t* omega = nullptr;
+    const uint8_t* shift = nullptr;  // null: 1
+};
+struct NttBatchPlan;
+int ntt_batch_run(Ctx* c, const NttJob* jobs, size_t count);
+int ntt_plan_create(Ctx* c, const NttJob* jobs, size_t count, bool graph, NttBatchPlan** out);
+int ntt_plan_run(Ctx* c, NttBatchPlan* plan);
+uint64_t ntt_plan_kernels(const NttBatchPlan* plan);
+void ntt_plan_destroy(Ctx* c, NttBatchPlan* plan);
 
 }  // namespace zk
 
@@ -113,9 +170,20 @@ struct zk_ctx {
 
 struct zk_bases {
     zk_ctx* ctx;
-    zk::affine_t* dev;  // Montgomery affine, (0, 0) = infinity
+    zk::affine_t* dev;  // G1: Montgomery affine, (0, 0) = infinity (null for G2 bases)
     size_t n;
+    zk::affine2_t* dev2 = nullptr;  // G2: Montgomery affine over Fq2 (null for G1 bases)
     zk::affine_t* shifted = nullptr;  // fixed-base rows [2^(c j)] P_i, j < shifted_windows, row stride n
     uint32_t shifted_c = 0;
     uint32_t shifted_windows = 0;
+};
+
+struct zk_msm_plan {
+    zk_ctx* ctx;
+    zk::MsmPlan* impl;
+};
+
+struct zk_ntt_plan {
+    zk_ctx* ctx;
+    zk::NttBatchPlan* impl;
 };

@@ -420,32 +420,24 @@ def register_gb300_kernels(registry, *, ir: Any = None) -> None:
         return {"outputs": {out_id: Buffer(id=out_id, device=Device.CPU, dtype=DType.G1, data=pt)}}
 
     def _msm_many(rt: GpuRuntime, points, scalar_lists, attrs) -> List[Any]:
+        """Instance k = MSM of scalar_lists[k] over points[:len(scalar_lists[k])]
+        (msm_pippenger_batch semantics, crypto/msm/pippenger.py:124-214): one batched call,
+        one pipeline per window size (zk_msm_g1_batch)."""
         lens = [len(s) for s in scalar_lists]
         total = sum(lens)
-        outs: List[Any] = []
         if total == 0:
             return [_g1_point(None) for _ in scalar_lists]
         bases = rt.bases_for(points)
+        _fixed_base(rt, bases, max(lens), attrs)
         flat = rt.zk.alloc(total * 32)
         flat.upload(np.frombuffer(_ints_to_bytes(v for s in scalar_lists for v in s), dtype=np.uint8))
-        off = 0
-        import ctypes
-
-        L = N.load()
-        out = (ctypes.c_uint8 * 64)()
-        inf = ctypes.c_int()
+        ptrs, off = [], 0
         for ln in lens:
-            if ln == 0:
-                outs.append(_g1_point(None))
-                continue
-            N.check(L.zk_msm_g1(rt.zk.handle, bases.handle, 0, flat.ptr + 32 * off, ln, 0, _window_hint(attrs),
-                                out, ctypes.byref(inf)), "zk_msm_g1")
-            raw = bytes(out)
-            outs.append(_g1_point(None if inf.value else (int.from_bytes(raw[:32], "little"),
-                                                          int.from_bytes(raw[32:], "little"))))
+            ptrs.append(flat.ptr + 32 * off)
             off += ln
+        res = rt.zk.msm_g1_batch(bases, ptrs, lens, scalars_mont=False, window_bits=_window_hint(attrs))
         flat.free()
-        return outs
+        return [_g1_point(r) for r in res]
 
     def kzg_batch_commit(ctx):
         node = ctx["node"]

@@ -110,3 +110,28 @@ def test_shim_curve_identities_and_pairing():
     p = O.g1_mul(O.G1_GENERATOR, 123456789)
     q = b.normalize(b.multiply(b.G1, 123456789))
     assert O.affine_to_ints(p) == (int(q[0]), int(q[1]))
+
+
+def test_oracle_g2_matches_shim_and_known_answer():
+    """G2 (crypto/ecc/bn254.py g2_mul / g2_add over py_ecc FQ2): the oracle's Jacobian Fq2
+    arithmetic agrees with the stand-in, and its MSM_G2 with the dlog identity."""
+    from py_ecc import optimized_bn128 as b
+
+    def shim(k):
+        p = b.normalize(b.multiply(b.G2, k))
+        return (int(p[0].coeffs[0]), int(p[0].coeffs[1])), (int(p[1].coeffs[0]), int(p[1].coeffs[1]))
+
+    for k in (1, 2, 3, 0xDEADBEEF, O.FR_MODULUS - 1, (1 << 250) + 12345):
+        assert O.g2_to_ints(O.g2_mul(O.G2_GENERATOR, k)) == shim(k), k
+    assert not O.g2_mul(O.G2_GENERATOR, O.FR_MODULUS).any()  # r G2 = infinity
+    p5, p7 = O.g2_mul(O.G2_GENERATOR, 5), O.g2_mul(O.G2_GENERATOR, 7)
+    assert (O.g2_add(p5, p7) == O.g2_mul(O.G2_GENERATOR, 12)).all()
+    assert (O.g2_add(p5, p5) == O.g2_mul(O.G2_GENERATOR, 10)).all()
+    assert not O.g2_add(p5, O.g2_mul(O.G2_GENERATOR, O.FR_MODULUS - 5)).any()
+    k = synth.base_dlogs(31, 200)
+    k[7] = 0
+    bases = O.g2_fixed_base_mul(O.G2_GENERATOR, k)
+    assert (bases[3] == O.g2_mul(O.G2_GENERATOR, int(synth.limbs_to_ints(k[3:4])[0]))).all()
+    assert not bases[7].any()
+    s = synth.fr_witness_like(32, 200)
+    assert (O.g2_msm(bases, s) == O.g2_msm_known_answer(k, s)).all()
