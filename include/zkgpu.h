@@ -115,6 +115,8 @@ int zk_fq_from_mont(zk_ctx *ctx, void *out, const void *in, size_t n);
 int zk_fr_mul(zk_ctx *ctx, void *out, const void *a, const void *b, size_t n);
 /* out[i] = a[i] - b[i]: POLY_SUB on equal lengths, runtime/kernels/metal/kernels.py:122-167. */
 int zk_fr_sub(zk_ctx *ctx, void *out, const void *a, const void *b, size_t n);
+/* out[i] = a[i] + b[i] (the Groth16 setup's query exponents). */
+int zk_fr_add(zk_ctx *ctx, void *out, const void *a, const void *b, size_t n);
 /* *out = 1 + index of the last non-zero element of a[0..n) (0 if all are zero): the
  * trailing-zero trim of crypto/poly/cpu_ref.py:_trim used by poly_sub (:18-25). Blocks. */
 int zk_fr_trimmed_len(zk_ctx *ctx, const void *a, size_t n, size_t *out);
@@ -166,6 +168,65 @@ int zk_ntt_plan_create(zk_ctx *ctx, size_t count, const int *modes, void *const 
 int zk_ntt_plan_run(zk_ntt_plan *plan);
 int zk_ntt_plan_launches(zk_ntt_plan *plan, uint64_t *kernels);
 int zk_ntt_plan_destroy(zk_ntt_plan *plan);
+
+/*
+ * Groth16 prover vectors (protocols/groth16/prove.py:80-126, r1cs.py:84-92,
+ * qap.py:53-101). Fr vectors are Montgomery device arrays; all asynchronous on the
+ * context stream except zk_fr_r1cs_check and zk_fr_div_xn_minus_1, which block.
+ *   zk_fr_spmv          out[i] = sum_{j in row i} coeffs[j] * x[cols[j]]: a CSR matrix
+ *                       (row_ptr nrows + 1, cols, coeffs Montgomery) times x -- the
+ *                       R1CS rows A w, B w, C w of eval_r1cs_vectors.
+ *   zk_fr_r1cs_check    *bad = #{i : a[i] b[i] != c[i]}: zero iff A B - C vanishes on the
+ *                       domain, i.e. the remainder of qap.py:94-95 is empty.
+ *   zk_fr_qap_quotient  out[i] = (a[i] b[i] - c[i]) * zinv (zinv canonical): on the coset
+ *                       shift * <omega>, zinv = (shift^n - 1)^-1 divides by X^n - 1.
+ *   zk_fr_gather        out[i] = in[idx[i]] (idx uint32 device).
+ *   zk_fr_scale         out[i] = in[i] * s (s canonical).
+ *   zk_fr_powers        out[i] = base^i (base canonical).
+ *   zk_fr_div_xn_minus_1  DIV_XN_MINUS_1 (crypto/poly/fast.py:8-37 through
+ *                       runtime/kernels/cpu/kernels.py:312-323): quotient and remainder
+ *                       of a[0..len) by X^n - 1, trailing zeros trimmed (*qlen, *rlen).
+ *                       q_out holds max(len - n, 0) elements, r_out n elements.
+ */
+int zk_fr_spmv(zk_ctx *ctx, uint32_t nrows, const uint32_t *row_ptr_dev, const uint32_t *cols_dev,
+               const void *coeffs_dev, const void *x_dev, void *out_dev);
+int zk_fr_r1cs_check(zk_ctx *ctx, const void *a, const void *b, const void *c, size_t n, uint64_t *bad);
+int zk_fr_qap_quotient(zk_ctx *ctx, void *out, const void *a, const void *b, const void *c, size_t n,
+                       const uint8_t zinv[32]);
+int zk_fr_gather(zk_ctx *ctx, void *out, const void *in, const uint32_t *idx_dev, size_t n);
+int zk_fr_scale(zk_ctx *ctx, void *out, const void *in, const uint8_t s[32], size_t n);
+int zk_fr_powers(zk_ctx *ctx, void *out, const uint8_t base[32], size_t n);
+int zk_fr_div_xn_minus_1(zk_ctx *ctx, const void *a, size_t len, size_t n, void *q_out, void *r_out, size_t *qlen,
+                         size_t *rlen);
+
+/*
+ * PLONK quotient step (protocols/plonk/prove.py:395-420).
+ *   zk_fr_batch_inv          BATCH_INV (crypto/field/batch.py:8-38 through
+ *                            runtime/kernels/cpu/kernels.py:_batch_inv): out[i] = in[i]^-1,
+ *                            0 for a zero input; out may equal in. Asynchronous.
+ *   zk_plonk_quotient_evals  PLONK_T_QUOTIENT_EVALS (runtime/kernels/cpu/kernels.py:
+ *                            _plonk_t_quotient_evals): from 15 extended-coset evaluation
+ *                            vectors of length m (a, b, c, z, pi, ql, qr, qm, qo, qc, s1, s2,
+ *                            s3, z(omega x), L1; Montgomery) and the op's attrs (canonical:
+ *                            omega_m, shift, shift_n, alpha, beta, gamma, k1, k2; n), writes
+ *                            num (gate + alpha perm + alpha^2 (z - 1) L1) and
+ *                            zh = shift_n (omega_m^n)^i - 1. Asynchronous.
+ */
+int zk_fr_batch_inv(zk_ctx *ctx, void *out, const void *in, size_t n);
+int zk_plonk_quotient_evals(zk_ctx *ctx, const void *const *inputs, size_t m, uint64_t n, const uint8_t omega_m[32],
+                            const uint8_t shift[32], const uint8_t shift_n[32], const uint8_t alpha[32],
+                            const uint8_t beta[32], const uint8_t gamma[32], const uint8_t k1[32],
+                            const uint8_t k2[32], void *num_out, void *zh_out);
+
+/*
+ * Host (CPU) point arithmetic for proof assembly, affine canonical in and out as above:
+ * g1_mul / g2_mul (crypto/ecc/bn254.py g1_mul / g2_mul; k reduced mod r) and g1_add /
+ * g2_add. No context, no device.
+ */
+int zk_host_g1_mul(const uint8_t p[64], const uint8_t k[32], uint8_t out[64]);
+int zk_host_g1_add(const uint8_t p[64], const uint8_t q[64], uint8_t out[64]);
+int zk_host_g2_mul(const uint8_t p[128], const uint8_t k[32], uint8_t out[128]);
+int zk_host_g2_add(const uint8_t p[128], const uint8_t q[128], uint8_t out[128]);
 
 /*
  * Tuning tables of a context (0 = the built-in rule). MSM: window bits for MSMs whose
@@ -263,6 +324,7 @@ int zk_msm_g1_batch(zk_ctx *ctx, size_t count, const zk_bases *const *bases, con
  * infinity). Same pipeline as G1 with Fq2 coordinates; no fixed-base mode.
  */
 int zk_bases_g2_create(zk_ctx *ctx, const void *xy_canonical_host, size_t n, zk_bases **out);
+int zk_bases_g2_create_dev(zk_ctx *ctx, const void *xy_canonical_dev, size_t n, zk_bases **out);
 /* out[i] = [k_i] P on G2 (P host canonical, 128 bytes; k and out as zk_g1_fixed_base_mul). */
 int zk_g2_fixed_base_mul(zk_ctx *ctx, const uint8_t point_xy[128], const void *k_dev, size_t n, void *out_xy_dev);
 int zk_msm_g2(zk_ctx *ctx, const zk_bases *bases, size_t offset, const void *scalars_dev, size_t n,

@@ -249,3 +249,28 @@ def g2_to_ints(p: np.ndarray):
 def affine_to_ints(p: np.ndarray):
     b = np.ascontiguousarray(p, dtype="<u8").tobytes()
     return int.from_bytes(b[:32], "little"), int.from_bytes(b[32:64], "little")
+
+
+def plonk_t_quotient_evals(vecs, n: int, omega_m: int, shift: int, shift_n: int, alpha: int, beta: int,
+                           gamma: int, k1: int, k2: int):
+    """runtime/kernels/cpu/kernels.py:_plonk_t_quotient_evals restated with plain ints (small m):
+    vecs = [a, b, c, z, pi, ql, qr, qm, qo, qc, s1, s2, s3, zshift, l1] (lists of ints).
+    Returns (num, zh)."""
+    r = FR_MODULUS
+    a_, b_, c_, z_, pi_, ql, qr, qm, qo, qc, s1, s2, s3, zs, l1 = vecs
+    m = len(a_)
+    alpha, beta, gamma, k1, k2 = (v % r for v in (alpha, beta, gamma, k1, k2))
+    u = pow(omega_m % r, n, r)
+    x, upow = shift % r, 1
+    num, zh = [], []
+    for i in range(m):
+        a, b, c, z = a_[i] % r, b_[i] % r, c_[i] % r, z_[i] % r
+        gate = (ql[i] * a + qr[i] * b + qm[i] * a * b + qo[i] * c + qc[i] + pi_[i]) % r
+        left = (a + beta * x + gamma) * (b + beta * k1 * x + gamma) * (c + beta * k2 * x + gamma) * z % r
+        right = (a + beta * s1[i] + gamma) * (b + beta * s2[i] + gamma) * (c + beta * s3[i] + gamma) * zs[i] % r
+        boundary = (z - 1) * l1[i] % r
+        num.append((gate + alpha * (left - right) + alpha * alpha * boundary) % r)
+        zh.append((shift_n * upow - 1) % r)
+        upow = upow * u % r
+        x = x * omega_m % r
+    return num, zh

@@ -37,7 +37,10 @@ EXPORTED_SYMBOLS = (
     "zk_ntt_batch", "zk_ntt_plan_create", "zk_ntt_plan_run", "zk_ntt_plan_launches", "zk_ntt_plan_destroy",
     "zk_tune_set_msm_window", "zk_tune_get_msm_window", "zk_tune_set_ntt_split", "zk_tune_get_ntt_split",
     "zk_autotune_msm", "zk_autotune_ntt", "zk_autotune_save", "zk_autotune_load", "zk_bases_g2_create",
-    "zk_msm_g2", "zk_msm_g2_batch", "zk_g2_fixed_base_mul",
+    "zk_msm_g2", "zk_msm_g2_batch", "zk_g2_fixed_base_mul", "zk_fr_spmv", "zk_fr_r1cs_check",
+    "zk_fr_qap_quotient", "zk_fr_gather", "zk_fr_scale", "zk_fr_powers", "zk_fr_div_xn_minus_1", "zk_host_g1_mul",
+    "zk_host_g1_add", "zk_host_g2_mul", "zk_host_g2_add", "zk_fr_add", "zk_bases_g2_create_dev", "zk_fr_batch_inv",
+    "zk_plonk_quotient_evals",
 )
 
 _lib: Optional[ctypes.CDLL] = None
@@ -126,6 +129,22 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_msm_g2": ([P, P, S, P, S, I, U32, P, ctypes.POINTER(ctypes.c_int)], I),
             "zk_msm_g2_batch": ([P, S, PP, P, PP, P, I, U32, P, P], I),
             "zk_g2_fixed_base_mul": ([P, P, P, S, P], I),
+            "zk_fr_spmv": ([P, U32, P, P, P, P, P], I),
+            "zk_fr_r1cs_check": ([P, P, P, P, S, ctypes.POINTER(ctypes.c_uint64)], I),
+            "zk_fr_qap_quotient": ([P, P, P, P, P, S, P], I),
+            "zk_fr_gather": ([P, P, P, P, S], I),
+            "zk_fr_scale": ([P, P, P, P, S], I),
+            "zk_fr_powers": ([P, P, P, S], I),
+            "zk_fr_div_xn_minus_1": ([P, P, S, S, P, P, ctypes.POINTER(ctypes.c_size_t),
+                                      ctypes.POINTER(ctypes.c_size_t)], I),
+            "zk_host_g1_mul": ([P, P, P], I),
+            "zk_host_g1_add": ([P, P, P], I),
+            "zk_host_g2_mul": ([P, P, P], I),
+            "zk_host_g2_add": ([P, P, P], I),
+            "zk_fr_add": ([P, P, P, P, S], I),
+            "zk_bases_g2_create_dev": ([P, P, S, PP], I),
+            "zk_fr_batch_inv": ([P, P, P, S], I),
+            "zk_plonk_quotient_evals": ([P, PP, S, ctypes.c_uint64, P, P, P, P, P, P, P, P, P, P], I),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -245,6 +264,53 @@ def _points_from(out: np.ndarray, inf: np.ndarray):
             b = out[k].tobytes()
             res.append((int.from_bytes(b[:32], "little"), int.from_bytes(b[32:], "little")))
     return res
+
+
+def host_g1_mul(p, k: int):
+    """[k] P on the host; p = (x, y) canonical ints or None (infinity); returns the same form."""
+    out = (ctypes.c_uint8 * 64)()
+    check(load().zk_host_g1_mul(_g1_bytes(p), _fr_bytes(k), out), "zk_host_g1_mul")
+    return _g1_from(bytes(out))
+
+
+def host_g1_add(p, q):
+    out = (ctypes.c_uint8 * 64)()
+    check(load().zk_host_g1_add(_g1_bytes(p), _g1_bytes(q), out), "zk_host_g1_add")
+    return _g1_from(bytes(out))
+
+
+def host_g2_mul(p, k: int):
+    """[k] P on G2; p = ((x0, x1), (y0, y1)) canonical ints or None."""
+    out = (ctypes.c_uint8 * 128)()
+    check(load().zk_host_g2_mul(_g2_bytes(p), _fr_bytes(k), out), "zk_host_g2_mul")
+    b = bytes(out)
+    return None if not any(b) else _g2_from(b)
+
+
+def host_g2_add(p, q):
+    out = (ctypes.c_uint8 * 128)()
+    check(load().zk_host_g2_add(_g2_bytes(p), _g2_bytes(q), out), "zk_host_g2_add")
+    b = bytes(out)
+    return None if not any(b) else _g2_from(b)
+
+
+def _g1_bytes(p) -> bytes:
+    if p is None:
+        return bytes(64)
+    return int(p[0]).to_bytes(32, "little") + int(p[1]).to_bytes(32, "little")
+
+
+def _g1_from(b: bytes):
+    if not any(b):
+        return None
+    return int.from_bytes(b[:32], "little"), int.from_bytes(b[32:], "little")
+
+
+def _g2_bytes(p) -> bytes:
+    if p is None:
+        return bytes(128)
+    (x0, x1), (y0, y1) = p
+    return b"".join(int(v).to_bytes(32, "little") for v in (x0, x1, y0, y1))
 
 
 def _g2_from(b: bytes):
@@ -433,6 +499,10 @@ class Context:
     def fr_sub(self, out: DeviceArray, a: DeviceArray, b: DeviceArray, n: int) -> None:
         check(load().zk_fr_sub(self.handle, out.ptr, a.ptr, b.ptr, n), "zk_fr_sub")
 
+    def fr_add(self, out, a, b, n: int) -> None:
+        check(load().zk_fr_add(self.handle, getattr(out, "ptr", out), getattr(a, "ptr", a), getattr(b, "ptr", b),
+                               int(n)), "zk_fr_add")
+
     def ntt(self, mode: int, out: DeviceArray, inp: Optional[DeviceArray], in_len: int, log_n: int, omega: int,
             shift: int = 1) -> None:
         om = int(omega).to_bytes(32, "little")
@@ -454,6 +524,11 @@ class Context:
         check(load().zk_bases_g2_create(self.handle, a.ctypes.data, a.shape[0], ctypes.byref(h)),
               "zk_bases_g2_create")
         return Bases(self, h.value, a.shape[0])
+
+    def bases_g2_from_device(self, xy: DeviceArray, n: int) -> Bases:
+        h = ctypes.c_void_p()
+        check(load().zk_bases_g2_create_dev(self.handle, xy.ptr, int(n), ctypes.byref(h)), "zk_bases_g2_create_dev")
+        return Bases(self, h.value, int(n))
 
     def msm_g2(self, bases: Bases, scalars: DeviceArray, n: int, *, offset: int = 0, scalars_mont: bool = True,
                window_bits: int = 0):
@@ -603,6 +678,55 @@ class Context:
 
     def autotune_load(self, path: str) -> None:
         check(load().zk_autotune_load(self.handle, os.fsencode(path)), "zk_autotune_load")
+
+    # ---- Groth16 prover vectors (Montgomery device arrays)
+    def fr_spmv(self, nrows: int, row_ptr: DeviceArray, cols: DeviceArray, coeffs: DeviceArray, x, out) -> None:
+        check(load().zk_fr_spmv(self.handle, int(nrows), row_ptr.ptr, cols.ptr, coeffs.ptr, getattr(x, "ptr", x),
+                                getattr(out, "ptr", out)), "zk_fr_spmv")
+
+    def fr_r1cs_check(self, a, b, c, n: int) -> int:
+        bad = ctypes.c_uint64()
+        check(load().zk_fr_r1cs_check(self.handle, getattr(a, "ptr", a), getattr(b, "ptr", b), getattr(c, "ptr", c),
+                                      int(n), ctypes.byref(bad)), "zk_fr_r1cs_check")
+        return int(bad.value)
+
+    def fr_qap_quotient(self, out, a, b, c, n: int, zinv: int) -> None:
+        check(load().zk_fr_qap_quotient(self.handle, getattr(out, "ptr", out), getattr(a, "ptr", a),
+                                        getattr(b, "ptr", b), getattr(c, "ptr", c), int(n), _fr_bytes(zinv)),
+              "zk_fr_qap_quotient")
+
+    def fr_gather(self, out, inp, idx: DeviceArray, n: int) -> None:
+        check(load().zk_fr_gather(self.handle, getattr(out, "ptr", out), getattr(inp, "ptr", inp), idx.ptr, int(n)),
+              "zk_fr_gather")
+
+    def fr_scale(self, out, inp, s: int, n: int) -> None:
+        check(load().zk_fr_scale(self.handle, getattr(out, "ptr", out), getattr(inp, "ptr", inp), _fr_bytes(s),
+                                 int(n)), "zk_fr_scale")
+
+    def fr_powers(self, out, base: int, n: int) -> None:
+        check(load().zk_fr_powers(self.handle, getattr(out, "ptr", out), _fr_bytes(base), int(n)), "zk_fr_powers")
+
+    def fr_batch_inv(self, out, inp, n: int) -> None:
+        check(load().zk_fr_batch_inv(self.handle, getattr(out, "ptr", out), getattr(inp, "ptr", inp), int(n)),
+              "zk_fr_batch_inv")
+
+    def plonk_quotient_evals(self, inputs, m: int, n: int, omega_m: int, shift: int, shift_n: int, alpha: int,
+                             beta: int, gamma: int, k1: int, k2: int, num_out, zh_out) -> None:
+        if len(inputs) != 15:
+            raise ValueError("PLONK quotient takes 15 evaluation vectors")
+        arr = (ctypes.c_void_p * 15)(*[getattr(x, "ptr", x) for x in inputs])
+        check(load().zk_plonk_quotient_evals(self.handle, arr, int(m), int(n), _fr_bytes(omega_m), _fr_bytes(shift),
+                                             _fr_bytes(shift_n), _fr_bytes(alpha), _fr_bytes(beta),
+                                             _fr_bytes(gamma), _fr_bytes(k1), _fr_bytes(k2),
+                                             getattr(num_out, "ptr", num_out), getattr(zh_out, "ptr", zh_out)),
+              "zk_plonk_quotient_evals")
+
+    def fr_div_xn_minus_1(self, a, length: int, n: int, q_out, r_out):
+        ql, rl = ctypes.c_size_t(), ctypes.c_size_t()
+        check(load().zk_fr_div_xn_minus_1(self.handle, getattr(a, "ptr", a), int(length), int(n),
+                                          getattr(q_out, "ptr", q_out), getattr(r_out, "ptr", r_out),
+                                          ctypes.byref(ql), ctypes.byref(rl)), "zk_fr_div_xn_minus_1")
+        return int(ql.value), int(rl.value)
 
     def g2_fixed_base_mul(self, point, k: DeviceArray, n: int, out: DeviceArray) -> None:
         """out[i] = [k_i] P on G2; point = ((x0, x1), (y0, y1)) canonical."""

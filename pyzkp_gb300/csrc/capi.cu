@@ -359,6 +359,11 @@ int zk_fr_sub(zk_ctx* ctx, void* out, const void* a, const void* b, size_t n) {
     return zk::fr_binary(&ctx->impl, 1, out, a, b, n);
 }
 
+int zk_fr_add(zk_ctx* ctx, void* out, const void* a, const void* b, size_t n) {
+    CTX_OR_FAIL(ctx);
+    return zk::fr_binary(&ctx->impl, 2, out, a, b, n);
+}
+
 int zk_ntt(zk_ctx* ctx, int mode, void* out_dev, const void* in_dev, size_t in_len, uint32_t log_n,
            const uint8_t omega[32], const uint8_t shift[32]) {
     CTX_OR_FAIL(ctx);
@@ -606,9 +611,9 @@ int zk_g2_fixed_base_mul(zk_ctx* ctx, const uint8_t point_xy[128], const void* k
     return zk::fixed_base_mul_g2(&ctx->impl, point_xy, k_dev, n, out_xy_dev);
 }
 
-int zk_bases_g2_create(zk_ctx* ctx, const void* xy_canonical_host, size_t n, zk_bases** out) {
+static int bases_g2_create(zk_ctx* ctx, const void* xy_canonical, size_t n, cudaMemcpyKind kind, zk_bases** out) {
     CTX_OR_FAIL(ctx);
-    if (out == nullptr || (n && xy_canonical_host == nullptr)) {
+    if (out == nullptr || (n && xy_canonical == nullptr)) {
         zk::set_error("null pointer");
         return ZK_EINVAL;
     }
@@ -622,8 +627,7 @@ int zk_bases_g2_create(zk_ctx* ctx, const void* xy_canonical_host, size_t n, zk_
         return rc;
     }
     if (n) {
-        cudaError_t e = cudaMemcpyAsync(b->dev2, xy_canonical_host, n * sizeof(zk::affine2_t), cudaMemcpyHostToDevice,
-                                        ctx->impl.stream);
+        cudaError_t e = cudaMemcpyAsync(b->dev2, xy_canonical, n * sizeof(zk::affine2_t), kind, ctx->impl.stream);
         // (x.c0, x.c1, y.c0, y.c1) canonical -> Montgomery, as 4n base-field elements in place
         if (e == cudaSuccess) rc = zk::convert<zk::FqP, 1>(&ctx->impl, b->dev2, b->dev2, 4 * n);
         else {
@@ -642,6 +646,14 @@ int zk_bases_g2_create(zk_ctx* ctx, const void* xy_canonical_host, size_t n, zk_
     }
     *out = b;
     return ZK_OK;
+}
+
+int zk_bases_g2_create(zk_ctx* ctx, const void* xy_canonical_host, size_t n, zk_bases** out) {
+    return bases_g2_create(ctx, xy_canonical_host, n, cudaMemcpyHostToDevice, out);
+}
+
+int zk_bases_g2_create_dev(zk_ctx* ctx, const void* xy_canonical_dev, size_t n, zk_bases** out) {
+    return bases_g2_create(ctx, xy_canonical_dev, n, cudaMemcpyDeviceToDevice, out);
 }
 
 int zk_msm_g2(zk_ctx* ctx, const zk_bases* bases, size_t offset, const void* scalars_dev, size_t n, int scalars_mont,

@@ -35,6 +35,11 @@ __global__ void fr_sub_kernel(fe* out, const fe* a, const fe* b, size_t n) {
         fe_store(out + i, fe_sub<FrP>(fe_ldg(a + i), fe_ldg(b + i)));
 }
 
+__global__ void fr_add_kernel(fe* out, const fe* a, const fe* b, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        fe_store(out + i, fe_add<FrP>(fe_ldg(a + i), fe_ldg(b + i)));
+}
+
 __global__ void last_nonzero_kernel(const fe* a, size_t n, unsigned long long* out) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         if (!fe_is_zero(fe_ldg(a + i))) atomicMax(out, (unsigned long long)(i + 1));
@@ -80,8 +85,11 @@ int fr_binary(Ctx* c, int op, void* out, const void* a, const void* b, size_t n)
     if (op == 0)
         ZK_LAUNCH(c, "fr_mul", fr_mul_kernel, grid_for(n, 256, c->num_sms), 256, 0, static_cast<fe*>(out),
                   static_cast<const fe*>(a), static_cast<const fe*>(b), n);
-    else
+    else if (op == 1)
         ZK_LAUNCH(c, "fr_sub", fr_sub_kernel, grid_for(n, 256, c->num_sms), 256, 0, static_cast<fe*>(out),
+                  static_cast<const fe*>(a), static_cast<const fe*>(b), n);
+    else
+        ZK_LAUNCH(c, "fr_add", fr_add_kernel, grid_for(n, 256, c->num_sms), 256, 0, static_cast<fe*>(out),
                   static_cast<const fe*>(a), static_cast<const fe*>(b), n);
     ZK_TRY_CUDA(cudaGetLastError());
     return ZK_OK;

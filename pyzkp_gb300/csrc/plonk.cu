@@ -1,0 +1,219 @@
+// plonk.cu -- the PLONK quotient step on the device: BATCH_INV and the fused
+// PLONK_T_QUOTIENT_EVALS op.
+//
+// BATCH_INV (runtime/kernels/cpu/kernels.py:_batch_inv -> crypto/field/batch.py:8-38):
+// out[i] = in[i]^-1, and 0 where in[i] == 0. Each thread inverts a chunk of kInvChunk
+// elements with Montgomery's trick (prefix products, one Fermat inversion, a backward
+// pass), so an element costs about three multiplications plus 1/kInvChunk of an inversion.
+//
+// PLONK_T_QUOTIENT_EVALS (runtime/kernels/cpu/kernels.py:_plonk_t_quotient_evals, used by
+// protocols/plonk/prove.py:395-416): at x_i = shift * omega_m^i, i < m, from the
+// extended-coset evaluations of a, b, c, z, pi, ql, qr, qm, qo, qc, s1, s2, s3, z(omega x)
+// and L1, with u = omega_m^n:
+//   gate  = ql a + qr b + qm a b + qo c + qc + pi
+//   perm  = (a + beta x + gamma)(b + beta k1 x + gamma)(c + beta k2 x + gamma) z
+//         - (a + beta s1 + gamma)(b + beta s2 + gamma)(c + beta s3 + gamma) z(omega x)
+//   num_i = gate + alpha perm + alpha^2 (z - 1) L1
+//   zh_i  = shift_n u^i - 1
+// One thread per chunk of kQChunk consecutive points, the powers of omega_m and u carried
+// from the chunk start (computed by square-and-multiply).
+#include <cstring>
+
+#include "zk_internal.cuh"
+
+namespace zk {
+
+static constexpr uint32_t kInvChunk = 32;
+static constexpr uint32_t kQChunk = 16;
+
+template <class F>
+__device__ fe fe_pow_fermat_inv(const fe& a) {
+    // a^(p - 2), left-to-right over the constant exponent
+    fe r = fe_one<F>();
+    for (int limb = 7; limb >= 0; limb--) {
+        const uint32_t e = limb == 0 ? F::P(0) - 2u : F::P(limb);
+        for (int b = 31; b >= 0; b--) {
+            r = fe_sqr<F>(r);
+            if ((e >> b) & 1) r = fe_mul<F>(r, a);
+        }
+    }
+    return r;
+}
+
+__device__ __forceinline__ fe fr_pow_u64(fe base, uint64_t e) {
+    fe acc = fe_one<FrP>();
+    for (; e; e >>= 1) {
+        if (e & 1) acc = fe_mul<FrP>(acc, base);
+        base = fe_mul<FrP>(base, base);
+    }
+    return acc;
+}
+
+// out must not alias in: the backward pass reads in[] again (out holds the prefixes).
+__global__ void fr_batch_inv_kernel(fe* __restrict__ out, const fe* __restrict__ in, size_t n) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t i0 = t * kInvChunk;
+    if (i0 >= n) return;
+    const size_t i1 = i0 + kInvChunk < n ? i0 + kInvChunk : n;
+    fe acc = fe_one<FrP>();
+    for (size_t i = i0; i < i1; i++) {
+        fe_store(out + i, acc);  // product of the non-zero inputs before i
+        const fe x = fe_ldg(in + i);
+        if (!fe_is_zero(x)) acc = fe_mul<FrP>(acc, x);
+    }
+    fe inv = fe_pow_fermat_inv<FrP>(acc);  // acc != 0: a product of non-zero field elements
+    for (size_t i = i1; i-- > i0;) {
+        const fe x = fe_ldg(in + i);
+        if (fe_is_zero(x)) {
+            fe_store(out + i, fe_zero());
+        } else {
+            fe_store(out + i, fe_mul<FrP>(fe_load(out + i), inv));
+            inv = fe_mul<FrP>(inv, x);
+        }
+    }
+}
+
+struct QuotientIn {
+    const fe* v[15];  // a b c z pi ql qr qm qo qc s1 s2 s3 zshift l1 (Montgomery)
+};
+
+struct QuotientK {  // Montgomery constants
+    fe omega_m, u, shift, shift_n, alpha, alpha2, beta, gamma, beta_k1, beta_k2, one;
+};
+
+__global__ void plonk_quotient_kernel(QuotientIn in, QuotientK K, size_t m, fe* __restrict__ num,
+                                      fe* __restrict__ zh) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t i0 = t * kQChunk;
+    if (i0 >= m) return;
+    const size_t i1 = i0 + kQChunk < m ? i0 + kQChunk : m;
+    fe x = fe_mul<FrP>(K.shift, fr_pow_u64(K.omega_m, i0));
+    fe un = fr_pow_u64(K.u, i0);
+    for (size_t i = i0; i < i1; i++) {
+        const fe a = fe_ldg(in.v[0] + i), b = fe_ldg(in.v[1] + i), c = fe_ldg(in.v[2] + i);
+        const fe z = fe_ldg(in.v[3] + i);
+        fe gate = fe_add<FrP>(fe_mul<FrP>(fe_ldg(in.v[5] + i), a), fe_mul<FrP>(fe_ldg(in.v[6] + i), b));
+        gate = fe_add<FrP>(gate, fe_mul<FrP>(fe_mul<FrP>(fe_ldg(in.v[7] + i), a), b));
+        gate = fe_add<FrP>(gate, fe_mul<FrP>(fe_ldg(in.v[8] + i), c));
+        gate = fe_add<FrP>(gate, fe_add<FrP>(fe_ldg(in.v[9] + i), fe_ldg(in.v[4] + i)));
+        const fe t1 = fe_add<FrP>(fe_add<FrP>(a, fe_mul<FrP>(K.beta, x)), K.gamma);
+        const fe t2 = fe_add<FrP>(fe_add<FrP>(b, fe_mul<FrP>(K.beta_k1, x)), K.gamma);
+        const fe t3 = fe_add<FrP>(fe_add<FrP>(c, fe_mul<FrP>(K.beta_k2, x)), K.gamma);
+        const fe left = fe_mul<FrP>(fe_mul<FrP>(fe_mul<FrP>(t1, t2), t3), z);
+        const fe u1 = fe_add<FrP>(fe_add<FrP>(a, fe_mul<FrP>(K.beta, fe_ldg(in.v[10] + i))), K.gamma);
+        const fe u2 = fe_add<FrP>(fe_add<FrP>(b, fe_mul<FrP>(K.beta, fe_ldg(in.v[11] + i))), K.gamma);
+        const fe u3 = fe_add<FrP>(fe_add<FrP>(c, fe_mul<FrP>(K.beta, fe_ldg(in.v[12] + i))), K.gamma);
+        const fe right = fe_mul<FrP>(fe_mul<FrP>(fe_mul<FrP>(u1, u2), u3), fe_ldg(in.v[13] + i));
+        const fe perm = fe_sub<FrP>(left, right);
+        const fe boundary = fe_mul<FrP>(fe_sub<FrP>(z, K.one), fe_ldg(in.v[14] + i));
+        const fe v = fe_add<FrP>(gate, fe_add<FrP>(fe_mul<FrP>(K.alpha, perm), fe_mul<FrP>(K.alpha2, boundary)));
+        fe_store(num + i, v);
+        fe_store(zh + i, fe_sub<FrP>(fe_mul<FrP>(K.shift_n, un), K.one));
+        un = fe_mul<FrP>(un, K.u);
+        x = fe_mul<FrP>(x, K.omega_m);
+    }
+}
+
+static fe mont_fr(const uint8_t canonical[32]) {
+    zkh::F4 v;
+    std::memcpy(v.v, canonical, 32);
+    const zkh::F4 m = zkh::to_mont(zkh::fr(), v);
+    fe r;
+    std::memcpy(r.v, m.v, 32);
+    return r;
+}
+
+static fe mont_of(const zkh::F4& m) {
+    fe r;
+    std::memcpy(r.v, m.v, 32);
+    return r;
+}
+
+}  // namespace zk
+
+using zk::fe;
+
+extern "C" {
+
+int zk_fr_batch_inv(zk_ctx* ctx, void* out, const void* in, size_t n) {
+    if (ctx == nullptr) {
+        zk::set_error("null zk_ctx");
+        return ZK_EINVAL;
+    }
+    if (n == 0) return ZK_OK;
+    if (!out || !in) {
+        zk::set_error("null buffer");
+        return ZK_EINVAL;
+    }
+    ZK_TRY_CUDA(cudaSetDevice(ctx->impl.device));
+    zk::Ctx* c = &ctx->impl;
+    const fe* src = static_cast<const fe*>(in);
+    void* copy = nullptr;
+    if (out == in) {  // the kernel keeps its prefixes in out and re-reads in: copy the input
+        int rc = zk::scratch_alloc(c, n * 32, &copy);
+        if (rc != ZK_OK) return rc;
+        ZK_TRY_CUDA(cudaMemcpyAsync(copy, in, n * 32, cudaMemcpyDeviceToDevice, c->stream));
+        src = static_cast<const fe*>(copy);
+    }
+    const size_t chunks = (n + zk::kInvChunk - 1) / zk::kInvChunk;
+    ZK_LAUNCH(c, "fr_batch_inv", zk::fr_batch_inv_kernel, (unsigned)((chunks + 127) / 128), 128, 0,
+              static_cast<fe*>(out), src, n);
+    ZK_TRY_CUDA(cudaGetLastError());
+    if (copy) zk::scratch_free(c, copy);
+    return ZK_OK;
+}
+
+int zk_plonk_quotient_evals(zk_ctx* ctx, const void* const* inputs, size_t m, uint64_t n, const uint8_t omega_m[32],
+                            const uint8_t shift[32], const uint8_t shift_n[32], const uint8_t alpha[32],
+                            const uint8_t beta[32], const uint8_t gamma[32], const uint8_t k1[32],
+                            const uint8_t k2[32], void* num_out, void* zh_out) {
+    if (ctx == nullptr) {
+        zk::set_error("null zk_ctx");
+        return ZK_EINVAL;
+    }
+    if (m == 0) return ZK_OK;
+    if (!inputs || !num_out || !zh_out || !omega_m || !shift || !shift_n || !alpha || !beta || !gamma || !k1 || !k2) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    ZK_TRY_CUDA(cudaSetDevice(ctx->impl.device));
+    zk::QuotientIn in;
+    for (int i = 0; i < 15; i++) {
+        if (inputs[i] == nullptr) {
+            zk::set_error("null input vector");
+            return ZK_EINVAL;
+        }
+        in.v[i] = static_cast<const fe*>(inputs[i]);
+    }
+    const zkh::Field& F = zkh::fr();
+    zk::QuotientK K;
+    K.omega_m = zk::mont_fr(omega_m);
+    zkh::F4 om;
+    std::memcpy(om.v, omega_m, 32);
+    K.u = zk::mont_of(zkh::pow_u64(F, zkh::to_mont(F, om), n));
+    K.shift = zk::mont_fr(shift);
+    K.shift_n = zk::mont_fr(shift_n);
+    K.alpha = zk::mont_fr(alpha);
+    zkh::F4 a;
+    std::memcpy(a.v, alpha, 32);
+    const zkh::F4 am = zkh::to_mont(F, a);
+    K.alpha2 = zk::mont_of(zkh::mul(F, am, am));
+    K.beta = zk::mont_fr(beta);
+    K.gamma = zk::mont_fr(gamma);
+    zkh::F4 b, kk1, kk2;
+    std::memcpy(b.v, beta, 32);
+    std::memcpy(kk1.v, k1, 32);
+    std::memcpy(kk2.v, k2, 32);
+    const zkh::F4 bm = zkh::to_mont(F, b);
+    K.beta_k1 = zk::mont_of(zkh::mul(F, bm, zkh::to_mont(F, kk1)));
+    K.beta_k2 = zk::mont_of(zkh::mul(F, bm, zkh::to_mont(F, kk2)));
+    K.one = zk::mont_of(zkh::one(F));
+    zk::Ctx* c = &ctx->impl;
+    const size_t chunks = (m + zk::kQChunk - 1) / zk::kQChunk;
+    ZK_LAUNCH(c, "plonk_quotient", zk::plonk_quotient_kernel, (unsigned)((chunks + 127) / 128), 128, 0, in, K, m,
+              static_cast<fe*>(num_out), static_cast<fe*>(zh_out));
+    ZK_TRY_CUDA(cudaGetLastError());
+    return ZK_OK;
+}
+
+}  // extern "C"

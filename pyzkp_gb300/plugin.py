@@ -4,7 +4,9 @@
 ``register_metal_kernels`` (runtime/kernels/metal/kernels.py:12-20), i.e.
 ``(OpType.X, Device.METAL, Backend.METAL)`` for POINTWISE_MUL, POLY_SUB,
 ROOTS_EVALS_FROM_COEFFS, ROOTS_COEFFS_FROM_EVALS, COSET_EVALS_FROM_COEFFS,
-COSET_COEFFS_FROM_EVALS, MSM_G1, KZG_BATCH_COMMIT (plus MSM_G1_BATCH), and
+COSET_COEFFS_FROM_EVALS, MSM_G1, KZG_BATCH_COMMIT (plus MSM_G1_BATCH, and MSM_G2,
+POLY_MUL_NTT, DIV_XN_MINUS_1, BATCH_INV and PLONK_T_QUOTIENT_EVALS, which the reference
+runs on the CPU only), and
 replaces the transfer kernels (TO_DEVICE on CPU, FROM_DEVICE on CPU and METAL,
 runtime/kernels/cpu/kernels.py:75-77,98-172) so that device data lives in GB300
 memory. ``Executor._run_node`` (runtime/executor.py:167-218) calls them unchanged.
@@ -57,6 +59,26 @@ class GpuBuffer:
     def __len__(self) -> int:
         return int(self.n)
 
+    def to_host(self) -> List[int]:
+        """The canonical values (one device-to-host read; Montgomery -> canonical on the device)."""
+        n = int(self.n)
+        if n == 0:
+            return []
+        zk = self.mtl_buffer.ctx
+        tmp = zk.alloc(n * 32)
+        zk.fr_from_mont(tmp, self.mtl_buffer, n)
+        vals = _bytes_to_ints(tmp.download(n * 32), n)
+        tmp.free()
+        return vals
+
+    # Callers that read kept device outputs as lists (protocols/groth16/qap.py:93-97 does
+    # list(g.buffers[...].data)) get the canonical values.
+    def __iter__(self):
+        return iter(self.to_host())
+
+    def __getitem__(self, i):
+        return self.to_host()[i]
+
 
 class _DeviceAllocator:
     """The ``rt.device.newBufferWithLength_options_`` protocol used by MemoryPool.alloc_metal
@@ -86,21 +108,22 @@ class GpuRuntime:
         return GpuRuntime(N.Context(device))
 
     # -- resident bases ------------------------------------------------------
-    def bases_for(self, points) -> N.Bases:
-        """Montgomery affine copy of ``points`` on the device.
+    def bases_for(self, points, g2: bool = False) -> N.Bases:
+        """Montgomery affine copy of ``points`` (G1, or G2 with ``g2``) on the device.
 
         Tuples (the reference's ``cached_points_tuple`` form, runtime/warmup.py:17-26)
         are cached by identity while a reference is held; lists by identity plus a
         fingerprint of sampled coordinates, since they can be mutated in place.
         """
-        key = ("t", id(points)) if isinstance(points, tuple) else ("l", id(points), _fingerprint(points))
+        tag = "t2" if g2 else "t"
+        key = (tag, id(points)) if isinstance(points, tuple) else ("l" + tag, id(points), _fingerprint(points))
         hit = self._bases.get(key)
         if hit is not None and hit[0] is points:
             self._bases_order.remove(key)
             self._bases_order.append(key)
             return hit[1]
-        xy = points_to_affine_array(points)
-        b = self.zk.bases_from_host(xy)
+        xy = points_g2_to_affine_array(points) if g2 else points_to_affine_array(points)
+        b = self.zk.bases_g2_from_host(xy) if g2 else self.zk.bases_from_host(xy)
         size = xy.nbytes
         while self._bases_order and self._bases_bytes + size > self._bases_budget:
             old = self._bases_order.pop(0)
@@ -126,7 +149,9 @@ def _fingerprint(points) -> int:
     acc = [n]
     for i in idx:
         p = points[i]
-        acc.extend(int(c) if not isinstance(c, tuple) else 0 for c in p)
+        for c in p:
+            coeffs = getattr(c, "coeffs", None)
+            acc.extend(int(v) for v in coeffs) if coeffs is not None else acc.append(int(c))
     return hash(tuple(acc))
 
 
@@ -154,6 +179,43 @@ def points_to_affine_array(points) -> np.ndarray:
         out[64 * i:64 * i + 32] = x.to_bytes(32, "little")
         out[64 * i + 32:64 * i + 64] = y.to_bytes(32, "little")
     return np.frombuffer(bytes(out), dtype="<u8").reshape(n, 8).astype(np.uint64) if n else np.zeros((0, 8), np.uint64)
+
+
+def points_g2_to_affine_array(points) -> np.ndarray:
+    """Sequence of py_ecc G2 points (FQ2 coordinates) -> uint64[n, 16] affine canonical
+    (x.c0, x.c1, y.c0, y.c1), all zero for infinity."""
+    n = len(points)
+    out = bytearray(128 * n)
+    b = None
+    for i, p in enumerate(points):
+        z = p[2]
+        if all(int(v) == 0 for v in z.coeffs):
+            continue
+        if int(z.coeffs[0]) == 1 and int(z.coeffs[1]) == 0:
+            x, y = p[0], p[1]
+        else:
+            if b is None:
+                b = _py_ecc()
+            x, y = b.normalize(p)
+        vals = (int(x.coeffs[0]), int(x.coeffs[1]), int(y.coeffs[0]), int(y.coeffs[1]))
+        out[128 * i:128 * i + 128] = b"".join(v.to_bytes(32, "little") for v in vals)
+    return np.frombuffer(bytes(out), dtype="<u8").reshape(n, 16).astype(np.uint64) if n else np.zeros((0, 16),
+                                                                                                     np.uint64)
+
+
+def _g2_point(res):
+    """((x0, x1), (y0, y1)) or None -> the reference's G2 object (FQ2 coordinates)."""
+    b = _py_ecc()
+    if res is None:
+        return b.Z2
+    (x0, x1), (y0, y1) = res
+    return (b.FQ2([x0, x1]), b.FQ2([y0, y1]), b.FQ2.one())
+
+
+def _omega_for_size(n: int) -> int:
+    """crypto/poly/ntt.py:13-24 (ROOT_2_28 of ntt.py:8)."""
+    root = 19103219067921713944291392827692070036145651957329286315305642004821462161904
+    return pow(root, 1 << (_MAX_LOG_N - _log2_exact(n)), FR_MODULUS)
 
 
 def _g1_point(res):
@@ -419,6 +481,112 @@ def register_gb300_kernels(registry, *, ir: Any = None) -> None:
             pt = _g1_point(rt.zk.msm_g1(bases, gs.mtl_buffer, num, window_bits=_window_hint(ctx["attrs"])))
         return {"outputs": {out_id: Buffer(id=out_id, device=Device.CPU, dtype=DType.G1, data=pt)}}
 
+    def msm_g2(ctx):
+        """MSM_G2 (runtime/kernels/cpu/kernels.py:338-348,574-582; CPU-only in the reference)."""
+        node = ctx["node"]
+        points, scalars = ctx["inputs"][0], ctx["inputs"][1]
+        out_id = node.outputs[0]
+        rt = _runtime(ctx, "msm_g2")
+        if scalars.dtype != DType.FR:
+            raise ValueError("gb300 msm_g2 scalars must be FR")
+        gs = _device_fr(ctx, scalars, "msm_g2")
+        num = int(gs.n)
+        if num > len(points.data):
+            raise ValueError("scalars length exceeds points length")
+        if num == 0:
+            pt = _g2_point(None)
+        else:
+            bases = rt.bases_for(points.data, g2=True)
+            pt = _g2_point(rt.zk.msm_g2(bases, gs.mtl_buffer, num, window_bits=_window_hint(ctx["attrs"])))
+        return {"outputs": {out_id: Buffer(id=out_id, device=Device.CPU, dtype=DType.G2, data=pt)}}
+
+    def poly_mul_ntt(ctx):
+        """POLY_MUL_NTT (runtime/kernels/cpu/kernels.py:288-298 -> crypto/poly/ntt.py:149-162):
+        a * b through NTTs of size 2^ceil(log2(len a + len b - 1)), trailing zeros trimmed."""
+        node = ctx["node"]
+        a, b = ctx["inputs"][0], ctx["inputs"][1]
+        out_id = node.outputs[0]
+        if a.dtype != DType.FR or b.dtype != DType.FR:
+            raise ValueError("gb300 poly_mul_ntt supports FR only")
+        ga, gb_ = _device_fr(ctx, a, "poly_mul_ntt"), _device_fr(ctx, b, "poly_mul_ntt")
+        rt = _runtime(ctx, "poly_mul_ntt")
+        na, nb = int(ga.n), int(gb_.n)
+        if na == 0 or nb == 0:
+            res = GpuBuffer(dtype="fr_mont_u64x4", n=0, mtl_buffer=rt.zk.alloc(16))
+            return {"outputs": {out_id: Buffer(id=out_id, device=METAL, dtype=DType.FR, data=res, meta={"n": 0})}}
+        need = na + nb - 1
+        n = 1 << (need - 1).bit_length()
+        lg, om = _log2_exact(n), _omega_for_size(n)
+        ea = _alloc(ctx, rt, n * 32)
+        eb = rt.zk.alloc(n * 32)
+        rt.zk.ntt_batch([(N.NTT_EVALS_FROM_COEFFS, ea, ga.mtl_buffer, na, lg, om, 1),
+                         (N.NTT_EVALS_FROM_COEFFS, eb, gb_.mtl_buffer, nb, lg, om, 1)])
+        rt.zk.fr_mul(ea, ea, eb, n)
+        rt.zk.ntt(N.NTT_COEFFS_FROM_EVALS, ea, ea, n, lg, om)
+        out_n = rt.zk.fr_trimmed_len(ea, need)
+        eb.free()
+        res = GpuBuffer(dtype="fr_mont_u64x4", n=out_n, mtl_buffer=ea)
+        return {"outputs": {out_id: Buffer(id=out_id, device=METAL, dtype=DType.FR, data=res, meta={"n": out_n})}}
+
+    def div_xn_minus_1(ctx):
+        """DIV_XN_MINUS_1 (runtime/kernels/cpu/kernels.py:312-323 -> crypto/poly/fast.py:8-37):
+        quotient and remainder by X^n - 1, both trimmed."""
+        node = ctx["node"]
+        inp = ctx["inputs"][0]
+        n = int(ctx["attrs"]["n"])
+        if n <= 0:
+            raise ValueError("n must be positive")
+        if inp.dtype != DType.FR:
+            raise ValueError("gb300 div_xn_minus_1 supports FR only")
+        g = _device_fr(ctx, inp, "div_xn_minus_1")
+        rt = _runtime(ctx, "div_xn_minus_1")
+        length = int(g.n)
+        q = _alloc(ctx, rt, max(1, length - n) * 32)
+        r = _alloc(ctx, rt, n * 32)
+        ql, rl = rt.zk.fr_div_xn_minus_1(g.mtl_buffer, length, n, q, r)
+        q_id, r_id = node.outputs[0], node.outputs[1]
+        qb = GpuBuffer(dtype="fr_mont_u64x4", n=ql, mtl_buffer=q)
+        rb = GpuBuffer(dtype="fr_mont_u64x4", n=rl, mtl_buffer=r)
+        return {"outputs": {q_id: Buffer(id=q_id, device=METAL, dtype=DType.FR, data=qb, meta={"n": ql}),
+                            r_id: Buffer(id=r_id, device=METAL, dtype=DType.FR, data=rb, meta={"n": rl})}}
+
+    def batch_inv(ctx):
+        """BATCH_INV (runtime/kernels/cpu/kernels.py:_batch_inv): inverses, 0 for 0."""
+        node = ctx["node"]
+        inp = ctx["inputs"][0]
+        out_id = node.outputs[0]
+        if inp.dtype != DType.FR:
+            raise ValueError("gb300 batch_inv supports FR only")
+        g = _device_fr(ctx, inp, "batch_inv")
+        rt = _runtime(ctx, "batch_inv")
+        n = int(g.n)
+        out = _alloc(ctx, rt, max(1, n) * 32)
+        rt.zk.fr_batch_inv(out, g.mtl_buffer, n)
+        res = GpuBuffer(dtype="fr_mont_u64x4", n=n, mtl_buffer=out)
+        return {"outputs": {out_id: Buffer(id=out_id, device=METAL, dtype=DType.FR, data=res, meta=inp.meta)}}
+
+    def plonk_t_quotient_evals(ctx):
+        """PLONK_T_QUOTIENT_EVALS (runtime/kernels/cpu/kernels.py:_plonk_t_quotient_evals), fused."""
+        node = ctx["node"]
+        attrs = ctx["attrs"]
+        rt = _runtime(ctx, "plonk_t_quotient_evals")
+        m = int(attrs["m"])
+        bufs = [_device_fr(ctx, b, "plonk_t_quotient_evals") for b in ctx["inputs"][:15]]
+        if len(bufs) != 15 or any(int(b.n) != m for b in bufs):
+            raise ValueError("eval length mismatch")
+        num = _alloc(ctx, rt, max(1, m) * 32)
+        zh = _alloc(ctx, rt, max(1, m) * 32)
+        rt.zk.plonk_quotient_evals([b.mtl_buffer for b in bufs], m, int(attrs["n"]), int(attrs["omega_m"]),
+                                   int(attrs["shift"]), int(attrs["shift_n"]), int(attrs["alpha"]),
+                                   int(attrs["beta"]), int(attrs["gamma"]), int(attrs["k1"]), int(attrs["k2"]),
+                                   num, zh)
+        o_num, o_zh = node.outputs[0], node.outputs[1]
+        return {"outputs": {
+            o_num: Buffer(id=o_num, device=METAL, dtype=DType.FR,
+                          data=GpuBuffer(dtype="fr_mont_u64x4", n=m, mtl_buffer=num), meta={"m": m}),
+            o_zh: Buffer(id=o_zh, device=METAL, dtype=DType.FR,
+                         data=GpuBuffer(dtype="fr_mont_u64x4", n=m, mtl_buffer=zh), meta={"m": m})}}
+
     def _msm_many(rt: GpuRuntime, points, scalar_lists, attrs) -> List[Any]:
         """Instance k = MSM of scalar_lists[k] over points[:len(scalar_lists[k])]
         (msm_pippenger_batch semantics, crypto/msm/pippenger.py:124-214): one batched call,
@@ -473,6 +641,11 @@ def register_gb300_kernels(registry, *, ir: Any = None) -> None:
         (OpType.MSM_G1, METAL): msm_g1,
         (OpType.KZG_BATCH_COMMIT, METAL): kzg_batch_commit,
         (OpType.MSM_G1_BATCH, METAL): msm_g1_batch,
+        (OpType.MSM_G2, METAL): msm_g2,
+        (OpType.POLY_MUL_NTT, METAL): poly_mul_ntt,
+        (OpType.DIV_XN_MINUS_1, METAL): div_xn_minus_1,
+        (OpType.BATCH_INV, METAL): batch_inv,
+        (OpType.PLONK_T_QUOTIENT_EVALS, METAL): plonk_t_quotient_evals,
         (OpType.TO_DEVICE, Device.CPU): to_device,
         (OpType.FROM_DEVICE, Device.CPU): from_device,
         (OpType.FROM_DEVICE, METAL): from_device,
@@ -484,7 +657,8 @@ def register_gb300_kernels(registry, *, ir: Any = None) -> None:
 
 
 GB300_OPS = ("POINTWISE_MUL", "POLY_SUB", "ROOTS_EVALS_FROM_COEFFS", "ROOTS_COEFFS_FROM_EVALS",
-             "COSET_EVALS_FROM_COEFFS", "COSET_COEFFS_FROM_EVALS", "MSM_G1", "KZG_BATCH_COMMIT", "MSM_G1_BATCH")
+             "COSET_EVALS_FROM_COEFFS", "COSET_COEFFS_FROM_EVALS", "MSM_G1", "KZG_BATCH_COMMIT", "MSM_G1_BATCH",
+             "MSM_G2", "POLY_MUL_NTT", "DIV_XN_MINUS_1", "BATCH_INV", "PLONK_T_QUOTIENT_EVALS")
 
 
 def install() -> None:

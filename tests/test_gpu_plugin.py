@@ -247,3 +247,131 @@ def test_missing_gpu_context_raises_runtime_error():
     node = R.Node(op=R.OpType.MSM_G1, inputs=["p", "s"], outputs=["o"], attrs={})
     with pytest.raises(RuntimeError):
         fn({"node": node, "inputs": [None, None], "attrs": {}, "pool": None, "context": R.CPUContext()})
+
+
+def _poly_mul(a, b):
+    out = [0] * (len(a) + len(b) - 1)
+    for i, x in enumerate(a):
+        for j, y in enumerate(b):
+            out[i + j] = (out[i + j] + x * y) % FR
+    while out and out[-1] == 0:
+        out.pop()
+    return out
+
+
+def _div_xn(a, n):
+    """crypto/poly/fast.py:8-37 restated with plain ints."""
+    a = [x % FR for x in a]
+    while a and a[-1] == 0:
+        a.pop()
+    if not a:
+        return [], []
+    if len(a) <= n:
+        return [], a
+    q = [0] * (len(a) - n)
+    for k in range(len(a) - 1, n - 1, -1):
+        q[k - n] = (a[k] + (q[k] if k < len(q) else 0)) % FR
+    r = [(a[i] + (q[i] if i < len(q) else 0)) % FR for i in range(n)]
+    while q and q[-1] == 0:
+        q.pop()
+    while r and r[-1] == 0:
+        r.pop()
+    return q, r
+
+
+def test_qap_graph_on_device_matches_cpu_algebra():
+    """The node sequence of compute_h_from_abc_on_roots (protocols/groth16/qap.py:79-91):
+    three iNTTs, POLY_MUL_NTT, POLY_SUB, DIV_XN_MINUS_1 -- all on the device."""
+    n = 32
+    om = O.omega_for_size(n)
+    rng = synth.fr_uniform(901, 2 * n)
+    a = synth.limbs_to_ints(rng[:n])
+    b = synth.limbs_to_ints(rng[n:])
+    c = [x * y % FR for x, y in zip(a, b)]
+    for broken in (False, True):
+        cc = list(c)
+        if broken:
+            cc[3] = (cc[3] + 1) % FR
+        exe, _ = _exe()
+        g = R.Graph()
+        for name, v in (("a_eval", a), ("b_eval", b), ("c_eval", cc)):
+            g.add_buffer(id=name, device=R.Device.CPU, dtype=R.DType.FR, data=list(v))
+        for x in "abc":
+            g.add_node(op=R.OpType.ROOTS_COEFFS_FROM_EVALS, inputs=[f"{x}_eval"], outputs=[f"{x}_coeff"],
+                       attrs={"omega": om})
+        g.add_node(op=R.OpType.POLY_MUL_NTT, inputs=["a_coeff", "b_coeff"], outputs=["ab_coeff"])
+        g.add_node(op=R.OpType.POLY_SUB, inputs=["ab_coeff", "c_coeff"], outputs=["p_coeff"])
+        g.add_node(op=R.OpType.DIV_XN_MINUS_1, inputs=["p_coeff"], outputs=["h_coeff", "rem"], attrs={"n": n})
+        exe.run(g, runtime_config=_cfg(), keep=["a_coeff", "b_coeff", "c_coeff", "ab_coeff", "h_coeff", "rem"])
+        coeff = {x: O.ntt_op(1, synth.ints_to_limbs(v), n, om) for x, v in (("a", a), ("b", b), ("c", cc))}
+        ac, bc, ccf = (synth.limbs_to_ints(coeff[x]) for x in "abc")
+        ab = _poly_mul(ac, bc)
+        assert list(g.buffers["ab_coeff"].data) == ab
+        p = [(x - (ccf[i] if i < len(ccf) else 0)) % FR for i, x in enumerate(ab)]
+        while p and p[-1] == 0:
+            p.pop()
+        q, r = _div_xn(p, n)
+        assert list(g.buffers["h_coeff"].data) == q
+        assert list(g.buffers["rem"].data) == r
+        assert (len(r) != 0) == broken
+
+
+def test_div_xn_minus_1_edge_cases():
+    exe, _ = _exe()
+    for vals, n in (([], 4), ([5, 0, 0], 4), ([1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11], 3), ([0, 0, 7, 0, 0, 0, 9], 2)):
+        g = R.Graph()
+        g.add_buffer(id="p", device=R.Device.CPU, dtype=R.DType.FR, data=list(vals))
+        g.add_node(op=R.OpType.DIV_XN_MINUS_1, inputs=["p"], outputs=["q", "r"], attrs={"n": n})
+        exe.run(g, runtime_config=_cfg(), keep=["q", "r"])
+        assert (list(g.buffers["q"].data), list(g.buffers["r"].data)) == _div_xn(vals, n), (vals, n)
+
+
+def test_msm_g2_op_matches_oracle():
+    n = 300
+    k = synth.base_dlogs(902, n)
+    pts = [bn.multiply(bn.G2, int(v)) for v in synth.limbs_to_ints(k[:20])]
+    pts += [bn.normalize(p) + (bn.FQ2.one(),) for p in pts[:5]]  # affine (z = 1) forms too
+    pts.append(bn.Z2)
+    s = synth.limbs_to_ints(synth.fr_uniform(903, len(pts)))
+    exe, _ = _exe()
+    g = R.Graph()
+    g.add_buffer(id="pts", device=R.Device.CPU, dtype=R.DType.G2, data=tuple(pts))
+    g.add_buffer(id="s", device=R.Device.CPU, dtype=R.DType.FR, data=list(s))
+    g.add_node(op=R.OpType.MSM_G2, inputs=["pts", "s"], outputs=["o"])
+    exe.run(g, runtime_config=_cfg(), keep=["o"])
+    got = bn.normalize(g.buffers["o"].data)
+    exp = bn.Z2
+    for p, v in zip(pts, s):
+        exp = bn.add(exp, bn.multiply(p, v))
+    exp = bn.normalize(exp)
+    assert [int(c) for c in got[0].coeffs] == [int(c) for c in exp[0].coeffs]
+    assert [int(c) for c in got[1].coeffs] == [int(c) for c in exp[1].coeffs]
+
+
+def test_batch_inv_op_zero_maps_to_zero():
+    vals = synth.limbs_to_ints(synth.fr_uniform(904, 1000))
+    for i in (0, 17, 31, 32, 33, 999):
+        vals[i] = 0
+    got = _run_unary(R.OpType.BATCH_INV, vals, {})
+    assert got == [pow(v, FR - 2, FR) if v else 0 for v in vals]
+
+
+def test_plonk_t_quotient_evals_op_matches_cpu_kernel():
+    m, n = 64, 16
+    om = O.omega_for_size(m)
+    vecs = [synth.limbs_to_ints(synth.fr_uniform(910 + j, m)) for j in range(15)]
+    attrs = {"n": n, "m": m, "omega_m": om, "shift": 7, "shift_n": pow(7, n, FR), "alpha": 11111, "beta": 22222,
+             "gamma": 33333, "k1": 2, "k2": 3}
+    exp_num, exp_zh = O.plonk_t_quotient_evals(vecs, n, om, 7, pow(7, n, FR), 11111, 22222, 33333, 2, 3)
+    exe, _ = _exe()
+    g = R.Graph()
+    names = [f"v{j}" for j in range(15)]
+    for name, v in zip(names, vecs):
+        g.add_buffer(id=name, device=R.Device.CPU, dtype=R.DType.FR, data=list(v))
+    g.add_node(op=R.OpType.PLONK_T_QUOTIENT_EVALS, inputs=names, outputs=["num", "zh"], attrs=attrs)
+    g.add_node(op=R.OpType.BATCH_INV, inputs=["zh"], outputs=["inv_zh"])
+    g.add_node(op=R.OpType.POINTWISE_MUL, inputs=["num", "inv_zh"], outputs=["t"])
+    exe.run(g, runtime_config=_cfg(), keep=["num", "zh", "t"])
+    assert list(g.buffers["num"].data) == exp_num
+    assert list(g.buffers["zh"].data) == exp_zh
+    assert list(g.buffers["t"].data) == [x * pow(z, FR - 2, FR) % FR if z else 0 for x, z in zip(exp_num, exp_zh)]
