@@ -141,7 +141,7 @@ def test_plugin_registers_into_reference_registry():
         assert reg.has(getattr(ir.OpType, name), ir.Device.METAL, backend=ir.Backend.METAL), name
     assert reg.get(ir.OpType.TO_DEVICE, ir.Device.CPU, backend=ir.Backend.METAL) is not cpu_to_dev
     # ops without a GB300 kernel stay on the reference CPU kernels
-    assert not reg.has(ir.OpType.POLY_MUL_NTT, ir.Device.METAL, backend=ir.Backend.METAL)
+    assert not reg.has(ir.OpType.KZG_OPEN, ir.Device.METAL, backend=ir.Backend.METAL)
 
 
 def test_install_redirects_reference_metal_entry_points():
