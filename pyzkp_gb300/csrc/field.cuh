@@ -12,7 +12,14 @@
 // map to IMAD with carry in/out), so carries stay in the condition-code register.
 // Both moduli are below 2^254, so the running value stays below 2^288 (9 limbs)
 // and below 2p after each row; one conditional subtraction yields the canonical
-// representative in [0, p). All results are fully reduced: equal values have equal bits.
+// representative in [0, p).
+//
+// Fr values are always fully reduced (equal values have equal bits: NTT outputs are
+// stored and compared). Fq values inside the curve formulas are kept "lazy", in [0, 2p)
+// (F::LAZY): since 4p < 2^256, a product of inputs below 2p is already below 2p without
+// the final subtraction, sums subtract 2p when >= 2p, differences add 2p on a borrow, and
+// zero tests accept 0 and p. fe_from_mont returns the canonical value; host code that
+// reads device Fq values reduces them once more.
 #pragma once
 #include <cstdint>
 
@@ -24,6 +31,7 @@ struct FrP {
     __host__ __device__ static constexpr uint32_t P(int i) { return i == 0 ? 0xf0000001u : i == 1 ? 0x43e1f593u : i == 2 ? 0x79b97091u : i == 3 ? 0x2833e848u : i == 4 ? 0x8181585du : i == 5 ? 0xb85045b6u : i == 6 ? 0xe131a029u : 0x30644e72u; }
     static constexpr uint32_t INV = 0xefffffffu  /* -r^-1 mod 2^32 */;
     static constexpr int MUL_STYLE = 4;
+    static constexpr bool LAZY = false;
     __host__ __device__ static constexpr uint32_t ONE(int i) { return i == 0 ? 0x4ffffffbu : i == 1 ? 0xac96341cu : i == 2 ? 0x9f60cd29u : i == 3 ? 0x36fc7695u : i == 4 ? 0x7879462eu : i == 5 ? 0x666ea36fu : i == 6 ? 0x9a07df2fu : 0x0e0a77c1u; }
     __host__ __device__ static constexpr uint32_t R2(int i) { return i == 0 ? 0xae216da7u : i == 1 ? 0x1bb8e645u : i == 2 ? 0xe35c59e3u : i == 3 ? 0x53fe3ab1u : i == 4 ? 0x53bb8085u : i == 5 ? 0x8c49833du : i == 6 ? 0x7f4e44a5u : 0x0216d0b1u; }
 };
@@ -32,6 +40,11 @@ struct FqP {
     __host__ __device__ static constexpr uint32_t P(int i) { return i == 0 ? 0xd87cfd47u : i == 1 ? 0x3c208c16u : i == 2 ? 0x6871ca8du : i == 3 ? 0x97816a91u : i == 4 ? 0x8181585du : i == 5 ? 0xb85045b6u : i == 6 ? 0xe131a029u : 0x30644e72u; }
     static constexpr uint32_t INV = 0xe4866389u  /* -q^-1 mod 2^32 */;
     static constexpr int MUL_STYLE = 3;
+#ifdef ZK_FQ_STRICT
+    static constexpr bool LAZY = false;
+#else
+    static constexpr bool LAZY = true;
+#endif
     __host__ __device__ static constexpr uint32_t ONE(int i) { return i == 0 ? 0xc58f0d9du : i == 1 ? 0xd35d438du : i == 2 ? 0xf5c70b3du : i == 3 ? 0x0a78eb28u : i == 4 ? 0x7879462cu : i == 5 ? 0x666ea36fu : i == 6 ? 0x9a07df2fu : 0x0e0a77c1u; }
     __host__ __device__ static constexpr uint32_t R2(int i) { return i == 0 ? 0x538afa89u : i == 1 ? 0xf32cfc5bu : i == 2 ? 0xd44501fbu : i == 3 ? 0xb5e71911u : i == 4 ? 0x0a417ff6u : i == 5 ? 0x47ab1effu : i == 6 ? 0xcab8351fu : 0x06d89f71u; }
 };
@@ -66,6 +79,59 @@ __device__ __forceinline__ bool fe_eq(const fe& a, const fe& b) {
 #pragma unroll
     for (int i = 0; i < 8; i++) x |= a.v[i] ^ b.v[i];
     return x == 0;
+}
+
+// limb i of 2p
+template <class F>
+__host__ __device__ constexpr uint32_t p2_limb(int i) {
+    return (F::P(i) << 1) | (i ? (F::P(i - 1) >> 31) : 0u);
+}
+
+// the modulus of the field's representation: 2p when lazy (values in [0, 2p)), else p
+template <class F>
+__host__ __device__ constexpr uint32_t mod_limb(int i) {
+    return F::LAZY ? p2_limb<F>(i) : F::P(i);
+}
+
+// a == 0 mod p for a value of the field's representation ([0, p), or [0, 2p) when lazy)
+template <class F>
+__device__ __forceinline__ bool fe_is_zero_mod(const fe& a) {
+    if constexpr (F::LAZY) {
+        uint32_t z = 0, e = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            z |= a.v[i];
+            e |= a.v[i] ^ F::P(i);
+        }
+        return z == 0 || e == 0;
+    } else {
+        return fe_is_zero(a);
+    }
+}
+
+// r = t - 2p if t >= 2p else t, for t < 4p (< 2^256).
+template <class F>
+__device__ __forceinline__ fe fe_reduce_2p(const fe& t) {
+    fe s;
+    uint32_t borrow;
+    asm("sub.cc.u32  %0, %9, %17;\n\t"
+        "subc.cc.u32 %1, %10, %18;\n\t"
+        "subc.cc.u32 %2, %11, %19;\n\t"
+        "subc.cc.u32 %3, %12, %20;\n\t"
+        "subc.cc.u32 %4, %13, %21;\n\t"
+        "subc.cc.u32 %5, %14, %22;\n\t"
+        "subc.cc.u32 %6, %15, %23;\n\t"
+        "subc.cc.u32 %7, %16, %24;\n\t"
+        "subc.u32    %8, 0, 0;"
+        : "=r"(s.v[0]), "=r"(s.v[1]), "=r"(s.v[2]), "=r"(s.v[3]), "=r"(s.v[4]), "=r"(s.v[5]), "=r"(s.v[6]),
+          "=r"(s.v[7]), "=r"(borrow)
+        : "r"(t.v[0]), "r"(t.v[1]), "r"(t.v[2]), "r"(t.v[3]), "r"(t.v[4]), "r"(t.v[5]), "r"(t.v[6]), "r"(t.v[7]),
+          "n"(p2_limb<F>(0)), "n"(p2_limb<F>(1)), "n"(p2_limb<F>(2)), "n"(p2_limb<F>(3)), "n"(p2_limb<F>(4)),
+          "n"(p2_limb<F>(5)), "n"(p2_limb<F>(6)), "n"(p2_limb<F>(7)));
+    fe r;
+#pragma unroll
+    for (int i = 0; i < 8; i++) r.v[i] = borrow ? t.v[i] : s.v[i];
+    return r;
 }
 
 // r = t - p if t >= p else t, for t < 2p (< 2^255).
@@ -108,7 +174,8 @@ __device__ __forceinline__ fe fe_add(const fe& a, const fe& b) {
           "=r"(t.v[7])
         : "r"(a.v[0]), "r"(a.v[1]), "r"(a.v[2]), "r"(a.v[3]), "r"(a.v[4]), "r"(a.v[5]), "r"(a.v[6]), "r"(a.v[7]),
           "r"(b.v[0]), "r"(b.v[1]), "r"(b.v[2]), "r"(b.v[3]), "r"(b.v[4]), "r"(b.v[5]), "r"(b.v[6]), "r"(b.v[7]));
-    return fe_reduce_once<F>(t);
+    if constexpr (F::LAZY) return fe_reduce_2p<F>(t);
+    else return fe_reduce_once<F>(t);
 }
 
 template <class F>
@@ -140,8 +207,8 @@ __device__ __forceinline__ fe fe_sub(const fe& a, const fe& b) {
         : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]), "=r"(r.v[4]), "=r"(r.v[5]), "=r"(r.v[6]),
           "=r"(r.v[7])
         : "r"(t.v[0]), "r"(t.v[1]), "r"(t.v[2]), "r"(t.v[3]), "r"(t.v[4]), "r"(t.v[5]), "r"(t.v[6]), "r"(t.v[7]),
-          "r"(F::P(0) & m), "r"(F::P(1) & m), "r"(F::P(2) & m), "r"(F::P(3) & m), "r"(F::P(4) & m),
-          "r"(F::P(5) & m), "r"(F::P(6) & m), "r"(F::P(7) & m));
+          "r"(mod_limb<F>(0) & m), "r"(mod_limb<F>(1) & m), "r"(mod_limb<F>(2) & m), "r"(mod_limb<F>(3) & m),
+          "r"(mod_limb<F>(4) & m), "r"(mod_limb<F>(5) & m), "r"(mod_limb<F>(6) & m), "r"(mod_limb<F>(7) & m));
     return r;
 }
 
@@ -243,7 +310,8 @@ __device__ __forceinline__ fe fe_mul_unrolled(const fe& a, const fe& b) {
     t.v[5] = t5;
     t.v[6] = t6;
     t.v[7] = t7;
-    return fe_reduce_once<F>(t);
+    if constexpr (F::LAZY) return t;
+    else return fe_reduce_once<F>(t);
 }
 
 template <class F>
@@ -271,7 +339,8 @@ __device__ __forceinline__ fe fe_mul_rolled(const fe& a, const fe& b) {
     t.v[5] = t5;
     t.v[6] = t6;
     t.v[7] = t7;
-    return fe_reduce_once<F>(t);
+    if constexpr (F::LAZY) return t;
+    else return fe_reduce_once<F>(t);
 }
 
 // CIOS on full-width products: mul.wide.u32 (IMAD.WIDE) yields lo and hi of a_j * b_i
@@ -305,23 +374,74 @@ __device__ __forceinline__ fe fe_mul_rolled(const fe& a, const fe& b) {
           "r"((uint32_t)((p3) >> 32)), "r"((uint32_t)((p4) >> 32)), "r"((uint32_t)((p5) >> 32)),              \
           "r"((uint32_t)((p6) >> 32)), "r"((uint32_t)((p7) >> 32)))
 
+// Rows (bit i = row i) whose reduction half m * p uses mad.lo.cc / madc.hi.cc chains
+// (IMAD pipe) instead of mul.wide + add chains (IMAD.WIDE + ALU pipe).
+#ifndef ZK_MIX_ROWS
+#define ZK_MIX_ROWS 0
+#endif
+#define ZK_RED_MAD_ROW(F, m_)                                                                                  \
+    do {                                                                                                       \
+        asm("mad.lo.cc.u32  %0, %9, %10, %0;\n\t"                                                              \
+            "madc.lo.cc.u32 %1, %9, %11, %1;\n\t"                                                              \
+            "madc.lo.cc.u32 %2, %9, %12, %2;\n\t"                                                              \
+            "madc.lo.cc.u32 %3, %9, %13, %3;\n\t"                                                              \
+            "madc.lo.cc.u32 %4, %9, %14, %4;\n\t"                                                              \
+            "madc.lo.cc.u32 %5, %9, %15, %5;\n\t"                                                              \
+            "madc.lo.cc.u32 %6, %9, %16, %6;\n\t"                                                              \
+            "madc.lo.cc.u32 %7, %9, %17, %7;\n\t"                                                              \
+            "addc.u32       %8, %8, 0;"                                                                        \
+            : "+r"(t0), "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8)        \
+            : "r"(m_), "n"(F::P(0)), "n"(F::P(1)), "n"(F::P(2)), "n"(F::P(3)), "n"(F::P(4)), "n"(F::P(5)),   \
+              "n"(F::P(6)), "n"(F::P(7)));                                                                     \
+        asm("mad.hi.cc.u32  %0, %8, %9, %0;\n\t"                                                               \
+            "madc.hi.cc.u32 %1, %8, %10, %1;\n\t"                                                              \
+            "madc.hi.cc.u32 %2, %8, %11, %2;\n\t"                                                              \
+            "madc.hi.cc.u32 %3, %8, %12, %3;\n\t"                                                              \
+            "madc.hi.cc.u32 %4, %8, %13, %4;\n\t"                                                              \
+            "madc.hi.cc.u32 %5, %8, %14, %5;\n\t"                                                              \
+            "madc.hi.cc.u32 %6, %8, %15, %6;\n\t"                                                              \
+            "madc.hi.u32    %7, %8, %16, %7;"                                                                  \
+            : "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8)                   \
+            : "r"(m_), "n"(F::P(0)), "n"(F::P(1)), "n"(F::P(2)), "n"(F::P(3)), "n"(F::P(4)), "n"(F::P(5)),   \
+              "n"(F::P(6)), "n"(F::P(7)));                                                                     \
+    } while (0)
+
+// Row of the carry-save form: x_j = a_j * b + t_j as one 64-bit multiply-add each
+// (mul.wide with a 64-bit addend: (2^32 - 1)^2 + (2^32 - 1) < 2^64, no overflow), then a
+// single add-carry chain t_j = lo(x_j) + hi(x_{j-1}), t_8 += hi(x_7): one ALU addition per
+// partial product instead of two (the low halves ride in the multiply).
+#define ZK_ROW_ACC(a0, a1, a2, a3, a4, a5, a6, a7, bi)                                                          \
+    do {                                                                                                       \
+        const uint64_t x0 = (uint64_t)(a0) * (bi) + t0, x1 = (uint64_t)(a1) * (bi) + t1,                      \
+                       x2 = (uint64_t)(a2) * (bi) + t2, x3 = (uint64_t)(a3) * (bi) + t3,                      \
+                       x4 = (uint64_t)(a4) * (bi) + t4, x5 = (uint64_t)(a5) * (bi) + t5,                      \
+                       x6 = (uint64_t)(a6) * (bi) + t6, x7 = (uint64_t)(a7) * (bi) + t7;                      \
+        t0 = (uint32_t)x0;                                                                                     \
+        asm("add.cc.u32  %0, %8, %15;\n\t"                                                                      \
+            "addc.cc.u32 %1, %9, %16;\n\t"                                                                      \
+            "addc.cc.u32 %2, %10, %17;\n\t"                                                                     \
+            "addc.cc.u32 %3, %11, %18;\n\t"                                                                     \
+            "addc.cc.u32 %4, %12, %19;\n\t"                                                                     \
+            "addc.cc.u32 %5, %13, %20;\n\t"                                                                     \
+            "addc.cc.u32 %6, %14, %21;\n\t"                                                                     \
+            "addc.u32    %7, %7, %22;"                                                                         \
+            : "=r"(t1), "=r"(t2), "=r"(t3), "=r"(t4), "=r"(t5), "=r"(t6), "=r"(t7), "+r"(t8)                   \
+            : "r"((uint32_t)x1), "r"((uint32_t)x2), "r"((uint32_t)x3), "r"((uint32_t)x4), "r"((uint32_t)x5),   \
+              "r"((uint32_t)x6), "r"((uint32_t)x7), "r"((uint32_t)(x0 >> 32)), "r"((uint32_t)(x1 >> 32)),     \
+              "r"((uint32_t)(x2 >> 32)), "r"((uint32_t)(x3 >> 32)), "r"((uint32_t)(x4 >> 32)),                 \
+              "r"((uint32_t)(x5 >> 32)), "r"((uint32_t)(x6 >> 32)), "r"((uint32_t)(x7 >> 32)));                \
+    } while (0)
+
+// CIOS on the carry-save rows: per row 16 multiply-adds and two 8-long carry chains.
 template <class F>
-__device__ __forceinline__ fe fe_mul_wide_unrolled(const fe& a, const fe& b) {
+__device__ __forceinline__ fe fe_mul_acc_unrolled(const fe& a, const fe& b) {
     uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0, t8 = 0;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
-        const uint32_t bi = b.v[i];
-        const uint64_t p0 = (uint64_t)a.v[0] * bi, p1 = (uint64_t)a.v[1] * bi, p2 = (uint64_t)a.v[2] * bi,
-                       p3 = (uint64_t)a.v[3] * bi, p4 = (uint64_t)a.v[4] * bi, p5 = (uint64_t)a.v[5] * bi,
-                       p6 = (uint64_t)a.v[6] * bi, p7 = (uint64_t)a.v[7] * bi;
-        ZK_ADD_LO_CHAIN(p0, p1, p2, p3, p4, p5, p6, p7);
-        ZK_ADD_HI_CHAIN(p0, p1, p2, p3, p4, p5, p6, p7);
+        ZK_ROW_ACC(a.v[0], a.v[1], a.v[2], a.v[3], a.v[4], a.v[5], a.v[6], a.v[7], b.v[i]);
         const uint32_t m = t0 * F::INV;
-        const uint64_t q0 = (uint64_t)m * F::P(0), q1 = (uint64_t)m * F::P(1), q2 = (uint64_t)m * F::P(2),
-                       q3 = (uint64_t)m * F::P(3), q4 = (uint64_t)m * F::P(4), q5 = (uint64_t)m * F::P(5),
-                       q6 = (uint64_t)m * F::P(6), q7 = (uint64_t)m * F::P(7);
-        ZK_ADD_LO_CHAIN(q0, q1, q2, q3, q4, q5, q6, q7);
-        ZK_ADD_HI_CHAIN(q0, q1, q2, q3, q4, q5, q6, q7);
+        ZK_ROW_ACC(F::P(0), F::P(1), F::P(2), F::P(3), F::P(4), F::P(5), F::P(6), F::P(7), m);
+        // t0 == 0 now (m was chosen so); shift one limb
         t0 = t1;
         t1 = t2;
         t2 = t3;
@@ -341,7 +461,53 @@ __device__ __forceinline__ fe fe_mul_wide_unrolled(const fe& a, const fe& b) {
     t.v[5] = t5;
     t.v[6] = t6;
     t.v[7] = t7;
-    return fe_reduce_once<F>(t);
+    if constexpr (F::LAZY) return t;
+    else return fe_reduce_once<F>(t);
+}
+
+template <class F>
+__device__ __forceinline__ fe fe_mul_wide_unrolled(const fe& a, const fe& b) {
+    uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0, t8 = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const uint32_t bi = b.v[i];
+        const uint64_t p0 = (uint64_t)a.v[0] * bi, p1 = (uint64_t)a.v[1] * bi, p2 = (uint64_t)a.v[2] * bi,
+                       p3 = (uint64_t)a.v[3] * bi, p4 = (uint64_t)a.v[4] * bi, p5 = (uint64_t)a.v[5] * bi,
+                       p6 = (uint64_t)a.v[6] * bi, p7 = (uint64_t)a.v[7] * bi;
+        ZK_ADD_LO_CHAIN(p0, p1, p2, p3, p4, p5, p6, p7);
+        ZK_ADD_HI_CHAIN(p0, p1, p2, p3, p4, p5, p6, p7);
+        const uint32_t m = t0 * F::INV;
+        if ((ZK_MIX_ROWS >> i) & 1) {
+            // this row's m * p on the IMAD pipe (multiply-add with carry), balancing the ALU pipe
+            ZK_RED_MAD_ROW(F, m);
+        } else {
+            const uint64_t q0 = (uint64_t)m * F::P(0), q1 = (uint64_t)m * F::P(1), q2 = (uint64_t)m * F::P(2),
+                           q3 = (uint64_t)m * F::P(3), q4 = (uint64_t)m * F::P(4), q5 = (uint64_t)m * F::P(5),
+                           q6 = (uint64_t)m * F::P(6), q7 = (uint64_t)m * F::P(7);
+            ZK_ADD_LO_CHAIN(q0, q1, q2, q3, q4, q5, q6, q7);
+            ZK_ADD_HI_CHAIN(q0, q1, q2, q3, q4, q5, q6, q7);
+        }
+        t0 = t1;
+        t1 = t2;
+        t2 = t3;
+        t3 = t4;
+        t4 = t5;
+        t5 = t6;
+        t6 = t7;
+        t7 = t8;
+        t8 = 0;
+    }
+    fe t;
+    t.v[0] = t0;
+    t.v[1] = t1;
+    t.v[2] = t2;
+    t.v[3] = t3;
+    t.v[4] = t4;
+    t.v[5] = t5;
+    t.v[6] = t6;
+    t.v[7] = t7;
+    if constexpr (F::LAZY) return t;
+    else return fe_reduce_once<F>(t);
 }
 
 // Two independent products a*b and c*d with their rows interleaved: the carry chains of
@@ -412,8 +578,13 @@ __device__ __forceinline__ fe2 fe_mul2_wide_unrolled(const fe& a, const fe& b, c
     x.v[0] = t0, x.v[1] = t1, x.v[2] = t2, x.v[3] = t3, x.v[4] = t4, x.v[5] = t5, x.v[6] = t6, x.v[7] = t7;
     y.v[0] = u0, y.v[1] = u1, y.v[2] = u2, y.v[3] = u3, y.v[4] = u4, y.v[5] = u5, y.v[6] = u6, y.v[7] = u7;
     fe2 r;
-    r.x = fe_reduce_once<F>(x);
-    r.y = fe_reduce_once<F>(y);
+    if constexpr (F::LAZY) {
+        r.x = x;
+        r.y = y;
+    } else {
+        r.x = fe_reduce_once<F>(x);
+        r.y = fe_reduce_once<F>(y);
+    }
     return r;
 }
 
@@ -434,7 +605,11 @@ __device__ __noinline__ fe fe_mul_call(const fe a, const fe b) {
 
 template <class F>
 __device__ __noinline__ fe fe_mul_wide_call(const fe a, const fe b) {
+#ifdef ZK_WIDE_ACC
+    return fe_mul_acc_unrolled<F>(a, b);
+#else
     return fe_mul_wide_unrolled<F>(a, b);
+#endif
 }
 
 // r = a * b * 2^-256 mod p (CIOS, see the file header).
@@ -452,7 +627,11 @@ __device__ __forceinline__ fe fe_mul(const fe& a, const fe& b) {
     } else if constexpr (style == 3) {
         return fe_mul_wide_call<F>(a, b);
     } else if constexpr (style == 4) {
+#ifdef ZK_WIDE_ACC
+        return fe_mul_acc_unrolled<F>(a, b);
+#else
         return fe_mul_wide_unrolled<F>(a, b);
+#endif
     } else {
         return fe_mul_rolled<F>(a, b);
     }
@@ -511,12 +690,15 @@ __device__ __forceinline__ fe fe_to_mont(fe a) {
     return fe_mul<F>(a, r2);
 }
 
+// Montgomery -> canonical in [0, p) (also for lazy inputs below 2p: a * 1 * 2^-256 <= p).
 template <class F>
 __device__ __forceinline__ fe fe_from_mont(const fe& a) {
     fe one;
 #pragma unroll
     for (int i = 0; i < 8; i++) one.v[i] = i == 0 ? 1u : 0u;
-    return fe_mul<F>(a, one);
+    const fe r = fe_mul<F>(a, one);
+    if constexpr (F::LAZY) return fe_reduce_once<F>(r);
+    else return r;
 }
 
 // 32-byte element loads / stores as two 16-byte vector accesses

@@ -211,6 +211,14 @@ inline F2 cone<F2>() {
     return {one(fq()), F4{{0, 0, 0, 0}}};
 }
 
+// Device Fq values may be lazy in [0, 2p): one conditional subtraction makes them canonical.
+inline F4 cnorm(const F4& a) {
+    F4 r = a;
+    if (geq(r.v, fq().p)) sub4(r.v, r.v, fq().p);
+    return r;
+}
+inline F2 cnorm(const F2& a) { return {cnorm(a.c0), cnorm(a.c1)}; }
+
 // ---- XYZZ points over either coordinate field --------------------------------------------
 template <class T>
 struct XyzzT {

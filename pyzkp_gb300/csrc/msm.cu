@@ -480,6 +480,10 @@ static zkh::XyzzT<typename HostOf<C>::T> to_host(const typename C::P& d) {
     static_assert(sizeof(typename C::P) == sizeof(zkh::XyzzT<typename HostOf<C>::T>), "layout");
     zkh::XyzzT<typename HostOf<C>::T> h;
     std::memcpy(&h, &d, sizeof(h));
+    h.X = zkh::cnorm(h.X);  // device Fq values are lazy in [0, 2q)
+    h.Y = zkh::cnorm(h.Y);
+    h.ZZ = zkh::cnorm(h.ZZ);
+    h.ZZZ = zkh::cnorm(h.ZZZ);
     return h;
 }
 
