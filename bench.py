@@ -230,8 +230,8 @@ def run_gpu(args, ranks: Ranks) -> dict:
     # 32x32->64 multiply-accumulates, i.e. 272 IMAD (lo + hi) instructions.
     acc_imad = entries * 10 * 272
     acc_tops = acc_imad / (acc_ms_launch * 1e-3) / 1e12
-    # algorithmic bytes: per entry the 4-byte CSR entry + 4-byte key + the 64-byte affine base
-    acc_bytes = entries * 72
+    # algorithmic bytes: per entry the 4-byte CSR entry + the 64-byte affine base
+    acc_bytes = entries * 68
     peaks = load_peaks()
     hbm_peak = peaks.get("hbm_gbs") or 6800.0
     roofline = {
@@ -251,7 +251,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
         "hbm": {"achieved": round(acc_bytes / (acc_ms_launch * 1e-3) / 1e9, 1), "peak": hbm_peak,
                 "unit": "GB/s", "frac": round(acc_bytes / (acc_ms_launch * 1e-3) / 1e9 / hbm_peak, 4),
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks.get("hbm_gbs") else "fallback 6800"},
-        "algorithmic_work": f"{entries} CSR entries x 10 Fq mults x 272 IMAD; {entries} x 72 B",
+        "algorithmic_work": f"{entries} CSR entries x 10 Fq mults x 272 IMAD; {entries} x 68 B",
     }
     kernels = {name: {"launches": la // prof_steps, "ms_per_step": round(ms / prof_steps, 4)}
                for name, (la, ms) in sorted(table.items())}

@@ -49,6 +49,16 @@ struct FqP {
     __host__ __device__ static constexpr uint32_t R2(int i) { return i == 0 ? 0x538afa89u : i == 1 ? 0xf32cfc5bu : i == 2 ? 0xd44501fbu : i == 3 ? 0xb5e71911u : i == 4 ? 0x0a417ff6u : i == 5 ? 0x47ab1effu : i == 6 ? 0xcab8351fu : 0x06d89f71u; }
 };
 
+// Fr with lazy values in [0, 2r): for the NTT pass kernel only, whose last pass reduces
+// every output once more (all other Fr code sees canonical values).
+struct FrLazyP : FrP {
+#ifdef ZK_NTT_STRICT
+    static constexpr bool LAZY = false;
+#else
+    static constexpr bool LAZY = true;
+#endif
+};
+
 // One field element: 8 little-endian 32-bit limbs (32 bytes, 32-byte aligned in memory).
 struct __align__(16) fe {
     uint32_t v[8];

@@ -8,15 +8,20 @@
 // (:499-535), one thread per window reduce (:540-566), CPU Horner (msm.py:322-332).
 //
 // This pipeline (all on the device except the last ~W*13 point additions):
-//  1. msm_digits_kernel   scalar -> W signed c-bit digits (|d| <= 2^(c-1)); CSR
-//                         histogram with warp-aggregated atomics (__match_any_sync).
+//  1. msm_digits_kernel   scalar -> reduced scalar (zero for an infinity base) and the CSR
+//                         histogram of its W signed c-bit digits (|d| <= 2^(c-1)),
+//                         counted with warp-aggregated atomics (__match_any_sync).
 //  2. device scan         counters -> CSR row pointers (scan.cu).
-//  3. msm_scatter_kernel  (window, |digit|) buckets: entry = point index | sign << 31.
+//  3. msm_scatter_kernel  the digits again; entry = point index | sign << 31 in the range
+//                         of its (window, |digit|) bucket (no per-entry bucket id is
+//                         stored: the row pointers imply it).
 //  4. msm_accumulate_*    equal-size segments of S entries per thread (load balanced
-//                         even when one bucket holds 5% of all points); buckets wholly
-//                         inside a segment are final; a bucket that straddles segment
-//                         boundaries leaves partial sums that tree rounds (pairs, then
-//                         groups of 4 units) merge, deciding "straddles" from the row pointers.
+//                         even when one bucket holds 5% of all points; a segment finds
+//                         its first bucket by binary search over the row pointers);
+//                         buckets wholly inside a segment are final; a bucket that
+//                         straddles segment boundaries leaves partial sums that tree
+//                         rounds (pairs, then groups of 4 units) merge, deciding
+//                         "straddles" from the row pointers.
 //  5. msm_bucket_blocks   per window, blocks of g buckets: sum_b b*B_b = sum_j E_j + g*WS(Y)
 //                         with Y_j the block sums and E_j = -(sum of the g-1 prefix sums).
 //  6. msm_targets_kernel  WS(Y) = sum_j Y_j + sum_k 2^k M_k with M_k the sum of the Y_j
@@ -25,6 +30,8 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
+#include <functional>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -44,6 +51,9 @@ static constexpr uint32_t kNone = 0xffffffffu;
 #endif
 #ifndef ZK_MSM_BLOCKG
 #define ZK_MSM_BLOCKG 8
+#endif
+#ifndef ZK_ACC_MINB
+#define ZK_ACC_MINB 1  // minimum resident CTAs per SM asked of the accumulation kernel
 #endif
 #ifndef ZK_MSM_GROUP
 #define ZK_MSM_GROUP 4  // measured at 2^20 / 2^22: merge 0.73 / 1.36 ms with 16, 0.48 / 1.02 ms with 4
@@ -138,9 +148,24 @@ __device__ __forceinline__ uint32_t find_inst(const uint32_t* __restrict__ offs,
     return lo;
 }
 
+// Signed digit of window w (|d| <= 2^(c-1)); `carry` runs from window to window.
+// Returns mag | neg << 31, or 0 for a zero digit.
+__device__ __forceinline__ uint32_t signed_digit(const fe& s, uint32_t w, const MsmShape& sh, uint32_t& carry) {
+    const uint32_t v = bits_at(s, w * sh.c, sh.c) + carry;
+    if (w + 1 < sh.W && v > (1u << (sh.c - 1))) {  // v in (2^(c-1), 2^c]: digit v - 2^c in [-2^(c-1)+1, 0]
+        carry = 1;
+        const uint32_t mag = (1u << sh.c) - v;
+        return mag ? (mag | 0x80000000u) : 0u;  // v == 2^c: digit 0, only the carry moves on
+    }
+    carry = 0;  // v in [0, 2^(c-1)] (the top window is at most 2^(c-1), see make_shape)
+    return v;
+}
+
+// Canonical scalars (reduced mod r; zero where the base is infinity) to `reduced` for the
+// scatter, and the CSR histogram of the digits.
 template <class C>
 __global__ void msm_digits_kernel(const MsmInst* __restrict__ insts, const uint32_t* __restrict__ offs, uint32_t N,
-                                  int scalars_mont, MsmShape sh, uint32_t* __restrict__ digits,
+                                  int scalars_mont, MsmShape sh, fe* __restrict__ reduced,
                                   uint32_t* __restrict__ counts) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = j < N;
@@ -153,44 +178,37 @@ __global__ void msm_digits_kernel(const MsmInst* __restrict__ insts, const uint3
         s = scalars_mont ? fe_from_mont<FrP>(s) : fe_from_mont<FrP>(fe_to_mont<FrP>(s));
         if (affine_is_inf(affine_load(static_cast<const typename C::A*>(insts[k].bases) + i))) s = fe_zero();
         set0 = k * sh.Wr;
+        fe_store(reduced + j, s);
     }
     uint32_t carry = 0;
-    const uint32_t half = 1u << (sh.c - 1);
     for (uint32_t w = 0; w < sh.W; w++) {
-        uint32_t v = bits_at(s, w * sh.c, sh.c) + carry;
-        uint32_t mag, neg;
-        if (w + 1 < sh.W && v > half) {  // v in (2^(c-1), 2^c]: digit v - 2^c in [-2^(c-1)+1, 0]
-            mag = (1u << sh.c) - v;
-            neg = 1;
-            carry = 1;
-        } else {  // v in [0, 2^(c-1)] (the top window is at most 2^(c-1), see make_shape)
-            mag = v;
-            neg = 0;
-            carry = 0;
-        }
-        const bool nz = valid && mag != 0;
-        if (valid) digits[(size_t)w * N + j] = nz ? (mag | (neg << 31)) : 0u;
-        warp_aggregated_inc(counts, (set0 + (sh.shared ? 0u : w)) * sh.B + (mag - 1), nz);
+        const uint32_t d = signed_digit(s, w, sh, carry);
+        const uint32_t mag = d & 0x7fffffffu;
+        warp_aggregated_inc(counts, (set0 + (sh.shared ? 0u : w)) * sh.B + (mag - 1), valid && mag != 0);
     }
 }
 
 // ---- 3. scatter into CSR ------------------------------------------------------
-__global__ void msm_scatter_kernel(const uint32_t* __restrict__ digits, const MsmInst* __restrict__ insts,
+// The digits again from the reduced scalars; entry = point index | sign << 31, placed in
+// its bucket's CSR range (the bucket of an entry is implied by the row pointers).
+__global__ void msm_scatter_kernel(const fe* __restrict__ reduced, const MsmInst* __restrict__ insts,
                                    const uint32_t* __restrict__ offs, uint32_t N, MsmShape sh,
-                                   uint32_t* __restrict__ cursor, uint32_t* __restrict__ entries,
-                                   uint32_t* __restrict__ keys) {
+                                   uint32_t* __restrict__ cursor, uint32_t* __restrict__ entries) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = j < N;
     uint32_t set0 = 0, i = 0, stride = 0;
+    fe s = fe_zero();
     if (valid) {
         const uint32_t k = find_inst(offs, sh.inst, j);
         i = j - __ldg(offs + k);
         set0 = k * sh.Wr;
         stride = insts[k].stride;
+        s = fe_load(reduced + j);
     }
+    uint32_t carry = 0;
     for (uint32_t w = 0; w < sh.W; w++) {
-        const uint32_t d = valid ? digits[(size_t)w * N + j] : 0u;
-        const bool nz = d != 0;
+        const uint32_t d = signed_digit(s, w, sh, carry);
+        const bool nz = valid && d != 0;
         const uint32_t key = (set0 + (sh.shared ? 0u : w)) * sh.B + (d & 0x7fffffffu) - 1;
         const uint32_t point = sh.shared ? w * stride + i : i;  // fixed-base: row w of the shifted bases
         const uint32_t live = __ballot_sync(0xffffffffu, nz);
@@ -203,7 +221,6 @@ __global__ void msm_scatter_kernel(const uint32_t* __restrict__ digits, const Ms
             base = __shfl_sync(peers, base, leader);
             const uint32_t rank = __popc(peers & ((1u << lane) - 1));
             entries[base + rank] = point | (d & 0x80000000u);
-            keys[base + rank] = key;
         }
     }
 }
@@ -234,9 +251,19 @@ __device__ __forceinline__ const typename C::A* key_bases(const MsmInst* __restr
     return static_cast<const typename C::A*>(insts[sh.inst == 1 ? 0u : key / (sh.Wr * sh.B)].bases);
 }
 
+// The non-empty bucket holding CSR entry e: the largest k with row_ptr[k] <= e.
+__device__ __forceinline__ uint32_t bucket_of(const uint32_t* __restrict__ row_ptr, uint32_t nbuckets, uint32_t e) {
+    uint32_t lo = 0, hi = nbuckets;  // row_ptr[lo] <= e < row_ptr[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(row_ptr + mid) <= e) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 template <class C>
-__global__ void __launch_bounds__(128) msm_accumulate_kernel(const uint32_t* __restrict__ entries,
-                                                             const uint32_t* __restrict__ keys,
+__global__ void __launch_bounds__(128, ZK_ACC_MINB) msm_accumulate_kernel(const uint32_t* __restrict__ entries,
                                                              const uint32_t* __restrict__ d_total,
                                                              const uint32_t* __restrict__ row_ptr,
                                                              const MsmInst* __restrict__ insts, MsmShape sh,
@@ -253,14 +280,17 @@ __global__ void __launch_bounds__(128) msm_accumulate_kernel(const uint32_t* __r
     const uint32_t e0 = u * kSegment;
     if (e0 >= M) return;
     const uint32_t e1 = min(e0 + kSegment, M);
-    uint32_t cur = keys[e0];
+    uint32_t cur = bucket_of(row_ptr, sh.sets * sh.B, e0);
+    uint32_t end = row_ptr[cur + 1];  // > e0
     const A* bases = key_bases<C>(insts, sh, cur);
     P acc = xyzz_inf<typename C::T>();
     for (uint32_t e = e0; e < e1; e++) {
-        const uint32_t k = keys[e];
-        if (k != cur) {
+        if (e == end) {  // bucket cur ends here: emit it, move to the next non-empty bucket
             emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
-            cur = k;
+            do {
+                cur++;
+                end = row_ptr[cur + 1];
+            } while (end == e);
             bases = key_bases<C>(insts, sh, cur);
             acc = xyzz_inf<typename C::T>();
         }
@@ -308,6 +338,64 @@ __global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restri
         acc = xyzz_add(acc, xyzz_load(in_pts + s));
     }
     if (cur != kNone) emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
+}
+
+// Fixup instead of merge rounds (when buckets are short): a bucket k whose entries
+// [row_ptr[k], row_ptr[k+1]) span units u0 < u1 left its pieces in slot 1 of unit u0 (the
+// bucket continues past the segment) and in slot 0 of every unit u0 < u <= u1 (the bucket
+// began before the segment). One thread per bucket adds up to kFixupMax + 1 pieces; longer
+// buckets are listed for msm_fixup_long_kernel, one CTA each.
+static constexpr uint32_t kFixupMax = 8;
+static constexpr uint64_t kFixupDensity = 48;  // CSR entries per bucket up to which the fixup is used
+static constexpr int kFixupLongThreads = 128;
+
+template <class C>
+__global__ void __launch_bounds__(128) msm_fixup_kernel(const uint32_t* __restrict__ row_ptr, uint32_t nbuckets,
+                                                        const typename C::P* __restrict__ slot_pts,
+                                                        typename C::P* __restrict__ buckets,
+                                                        uint32_t* __restrict__ long_list,
+                                                        uint32_t* __restrict__ long_count) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nbuckets) return;
+    const uint32_t b0 = row_ptr[k], b1 = row_ptr[k + 1];
+    if (b1 == b0) return;
+    const uint32_t u0 = b0 / kSegment, u1 = (b1 - 1) / kSegment;
+    if (u0 == u1) return;  // final already (written by the accumulation)
+    if (u1 - u0 > kFixupMax) {
+        long_list[atomicAdd(long_count, 1u)] = k;
+        return;
+    }
+    typename C::P acc = xyzz_load(slot_pts + 2 * (size_t)u0 + 1);
+    for (uint32_t u = u0 + 1; u <= u1; u++) acc = xyzz_add(acc, xyzz_load(slot_pts + 2 * (size_t)u));
+    xyzz_store(buckets + k, acc);
+}
+
+// One CTA per listed bucket (grid-stride over the list): strided partial sums, then a
+// shared-memory tree.
+template <class C>
+__global__ void __launch_bounds__(kFixupLongThreads) msm_fixup_long_kernel(const uint32_t* __restrict__ row_ptr,
+                                                                           const typename C::P* __restrict__ slot_pts,
+                                                                           typename C::P* __restrict__ buckets,
+                                                                           const uint32_t* __restrict__ long_list,
+                                                                           const uint32_t* __restrict__ long_count) {
+    using P = typename C::P;
+    __shared__ P red[kFixupLongThreads];
+    const uint32_t count = *long_count;
+    for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
+        const uint32_t k = long_list[item];
+        const uint32_t u0 = row_ptr[k] / kSegment, u1 = (row_ptr[k + 1] - 1) / kSegment;
+        P acc = xyzz_inf<typename C::T>();
+        for (uint32_t u = u0 + threadIdx.x; u <= u1; u += blockDim.x)
+            acc = xyzz_add(acc, xyzz_load(slot_pts + 2 * (size_t)u + (u == u0 ? 1 : 0)));
+        red[threadIdx.x] = acc;
+        __syncthreads();
+        for (uint32_t off = blockDim.x / 2; off > 0; off >>= 1) {
+            if (threadIdx.x < off) red[threadIdx.x] = xyzz_add(red[threadIdx.x], red[threadIdx.x + off]);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) xyzz_store(buckets + k, red[0]);
+        __syncthreads();
+    }
 }
 
 // ---- 5. window reduction ----------------------------------------------------------------
@@ -516,10 +604,10 @@ struct MsmPipeT {
     std::vector<size_t> out_index;  // result slot of each instance
     MsmInst* d_inst = nullptr;
     uint32_t* d_offs = nullptr;
-    uint32_t *digits = nullptr, *row_ptr = nullptr, *cursor = nullptr, *entries = nullptr, *keys = nullptr,
-             *scan_tmp = nullptr;
+    uint32_t *digits = nullptr, *row_ptr = nullptr, *cursor = nullptr, *entries = nullptr, *scan_tmp = nullptr;
     uint32_t *slot_keys_a = nullptr, *slot_keys_b = nullptr;
     P *slot_pts_a = nullptr, *slot_pts_b = nullptr;
+    uint32_t *long_list = nullptr, *long_count = nullptr;  // fixup mode
     P *buckets = nullptr, *Yb = nullptr, *Eb = nullptr, *Y2 = nullptr, *E2 = nullptr, *F2 = nullptr, *tgt = nullptr;
     P* h_tgt = nullptr;  // host copy of the per-set targets (sets * targets)
     uint32_t* h_total = nullptr;
@@ -574,16 +662,17 @@ static size_t pipe_layout(MsmPipeT<C>& p, char* base) {
     const size_t first_out = (p.units + kFirstGroup - 1) / kFirstGroup;
     p.d_inst = reinterpret_cast<MsmInst*>(take(p.inst.size() * sizeof(MsmInst)));
     p.d_offs = reinterpret_cast<uint32_t*>(take(p.offs.size() * 4));
-    p.digits = reinterpret_cast<uint32_t*>(take(p.max_entries * 4));
+    p.digits = reinterpret_cast<uint32_t*>(take(std::max<uint64_t>(p.max_entries * 4, p.N * sizeof(fe))));
     p.row_ptr = reinterpret_cast<uint32_t*>(take((p.nbuckets + 1) * 4));
     p.cursor = reinterpret_cast<uint32_t*>(take(p.nbuckets * 4));
     p.entries = reinterpret_cast<uint32_t*>(take(p.max_entries * 4));
-    p.keys = reinterpret_cast<uint32_t*>(take(p.max_entries * 4));
     p.scan_tmp = reinterpret_cast<uint32_t*>(take(scan_scratch_elems(p.nbuckets) * 4));
     p.slot_keys_a = reinterpret_cast<uint32_t*>(take((size_t)2 * p.units * 4));
     p.slot_pts_a = reinterpret_cast<P*>(take((size_t)2 * p.units * sizeof(P)));
     p.slot_keys_b = reinterpret_cast<uint32_t*>(take(2 * first_out * 4));
     p.slot_pts_b = reinterpret_cast<P*>(take(2 * first_out * sizeof(P)));
+    p.long_list = reinterpret_cast<uint32_t*>(take(((size_t)p.units / kFixupMax + 2) * 4));
+    p.long_count = reinterpret_cast<uint32_t*>(take(4));
     p.buckets = reinterpret_cast<P*>(take(p.nbuckets * sizeof(P)));
     p.Yb = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G * sizeof(P)));
     p.Eb = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G * sizeof(P)));
@@ -611,37 +700,50 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
     ZK_TRY_CUDA(cudaMemsetAsync(p.buckets, 0, p.nbuckets * sizeof(P), st));
     const uint32_t N = (uint32_t)p.N;
     const unsigned nblk = (unsigned)((p.N + 255) / 256);
-    ZK_LAUNCH(c, "msm_digits", msm_digits_kernel<C>, nblk, 256, 0, p.d_inst, p.d_offs, N, scalars_mont, sh, p.digits,
-              p.row_ptr);
+    ZK_LAUNCH(c, "msm_digits", msm_digits_kernel<C>, nblk, 256, 0, p.d_inst, p.d_offs, N, scalars_mont, sh,
+              reinterpret_cast<fe*>(p.digits), p.row_ptr);
     ZK_TRY_CUDA(cudaGetLastError());
     // row_ptr[0..nbuckets) := exclusive scan; row_ptr[nbuckets] := total
     int rc = device_exclusive_scan(c, p.row_ptr, p.nbuckets, p.row_ptr + p.nbuckets, p.scan_tmp);
     if (rc != ZK_OK) return rc;
     ZK_TRY_CUDA(cudaMemcpyAsync(p.cursor, p.row_ptr, p.nbuckets * 4, cudaMemcpyDeviceToDevice, st));
-    ZK_LAUNCH(c, "msm_scatter", msm_scatter_kernel, nblk, 256, 0, p.digits, p.d_inst, p.d_offs, N, sh, p.cursor,
-              p.entries, p.keys);
+    ZK_LAUNCH(c, "msm_scatter", msm_scatter_kernel, nblk, 256, 0, reinterpret_cast<const fe*>(p.digits), p.d_inst,
+              p.d_offs, N, sh, p.cursor, p.entries);
     ZK_TRY_CUDA(cudaGetLastError());
 
     // accumulation rounds
     const uint32_t* d_total = p.row_ptr + p.nbuckets;
-    ZK_LAUNCH(c, "msm_accumulate", msm_accumulate_kernel<C>, (p.units + 127) / 128, 128, 0, p.entries, p.keys, d_total,
+    ZK_LAUNCH(c, "msm_accumulate", msm_accumulate_kernel<C>, (p.units + 127) / 128, 128, 0, p.entries, d_total,
               p.row_ptr, p.d_inst, sh, p.units, p.buckets, p.slot_keys_a, p.slot_pts_a);
     ZK_TRY_CUDA(cudaGetLastError());
-    uint64_t span = kSegment;
-    uint32_t in_units = p.units;
-    uint32_t *ik = p.slot_keys_a, *ok = p.slot_keys_b;
-    typename C::P *ip = p.slot_pts_a, *op = p.slot_pts_b;
-    uint32_t group = kFirstGroup;
-    while (in_units > 1) {
-        const uint32_t out_units = (in_units + group - 1) / group;
-        span *= group;
-        ZK_LAUNCH(c, group == kFirstGroup ? "msm_merge_pairs" : "msm_merge", msm_merge_kernel<C>, (out_units + 127) / 128,
-                  128, 0, ik, ip, in_units, group, d_total, p.row_ptr, span, out_units, p.buckets, ok, op);
+    // Partial sums of straddling buckets: short buckets (at most ~1.5 segments on average)
+    // by one fixup pass, longer ones by merge rounds (measured at 2^20 / 2^22: fixup 0.33 vs
+    // rounds 0.48 ms; rounds 1.0 vs fixup 2.1 ms, when most buckets span 4+ segments).
+    if (p.max_entries <= (uint64_t)p.nbuckets * kFixupDensity) {
+        ZK_TRY_CUDA(cudaMemsetAsync(p.long_count, 0, 4, st));
+        ZK_LAUNCH(c, "msm_fixup", msm_fixup_kernel<C>, (unsigned)((p.nbuckets + 127) / 128), 128, 0, p.row_ptr,
+                  (uint32_t)p.nbuckets, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
         ZK_TRY_CUDA(cudaGetLastError());
-        std::swap(ik, ok);
-        std::swap(ip, op);
-        in_units = out_units;
-        group = kGroup;
+        ZK_LAUNCH(c, "msm_fixup_long", msm_fixup_long_kernel<C>, (unsigned)(c->num_sms * 2), kFixupLongThreads, 0,
+                  p.row_ptr, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
+        ZK_TRY_CUDA(cudaGetLastError());
+    } else {
+        uint64_t span = kSegment;
+        uint32_t in_units = p.units;
+        uint32_t *ik = p.slot_keys_a, *ok = p.slot_keys_b;
+        typename C::P *ip = p.slot_pts_a, *op = p.slot_pts_b;
+        uint32_t group = kFirstGroup;
+        while (in_units > 1) {
+            const uint32_t out_units = (in_units + group - 1) / group;
+            span *= group;
+            ZK_LAUNCH(c, group == kFirstGroup ? "msm_merge_pairs" : "msm_merge", msm_merge_kernel<C>, (out_units + 127) / 128,
+                      128, 0, ik, ip, in_units, group, d_total, p.row_ptr, span, out_units, p.buckets, ok, op);
+            ZK_TRY_CUDA(cudaGetLastError());
+            std::swap(ik, ok);
+            std::swap(ip, op);
+            in_units = out_units;
+            group = kGroup;
+        }
     }
 
     // window reduction
@@ -665,35 +767,108 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
     return ZK_OK;
 }
 
-// Host: instance k of pipeline p from its per-set targets.
+// A persistent pool of host threads for the combination step (created on first use,
+// never destroyed: its threads sleep between jobs). run() executes fn(0 .. count-1) on the
+// workers and the calling thread and returns when all are done; calls are serialised.
+class HostPool {
+   public:
+    static HostPool& get() {
+        static HostPool* pool = new HostPool();
+        return *pool;
+    }
+
+    void run(size_t count, const std::function<void(size_t)>& fn) {
+        if (count == 0) return;
+        if (count == 1 || workers_ == 0) {
+            for (size_t i = 0; i < count; i++) fn(i);
+            return;
+        }
+        std::lock_guard<std::mutex> serial(run_mu_);
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            fn_ = &fn;
+            count_ = count;
+            next_.store(0);
+            active_ = workers_;
+            gen_++;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> g(mu_);
+        done_cv_.wait(g, [&] { return active_ == 0; });
+    }
+
+   private:
+    HostPool() {
+        const size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
+        workers_ = std::min<size_t>(hw, 16) - 1;
+        for (size_t i = 0; i < workers_; i++) std::thread([this] { loop(); }).detach();
+    }
+
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> g(mu_);
+                cv_.wait(g, [&] { return gen_ != seen; });
+                seen = gen_;
+            }
+            work();
+            std::lock_guard<std::mutex> g(mu_);
+            if (--active_ == 0) done_cv_.notify_one();
+        }
+    }
+
+    void work() {
+        for (size_t i; (i = next_.fetch_add(1)) < count_;) (*fn_)(i);
+    }
+
+    size_t workers_ = 0;
+    std::mutex run_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(size_t)>* fn_ = nullptr;
+    size_t count_ = 0;
+    std::atomic<size_t> next_{0};
+    size_t active_ = 0;
+    uint64_t gen_ = 0;
+};
+
+// Host: the sum S_w of window (or set) w of instance k from its targets:
 //   one level   S_w = T0 + g (T1 + H)            (T0 = sum E1, T1 = sum Y1)
 //   two levels  S_w = T0 + g (T1 + g2 (T2 + H))  (T0 = sum F2 = sum E1, T1 = sum E2, T2 = sum Y2)
-// with H = sum_k 2^k M_k (Horner); then total = sum_w 2^(c w) S_w (Horner over windows; one
-// set in fixed-base mode, where the window shifts are already in the bases).
+// with H = sum_k 2^k M_k (Horner).
 template <class C>
-static void pipe_combine(const MsmPipeT<C>& p, uint32_t k, uint8_t* out_xy, int32_t* out_is_inf) {
+static zkh::XyzzT<typename HostOf<C>::T> window_sum(const MsmPipeT<C>& p, uint32_t k, uint32_t w) {
     using H = typename HostOf<C>::T;
     const MsmShape& sh = p.sh;
     uint32_t log_g = 0, log_g2 = 0;
     while ((1u << log_g) < sh.g) log_g++;
     while ((1u << log_g2) < sh.g2) log_g2++;
+    const typename C::P* T = p.h_tgt + ((size_t)k * sh.Wr + (size_t)w) * sh.targets;
+    zkh::XyzzT<H> h = zkh::xyzz_inf<H>();
+    for (int b = (int)sh.K - 1; b >= 0; b--) {
+        h = zkh::xyzz_dbl(h);
+        h = zkh::xyzz_add(h, to_host<C>(T[sh.plain + b]));
+    }
+    zkh::XyzzT<H> sw = zkh::xyzz_add(h, to_host<C>(T[sh.plain - 1]));
+    if (sh.plain == 3) {
+        sw = host_dbl_n(sw, log_g2);
+        sw = zkh::xyzz_add(sw, to_host<C>(T[1]));
+    }
+    sw = host_dbl_n(sw, log_g);
+    return zkh::xyzz_add(sw, to_host<C>(T[0]));
+}
+
+// total = sum_w 2^(c w) S_w by Horner over the windows (one set in fixed-base mode, where
+// the window shifts are already in the bases), as canonical affine bytes.
+template <class C>
+static void horner_out(const MsmPipeT<C>& p, const zkh::XyzzT<typename HostOf<C>::T>* sw, uint8_t* out_xy,
+                       int32_t* out_is_inf) {
+    using H = typename HostOf<C>::T;
     zkh::XyzzT<H> total = zkh::xyzz_inf<H>();
-    for (int w = (int)sh.Wr - 1; w >= 0; w--) {
-        const typename C::P* T = p.h_tgt + ((size_t)k * sh.Wr + (size_t)w) * sh.targets;
-        zkh::XyzzT<H> h = zkh::xyzz_inf<H>();
-        for (int b = (int)sh.K - 1; b >= 0; b--) {
-            h = zkh::xyzz_dbl(h);
-            h = zkh::xyzz_add(h, to_host<C>(T[sh.plain + b]));
-        }
-        zkh::XyzzT<H> sw = zkh::xyzz_add(h, to_host<C>(T[sh.plain - 1]));
-        if (sh.plain == 3) {
-            sw = host_dbl_n(sw, log_g2);
-            sw = zkh::xyzz_add(sw, to_host<C>(T[1]));
-        }
-        sw = host_dbl_n(sw, log_g);
-        sw = zkh::xyzz_add(sw, to_host<C>(T[0]));
-        total = host_dbl_n(total, sh.c);
-        total = zkh::xyzz_add(total, sw);
+    for (int w = (int)p.sh.Wr - 1; w >= 0; w--) {
+        total = host_dbl_n(total, p.sh.c);
+        total = zkh::xyzz_add(total, sw[w]);
     }
     H x, y;
     *out_is_inf = zkh::xyzz_to_affine_canonical(total, &x, &y) ? 1 : 0;
@@ -701,35 +876,38 @@ static void pipe_combine(const MsmPipeT<C>& p, uint32_t k, uint8_t* out_xy, int3
     std::memcpy(out_xy + sizeof(H), &y, sizeof(H));
 }
 
-// Combine every instance of `pipes` (in parallel host threads when there are several).
+// Combine every instance of `pipes`: the window sums of all instances in parallel on the
+// host pool, then each instance's Horner (in parallel across instances).
 template <class C>
 static void combine_all(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, uint8_t* out_xy, int32_t* out_is_inf) {
-    constexpr size_t kOut = 2 * sizeof(typename HostOf<C>::T);  // bytes of one affine result
+    using H = typename HostOf<C>::T;
+    constexpr size_t kOut = 2 * sizeof(H);  // bytes of one affine result
     const auto t0 = std::chrono::steady_clock::now();
-    std::vector<std::pair<uint32_t, uint32_t>> tasks;
+    struct Inst {
+        uint32_t q, k;
+        size_t first;  // index of its first window sum
+    };
+    std::vector<Inst> insts;
+    std::vector<std::pair<uint32_t, uint32_t>> win;  // (instance, window)
     uint64_t entries = 0;
     for (uint32_t q = 0; q < pipes.size(); q++) {
         entries += *pipes[q].h_total;
-        for (uint32_t k = 0; k < pipes[q].sh.inst; k++) tasks.emplace_back(q, k);
+        for (uint32_t k = 0; k < pipes[q].sh.inst; k++) {
+            insts.push_back({q, k, win.size()});
+            for (uint32_t w = 0; w < pipes[q].sh.Wr; w++) win.emplace_back((uint32_t)insts.size() - 1, w);
+        }
     }
-    auto run = [&](size_t t) {
-        const MsmPipeT<C>& p = pipes[tasks[t].first];
-        const size_t o = p.out_index[tasks[t].second];
-        pipe_combine(p, tasks[t].second, out_xy + kOut * o, out_is_inf + o);
-    };
-    const size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
-    const size_t nthreads = std::min<size_t>({tasks.size(), hw, 16});
-    if (nthreads <= 1) {
-        for (size_t t = 0; t < tasks.size(); t++) run(t);
-    } else {
-        std::atomic<size_t> next{0};
-        std::vector<std::thread> th;
-        for (size_t i = 0; i < nthreads; i++)
-            th.emplace_back([&]() {
-                for (size_t t; (t = next.fetch_add(1)) < tasks.size();) run(t);
-            });
-        for (auto& t : th) t.join();
-    }
+    std::vector<zkh::XyzzT<H>> sums(win.size());
+    HostPool& pool = HostPool::get();
+    pool.run(win.size(), [&](size_t t) {
+        const Inst& in = insts[win[t].first];
+        sums[t] = window_sum<C>(pipes[in.q], in.k, win[t].second);
+    });
+    pool.run(insts.size(), [&](size_t t) {
+        const Inst& in = insts[t];
+        const size_t o = pipes[in.q].out_index[in.k];
+        horner_out<C>(pipes[in.q], sums.data() + in.first, out_xy + kOut * o, out_is_inf + o);
+    });
     prof_host(c, "msm_host_combine",
               std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
     c->msm_entries = entries;

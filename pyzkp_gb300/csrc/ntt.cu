@@ -48,13 +48,18 @@ struct NttPassParams {
     uint32_t log_t;
     uint32_t log_l;
     uint32_t s_bits;
+    uint32_t last;  // 1 on the last pass: outputs reduced to [0, r)
 };
+
+// Butterflies, twiddles and scales run on lazy Fr values in [0, 2r) (FrLazyP); inputs are
+// canonical, intermediate passes store lazy values, the last pass stores canonical ones.
+using FrN = FrLazyP;
 
 __device__ __forceinline__ fe lookup2(const fe* lo, const fe* hi, uint32_t e, uint32_t s_bits) {
     fe a = fe_ldg(lo + (e & ((1u << s_bits) - 1)));
     uint32_t h = e >> s_bits;
     if (h == 0) return a;
-    return fe_mul<FrP>(a, fe_ldg(hi + h));
+    return fe_mul<FrN>(a, fe_ldg(hi + h));
 }
 
 __device__ __forceinline__ uint32_t swz(uint32_t pos, uint32_t log_r) {
@@ -97,10 +102,10 @@ __device__ __forceinline__ void ntt_pass_body(const NttPassParams& P, uint32_t t
         const uint32_t col = c0 + t;
         const uint32_t g = col + (m << stride_log);
         fe v = g < P.in_len ? fe_ldg(P.in + g) : fe_zero();
-        if (P.pre_lo != nullptr && g < P.in_len) v = fe_mul<FrP>(v, lookup2(P.pre_lo, P.pre_hi, g, P.s_bits));
+        if (P.pre_lo != nullptr && g < P.in_len) v = fe_mul<FrN>(v, lookup2(P.pre_lo, P.pre_hi, g, P.s_bits));
         if (P.log_l != 0) {
             const uint32_t e = (m * (col & l_mask)) << tw_shift;
-            if (e != 0) v = fe_mul<FrP>(v, lookup2(P.tw_lo, P.tw_hi, e, P.s_bits));
+            if (e != 0) v = fe_mul<FrN>(v, lookup2(P.tw_lo, P.tw_hi, e, P.s_bits));
         }
         smem_put(s_lo, s_hi, (swz(m, log_r) << log_t) + t, v);
     }
@@ -118,9 +123,9 @@ __device__ __forceinline__ void ntt_pass_body(const NttPassParams& P, uint32_t t
             const uint32_t a1 = (swz(i0 + h, log_r) << log_t) + t;
             fe u = smem_get(s_lo, s_hi, a0);
             fe v = smem_get(s_lo, s_hi, a1);
-            fe sum = fe_add<FrP>(u, v);
-            fe diff = fe_sub<FrP>(u, v);
-            if (j != 0) diff = fe_mul<FrP>(diff, fe_ldg(P.radix_tw + (j << st)));
+            fe sum = fe_add<FrN>(u, v);
+            fe diff = fe_sub<FrN>(u, v);
+            if (j != 0) diff = fe_mul<FrN>(diff, fe_ldg(P.radix_tw + (j << st)));
             smem_put(s_lo, s_hi, a0, sum);
             smem_put(s_lo, s_hi, a1, diff);
         }
@@ -143,8 +148,9 @@ __device__ __forceinline__ void ntt_pass_body(const NttPassParams& P, uint32_t t
         const uint32_t o = ((col >> P.log_l) << (log_r + P.log_l)) + (col & l_mask) + (q << P.log_l);
         if (P.post_lo != nullptr) {
             fe s = P.post_hi != nullptr ? lookup2(P.post_lo, P.post_hi, o, P.s_bits) : fe_ldg(P.post_lo);
-            val = fe_mul<FrP>(val, s);
+            val = fe_mul<FrN>(val, s);
         }
+        if (P.last) val = fe_reduce_once<FrP>(val);
         fe_store(P.out + o, val);
     }
 }
@@ -365,6 +371,7 @@ static void make_passes(const NttPlan* plan, fe* out, const fe* in, uint32_t val
         P.post_lo = plan->post_lo;
         P.post_hi = plan->post_hi;
         P.in_len = valid;
+        P.last = 1;
         launches->push_back({P, 1, 32, 2 * 16});
         return;
     }
@@ -393,6 +400,7 @@ static void make_passes(const NttPlan* plan, fe* out, const fe* in, uint32_t val
         P.log_r = lr;
         P.log_t = lt;
         P.log_l = log_l;
+        P.last = remaining == 0 ? 1u : 0u;
         const uint32_t elems = 1u << (lr + lt);
         const uint32_t threads = elems / 2 < (uint32_t)kNttThreads ? (elems / 2 < 32 ? 32 : elems / 2) : kNttThreads;
         launches->push_back({P, (uint32_t)(n >> (lr + lt)), threads, elems * 32});
@@ -800,6 +808,7 @@ static int ntt_run_noalloc(Ctx* c, int mode, fe* out, const fe* in, size_t in_le
         P.post_lo = has_post ? tables + off_post_lo : nullptr;
         P.post_hi = (has_post && !post_const) ? tables + off_post_hi : nullptr;
         P.in_len = valid;
+        P.last = 1;
         ZK_LAUNCH(c, "ntt_pass", ntt_pass_kernel, 1, 32, 2 * 16, P);
         ZK_TRY_CUDA(cudaGetLastError());
         return ZK_OK;
@@ -825,6 +834,7 @@ static int ntt_run_noalloc(Ctx* c, int mode, fe* out, const fe* in, size_t in_le
         P.log_r = lr;
         P.log_t = lt;
         P.log_l = log_l;
+        P.last = last ? 1u : 0u;
         const uint32_t elems = 1u << (lr + lt);
         const uint32_t threads = elems / 2 < (uint32_t)kNttThreads ? (elems / 2 < 32 ? 32 : elems / 2) : kNttThreads;
         const uint32_t blocks = (uint32_t)(n >> (lr + lt));

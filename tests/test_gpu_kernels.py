@@ -276,3 +276,22 @@ def test_msm_fixed_base_precompute_matches_oracle(gpu_ctx, kind):
         # prefix with offset over the shifted rows
         m = 777
         assert gpu_ctx.msm_g1(b, ds, m, offset=100) == O.affine_to_ints(O.msm_known_answer(k[100:100 + m], s[:m]))
+
+
+def test_msm_zero_digit_after_carry(gpu_ctx):
+    """A window whose bits are all ones and that receives the carry of a negative digit below
+    yields digit 0 with a carry onwards (v = 2^c); every window size must skip that digit."""
+    n = 64
+    k = synth.base_dlogs(4700, n)
+    bases = O.g1_fixed_base_mul(O.G1_GENERATOR, k)
+    vals = []
+    for c in range(4, 17):
+        # window 0 above half (carry 1), window 1 all ones -> 2^c, then the same pattern higher up
+        v = ((1 << (c - 1)) + 1) | (((1 << c) - 1) << c)
+        v |= v << (4 * c)
+        vals.append(v % R)
+    vals += [(R - 1), (1 << 253) - 1, (1 << 200) - 1]
+    s = synth.ints_to_limbs((vals * (n // len(vals) + 1))[:n])
+    exp = O.affine_to_ints(O.msm_known_answer(k, s))
+    for c in (0, 4, 5, 6, 7, 8, 11, 13, 16, 20):
+        assert gpu_msm(gpu_ctx, bases, s, window_bits=c) == exp, c
