@@ -296,6 +296,9 @@ def run_gpu(args, ranks: Ranks) -> dict:
     clocks = sampler.stop()
     sweep = run_gpu_msm_sweep(ctx, args, flush) if ranks.world == 1 else None
     fixed = run_gpu_fixed_base(ctx, args, flush) if ranks.world == 1 else None
+    fixed_sweep = ({f"2^{lg}": run_gpu_fixed_base(ctx, args, flush, log_n=lg, calls=6) for lg in (16, 18, 20, 22)}
+                   if ranks.world == 1 else None)
+    ntt_sweep = run_gpu_ntt_sweep(ctx, args, flush) if ranks.world == 1 else None
     batch = run_gpu_batch(ctx, args, flush) if ranks.world == 1 else None
     serve_res = run_gpu_serve(ctx, args) if ranks.world == 1 else None
 
@@ -328,6 +331,8 @@ def run_gpu(args, ranks: Ranks) -> dict:
         "ntt_2_22": ntt22,
         "msm_sweep": sweep,
         "msm_fixed_base_2_20": fixed,
+        "msm_fixed_base_sweep": fixed_sweep,
+        "ntt_sweep": ntt_sweep,
         "batch_64": batch,
         "groth16_serve": serve_res,
         "clocks": clocks,
@@ -407,6 +412,39 @@ def run_gpu_ntt(ctx, args, ranks, log_n, flush, imad_tops, hbm_peak, brief=False
         tot = ranks.max(sum(ts))
         out["e2e"] = {"value": round(n * args.steps * ranks.world / (tot * 1e-3) / 1e6, 2), "unit": "Melem/s",
                       "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 32}
+    return out
+
+
+def run_gpu_ntt_sweep(ctx, args, flush, sizes=(12, 16, 20, 22)) -> dict:
+    """Config 1: the four transforms (ROOTS_/COSET_ EVALS/COEFFS, shift 5) at every size,
+    device-resident Montgomery data, L2 flushed before each step (median of the steps)."""
+    from pyzkp_gb300 import _native as N
+    from pyzkp_gb300 import synth
+
+    modes = (("evals_from_coeffs", N.NTT_EVALS_FROM_COEFFS, 1), ("coeffs_from_evals", N.NTT_COEFFS_FROM_EVALS, 1),
+             ("coset_evals_from_coeffs", N.NTT_COSET_EVALS_FROM_COEFFS, 5),
+             ("coset_coeffs_from_evals", N.NTT_COSET_COEFFS_FROM_EVALS, 5))
+    out = {}
+    steps = max(3, min(args.steps, 10))
+    for log_n in sizes:
+        n = 1 << log_n
+        om = ntt_omega(n)
+        din = ctx.to_device(synth.fr_uniform(synth.seed_for(1, log_n), n))
+        ctx.fr_to_mont(din, din, n)
+        dout = ctx.alloc(n * 32)
+        row = {}
+        for name, mode, shift in modes:
+            for _ in range(2):
+                ctx.ntt(mode, dout, din, n, log_n, om, shift)
+            ts = []
+            for _ in range(steps):
+                ctx.memset(flush, 1)
+                ctx.timer_start()
+                ctx.ntt(mode, dout, din, n, log_n, om, shift)
+                ts.append(ctx.timer_stop())
+            ms = statistics.median(ts)
+            row[name] = {"Melem_s": round(n / (ms * 1e-3) / 1e6, 1), "ms": round(ms, 4)}
+        out[f"2^{log_n}"] = row
     return out
 
 

@@ -747,6 +747,9 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
     }
 
     // window reduction
+    // the targets' CTAs sum G2 points each: no more threads than the power of two covering G2
+    uint32_t target_threads = 32;
+    while (target_threads < sh.G2 && target_threads < (uint32_t)C::kTargetThreads) target_threads <<= 1;
     const uint32_t nb1 = sh.sets * sh.G;
     ZK_LAUNCH(c, "msm_bucket_blocks", msm_bucket_blocks_kernel<C>, (nb1 + 127) / 128, 128, 0, p.buckets, sh, p.Yb, p.Eb);
     ZK_TRY_CUDA(cudaGetLastError());
@@ -755,10 +758,10 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
         ZK_LAUNCH(c, "msm_bucket_blocks2", msm_bucket_blocks2_kernel<C>, (nb2 + 127) / 128, 128, 0, p.Yb, p.Eb, sh, p.Y2,
                   p.E2, p.F2);
         ZK_TRY_CUDA(cudaGetLastError());
-        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel<C>, sh.sets * sh.targets, C::kTargetThreads, 0, p.F2, p.E2, p.Y2,
+        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel<C>, sh.sets * sh.targets, target_threads, 0, p.F2, p.E2, p.Y2,
                   p.Y2, sh, p.tgt);
     } else {
-        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel<C>, sh.sets * sh.targets, C::kTargetThreads, 0, p.Eb, p.Yb, p.Yb,
+        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel<C>, sh.sets * sh.targets, target_threads, 0, p.Eb, p.Yb, p.Yb,
                   p.Yb, sh, p.tgt);
     }
     ZK_TRY_CUDA(cudaGetLastError());
