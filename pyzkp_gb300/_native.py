@@ -29,7 +29,7 @@ EXPORTED_SYMBOLS = (
     "zk_last_error", "zk_version", "zk_ctx_create", "zk_ctx_destroy", "zk_ctx_sync", "zk_ctx_stream",
     "zk_ctx_num_sms", "zk_alloc", "zk_free", "zk_h2d", "zk_d2h", "zk_host_alloc", "zk_host_free",
     "zk_fr_to_mont", "zk_fr_from_mont", "zk_fq_to_mont", "zk_fq_from_mont", "zk_fr_mul", "zk_fr_sub", "zk_ntt",
-    "zk_bases_create", "zk_bases_create_dev", "zk_bases_destroy", "zk_bases_count", "zk_msm_g1",
+    "zk_bases_create", "zk_bases_create_dev", "zk_bases_destroy", "zk_bases_count", "zk_msm_g1", "zk_msm_g1_host",
     "zk_g1_fixed_base_mul", "zk_memset", "zk_launch_count", "zk_prof_enable", "zk_prof_reset", "zk_prof_count",
     "zk_prof_get", "zk_timer_start", "zk_timer_stop", "zk_msm_last_stats", "zk_imad_peak", "zk_d2d",
     "zk_fr_trimmed_len", "zk_ntt_noalloc", "zk_imad_probe", "zk_bases_precompute", "zk_msm_g1_batch",
@@ -88,6 +88,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_bases_destroy": ([P], I),
             "zk_bases_count": ([P, ctypes.POINTER(ctypes.c_size_t)], I),
             "zk_msm_g1": ([P, P, S, P, S, I, U32, P, ctypes.POINTER(ctypes.c_int)], I),
+            "zk_msm_g1_host": ([P, P, P, S, I, U32, P, ctypes.POINTER(ctypes.c_int)], I),
             "zk_g1_fixed_base_mul": ([P, P, P, S, P], I),
             "zk_memset": ([P, P, I, S], I),
             "zk_launch_count": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
@@ -571,6 +572,26 @@ class Context:
         inf = ctypes.c_int()
         check(load().zk_msm_g1(self.handle, bases.handle, int(offset), scalars.ptr, int(n), 1 if scalars_mont else 0,
                                int(window_bits), out, ctypes.byref(inf)), "zk_msm_g1")
+        if inf.value:
+            return None
+        b = bytes(out)
+        return int.from_bytes(b[:32], "little"), int.from_bytes(b[32:], "little")
+
+    def msm_g1_host(self, xy, scalars, n: int, *, scalars_mont: bool = False, window_bits: int = 0):
+        """One-call MSM from host memory (zk_msm_g1_host): ``xy`` canonical affine points
+        (n x 64 bytes), ``scalars`` n x 32 bytes; numpy arrays or PinnedBuffer (pinned memory
+        makes the copies asynchronous). Returns (x, y) canonical ints, or None for infinity."""
+        def _ptr(a):
+            if hasattr(a, "ptr"):
+                return a.ptr
+            a = np.ascontiguousarray(a)
+            keep.append(a)
+            return a.ctypes.data
+        keep = []
+        out = (ctypes.c_uint8 * 64)()
+        inf = ctypes.c_int()
+        check(load().zk_msm_g1_host(self.handle, _ptr(xy), _ptr(scalars), int(n), 1 if scalars_mont else 0,
+                                    int(window_bits), out, ctypes.byref(inf)), "zk_msm_g1_host")
         if inf.value:
             return None
         b = bytes(out)

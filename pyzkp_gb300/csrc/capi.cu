@@ -156,6 +156,12 @@ int zk_ctx_destroy(zk_ctx* ctx) {
         for (void* p : kv.second->allocations) cudaFree(p);
         delete kv.second;
     }
+    if (ctx->impl.copy_stream) {
+        cudaStreamSynchronize(ctx->impl.copy_stream);
+        cudaStreamDestroy(ctx->impl.copy_stream);
+    }
+    if (ctx->impl.copy_go) cudaEventDestroy(ctx->impl.copy_go);
+    if (ctx->impl.copy_done) cudaEventDestroy(ctx->impl.copy_done);
     cudaStreamDestroy(ctx->impl.stream);
     delete ctx;
     return ZK_OK;
@@ -480,6 +486,65 @@ int zk_msm_g1(zk_ctx* ctx, const zk_bases* bases, size_t offset, const void* sca
     return zk::msm_run(&ctx->impl, bases->dev + offset, static_cast<const zk::fe*>(scalars_dev), n, scalars_mont,
                        window_bits, out_xy, out_is_inf, bases->shifted ? bases->shifted + offset : nullptr,
                        bases->shifted_c, bases->n);
+}
+
+int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scalars_host, size_t n, int scalars_mont,
+                   uint32_t window_bits, uint8_t out_xy[64], int* out_is_inf) {
+    CTX_OR_FAIL(ctx);
+    if (out_xy == nullptr || out_is_inf == nullptr || (n && (xy_canonical_host == nullptr || scalars_host == nullptr))) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    if (n == 0) {
+        std::memset(out_xy, 0, 64);
+        *out_is_inf = 1;
+        return ZK_OK;
+    }
+    Ctx* c = &ctx->impl;
+    if (c->copy_stream == nullptr) {
+        ZK_TRY_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_go, cudaEventDisableTiming));
+        ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
+    }
+    void* bases = nullptr;
+    void* scalars = nullptr;
+    int rc = zk::scratch_alloc(c, n * sizeof(zk::affine_t), &bases);
+    if (rc != ZK_OK) return rc;
+    if ((rc = zk::scratch_alloc(c, n * 32, &scalars)) != ZK_OK) {
+        zk::scratch_free(c, bases);
+        return rc;
+    }
+    // copy stream: bases upload + in-place conversion to Montgomery form, after the allocations
+    const cudaStream_t main_stream = c->stream;
+    cudaError_t e = cudaEventRecord(c->copy_go, main_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->copy_go, 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(bases, xy_canonical_host, n * 64, cudaMemcpyHostToDevice, c->copy_stream);
+    if (e == cudaSuccess) {
+        c->stream = c->copy_stream;  // the conversion kernel is launched on the copy stream
+        rc = zk::convert<zk::FqP, 1>(c, bases, bases, 2 * n);
+        c->stream = main_stream;
+        e = cudaEventRecord(c->copy_done, c->copy_stream);
+    }
+    // main stream: scalars, digits, sort; the accumulation waits for copy_done
+    if (e == cudaSuccess && rc == ZK_OK)
+        e = cudaMemcpyAsync(scalars, scalars_host, n * 32, cudaMemcpyHostToDevice, main_stream);
+    if (e == cudaSuccess && rc == ZK_OK) {
+        c->bases_wait = c->copy_done;
+        rc = zk::msm_run(c, static_cast<const zk::affine_t*>(bases), static_cast<const zk::fe*>(scalars), n,
+                         scalars_mont, window_bits, out_xy, out_is_inf);
+        c->bases_wait = nullptr;
+    }
+    // the frees are ordered on the main stream: after the copy stream is done with `bases`
+    cudaStreamWaitEvent(main_stream, c->copy_done, 0);
+    zk::scratch_free(c, scalars);
+    zk::scratch_free(c, bases);
+    if (e != cudaSuccess) {
+        zk::set_error(std::string("zk_msm_g1_host: ") + cudaGetErrorString(e));
+        cudaStreamSynchronize(main_stream);
+        return ZK_ECUDA;
+    }
+    return rc;
 }
 
 int zk_g1_fixed_base_mul(zk_ctx* ctx, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_xy_dev) {

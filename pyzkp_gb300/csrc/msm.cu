@@ -711,7 +711,8 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
               p.d_offs, N, sh, p.cursor, p.entries);
     ZK_TRY_CUDA(cudaGetLastError());
 
-    // accumulation rounds
+    // accumulation rounds (the first kernel that reads the points)
+    if (c->bases_wait != nullptr) ZK_TRY_CUDA(cudaStreamWaitEvent(st, c->bases_wait, 0));
     const uint32_t* d_total = p.row_ptr + p.nbuckets;
     ZK_LAUNCH(c, "msm_accumulate", msm_accumulate_kernel<C>, (p.units + 127) / 128, 128, 0, p.entries, d_total,
               p.row_ptr, p.d_inst, sh, p.units, p.buckets, p.slot_keys_a, p.slot_pts_a);

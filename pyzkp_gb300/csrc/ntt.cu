@@ -21,6 +21,7 @@
 // XOR-swizzled so the bit-reversed read-back does not hit one bank group.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 
@@ -30,7 +31,11 @@ namespace zk {
 
 static constexpr int kNttThreads = 256;
 static constexpr int kMaxLogR = 11;       // 2048 elements * 32 B = 64 KB of shared memory
-static constexpr int kTileLogElems = 11;  // R * T = 2048 elements per CTA
+static constexpr int kTileLogElems = 11;  // largest tile: R * T = 2048 elements per CTA
+// Default tile: 2^8 elements per CTA, or one radix-R column when R is larger. Measured on
+// GB300 (forward NTT, L2 flushed): 2^12 74 -> 22 us, 2^16 91 -> 34 us, 2^20 333 -> 298 us
+// against 2^11-element tiles; tiles of 2^6..2^8 are within 5% of one another at every size.
+static constexpr int kDefaultTileLog = 8;
 
 struct NttPassParams {
     const fe* in;
@@ -56,6 +61,7 @@ struct NttPassParams {
 using FrN = FrLazyP;
 
 __device__ __forceinline__ fe lookup2(const fe* lo, const fe* hi, uint32_t e, uint32_t s_bits) {
+    if (s_bits == kNttFullTable) return fe_ldg(lo + e);
     fe a = fe_ldg(lo + (e & ((1u << s_bits) - 1)));
     uint32_t h = e >> s_bits;
     if (h == 0) return a;
@@ -183,9 +189,26 @@ __global__ void __launch_bounds__(kNttThreads, 3) ntt_pass_batch_kernel(const Nt
     ntt_pass_body(sP, s_tile, smem);
 }
 
+// full[e] = lo[e mod 2^s] hi[e >> s] for e < n: a two-level table flattened into one
+// (canonical Montgomery values), so that a pass reads each factor with one load.
+__global__ void ntt_expand_table_kernel(fe* __restrict__ full, const fe* __restrict__ lo, const fe* __restrict__ hi,
+                                        uint32_t s_bits, uint32_t n) {
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        fe a = fe_ldg(lo + (e & ((1u << s_bits) - 1)));
+        const uint32_t h = e >> s_bits;
+        if (h != 0) a = fe_mul<FrP>(a, fe_ldg(hi + h));
+        fe_store(full + e, a);
+    }
+}
+
 // ------------------------------------------------------------------------------
 // host side: plans and launches
 // ------------------------------------------------------------------------------
+// Plans up to 2^kFullTableMaxLog keep full tables (n * 32 bytes per table, at most three
+// per plan) while the context holds less than kFullTableBudget bytes of them; larger or
+// later plans keep the two-level split (a second load and a product per factor).
+static constexpr uint32_t kFullTableMaxLog = 22;
+static constexpr size_t kFullTableBudget = (size_t)8 << 30;
 static zkh::F4 load_canon(const uint8_t b[32]) {
     zkh::F4 r;
     std::memcpy(r.v, b, 32);
@@ -284,6 +307,26 @@ static int build_plan(Ctx* c, int mode, uint32_t log_n, const zkh::F4& omega_m, 
             if ((rc = upload_table(c, plan, hi, &plan->post_hi)) != ZK_OK) return rc;
         }
     }
+    const size_t table_bytes = (size_t)n * 32;
+    const int tables = 1 + (plan->pre_hi != nullptr) + (plan->post_hi != nullptr);
+    if (log_n <= kFullTableMaxLog && c->ntt_full_table_bytes + tables * table_bytes <= kFullTableBudget) {
+        fe** lo_of[3] = {&plan->tw_lo, &plan->pre_lo, &plan->post_lo};
+        fe** hi_of[3] = {&plan->tw_hi, &plan->pre_hi, &plan->post_hi};
+        for (int t = 0; t < 3; t++) {
+            if (*hi_of[t] == nullptr) continue;  // absent, or a constant factor (post_lo[0])
+            void* p = nullptr;
+            ZK_TRY_CUDA(cudaMalloc(&p, table_bytes));
+            plan->allocations.push_back(p);
+            c->ntt_full_table_bytes += table_bytes;
+            const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)c->num_sms * 8);
+            ZK_LAUNCH(c, "ntt_table", ntt_expand_table_kernel, blocks, 256, 0, static_cast<fe*>(p), *lo_of[t],
+                      *hi_of[t], plan->s_bits, (uint32_t)n);
+            ZK_TRY_CUDA(cudaGetLastError());
+            *lo_of[t] = static_cast<fe*>(p);
+            *hi_of[t] = static_cast<fe*>(p);  // non-null: a table, not a constant
+        }
+        plan->s_bits = kNttFullTable;
+    }
     *out = plan;
     return ZK_OK;
 }
@@ -336,6 +379,20 @@ static int set_smem_attr(int device) {
     return ZK_OK;
 }
 
+// Columns per CTA of a radix-2^lr pass of a 2^log_n transform: fill a tile of up to
+// 2^tile_log elements, but not beyond the number of columns. ZK_NTT_TILE_LOG (5..11)
+// overrides kDefaultTileLog (read once per process).
+static uint32_t pass_log_t(uint32_t log_n, uint32_t lr) {
+    static const int tile_log = [] {
+        const char* e = std::getenv("ZK_NTT_TILE_LOG");
+        const int v = e ? std::atoi(e) : 0;
+        return (v >= 5 && v <= kTileLogElems) ? v : kDefaultTileLog;
+    }();
+    uint32_t lt = tile_log > (int)lr ? tile_log - lr : 0;
+    if (lt > log_n - lr) lt = log_n - lr;
+    return lt;
+}
+
 // One launch of one pass.
 struct PassLaunch {
     NttPassParams P;
@@ -380,9 +437,7 @@ static void make_passes(const NttPlan* plan, fe* out, const fe* in, uint32_t val
     const fe* src = in;
     for (int p = 0; p < plan->npass; p++) {
         const uint32_t lr = plan->pass_log_r[p];
-        // columns per CTA: fill the 2^11-element tile, but not beyond the number of columns
-        uint32_t lt = kTileLogElems > (int)lr ? kTileLogElems - lr : 0;
-        if (lt > log_n - lr) lt = log_n - lr;
+        const uint32_t lt = pass_log_t(log_n, lr);
         const int remaining = plan->npass - 1 - p;
         fe* dst;
         if (remaining == 0) dst = out;
@@ -817,8 +872,7 @@ static int ntt_run_noalloc(Ctx* c, int mode, fe* out, const fe* in, size_t in_le
     const fe* src = in;
     for (int p = 0; p < plan.npass; p++) {
         const uint32_t lr = plan.pass_log_r[p];
-        uint32_t lt = kTileLogElems > (int)lr ? kTileLogElems - lr : 0;
-        if (lt > log_n - lr) lt = log_n - lr;
+        const uint32_t lt = pass_log_t(log_n, lr);
         const int remaining = plan.npass - 1 - p;
         fe* dst = (remaining % 2 == 0) ? out : data;
         P.in = src;

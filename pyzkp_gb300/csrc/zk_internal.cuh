@@ -46,13 +46,17 @@ struct HostOf<CurveG2> {
         }                            \
     } while (0)
 
+// NttPlan::s_bits value of a plan whose twiddle and scale tables hold every power (one
+// load per factor) instead of the two-level lo/hi split (a load pair and a product).
+static constexpr uint32_t kNttFullTable = 31;
+
 // Device tables of one NTT configuration (transform size, root, coset shift, direction).
 struct NttPlan {
     uint32_t log_n = 0;
     int npass = 0;
     uint32_t pass_log_r[4] = {0, 0, 0, 0};
     fe* radix_tw[4] = {nullptr, nullptr, nullptr, nullptr};  // omega_R^i, i < R/2, per pass
-    uint32_t s_bits = 0;                                       // split of two-level tables
+    uint32_t s_bits = 0;  // split of two-level tables; kNttFullTable: tw/pre/post_lo are full tables
     fe* tw_lo = nullptr;                                       // omega^i, i < 2^s
     fe* tw_hi = nullptr;                                       // omega^(i 2^s), i < n / 2^s
     fe* pre_lo = nullptr;                                      // first-pass input scale (coset forward)
@@ -80,12 +84,18 @@ struct Ctx {
     cudaStream_t stream = nullptr;
     std::mutex mu;
     std::map<std::string, NttPlan*> ntt_plans;
+    size_t ntt_full_table_bytes = 0;  // device bytes held by full (one-load) NTT tables
     uint64_t launches = 0;
     bool prof_on = false;
     std::map<std::string, ProfEntry> prof;
     std::vector<ProfPending> prof_pending;
     std::vector<cudaEvent_t> event_pool;
     cudaEvent_t timer_start = nullptr, timer_stop = nullptr;
+    // zk_msm_g1_host: a second stream uploads and converts the bases while the scalars'
+    // digits are sorted; MSM pipelines wait on `bases_wait` (when set) before reading points.
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_go = nullptr, copy_done = nullptr;
+    cudaEvent_t bases_wait = nullptr;
     uint64_t msm_entries = 0;
     uint32_t msm_window_bits = 0, msm_windows = 0;
     // tuning tables (zk_tune_*, zk_autotune_*): 0 means the built-in rule

@@ -150,6 +150,46 @@ def test_ntt_2_22_oracle_and_roundtrip(gpu_ctx):
     assert (got == exp).all()
 
 
+def test_ntt_2_23_sparse_sampled_and_roundtrip(gpu_ctx):
+    """2^23: above the size whose plans keep full twiddle tables, so the two-level tables run.
+    Sparse input (16 terms): every output is a 16-term sum, checked exactly at 128 sampled
+    indices per mode; then a dense four-mode round trip."""
+    log_n = 23
+    n = 1 << log_n
+    om = O.omega_for_size(n)
+    rng = np.random.default_rng(2323)
+    pos = sorted(set(int(x) for x in rng.integers(0, n, 16)))
+    val = [int(x) for x in rng.integers(1, 1 << 62, len(pos))]
+    v = np.zeros((n, 4), dtype=np.uint64)
+    for p, x in zip(pos, val):
+        v[p, 0] = x
+    sample = [int(x) for x in rng.integers(0, n, 128)] + [0, n - 1]
+    n_inv = pow(n, R - 2, R)
+    for mode, shift in ((0, 1), (1, 1), (2, 5), (3, 5)):
+        got = gpu_ntt(gpu_ctx, mode, v, n, om, shift)
+        w = om if mode in (0, 2) else pow(om, R - 2, R)
+        for i in sample:
+            acc = sum(x * pow(w, i * p, R) for p, x in zip(pos, val))
+            if mode == 2:
+                acc = sum(x * pow(shift, p, R) * pow(w, i * p, R) for p, x in zip(pos, val))
+            if mode in (1, 3):
+                acc = acc * n_inv
+            if mode == 3:
+                acc = acc * pow(pow(shift, i, R), R - 2, R)
+            acc %= R
+            assert synth.limbs_to_ints(got[i : i + 1])[0] == acc, (mode, i)
+    dense = synth.fr_uniform(synth.seed_for(1, log_n), n)
+    d = gpu_ctx.to_device(dense)
+    gpu_ctx.fr_to_mont(d, d, n)
+    ev = gpu_ctx.alloc(n * 32)
+    gpu_ctx.ntt(N.NTT_COSET_EVALS_FROM_COEFFS, ev, d, n, log_n, om, 5)
+    gpu_ctx.ntt(N.NTT_COSET_COEFFS_FROM_EVALS, d, ev, n, log_n, om, 5)
+    gpu_ctx.ntt(N.NTT_EVALS_FROM_COEFFS, ev, d, n, log_n, om)
+    gpu_ctx.ntt(N.NTT_COEFFS_FROM_EVALS, d, ev, n, log_n, om)
+    gpu_ctx.fr_from_mont(d, d, n)
+    assert (d.download().view("<u8").reshape(n, 4) == dense).all()
+
+
 def test_ntt_coset_zero_shift_and_other_shift(gpu_ctx):
     n = 64
     v = synth.fr_uniform(99, n)
@@ -241,6 +281,38 @@ def test_msm_2_20_known_answer(gpu_ctx):
     m = 1000
     exp2 = O.affine_to_ints(O.msm_known_answer(k[7:7 + m], s[:m]))
     assert gpu_ctx.msm_g1(bases, ds, m, offset=7) == exp2
+
+
+def test_msm_g1_host_one_call(gpu_ctx):
+    """zk_msm_g1_host (points and scalars from host memory, points uploaded on a second
+    stream): same point as the oracle, from pinned and from pageable buffers, with
+    infinity points, both scalar forms, and repeated calls on one context."""
+    n = 1 << 15
+    seed = synth.seed_for(2, 15) + 11
+    k = synth.base_dlogs(seed, n)
+    k[3] = 0  # an infinity point
+    s = synth.fr_uniform(seed, n)
+    s[9] = 0
+    xy = O.g1_fixed_base_mul(O.G1_GENERATOR, k)
+    exp = O.affine_to_ints(O.msm_known_answer(k, s))
+    pin_xy = gpu_ctx.pinned(n * 64)
+    pin_xy.array[:] = xy.view(np.uint8).reshape(-1)
+    pin_s = gpu_ctx.pinned(n * 32)
+    pin_s.array[:] = s.view(np.uint8).reshape(-1)
+    for _ in range(3):
+        assert gpu_ctx.msm_g1_host(pin_xy, pin_s, n) == exp
+    assert gpu_ctx.msm_g1_host(xy, s, n) == exp  # pageable numpy buffers
+    assert gpu_ctx.msm_g1_host(xy, s, n, window_bits=9) == exp
+    # Montgomery-form scalars: to_mont on the device, read back
+    ds = gpu_ctx.to_device(s)
+    gpu_ctx.fr_to_mont(ds, ds, n)
+    s_mont = ds.download().view("<u8").reshape(n, 4)
+    assert gpu_ctx.msm_g1_host(xy, s_mont, n, scalars_mont=True) == exp
+    m = 1000  # a prefix
+    assert gpu_ctx.msm_g1_host(xy[:m], s[:m], m) == O.affine_to_ints(O.msm_known_answer(k[:m], s[:m]))
+    assert gpu_ctx.msm_g1_host(xy, s, 0) is None
+    pin_xy.free()
+    pin_s.free()
 
 
 def test_msm_empty_and_errors(gpu_ctx):
