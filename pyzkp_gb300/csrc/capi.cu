@@ -387,13 +387,15 @@ static int bases_from_dev_canonical(zk_ctx* ctx, const void* xy_dev, size_t n, z
     b->ctx = ctx;
     b->n = n;
     b->dev = nullptr;
-    int rc = zk::scratch_alloc(&ctx->impl, n * sizeof(zk::affine_t), reinterpret_cast<void**>(&b->dev));
+    int rc = zk::scratch_alloc(&ctx->impl, 2 * n * sizeof(zk::affine_t), reinterpret_cast<void**>(&b->dev));
     if (rc != ZK_OK) {
         delete b;
         return rc;
     }
-    // (x, y) canonical -> Montgomery, as 2n base-field elements; (0, 0) stays (0, 0)
+    // (x, y) canonical -> Montgomery, as 2n base-field elements; (0, 0) stays (0, 0); then
+    // the GLV images phi(P_i) behind them
     rc = zk::convert<zk::FqP, 1>(&ctx->impl, b->dev, xy_dev, 2 * n);
+    if (rc == ZK_OK) rc = zk::glv_phi(&ctx->impl, b->dev, n);
     if (rc != ZK_OK) {
         zk::scratch_free(&ctx->impl, b->dev);
         delete b;
@@ -485,7 +487,7 @@ int zk_msm_g1(zk_ctx* ctx, const zk_bases* bases, size_t offset, const void* sca
     }
     return zk::msm_run(&ctx->impl, bases->dev + offset, static_cast<const zk::fe*>(scalars_dev), n, scalars_mont,
                        window_bits, out_xy, out_is_inf, bases->shifted ? bases->shifted + offset : nullptr,
-                       bases->shifted_c, bases->n);
+                       bases->shifted_c, bases->n, /*glv=*/true);
 }
 
 int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scalars_host, size_t n, int scalars_mont,
@@ -508,7 +510,7 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
     }
     void* bases = nullptr;
     void* scalars = nullptr;
-    int rc = zk::scratch_alloc(c, n * sizeof(zk::affine_t), &bases);
+    int rc = zk::scratch_alloc(c, 2 * n * sizeof(zk::affine_t), &bases);
     if (rc != ZK_OK) return rc;
     if ((rc = zk::scratch_alloc(c, n * 32, &scalars)) != ZK_OK) {
         zk::scratch_free(c, bases);
@@ -521,8 +523,9 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(bases, xy_canonical_host, n * 64, cudaMemcpyHostToDevice, c->copy_stream);
     if (e == cudaSuccess) {
-        c->stream = c->copy_stream;  // the conversion kernel is launched on the copy stream
+        c->stream = c->copy_stream;  // the conversion and GLV kernels are launched on the copy stream
         rc = zk::convert<zk::FqP, 1>(c, bases, bases, 2 * n);
+        if (rc == ZK_OK) rc = zk::glv_phi(c, static_cast<zk::affine_t*>(bases), n);
         c->stream = main_stream;
         e = cudaEventRecord(c->copy_done, c->copy_stream);
     }
@@ -532,7 +535,7 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
     if (e == cudaSuccess && rc == ZK_OK) {
         c->bases_wait = c->copy_done;
         rc = zk::msm_run(c, static_cast<const zk::affine_t*>(bases), static_cast<const zk::fe*>(scalars), n,
-                         scalars_mont, window_bits, out_xy, out_is_inf);
+                         scalars_mont, window_bits, out_xy, out_is_inf, nullptr, 0, n, /*glv=*/true);
         c->bases_wait = nullptr;
     }
     // the frees are ordered on the main stream: after the copy stream is done with `bases`
@@ -592,6 +595,7 @@ static int make_jobs(size_t count, const zk_bases* const* bases, const uint64_t*
         } else {
             j.bases = b->dev + off;
             j.shifted = b->shifted ? b->shifted + off : nullptr;
+            j.glv = true;
         }
         j.shifted_c = b->shifted_c;
         j.stride = b->n;

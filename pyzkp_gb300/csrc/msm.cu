@@ -36,6 +36,7 @@
 #include <map>
 #include <memory>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "zk_internal.cuh"
@@ -62,6 +63,10 @@ static constexpr uint32_t kSegment = ZK_MSM_SEGMENT;  // entries per thread in t
 static constexpr uint32_t kFirstGroup = 2;            // units merged per thread in the first merge round
 static constexpr uint32_t kGroup = ZK_MSM_GROUP;      // units merged per thread in later rounds
 static constexpr uint32_t kBlockG = ZK_MSM_BLOCKG;    // buckets per block in the window reduction
+#ifndef ZK_MSM_BLOCKG2
+#define ZK_MSM_BLOCKG2 8
+#endif
+static constexpr uint32_t kBlockG2 = ZK_MSM_BLOCKG2;  // level-1 blocks per level-2 block
 
 struct MsmShape {
     uint32_t c;        // window bits
@@ -78,6 +83,8 @@ struct MsmShape {
     uint32_t Wr;       // bucket sets per instance: W, or 1 in fixed-base mode
     uint32_t inst;     // MSM instances in the pipeline
     uint32_t sets;     // bucket sets to reduce: inst * Wr
+    uint32_t glv;      // 1: each scalar is split k = k1 + k2 lambda (halves < 2^127, see glv_split);
+                       // the phi(P) half of every instance's bases sits at bases + stride
 };
 
 // One MSM of a pipeline: sum_{i < n} scalars[i] * bases[i] (fixed-base mode: bases holds the
@@ -90,14 +97,16 @@ struct MsmInst {
     uint32_t stride;
 };
 
-static MsmShape make_shape(uint32_t c) {
+static MsmShape make_shape(uint32_t c, bool glv = false) {
     MsmShape s;
     s.c = c;
-    s.W = (255 + c - 1) / c;  // W*c >= 255 so the top window never carries out (scalars < r < 2^254)
+    // W*c >= bits + 1 so that the top window never carries out: scalars < r < 2^254, or GLV
+    // halves < 2^127
+    s.W = ((glv ? 128u : 255u) + c - 1) / c;
     s.B = 1u << (c - 1);
     s.g = std::min<uint32_t>(kBlockG, s.B);
     s.G = s.B / s.g;
-    s.g2 = s.G >= 16 ? kBlockG : 1;
+    s.g2 = s.G >= 2 * kBlockG2 ? kBlockG2 : 1;
     s.G2 = s.G / s.g2;
     s.K = 0;
     while ((1u << s.K) < s.G2) s.K++;
@@ -107,6 +116,7 @@ static MsmShape make_shape(uint32_t c) {
     s.Wr = s.W;
     s.inst = 1;
     s.sets = s.W;
+    s.glv = glv ? 1u : 0u;
     return s;
 }
 
@@ -117,6 +127,143 @@ uint32_t msm_auto_window(size_t n) {
     if (c < 4) c = 4;
     if (c > 16) c = 16;
     return (uint32_t)c;
+}
+
+// GLV: the same rule over n scalars (2n half-scalars of 128 bits), lowered while the window
+// count stays the same (fewer buckets for the same entries: c = 14 -> 13, 12 stays).
+uint32_t msm_auto_window_glv(size_t n) {
+    uint32_t c = msm_auto_window(n);
+    while (c > 4 && (128 + c - 2) / (c - 1) == (128 + c - 1) / c) c--;
+    return c;
+}
+
+// ---- GLV scalar split -------------------------------------------------------------
+// BN254 G1 has the endomorphism phi(x, y) = (beta x, y) = [lambda](x, y), with beta a cube
+// root of unity in Fq and lambda one in Fr. The lattice {(a, b) : a + b lambda = 0 mod r} has
+// the reduced basis v1 = (a1, -b1), v2 = (a2, b2) (extended Euclid on (r, lambda), stopped
+// at the first remainder below sqrt(r); a1 b2 + a2 b1 = r). Babai rounding:
+//   c1 = round(k b2 / r), c2 = round(k b1 / r),  computed as (k g + 2^255) >> 256 with
+//   g = round(2^256 b / r);  k1 = k - c1 a1 - c2 a2,  k2 = c1 b1 - c2 b2,
+// so k1 + k2 lambda = k (mod r) and |k1|, |k2| <= (1/2 + 2^-3.4)(a1 + a2) < 2^126.1.
+// Constants as 32-bit limbs, least significant first.
+__device__ __constant__ uint32_t kGlvG1[3] = {0xc7e0b3d7u, 0xd91d232eu, 0x00000002u};  // round(2^256 b2 / r)
+__device__ __constant__ uint32_t kGlvG2[5] = {0x391eb18eu, 0x7a7bd9d4u, 0xa773d2cfu, 0x4ccef014u,
+                                              0x00000002u};                      // round(2^256 b1 / r)
+__device__ __constant__ uint32_t kGlvA1[2] = {0x94d213e3u, 0x89d32568u};         // a1 = b2
+__device__ __constant__ uint32_t kGlvA2[4] = {0x1221250bu, 0x0be4e154u, 0xeeb859fdu, 0x6f4d8248u};
+__device__ __constant__ uint32_t kGlvB1[4] = {0x7d4f1128u, 0x8211bbebu, 0xeeb859fcu, 0x6f4d8248u};
+
+// (k * g + 2^255) >> 256 for k < 2^256 (8 limbs) and g of NG limbs: NG limbs.
+template <int NG>
+__device__ __forceinline__ void glv_round(const fe& k, const uint32_t* g, uint32_t* c) {
+    uint32_t p[8 + NG];
+#pragma unroll
+    for (int i = 0; i < 8 + NG; i++) p[i] = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        uint64_t carry = 0;
+#pragma unroll
+        for (int j = 0; j < NG; j++) {
+            const uint64_t t = (uint64_t)k.v[i] * g[j] + p[i + j] + carry;
+            p[i + j] = (uint32_t)t;
+            carry = t >> 32;
+        }
+        p[i + NG] = (uint32_t)carry;
+    }
+    uint64_t t = (uint64_t)p[7] + 0x80000000u;
+#pragma unroll
+    for (int i = 8; i < 8 + NG; i++) {
+        t = (t >> 32) + p[i];
+        c[i - 8] = (uint32_t)t;
+    }
+}
+
+// acc -= a * b (mod 2^256) for a of NA limbs and b of NB limbs (sub = false: acc += a * b).
+template <int NA, int NB, bool SUB>
+__device__ __forceinline__ void glv_mac(uint32_t* acc, const uint32_t* a, const uint32_t* b) {
+    uint32_t p[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) p[i] = 0;
+#pragma unroll
+    for (int i = 0; i < NA; i++) {
+        uint64_t carry = 0;
+#pragma unroll
+        for (int j = 0; j < NB; j++) {
+            if (i + j < 8) {
+                const uint64_t t = (uint64_t)a[i] * b[j] + p[i + j] + carry;
+                p[i + j] = (uint32_t)t;
+                carry = t >> 32;
+            }
+        }
+        if (i + NB < 8) p[i + NB] = (uint32_t)carry;
+    }
+    uint64_t t = SUB ? 1 : 0;  // acc + ~p + 1 = acc - p
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        t += (uint64_t)acc[i] + (SUB ? (uint32_t)~p[i] : p[i]);
+        acc[i] = (uint32_t)t;
+        t >>= 32;
+    }
+}
+
+// |x| of a two's-complement 256-bit value with the sign in bit 255 of the result.
+__device__ __forceinline__ fe glv_sign_mag(const uint32_t* x) {
+    fe r;
+    const uint32_t neg = x[7] >> 31;
+    uint64_t t = neg;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        t += (uint64_t)(neg ? ~x[i] : x[i]);
+        r.v[i] = (uint32_t)t;
+        t >>= 32;
+    }
+    r.v[7] |= neg << 31;  // |x| < 2^127: bit 255 is free
+    return r;
+}
+
+// k (canonical, < r) -> (|k1| | s1 << 255, |k2| | s2 << 255) with k = k1 + k2 lambda (mod r).
+__device__ __forceinline__ void glv_split(const fe& k, fe& h0, fe& h1) {
+    uint32_t c1[3], c2[5];
+    glv_round<3>(k, kGlvG1, c1);
+    glv_round<5>(k, kGlvG2, c2);
+    uint32_t k1[8], k2[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        k1[i] = k.v[i];
+        k2[i] = 0;
+    }
+    glv_mac<3, 2, true>(k1, c1, kGlvA1);
+    glv_mac<5, 4, true>(k1, c2, kGlvA2);
+    glv_mac<3, 4, false>(k2, c1, kGlvB1);
+    glv_mac<5, 2, true>(k2, c2, kGlvA1);  // b2 = a1
+    h0 = glv_sign_mag(k1);
+    h1 = glv_sign_mag(k2);
+}
+
+// pts[n + i] = phi(pts[i]) = (beta x_i, y_i); infinity (0, 0) stays (0, 0).
+__global__ void glv_phi_kernel(affine_t* __restrict__ pts, size_t n, fe beta) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const affine_t p = affine_load(pts + i);
+        fe_store(&pts[n + i].x, fe_reduce_once<FqP>(fe_mul<FqP>(p.x, beta)));  // bases stay in [0, q)
+        fe_store(&pts[n + i].y, p.y);
+    }
+}
+
+int glv_phi(Ctx* c, affine_t* pts, size_t n) {
+    if (n == 0) return ZK_OK;
+    // beta = 0x59e26bcea0d48bacd4f263f1acdb5c4f5763473177fffffe, the cube root of unity in Fq
+    // with (beta x, y) = [lambda](x, y) for lambda = 0xb3c4d79d41a917585bfc41088d8daaa78b17ea66b99c90dd
+    static const fe beta_m = [] {
+        const zkh::F4 canon = {{0x5763473177fffffeull, 0xd4f263f1acdb5c4full, 0x59e26bcea0d48bacull, 0}};
+        const zkh::F4 m = zkh::to_mont(zkh::fq(), canon);
+        fe r;
+        std::memcpy(r.v, m.v, 32);
+        return r;
+    }();
+    const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)c->num_sms * 16);
+    ZK_LAUNCH(c, "glv_phi", glv_phi_kernel, blocks, 256, 0, pts, n, beta_m);
+    ZK_TRY_CUDA(cudaGetLastError());
+    return ZK_OK;
 }
 
 // ---- 1. digits + histogram ----------------------------------------------------
@@ -178,7 +325,25 @@ __global__ void msm_digits_kernel(const MsmInst* __restrict__ insts, const uint3
         s = scalars_mont ? fe_from_mont<FrP>(s) : fe_from_mont<FrP>(fe_to_mont<FrP>(s));
         if (affine_is_inf(affine_load(static_cast<const typename C::A*>(insts[k].bases) + i))) s = fe_zero();
         set0 = k * sh.Wr;
-        fe_store(reduced + j, s);
+        if (!sh.glv) fe_store(reduced + j, s);
+    }
+    if (sh.glv) {  // two half-scalars, both counted in the same window sets
+        fe h[2];
+        glv_split(s, h[0], h[1]);
+        if (valid) {
+            fe_store(reduced + 2 * (size_t)j, h[0]);
+            fe_store(reduced + 2 * (size_t)j + 1, h[1]);
+        }
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) {
+            h[hh].v[7] &= 0x7fffffffu;  // drop the sign flag
+            uint32_t carry = 0;
+            for (uint32_t w = 0; w < sh.W; w++) {
+                const uint32_t mag = signed_digit(h[hh], w, sh, carry) & 0x7fffffffu;
+                warp_aggregated_inc(counts, (set0 + w) * sh.B + (mag - 1), valid && mag != 0);
+            }
+        }
+        return;
     }
     uint32_t carry = 0;
     for (uint32_t w = 0; w < sh.W; w++) {
@@ -203,24 +368,32 @@ __global__ void msm_scatter_kernel(const fe* __restrict__ reduced, const MsmInst
         i = j - __ldg(offs + k);
         set0 = k * sh.Wr;
         stride = insts[k].stride;
-        s = fe_load(reduced + j);
     }
-    uint32_t carry = 0;
-    for (uint32_t w = 0; w < sh.W; w++) {
-        const uint32_t d = signed_digit(s, w, sh, carry);
-        const bool nz = valid && d != 0;
-        const uint32_t key = (set0 + (sh.shared ? 0u : w)) * sh.B + (d & 0x7fffffffu) - 1;
-        const uint32_t point = sh.shared ? w * stride + i : i;  // fixed-base: row w of the shifted bases
-        const uint32_t live = __ballot_sync(0xffffffffu, nz);
-        if (nz) {
-            const uint32_t peers = __match_any_sync(live, key);
-            const int lane = threadIdx.x & 31;
-            const int leader = __ffs(peers) - 1;
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(cursor + key, (uint32_t)__popc(peers));
-            base = __shfl_sync(peers, base, leader);
-            const uint32_t rank = __popc(peers & ((1u << lane) - 1));
-            entries[base + rank] = point | (d & 0x80000000u);
+    // GLV: half h of scalar j is reduced[2j + h] (sign flag in bit 255) on point i + h * stride
+    const uint32_t halves = sh.glv ? 2u : 1u;
+    for (uint32_t h = 0; h < halves; h++) {
+        fe s = fe_zero();
+        if (valid) s = fe_load(reduced + (size_t)j * halves + h);
+        const uint32_t flip = s.v[7] & 0x80000000u;  // zero unless a negative GLV half
+        s.v[7] &= 0x7fffffffu;
+        uint32_t carry = 0;
+        for (uint32_t w = 0; w < sh.W; w++) {
+            const uint32_t d = signed_digit(s, w, sh, carry);
+            const bool nz = valid && d != 0;
+            const uint32_t key = (set0 + (sh.shared ? 0u : w)) * sh.B + (d & 0x7fffffffu) - 1;
+            // fixed-base: row w of the shifted bases; GLV: the phi(P) half for h = 1
+            const uint32_t point = sh.shared ? w * stride + i : i + h * stride;
+            const uint32_t live = __ballot_sync(0xffffffffu, nz);
+            if (nz) {
+                const uint32_t peers = __match_any_sync(live, key);
+                const int lane = threadIdx.x & 31;
+                const int leader = __ffs(peers) - 1;
+                uint32_t base = 0;
+                if (lane == leader) base = atomicAdd(cursor + key, (uint32_t)__popc(peers));
+                base = __shfl_sync(peers, base, leader);
+                const uint32_t rank = __popc(peers & ((1u << lane) - 1));
+                entries[base + rank] = point | ((d & 0x80000000u) ^ flip);
+            }
         }
     }
 }
@@ -346,7 +519,10 @@ __global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restri
 // began before the segment). One thread per bucket adds up to kFixupMax + 1 pieces; longer
 // buckets are listed for msm_fixup_long_kernel, one CTA each.
 static constexpr uint32_t kFixupMax = 8;
-static constexpr uint64_t kFixupDensity = 48;  // CSR entries per bucket up to which the fixup is used
+#ifndef ZK_FIXUP_DENSITY
+#define ZK_FIXUP_DENSITY 48
+#endif
+static constexpr uint64_t kFixupDensity = ZK_FIXUP_DENSITY;  // CSR entries per bucket up to which the fixup is used
 static constexpr int kFixupLongThreads = 128;
 
 template <class C>
@@ -581,11 +757,11 @@ static zkh::XyzzT<H> host_dbl_n(zkh::XyzzT<H> p, uint32_t times) {
     return p;
 }
 
-uint32_t msm_window_for(const Ctx* c, size_t n) {
+uint32_t msm_window_for(const Ctx* c, size_t n, bool glv) {
     uint32_t lg = 0;
     while ((1ull << lg) < n) lg++;
     if (lg < sizeof(c->tune_msm_window) && c->tune_msm_window[lg] != 0) return c->tune_msm_window[lg];
-    return msm_auto_window(n);
+    return glv ? msm_auto_window_glv(n) : msm_auto_window(n);
 }
 
 // One pipeline: MSM instances with the same window size and mode, sharing every launch.
@@ -616,9 +792,9 @@ struct MsmPipeT {
 
 // Shape and limits of a pipeline over `jobs` (all with window c, fixed-base mode or not).
 template <class C>
-static int pipe_init(MsmPipeT<C>& p, uint32_t c, bool fixed, const std::vector<MsmInst>& jobs,
+static int pipe_init(MsmPipeT<C>& p, uint32_t c, bool fixed, bool glv, const std::vector<MsmInst>& jobs,
                      const std::vector<size_t>& out_index) {
-    p.sh = make_shape(c);
+    p.sh = make_shape(c, glv);
     if (fixed) {
         p.sh.shared = 1;
         p.sh.Wr = 1;
@@ -634,11 +810,13 @@ static int pipe_init(MsmPipeT<C>& p, uint32_t c, bool fixed, const std::vector<M
         N += jobs[k].n;
         if (fixed) ZK_CHECK_ARG((uint64_t)p.sh.W * jobs[k].stride < (1ull << 31),
                                 "fixed-base rows exceed 31-bit entry indices");
+        if (glv) ZK_CHECK_ARG((uint64_t)jobs[k].stride + jobs[k].n < (1ull << 31),
+                              "GLV bases exceed 31-bit entry indices");
     }
     ZK_CHECK_ARG(N < (1ull << 31), "MSM batch too large: total points must be below 2^31");
     p.offs[jobs.size()] = (uint32_t)N;
     p.N = N;
-    p.max_entries = N * p.sh.W;
+    p.max_entries = N * p.sh.W * (glv ? 2 : 1);
     ZK_CHECK_ARG(p.max_entries < (1ull << 32) - kSegment, "MSM too large for 32-bit CSR offsets");
     p.nbuckets = (uint64_t)p.sh.sets * p.sh.B;
     ZK_CHECK_ARG(p.nbuckets < (1ull << 32) - 1, "MSM batch has too many buckets for 32-bit keys");
@@ -662,7 +840,8 @@ static size_t pipe_layout(MsmPipeT<C>& p, char* base) {
     const size_t first_out = (p.units + kFirstGroup - 1) / kFirstGroup;
     p.d_inst = reinterpret_cast<MsmInst*>(take(p.inst.size() * sizeof(MsmInst)));
     p.d_offs = reinterpret_cast<uint32_t*>(take(p.offs.size() * 4));
-    p.digits = reinterpret_cast<uint32_t*>(take(std::max<uint64_t>(p.max_entries * 4, p.N * sizeof(fe))));
+    p.digits = reinterpret_cast<uint32_t*>(
+        take(std::max<uint64_t>(p.max_entries * 4, p.N * sizeof(fe) * (sh.glv ? 2 : 1))));
     p.row_ptr = reinterpret_cast<uint32_t*>(take((p.nbuckets + 1) * 4));
     p.cursor = reinterpret_cast<uint32_t*>(take(p.nbuckets * 4));
     p.entries = reinterpret_cast<uint32_t*>(take(p.max_entries * 4));
@@ -921,13 +1100,13 @@ static void combine_all(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, uint8_t* 
     }
 }
 
-// Group jobs into pipelines: one per (window bits, fixed-base mode), split where a group
-// would exceed the 31-bit point / 32-bit entry limits.
+// Group jobs into pipelines: one per (window bits, fixed-base mode, GLV), split where a
+// group would exceed the 31-bit point / 32-bit entry limits.
 template <class C>
 static int build_pipes(Ctx* c, const MsmJob* jobs, size_t count, uint32_t window_bits,
                        std::vector<MsmPipeT<C>>* out, std::vector<size_t>* empty) {
     ZK_CHECK_ARG(window_bits == 0 || (window_bits >= 4 && window_bits <= 20), "window_bits must be 0 or 4..20");
-    std::map<std::pair<uint32_t, bool>, std::vector<size_t>> groups;
+    std::map<std::tuple<uint32_t, bool, bool>, std::vector<size_t>> groups;
     for (size_t j = 0; j < count; j++) {
         const MsmJob& b = jobs[j];
         ZK_CHECK_ARG(b.n < (1ull << 31), "MSM size must be below 2^31 points");
@@ -936,20 +1115,22 @@ static int build_pipes(Ctx* c, const MsmJob* jobs, size_t count, uint32_t window
             continue;
         }
         const bool fixed = b.shifted != nullptr && (window_bits == 0 || window_bits == b.shifted_c);
-        const uint32_t cb = fixed ? b.shifted_c : (window_bits ? window_bits : msm_window_for(c, b.n));
-        groups[{cb, fixed}].push_back(j);
+        const bool glv = !fixed && b.glv;
+        const uint32_t cb = fixed ? b.shifted_c : (window_bits ? window_bits : msm_window_for(c, b.n, glv));
+        groups[std::make_tuple(cb, fixed, glv)].push_back(j);
     }
     for (auto& kv : groups) {
-        const uint32_t cb = kv.first.first;
-        const bool fixed = kv.first.second;
-        const uint64_t W = make_shape(cb).W;
+        const uint32_t cb = std::get<0>(kv.first);
+        const bool fixed = std::get<1>(kv.first);
+        const bool glv = std::get<2>(kv.first);
+        const uint64_t W = make_shape(cb, glv).W * (glv ? 2 : 1);  // entries per scalar
         std::vector<MsmInst> part;
         std::vector<size_t> idx;
         uint64_t N = 0;
         auto flush = [&]() -> int {
             if (part.empty()) return ZK_OK;
             out->emplace_back();
-            int rc = pipe_init<C>(out->back(), cb, fixed, part, idx);
+            int rc = pipe_init<C>(out->back(), cb, fixed, glv, part, idx);
             part.clear();
             idx.clear();
             N = 0;
@@ -965,7 +1146,7 @@ static int build_pipes(Ctx* c, const MsmJob* jobs, size_t count, uint32_t window
             mi.scalars = b.scalars;
             mi.bases = fixed ? b.shifted : b.bases;
             mi.n = (uint32_t)b.n;
-            mi.stride = fixed ? (uint32_t)b.stride : 0u;
+            mi.stride = (fixed || glv) ? (uint32_t)b.stride : 0u;
             part.push_back(mi);
             idx.push_back(j);
             N += b.n;
@@ -1034,7 +1215,8 @@ int msm_g2_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont,
 }
 
 int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
-            uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted, uint32_t shifted_c, uint64_t stride) {
+            uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted, uint32_t shifted_c, uint64_t stride,
+            bool glv) {
     MsmJob job;
     job.scalars = scalars;
     job.n = n;
@@ -1042,6 +1224,7 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
     job.shifted = shifted;
     job.shifted_c = shifted_c;
     job.stride = stride;
+    job.glv = glv;
     int32_t inf = 0;
     int rc = msm_batch_run(c, &job, 1, scalars_mont, window_bits, out_xy, &inf);
     *out_is_inf = inf;

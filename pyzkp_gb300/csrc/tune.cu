@@ -200,7 +200,7 @@ static int time_msm(Ctx* c, const zk_bases* b, const fe* scalars, size_t n, uint
     double best = 1e30;
     for (int r = 0; r < reps + 1; r++) {
         const auto t0 = std::chrono::steady_clock::now();
-        int rc = msm_run(c, b->dev, scalars, n, 1, cbits, xy, &inf);
+        int rc = msm_run(c, b->dev, scalars, n, 1, cbits, xy, &inf, nullptr, 0, b->n, /*glv=*/true);
         if (rc != ZK_OK) return rc;
         const double t = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         if (r > 0 && t < best) best = t;  // the first call warms the pool and caches
@@ -276,7 +276,7 @@ int zk_tune_get_msm_window(zk_ctx* ctx, uint64_t n, uint32_t* window_bits) {
         zk::set_error("null pointer");
         return ZK_EINVAL;
     }
-    *window_bits = zk::msm_window_for(&ctx->impl, n);
+    *window_bits = zk::msm_window_for(&ctx->impl, n, /*glv=*/true);  // the window of a G1 MSM
     return ZK_OK;
 }
 
@@ -351,7 +351,7 @@ int zk_autotune_msm(zk_ctx* ctx, const zk_bases* bases, const void* scalars_dev,
         return ZK_EINVAL;
     }
     const size_t n = (size_t)1 << log_n;
-    const uint32_t rule = zk::msm_auto_window(n);
+    const uint32_t rule = zk::msm_auto_window_glv(n);
     uint32_t best_c = rule;
     double best = 1e30;
     for (int d = -2; d <= 2; d++) {

@@ -127,7 +127,9 @@ int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log
             const uint8_t shift[32]);
 int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
             uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted = nullptr, uint32_t shifted_c = 0,
-            uint64_t stride = 0);
+            uint64_t stride = 0, bool glv = false);
+// G1 bases with the GLV half: pts[n + i] = phi(pts[i]) = (beta x_i, y_i) for i < n.
+int glv_phi(Ctx* c, affine_t* pts, size_t n);
 
 // One MSM of a batch: sum_{i < n} scalars[i] * bases[i]; `shifted` (optional) holds the
 // window-shifted rows [2^(c j)] bases[i] with row stride `stride` for fixed-base mode.
@@ -137,11 +139,13 @@ struct MsmJob {
     const void* bases = nullptr;  // affine_t (G1) or affine2_t (G2) points
     const affine_t* shifted = nullptr;
     uint32_t shifted_c = 0;
-    uint64_t stride = 0;
+    uint64_t stride = 0;  // points in the base set: row stride of `shifted`, offset of the GLV half
+    bool glv = false;     // G1 bases whose phi(P) half sits at bases + stride (GLV split scalars)
 };
 struct MsmPlan;
 uint32_t msm_auto_window(size_t n);
-uint32_t msm_window_for(const Ctx* c, size_t n);
+uint32_t msm_auto_window_glv(size_t n);
+uint32_t msm_window_for(const Ctx* c, size_t n, bool glv = false);
 int msm_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, uint8_t* out_xy,
                   int32_t* out_is_inf);
 // G2: out_xy holds 128 bytes per instance (x.c0, x.c1, y.c0, y.c1); no fixed-base mode
@@ -180,7 +184,9 @@ struct zk_ctx {
 
 struct zk_bases {
     zk_ctx* ctx;
-    zk::affine_t* dev;  // G1: Montgomery affine, (0, 0) = infinity (null for G2 bases)
+    // G1: 2n Montgomery affine points, (0, 0) = infinity: P_0..P_{n-1}, then their GLV images
+    // phi(P_i) = (beta x_i, y_i) (null for G2 bases)
+    zk::affine_t* dev;
     size_t n;
     zk::affine2_t* dev2 = nullptr;  // G2: Montgomery affine over Fq2 (null for G1 bases)
     zk::affine_t* shifted = nullptr;  // fixed-base rows [2^(c j)] P_i, j < shifted_windows, row stride n

@@ -315,6 +315,31 @@ def test_msm_g1_host_one_call(gpu_ctx):
     pin_s.free()
 
 
+def test_msm_glv_edge_scalars(gpu_ctx):
+    """G1 MSMs split every scalar k = k1 + k2 lambda (GLV): scalars at the ends of the range,
+    lambda itself, its negation and rounding midpoints, on random bases, for every window
+    size the split changes the window count of (W = ceil(128 / c))."""
+    lam = 0xB3C4D79D41A917585BFC41088D8DAAA78B17EA66B99C90DD
+    vals = [0, 1, 2, 3, R - 1, R - 2, lam, R - lam, lam + 1, (R - 1) // 2, (R + 1) // 2, R // 3, (2 * R) // 3,
+            (1 << 127) - 1, 1 << 127, (1 << 253) - 1]
+    vals += [int(x) for x in synth.limbs_to_ints(synth.fr_uniform(4242, 48))]
+    n = len(vals)
+    s = synth.ints_to_limbs(vals)
+    k = synth.base_dlogs(31, n)
+    k[5] = 0  # an infinity base
+    bases = O.g1_fixed_base_mul(O.G1_GENERATOR, k)
+    exp = O.affine_to_ints(O.msm_known_answer(k, s))
+    for c in (0, 4, 5, 7, 8, 11, 13, 16, 20):
+        assert gpu_msm(gpu_ctx, bases, s, window_bits=c) == exp, c
+    st = gpu_ctx.msm_last_stats()
+    assert st["window_bits"] == 20 and st["windows"] == (128 + 19) // 20
+    # one scalar at a time (each half alone in its buckets)
+    for v in vals[:16]:
+        one = synth.ints_to_limbs([v])
+        got = gpu_msm(gpu_ctx, bases[:1], one)
+        assert got == O.affine_to_ints(O.msm_known_answer(k[:1], one)), hex(v)
+
+
 def test_msm_empty_and_errors(gpu_ctx):
     bases = gpu_ctx.bases_from_host(O.g1_fixed_base_mul(O.G1_GENERATOR, synth.base_dlogs(1, 4)))
     ds = gpu_ctx.to_device(synth.fr_uniform(1, 4))
