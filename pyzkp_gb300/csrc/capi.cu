@@ -592,6 +592,7 @@ static int make_jobs(size_t count, const zk_bases* const* bases, const uint64_t*
         j.n = sizes[k];
         if (g2) {
             j.bases = b->dev2 + off;
+            j.glv = true;
         } else {
             j.bases = b->dev + off;
             j.shifted = b->shifted ? b->shifted + off : nullptr;
@@ -690,7 +691,7 @@ static int bases_g2_create(zk_ctx* ctx, const void* xy_canonical, size_t n, cuda
     b->ctx = ctx;
     b->n = n;
     b->dev = nullptr;
-    int rc = zk::scratch_alloc(&ctx->impl, n * sizeof(zk::affine2_t), reinterpret_cast<void**>(&b->dev2));
+    int rc = zk::scratch_alloc(&ctx->impl, 2 * n * sizeof(zk::affine2_t), reinterpret_cast<void**>(&b->dev2));
     if (rc != ZK_OK) {
         delete b;
         return rc;
@@ -698,8 +699,10 @@ static int bases_g2_create(zk_ctx* ctx, const void* xy_canonical, size_t n, cuda
     if (n) {
         cudaError_t e = cudaMemcpyAsync(b->dev2, xy_canonical, n * sizeof(zk::affine2_t), kind, ctx->impl.stream);
         // (x.c0, x.c1, y.c0, y.c1) canonical -> Montgomery, as 4n base-field elements in place
-        if (e == cudaSuccess) rc = zk::convert<zk::FqP, 1>(&ctx->impl, b->dev2, b->dev2, 4 * n);
-        else {
+        if (e == cudaSuccess) {
+            rc = zk::convert<zk::FqP, 1>(&ctx->impl, b->dev2, b->dev2, 4 * n);
+            if (rc == ZK_OK) rc = zk::glv_phi2(&ctx->impl, b->dev2, n);  // the GLV images behind them
+        } else {
             zk::set_error(std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
             rc = ZK_ECUDA;
         }

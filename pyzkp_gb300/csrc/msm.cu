@@ -64,7 +64,9 @@ static constexpr uint32_t kFirstGroup = 2;            // units merged per thread
 static constexpr uint32_t kGroup = ZK_MSM_GROUP;      // units merged per thread in later rounds
 static constexpr uint32_t kBlockG = ZK_MSM_BLOCKG;    // buckets per block in the window reduction
 #ifndef ZK_MSM_BLOCKG2
-#define ZK_MSM_BLOCKG2 8
+// measured at 2^20 (GLV, 8 windows): level-2 pass 0.154 ms with 8, 0.068 ms with 4 (its
+// threads are few and each runs a chain of g2 additions); the targets grow 0.078 -> 0.102 ms
+#define ZK_MSM_BLOCKG2 4
 #endif
 static constexpr uint32_t kBlockG2 = ZK_MSM_BLOCKG2;  // level-1 blocks per level-2 block
 
@@ -249,17 +251,42 @@ __global__ void glv_phi_kernel(affine_t* __restrict__ pts, size_t n, fe beta) {
     }
 }
 
+// G2: pts[n + i] = (beta^2 x_i, y_i) = [lambda] P_i (on the twist the same lambda goes with beta^2;
+// beta^2 multiplies both Fq coordinates of x in Fq2).
+__global__ void glv_phi2_kernel(affine2_t* __restrict__ pts, size_t n, fe beta2) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const affine2_t p = affine_load(pts + i);
+        fe_store(&pts[n + i].x.c0, fe_reduce_once<FqP>(fe_mul<FqP>(p.x.c0, beta2)));
+        fe_store(&pts[n + i].x.c1, fe_reduce_once<FqP>(fe_mul<FqP>(p.x.c1, beta2)));
+        fe_store(&pts[n + i].y.c0, p.y.c0);
+        fe_store(&pts[n + i].y.c1, p.y.c1);
+    }
+}
+
+// beta = 0x59e26bcea0d48bacd4f263f1acdb5c4f5763473177fffffe, the cube root of unity in Fq
+// with (beta x, y) = [lambda](x, y) on G1 for lambda = 0xb3c4d79d41a917585bfc41088d8daaa78b17ea66b99c90dd
+// (Montgomery form; squared for G2).
+static fe glv_beta_mont(bool squared) {
+    const zkh::F4 canon = {{0x5763473177fffffeull, 0xd4f263f1acdb5c4full, 0x59e26bcea0d48bacull, 0}};
+    zkh::F4 m = zkh::to_mont(zkh::fq(), canon);
+    if (squared) m = zkh::mul(zkh::fq(), m, m);
+    fe r;
+    std::memcpy(r.v, m.v, 32);
+    return r;
+}
+
+int glv_phi2(Ctx* c, affine2_t* pts, size_t n) {
+    if (n == 0) return ZK_OK;
+    static const fe beta2_m = glv_beta_mont(true);
+    const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)c->num_sms * 16);
+    ZK_LAUNCH(c, "glv_phi2", glv_phi2_kernel, blocks, 256, 0, pts, n, beta2_m);
+    ZK_TRY_CUDA(cudaGetLastError());
+    return ZK_OK;
+}
+
 int glv_phi(Ctx* c, affine_t* pts, size_t n) {
     if (n == 0) return ZK_OK;
-    // beta = 0x59e26bcea0d48bacd4f263f1acdb5c4f5763473177fffffe, the cube root of unity in Fq
-    // with (beta x, y) = [lambda](x, y) for lambda = 0xb3c4d79d41a917585bfc41088d8daaa78b17ea66b99c90dd
-    static const fe beta_m = [] {
-        const zkh::F4 canon = {{0x5763473177fffffeull, 0xd4f263f1acdb5c4full, 0x59e26bcea0d48bacull, 0}};
-        const zkh::F4 m = zkh::to_mont(zkh::fq(), canon);
-        fe r;
-        std::memcpy(r.v, m.v, 32);
-        return r;
-    }();
+    static const fe beta_m = glv_beta_mont(false);
     const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)c->num_sms * 16);
     ZK_LAUNCH(c, "glv_phi", glv_phi_kernel, blocks, 256, 0, pts, n, beta_m);
     ZK_TRY_CUDA(cudaGetLastError());
@@ -520,7 +547,9 @@ __global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restri
 // buckets are listed for msm_fixup_long_kernel, one CTA each.
 static constexpr uint32_t kFixupMax = 8;
 #ifndef ZK_FIXUP_DENSITY
-#define ZK_FIXUP_DENSITY 48
+// measured on GB300: 2^20 plain (32 entries per bucket) fixup 0.32 vs rounds 0.48 ms; 2^20 GLV
+// (64) fixup 0.27 vs rounds 0.48 ms; 2^22 GLV (256) rounds 1.0 vs fixup 6.8 ms
+#define ZK_FIXUP_DENSITY 96
 #endif
 static constexpr uint64_t kFixupDensity = ZK_FIXUP_DENSITY;  // CSR entries per bucket up to which the fixup is used
 static constexpr int kFixupLongThreads = 128;
@@ -896,9 +925,8 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
     ZK_LAUNCH(c, "msm_accumulate", msm_accumulate_kernel<C>, (p.units + 127) / 128, 128, 0, p.entries, d_total,
               p.row_ptr, p.d_inst, sh, p.units, p.buckets, p.slot_keys_a, p.slot_pts_a);
     ZK_TRY_CUDA(cudaGetLastError());
-    // Partial sums of straddling buckets: short buckets (at most ~1.5 segments on average)
-    // by one fixup pass, longer ones by merge rounds (measured at 2^20 / 2^22: fixup 0.33 vs
-    // rounds 0.48 ms; rounds 1.0 vs fixup 2.1 ms, when most buckets span 4+ segments).
+    // Partial sums of straddling buckets: short buckets (up to ~3 segments on average) by one
+    // fixup pass, longer ones by merge rounds (kFixupDensity).
     if (p.max_entries <= (uint64_t)p.nbuckets * kFixupDensity) {
         ZK_TRY_CUDA(cudaMemsetAsync(p.long_count, 0, 4, st));
         ZK_LAUNCH(c, "msm_fixup", msm_fixup_kernel<C>, (unsigned)((p.nbuckets + 127) / 128), 128, 0, p.row_ptr,

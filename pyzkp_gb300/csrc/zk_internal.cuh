@@ -130,6 +130,8 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
             uint64_t stride = 0, bool glv = false);
 // G1 bases with the GLV half: pts[n + i] = phi(pts[i]) = (beta x_i, y_i) for i < n.
 int glv_phi(Ctx* c, affine_t* pts, size_t n);
+// G2 bases with the GLV half: pts[n + i] = (beta^2 x_i, y_i) = [lambda] P_i.
+int glv_phi2(Ctx* c, affine2_t* pts, size_t n);
 
 // One MSM of a batch: sum_{i < n} scalars[i] * bases[i]; `shifted` (optional) holds the
 // window-shifted rows [2^(c j)] bases[i] with row stride `stride` for fixed-base mode.
@@ -188,7 +190,8 @@ struct zk_bases {
     // phi(P_i) = (beta x_i, y_i) (null for G2 bases)
     zk::affine_t* dev;
     size_t n;
-    zk::affine2_t* dev2 = nullptr;  // G2: Montgomery affine over Fq2 (null for G1 bases)
+    zk::affine2_t* dev2 = nullptr;  // G2: 2n Montgomery affine points over Fq2, then their GLV images
+                                    // (beta^2 x, y) (null for G1 bases)
     zk::affine_t* shifted = nullptr;  // fixed-base rows [2^(c j)] P_i, j < shifted_windows, row stride n
     uint32_t shifted_c = 0;
     uint32_t shifted_windows = 0;

@@ -83,3 +83,26 @@ def test_g2_fixed_base_mul_matches_oracle(gpu_ctx):
     gpu_ctx.g2_fixed_base_mul(gen, dk, n, out)
     got = out.download().view("<u8").reshape(n, 16)
     assert (got == O.g2_fixed_base_mul(O.G2_GENERATOR, k)).all()
+
+
+def test_msm_g2_glv_edge_scalars(gpu_ctx):
+    """G2 MSMs use the GLV split with phi(x, y) = (beta^2 x, y) = [lambda](x, y) on the twist:
+    scalars at the ends of the range, lambda, its negation and rounding midpoints."""
+    R = O.FR_MODULUS
+    lam = 0xB3C4D79D41A917585BFC41088D8DAAA78B17EA66B99C90DD
+    vals = [0, 1, 2, R - 1, R - 2, lam, R - lam, lam + 1, (R - 1) // 2, (R + 1) // 2, R // 3, (2 * R) // 3,
+            (1 << 127) - 1, 1 << 127, (1 << 253) - 1]
+    vals += [int(x) for x in synth.limbs_to_ints(synth.fr_uniform(4343, 17))]
+    n = len(vals)
+    s = synth.ints_to_limbs(vals)
+    k = synth.base_dlogs(4344, n)
+    k[3] = 0  # an infinity base
+    xy = O.g2_fixed_base_mul(O.G2_GENERATOR, k)
+    exp = _g2(O.g2_msm_known_answer(k, s))
+    b = gpu_ctx.bases_g2_from_host(xy)
+    ds = _dev(gpu_ctx, s)
+    for c in (0, 4, 5, 8, 13, 16):
+        assert gpu_ctx.msm_g2(b, ds, n, window_bits=c) == exp, c
+    for i in range(15):  # one scalar at a time, on its own base
+        one = _dev(gpu_ctx, s[i:i + 1])
+        assert gpu_ctx.msm_g2(b, one, 1, offset=i) == _g2(O.g2_msm_known_answer(k[i:i + 1], s[i:i + 1])), i
