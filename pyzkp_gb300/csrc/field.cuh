@@ -384,29 +384,6 @@ __device__ __forceinline__ fe fe_mul_rolled(const fe& a, const fe& b) {
           "r"((uint32_t)((p3) >> 32)), "r"((uint32_t)((p4) >> 32)), "r"((uint32_t)((p5) >> 32)),              \
           "r"((uint32_t)((p6) >> 32)), "r"((uint32_t)((p7) >> 32)))
 
-// The same high-half chain as multiply-adds by a register holding 1 (mad.lo.cc with a
-// multiplier the compiler cannot fold), for measurements of moving carry additions from the
-// ALU pipe to the multiply pipe: ZK_HI_MAD bit 0 = the a * b_i half, bit 1 = the m * p half.
-#ifndef ZK_HI_MAD
-#define ZK_HI_MAD 0
-#endif
-#define ZK_MAD_HI_CHAIN(one_, p0, p1, p2, p3, p4, p5, p6, p7)                                                   \
-    asm("mad.lo.cc.u32  %0, %8, %16, %0;\n\t"                                                                  \
-        "madc.lo.cc.u32 %1, %9, %16, %1;\n\t"                                                                  \
-        "madc.lo.cc.u32 %2, %10, %16, %2;\n\t"                                                                 \
-        "madc.lo.cc.u32 %3, %11, %16, %3;\n\t"                                                                 \
-        "madc.lo.cc.u32 %4, %12, %16, %4;\n\t"                                                                 \
-        "madc.lo.cc.u32 %5, %13, %16, %5;\n\t"                                                                 \
-        "madc.lo.cc.u32 %6, %14, %16, %6;\n\t"                                                                 \
-        "madc.lo.u32    %7, %15, %16, %7;"                                                                     \
-        : "+r"(t1), "+r"(t2), "+r"(t3), "+r"(t4), "+r"(t5), "+r"(t6), "+r"(t7), "+r"(t8)                       \
-        : "r"((uint32_t)((p0) >> 32)), "r"((uint32_t)((p1) >> 32)), "r"((uint32_t)((p2) >> 32)),              \
-          "r"((uint32_t)((p3) >> 32)), "r"((uint32_t)((p4) >> 32)), "r"((uint32_t)((p5) >> 32)),              \
-          "r"((uint32_t)((p6) >> 32)), "r"((uint32_t)((p7) >> 32)), "r"(one_))
-#if ZK_HI_MAD
-__device__ __constant__ uint32_t kOneWord = 1;
-#endif
-
 // Rows (bit i = row i) whose reduction half m * p uses mad.lo.cc / madc.hi.cc chains
 // (IMAD pipe) instead of mul.wide + add chains (IMAD.WIDE + ALU pipe).
 #ifndef ZK_MIX_ROWS
@@ -501,9 +478,6 @@ __device__ __forceinline__ fe fe_mul_acc_unrolled(const fe& a, const fe& b) {
 template <class F>
 __device__ __forceinline__ fe fe_mul_wide_unrolled(const fe& a, const fe& b) {
     uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0, t8 = 0;
-#if ZK_HI_MAD
-    const uint32_t one = kOneWord;
-#endif
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const uint32_t bi = b.v[i];
@@ -511,11 +485,7 @@ __device__ __forceinline__ fe fe_mul_wide_unrolled(const fe& a, const fe& b) {
                        p3 = (uint64_t)a.v[3] * bi, p4 = (uint64_t)a.v[4] * bi, p5 = (uint64_t)a.v[5] * bi,
                        p6 = (uint64_t)a.v[6] * bi, p7 = (uint64_t)a.v[7] * bi;
         ZK_ADD_LO_CHAIN(p0, p1, p2, p3, p4, p5, p6, p7);
-#if ZK_HI_MAD & 1
-        ZK_MAD_HI_CHAIN(one, p0, p1, p2, p3, p4, p5, p6, p7);
-#else
         ZK_ADD_HI_CHAIN(p0, p1, p2, p3, p4, p5, p6, p7);
-#endif
         const uint32_t m = t0 * F::INV;
         if ((ZK_MIX_ROWS >> i) & 1) {
             // this row's m * p on the IMAD pipe (multiply-add with carry), balancing the ALU pipe
@@ -525,11 +495,7 @@ __device__ __forceinline__ fe fe_mul_wide_unrolled(const fe& a, const fe& b) {
                            q3 = (uint64_t)m * F::P(3), q4 = (uint64_t)m * F::P(4), q5 = (uint64_t)m * F::P(5),
                            q6 = (uint64_t)m * F::P(6), q7 = (uint64_t)m * F::P(7);
             ZK_ADD_LO_CHAIN(q0, q1, q2, q3, q4, q5, q6, q7);
-#if ZK_HI_MAD & 2
-            ZK_MAD_HI_CHAIN(one, q0, q1, q2, q3, q4, q5, q6, q7);
-#else
             ZK_ADD_HI_CHAIN(q0, q1, q2, q3, q4, q5, q6, q7);
-#endif
         }
         t0 = t1;
         t1 = t2;
