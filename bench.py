@@ -247,11 +247,13 @@ def run_gpu(args, ranks: Ranks) -> dict:
         "imad_probes_T_per_s": imad_probes,
         "launch_ms": round(acc_ms_launch, 4),
         "share_of_step": round(acc_ms / max(1e-9, sum(v[1] for v in table.values())), 4),
-        "traffic": None,
+        "traffic": traffic_of("msm_accumulate", log_n),
+        "traffic_unit": "DRAM bytes per launch (ncu capture of this benchmark)",
         "hbm": {"achieved": round(acc_bytes / (acc_ms_launch * 1e-3) / 1e9, 1), "peak": hbm_peak,
                 "unit": "GB/s", "frac": round(acc_bytes / (acc_ms_launch * 1e-3) / 1e9 / hbm_peak, 4),
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks.get("hbm_gbs") else "fallback 6800"},
         "algorithmic_work": f"{entries} CSR entries x 10 Fq mults x 272 IMAD; {entries} x 68 B",
+        "whole_msm_model": msm_model(n, total_ms / args.steps, imad_tops),
     }
     kernels = {name: {"launches": la // prof_steps, "ms_per_step": round(ms / prof_steps, 4)}
                for name, (la, ms) in sorted(table.items())}
@@ -393,7 +395,7 @@ def run_gpu_ntt(ctx, args, ranks, log_n, flush, imad_tops, hbm_peak, brief=False
     tops = pass_imad / (pass_ms * 1e-3) / 1e12
     out["roofline"] = {"kernel": "ntt_pass", "bound": "imad", "achieved": round(tops, 3), "peak": round(imad_tops, 3),
                        "unit": "T IMAD/s", "frac": round(tops / imad_tops, 4), "passes": passes,
-                       "launch_ms": round(pass_ms, 4), "traffic": None,
+                       "launch_ms": round(pass_ms, 4), "traffic": traffic_of("ntt_pass", log_n),
                        "hbm": {"achieved": round(gbs, 1), "peak": hbm_peak, "unit": "GB/s",
                                "frac": round(gbs / hbm_peak, 4)},
                        "algorithmic_work": "per pass 64 B/element; (n/2) log2(R) butterflies x 272 IMAD"}
@@ -456,6 +458,35 @@ def run_gpu_ntt_sweep(ctx, args, flush, sizes=(12, 16, 20, 22)) -> dict:
             row[name] = {"Melem_s": round(n / (ms * 1e-3) / 1e6, 1), "ms": round(ms, 4)}
         out[f"2^{log_n}"] = row
     return out
+
+
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant
+# kernels, from one ncu capture of this benchmark on a GB300 with the current build:
+#   ncu --set full --clock-control none -k regex:<kernel> -s <skip> -c 1 -o <report>
+#       python bench.py --only <msm|ntt> [--log-n 22] --steps 2 --warmup 3 --no-cpu-baseline
+# keyed by (kernel, log2 n); the NTT figure is for the first pass of a 2^22 transform.
+NCU_TRAFFIC_BYTES = {("msm_accumulate", 20): 1326.720e6 + 102.674e6, ("ntt_pass", 22): 134.305e6 + 81.835e6}
+
+
+def traffic_of(kernel: str, log_n: int):
+    """DRAM bytes of one launch from the ncu capture, or None for a workload not captured."""
+    t = NCU_TRAFFIC_BYTES.get((kernel, log_n))
+    return None if t is None else int(t)
+
+
+def msm_model(n: int, ms: float, imad_tops: float) -> dict:
+    """Implementation-independent work of a whole G1 MSM of n points: with the window c* that
+    minimises the model (not the implementation's window), W = ceil(255/c*),
+    M = [n W 10 (mixed XYZZ additions) + 2 W 2^(c*-1) 14 (bucket running sums) + W c* 10
+    (doublings)] Fq multiplications of 136 wide MACs (272 IMAD) each."""
+    def fq_mults(c):
+        W = -(-255 // c)
+        return n * W * 10 + 2 * W * (1 << (c - 1)) * 14 + W * c * 10
+    c_star = min(range(4, 25), key=fq_mults)
+    m = fq_mults(c_star)
+    tops = m * 272 / (ms * 1e-3) / 1e12
+    return {"c_star": c_star, "fq_mults": m, "wide_macs": m * 136, "achieved_T_IMAD_s": round(tops, 3),
+            "frac": round(tops / imad_tops, 4), "ms": round(ms, 4)}
 
 
 def imad_peak(ctx):

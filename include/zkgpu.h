@@ -34,6 +34,7 @@ extern "C" {
 #define ZK_ECUDA 2  /* CUDA runtime failure; RuntimeError */
 #define ZK_ENOMEM 3 /* device memory exhausted; MemoryError */
 #define ZK_ENODEV 4 /* no usable CUDA device; RuntimeError (runtime/context.py:33-34) */
+#define ZK_ETIMEOUT 5 /* zk_batch_wait: the batch is still running when the time limit passed */
 
 typedef struct zk_ctx zk_ctx;
 typedef struct zk_bases zk_bases;
@@ -343,6 +344,29 @@ int zk_msm_g2(zk_ctx *ctx, const zk_bases *bases, size_t offset, const void *sca
 int zk_msm_g2_batch(zk_ctx *ctx, size_t count, const zk_bases *const *bases, const uint64_t *offsets,
                     const void *const *scalars_dev, const uint64_t *sizes, int scalars_mont, uint32_t window_bits,
                     uint8_t *out_xy, int32_t *out_is_inf);
+
+/*
+ * Asynchronous batches (the batch_submit / batch_wait pair of the serving layer, which
+ * calls the library from its own loop thread while the reference's KernelFns are
+ * synchronous: runtime/executor.py:167-218). zk_msm_g1_batch_submit / zk_msm_g2_batch_submit
+ * take the arguments of zk_msm_g1_batch / zk_msm_g2_batch, enqueue the device work on the
+ * context stream and return; a library thread combines the windows on the host when the
+ * device is done. zk_batch_wait returns ZK_OK once out_xy / out_is_inf are written,
+ * ZK_ETIMEOUT if timeout_ms (>= 0; negative waits without a limit) passed first (call it
+ * again), or the batch's error. Scalars, bases and the output arrays must stay valid until
+ * then; zk_batch_destroy waits for the batch and frees it, and every batch of a context
+ * must be destroyed before the context. Work enqueued on the context after a submit runs
+ * after that batch's device part (one stream).
+ */
+typedef struct zk_batch zk_batch;
+int zk_msm_g1_batch_submit(zk_ctx *ctx, size_t count, const zk_bases *const *bases, const uint64_t *offsets,
+                           const void *const *scalars_dev, const uint64_t *sizes, int scalars_mont,
+                           uint32_t window_bits, uint8_t *out_xy, int32_t *out_is_inf, zk_batch **out);
+int zk_msm_g2_batch_submit(zk_ctx *ctx, size_t count, const zk_bases *const *bases, const uint64_t *offsets,
+                           const void *const *scalars_dev, const uint64_t *sizes, int scalars_mont,
+                           uint32_t window_bits, uint8_t *out_xy, int32_t *out_is_inf, zk_batch **out);
+int zk_batch_wait(zk_batch *batch, int timeout_ms);
+int zk_batch_destroy(zk_batch *batch);
 
 /*
  * Batch plan: a zk_msm_g1_batch with fixed shapes, prepared once and run many times

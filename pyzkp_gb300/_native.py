@@ -18,7 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("ZKGPU_LIB") or os.path.join(HERE, "_lib", "libzkgpu.so")
 
-ZK_OK, ZK_EINVAL, ZK_ECUDA, ZK_ENOMEM, ZK_ENODEV = 0, 1, 2, 3, 4
+ZK_OK, ZK_EINVAL, ZK_ECUDA, ZK_ENOMEM, ZK_ENODEV, ZK_ETIMEOUT = 0, 1, 2, 3, 4, 5
 
 NTT_EVALS_FROM_COEFFS = 0
 NTT_COEFFS_FROM_EVALS = 1
@@ -29,7 +29,8 @@ EXPORTED_SYMBOLS = (
     "zk_last_error", "zk_version", "zk_ctx_create", "zk_ctx_destroy", "zk_ctx_sync", "zk_ctx_stream",
     "zk_ctx_num_sms", "zk_alloc", "zk_free", "zk_h2d", "zk_d2h", "zk_host_alloc", "zk_host_free",
     "zk_fr_to_mont", "zk_fr_from_mont", "zk_fq_to_mont", "zk_fq_from_mont", "zk_fr_mul", "zk_fr_sub", "zk_ntt",
-    "zk_bases_create", "zk_bases_create_dev", "zk_bases_destroy", "zk_bases_count", "zk_msm_g1", "zk_msm_g1_host",
+    "zk_bases_create", "zk_bases_create_dev", "zk_bases_destroy", "zk_bases_count", "zk_msm_g1", "zk_msm_g1_host", "zk_msm_g1_batch_submit",
+    "zk_msm_g2_batch_submit", "zk_batch_wait", "zk_batch_destroy",
     "zk_g1_fixed_base_mul", "zk_memset", "zk_launch_count", "zk_prof_enable", "zk_prof_reset", "zk_prof_count",
     "zk_prof_get", "zk_timer_start", "zk_timer_stop", "zk_msm_last_stats", "zk_imad_peak", "zk_d2d",
     "zk_fr_trimmed_len", "zk_ntt_noalloc", "zk_imad_probe", "zk_bases_precompute", "zk_msm_g1_batch",
@@ -129,6 +130,10 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_bases_g2_create": ([P, P, S, PP], I),
             "zk_msm_g2": ([P, P, S, P, S, I, U32, P, ctypes.POINTER(ctypes.c_int)], I),
             "zk_msm_g2_batch": ([P, S, PP, P, PP, P, I, U32, P, P], I),
+            "zk_msm_g1_batch_submit": ([P, S, PP, P, PP, P, I, U32, P, P, ctypes.POINTER(ctypes.c_void_p)], I),
+            "zk_msm_g2_batch_submit": ([P, S, PP, P, PP, P, I, U32, P, P, ctypes.POINTER(ctypes.c_void_p)], I),
+            "zk_batch_wait": ([P, I], I),
+            "zk_batch_destroy": ([P], I),
             "zk_g2_fixed_base_mul": ([P, P, P, S, P], I),
             "zk_fr_spmv": ([P, U32, P, P, P, P, P], I),
             "zk_fr_r1cs_check": ([P, P, P, P, S, ctypes.POINTER(ctypes.c_uint64)], I),
@@ -164,7 +169,42 @@ def check(rc: int, what: str = "") -> None:
         raise ValueError(text)
     if rc == ZK_ENOMEM:
         raise MemoryError(text)
+    if rc == ZK_ETIMEOUT:
+        raise TimeoutError(text)
     raise ZkError(text)
+
+
+class MsmBatch:
+    """An in-flight asynchronous MSM batch (zk_batch)."""
+
+    def __init__(self, handle, count, g2, out, inf, keep) -> None:
+        self.handle, self.count, self.g2, self._out, self._inf, self._keep = handle, count, g2, out, inf, keep
+
+    def wait(self, timeout_ms: int = -1):
+        """Results once the batch is done (TimeoutError if timeout_ms >= 0 passes first)."""
+        check(load().zk_batch_wait(self.handle, int(timeout_ms)), "zk_batch_wait")
+        if self.g2:
+            return [None if self._inf[k] else _g2_from(self._out[k].tobytes()) for k in range(self.count)]
+        return _points_from(self._out[:self.count], self._inf[:self.count])
+
+    def done(self) -> bool:
+        try:
+            check(load().zk_batch_wait(self.handle, 0), "zk_batch_wait")
+            return True
+        except TimeoutError:
+            return False
+
+    def destroy(self) -> None:
+        if self.handle is not None:
+            load().zk_batch_destroy(self.handle)
+            self.handle = None
+            self._keep = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
 
 
 class DeviceArray:
@@ -555,6 +595,27 @@ class Context:
                                      sz.ctypes.data, 1 if scalars_mont else 0, int(window_bits), out.ctypes.data,
                                      inf.ctypes.data), "zk_msm_g2_batch")
         return [None if inf[k] else _g2_from(out[k].tobytes()) for k in range(count)]
+
+    def msm_batch_submit(self, bases, scalars, sizes, *, g2: bool = False, offsets=None,
+                         scalars_mont: bool = True, window_bits: int = 0) -> "MsmBatch":
+        """Asynchronous batched MSM (zk_msm_g1_batch_submit / zk_msm_g2_batch_submit): returns
+        at once; ``MsmBatch.wait(timeout_ms)`` gives the results of msm_g1_batch / msm_g2_batch."""
+        count = len(sizes)
+        if isinstance(bases, Bases):
+            bases = [bases] * count
+        bh = (ctypes.c_void_p * count)(*[b.handle for b in bases])
+        sp = (ctypes.c_void_p * count)(*[getattr(s, "ptr", s) for s in scalars])
+        sz = np.ascontiguousarray(sizes, dtype=np.uint64)
+        off = None if offsets is None else np.ascontiguousarray(offsets, dtype=np.uint64)
+        out = np.zeros((max(count, 1), 128 if g2 else 64), dtype=np.uint8)
+        inf = np.zeros(max(count, 1), dtype=np.int32)
+        h = ctypes.c_void_p()
+        fn = load().zk_msm_g2_batch_submit if g2 else load().zk_msm_g1_batch_submit
+        check(fn(self.handle, count, bh, None if off is None else off.ctypes.data, sp, sz.ctypes.data,
+                 1 if scalars_mont else 0, int(window_bits), out.ctypes.data, inf.ctypes.data, ctypes.byref(h)),
+              "zk_msm_batch_submit")
+        # the arrays the library reads or writes until the batch completes stay referenced
+        return MsmBatch(h.value, count, g2, out, inf, keep=(bh, sp, sz, off, scalars, bases))
 
     def bases_precompute(self, bases: "Bases", window_bits: int) -> None:
         """Window-shifted rows for fixed-base MSMs on ``bases`` (zk_bases_precompute)."""

@@ -618,6 +618,55 @@ int zk_msm_g1_batch(zk_ctx* ctx, size_t count, const zk_bases* const* bases, con
     return zk::msm_batch_run(&ctx->impl, jobs.data(), count, scalars_mont, window_bits, out_xy, out_is_inf);
 }
 
+static int batch_submit_common(zk_ctx* ctx, bool g2, size_t count, const zk_bases* const* bases,
+                               const uint64_t* offsets, const void* const* scalars_dev, const uint64_t* sizes,
+                               int scalars_mont, uint32_t window_bits, uint8_t* out_xy, int32_t* out_is_inf,
+                               zk_batch** out) {
+    CTX_OR_FAIL(ctx);
+    if (out == nullptr || (count && (scalars_dev == nullptr || out_xy == nullptr || out_is_inf == nullptr))) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    *out = nullptr;
+    std::vector<zk::MsmJob> jobs;
+    int rc = make_jobs(count, bases, offsets, scalars_dev, sizes, &jobs, g2);
+    if (rc != ZK_OK) return rc;
+    zk::MsmAsync* a = nullptr;
+    rc = zk::msm_batch_submit(&ctx->impl, jobs.data(), count, scalars_mont, window_bits, g2, out_xy, out_is_inf, &a);
+    if (rc != ZK_OK) return rc;
+    *out = new zk_batch{a};
+    return ZK_OK;
+}
+
+int zk_msm_g1_batch_submit(zk_ctx* ctx, size_t count, const zk_bases* const* bases, const uint64_t* offsets,
+                           const void* const* scalars_dev, const uint64_t* sizes, int scalars_mont,
+                           uint32_t window_bits, uint8_t* out_xy, int32_t* out_is_inf, zk_batch** out) {
+    return batch_submit_common(ctx, false, count, bases, offsets, scalars_dev, sizes, scalars_mont, window_bits,
+                               out_xy, out_is_inf, out);
+}
+
+int zk_msm_g2_batch_submit(zk_ctx* ctx, size_t count, const zk_bases* const* bases, const uint64_t* offsets,
+                           const void* const* scalars_dev, const uint64_t* sizes, int scalars_mont,
+                           uint32_t window_bits, uint8_t* out_xy, int32_t* out_is_inf, zk_batch** out) {
+    return batch_submit_common(ctx, true, count, bases, offsets, scalars_dev, sizes, scalars_mont, window_bits,
+                               out_xy, out_is_inf, out);
+}
+
+int zk_batch_wait(zk_batch* batch, int timeout_ms) {
+    if (batch == nullptr) {
+        zk::set_error("null zk_batch");
+        return ZK_EINVAL;
+    }
+    return zk::msm_batch_wait(batch->impl, timeout_ms);
+}
+
+int zk_batch_destroy(zk_batch* batch) {
+    if (batch == nullptr) return ZK_OK;
+    zk::msm_batch_release(batch->impl);
+    delete batch;
+    return ZK_OK;
+}
+
 int zk_msm_plan_create(zk_ctx* ctx, size_t count, const zk_bases* const* bases, const uint64_t* offsets,
                        const uint64_t* sizes, int scalars_mont, uint32_t window_bits, int use_graph,
                        zk_msm_plan** out) {

@@ -35,6 +35,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <string>
 #include <thread>
 #include <tuple>
 #include <vector>
@@ -1090,7 +1091,8 @@ static void horner_out(const MsmPipeT<C>& p, const zkh::XyzzT<typename HostOf<C>
 // Combine every instance of `pipes`: the window sums of all instances in parallel on the
 // host pool, then each instance's Horner (in parallel across instances).
 template <class C>
-static void combine_all(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, uint8_t* out_xy, int32_t* out_is_inf) {
+static void combine_all(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, uint8_t* out_xy, int32_t* out_is_inf,
+                        bool record = true) {
     using H = typename HostOf<C>::T;
     constexpr size_t kOut = 2 * sizeof(H);  // bytes of one affine result
     const auto t0 = std::chrono::steady_clock::now();
@@ -1119,6 +1121,7 @@ static void combine_all(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, uint8_t* 
         const size_t o = pipes[in.q].out_index[in.k];
         horner_out<C>(pipes[in.q], sums.data() + in.first, out_xy + kOut * o, out_is_inf + o);
     });
+    if (!record) return;  // a worker thread of an asynchronous batch leaves the context's tables alone
     prof_host(c, "msm_host_combine",
               std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
     c->msm_entries = entries;
@@ -1229,6 +1232,128 @@ static int batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont,
     ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
     combine_all<C>(c, pipes, out_xy, out_is_inf);
     return ZK_OK;
+}
+
+// ---- asynchronous batches: the device part is enqueued and the call returns; a worker
+// thread waits for the device, combines the windows on the host and signals completion ----
+struct MsmAsync {
+    cudaEvent_t done_ev = nullptr;
+    void* pinned = nullptr;  // per-set targets and entry totals of every pipeline
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv;
+    bool done = false;
+    int rc = ZK_OK;
+    std::string error;
+    virtual ~MsmAsync() {
+        if (worker.joinable()) worker.join();
+        if (done_ev) cudaEventDestroy(done_ev);
+        if (pinned) cudaFreeHost(pinned);
+    }
+    void finish(int code, const std::string& err) {
+        std::lock_guard<std::mutex> g(mu);
+        rc = code;
+        error = err;
+        done = true;
+        cv.notify_all();
+    }
+};
+
+template <class C>
+struct MsmAsyncT : MsmAsync {
+    std::vector<MsmPipeT<C>> pipes;
+};
+
+template <class C>
+static int batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits,
+                        uint8_t* out_xy, int32_t* out_is_inf, MsmAsync** out) {
+    std::unique_ptr<MsmAsyncT<C>> a(new MsmAsyncT<C>());
+    std::vector<size_t> empty;
+    int rc = build_pipes<C>(c, jobs, count, window_bits, &a->pipes, &empty);
+    if (rc != ZK_OK) return rc;
+    set_infinity(out_xy, out_is_inf, empty, 2 * sizeof(typename HostOf<C>::T));
+    if (a->pipes.empty()) {
+        a->done = true;
+        *out = a.release();
+        return ZK_OK;
+    }
+    std::vector<MsmPipeT<C>>& pipes = a->pipes;
+    size_t bytes = 0, host_elems = 0;
+    std::vector<size_t> at(pipes.size());
+    for (size_t q = 0; q < pipes.size(); q++) {
+        at[q] = bytes;
+        bytes += (pipe_layout(pipes[q], nullptr) + 255) & ~(size_t)255;
+        host_elems += pipes[q].host_elems();
+    }
+    // pinned host targets: the device-to-host copies stay asynchronous
+    const size_t host_bytes = host_elems * sizeof(typename C::P) + pipes.size() * sizeof(uint32_t);
+    ZK_TRY_CUDA(cudaMallocHost(&a->pinned, host_bytes));
+    ZK_TRY_CUDA(cudaEventCreateWithFlags(&a->done_ev, cudaEventDisableTiming));
+    char* arena = nullptr;
+    if ((rc = scratch_alloc(c, bytes, reinterpret_cast<void**>(&arena))) != ZK_OK) return rc;
+    auto* host_t = static_cast<typename C::P*>(a->pinned);
+    auto* totals = reinterpret_cast<uint32_t*>(host_t + host_elems);
+    size_t h = 0;
+    for (size_t q = 0; q < pipes.size(); q++) {
+        pipe_layout(pipes[q], arena + at[q]);
+        pipes[q].h_tgt = host_t + h;
+        pipes[q].h_total = totals + q;
+        h += pipes[q].host_elems();
+        if ((rc = pipe_enqueue<C>(c, pipes[q], scalars_mont, true)) != ZK_OK) {
+            cudaStreamSynchronize(c->stream);
+            scratch_free(c, arena);
+            return rc;
+        }
+    }
+    scratch_free(c, arena);  // stream-ordered: reusable only by work enqueued after this batch
+    ZK_TRY_CUDA(cudaEventRecord(a->done_ev, c->stream));
+    MsmAsyncT<C>* raw = a.get();
+    const int device = c->device;
+    raw->worker = std::thread([c, raw, device, out_xy, out_is_inf]() {
+        cudaSetDevice(device);
+        const cudaError_t e = cudaEventSynchronize(raw->done_ev);
+        if (e != cudaSuccess) {
+            raw->finish(ZK_ECUDA, std::string("asynchronous MSM batch: ") + cudaGetErrorString(e));
+            return;
+        }
+        combine_all<C>(c, raw->pipes, out_xy, out_is_inf, /*record=*/false);
+        raw->finish(ZK_OK, "");
+    });
+    *out = a.release();
+    return ZK_OK;
+}
+
+int msm_batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, bool g2,
+                     uint8_t* out_xy, int32_t* out_is_inf, MsmAsync** out) {
+    *out = nullptr;
+    if (g2) {
+        for (size_t j = 0; j < count; j++) ZK_CHECK_ARG(jobs[j].shifted == nullptr, "G2 MSMs have no fixed-base mode");
+        return batch_submit<CurveG2>(c, jobs, count, scalars_mont, window_bits, out_xy, out_is_inf, out);
+    }
+    return batch_submit<CurveG1>(c, jobs, count, scalars_mont, window_bits, out_xy, out_is_inf, out);
+}
+
+// ZK_OK once the results are written, ZK_ETIMEOUT if timeout_ms (>= 0) passed first
+// (negative: wait without a limit), else the batch's error.
+int msm_batch_wait(MsmAsync* a, int timeout_ms) {
+    std::unique_lock<std::mutex> g(a->mu);
+    if (timeout_ms < 0) {
+        a->cv.wait(g, [a] { return a->done; });
+    } else if (!a->cv.wait_for(g, std::chrono::milliseconds(timeout_ms), [a] { return a->done; })) {
+        set_error("MSM batch still running");
+        return ZK_ETIMEOUT;
+    }
+    if (a->rc != ZK_OK) set_error(a->error);
+    return a->rc;
+}
+
+void msm_batch_release(MsmAsync* a) {
+    if (a == nullptr) return;
+    {
+        std::unique_lock<std::mutex> g(a->mu);
+        a->cv.wait(g, [a] { return a->done; });
+    }
+    delete a;
 }
 
 int msm_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, uint8_t* out_xy,

@@ -153,6 +153,11 @@ int msm_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, ui
 // G2: out_xy holds 128 bytes per instance (x.c0, x.c1, y.c0, y.c1); no fixed-base mode
 int msm_g2_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits,
                      uint8_t* out_xy, int32_t* out_is_inf);
+struct MsmAsync;
+int msm_batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, bool g2,
+                     uint8_t* out_xy, int32_t* out_is_inf, MsmAsync** out);
+int msm_batch_wait(MsmAsync* a, int timeout_ms);
+void msm_batch_release(MsmAsync* a);
 int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, bool graph,
                     MsmPlan** out);
 int msm_plan_slot(MsmPlan* plan, size_t index, void** dev);
@@ -195,6 +200,10 @@ struct zk_bases {
     zk::affine_t* shifted = nullptr;  // fixed-base rows [2^(c j)] P_i, j < shifted_windows, row stride n
     uint32_t shifted_c = 0;
     uint32_t shifted_windows = 0;
+};
+
+struct zk_batch {
+    zk::MsmAsync* impl;
 };
 
 struct zk_msm_plan {

@@ -262,3 +262,47 @@ def test_autotune_small_sizes(gpu_ctx):
     finally:
         gpu_ctx.tune_set_ntt_split(log_n, [])
         gpu_ctx.tune_set_msm_window(log_n, 0)
+
+
+def test_async_batches_match_sync(gpu_ctx):
+    """zk_msm_g1_batch_submit / zk_msm_g2_batch_submit + zk_batch_wait: the same points as the
+    synchronous batch calls, with two batches in flight at once, a time-limited wait, an
+    empty batch, and other work enqueued on the context between submit and wait."""
+    sizes = [3000, 0, 1, 4096, 777]
+    k, b = _bases(gpu_ctx, 5150, max(sizes), zero_at=(2,))
+    scal = [synth.fr_uniform(5151 + j, m) for j, m in enumerate(sizes)]
+    dev = [_upload(gpu_ctx, s) for s in scal]
+    exp = [_expect(k[:m], s) for m, s in zip(sizes, scal)]
+    first = gpu_ctx.msm_batch_submit(b, dev, sizes)
+    second = gpu_ctx.msm_batch_submit(b, dev[::-1], sizes[::-1])
+    busy = gpu_ctx.alloc(64 << 20)  # unrelated work on the same stream
+    gpu_ctx.memset(busy, 3)
+    done = False
+    for _ in range(2000):  # bounded polling with short waits
+        try:
+            got1 = first.wait(5)
+            done = True
+            break
+        except TimeoutError:
+            continue
+    assert done
+    assert got1 == exp
+    assert second.wait() == exp[::-1]
+    assert first.done() and second.done()
+    first.destroy()
+    second.destroy()
+    empty = gpu_ctx.msm_batch_submit(b, [], [])
+    assert empty.wait(0) == []
+    empty.destroy()
+    # G2
+    n2 = 600
+    k2 = synth.base_dlogs(5160, n2)
+    b2 = gpu_ctx.bases_g2_from_host(O.g2_fixed_base_mul(O.G2_GENERATOR, k2))
+    s2 = [synth.fr_uniform(5161, n2), synth.fr_uniform(5162, 250)]
+    d2 = [_upload(gpu_ctx, s) for s in s2]
+    g2 = gpu_ctx.msm_batch_submit(b2, d2, [n2, 250], g2=True)
+    res = g2.wait()
+    g2.destroy()
+    for s, r in zip(s2, res):
+        p = O.g2_msm_known_answer(k2[:s.shape[0]], s)
+        assert r == (None if not p.any() else O.g2_to_ints(p))
