@@ -260,6 +260,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
 
     if args.only == "msm":
         return {"metric": METRIC, "value": round(mpts, 3), "unit": "Mpts/s", "kernels": kernels,
+                "msm_result": [hex(res[0]), hex(res[1])] if res else None,
                 "roofline": roofline, "gpu_launches": launches, "clocks": sampler.stop()}
 
     # e2e through the C ABI from pinned host memory

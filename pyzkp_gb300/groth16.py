@@ -426,8 +426,11 @@ class Prover:
             g2_bases.append(k.b2.bases)
             g2_sc.append(sc["b"])  # b_query_g2 and b_query_g1 share their non-zero pattern
             g2_n.append(k.b2.count)
-        g1 = self._batch(ctx.msm_g1_batch, g1_bases, g1_sc, g1_n)
-        g2 = self._batch(ctx.msm_g2_batch, g2_bases, g2_sc, g2_n)
+        # both batches in flight: the G1 windows are combined on the host while the G2 MSMs run
+        g1_job = self._submit(ctx, g1_bases, g1_sc, g1_n, g2=False)
+        g2_job = self._submit(ctx, g2_bases, g2_sc, g2_n, g2=True)
+        g1 = self._collect(g1_job, len(g1_n))
+        g2 = self._collect(g2_job, len(g2_n))
 
         def one(i):
             q = live[i][0]
@@ -451,14 +454,25 @@ class Prover:
         return cls._executor
 
     @staticmethod
-    def _batch(fn, bases, scalars, sizes):
-        """One batched MSM over the non-empty instances (an empty one is the identity)."""
+    def _submit(ctx, bases, scalars, sizes, g2: bool):
+        """Submit one asynchronous batched MSM over the non-empty instances."""
         sel = [i for i, m in enumerate(sizes) if m]
-        out: List[Optional[tuple]] = [None] * len(sizes)
-        if sel:
-            res = fn([bases[i] for i in sel], [scalars[i] for i in sel], [sizes[i] for i in sel])
-            for i, v in zip(sel, res):
-                out[i] = v
+        if not sel:
+            return sel, None
+        return sel, ctx.msm_batch_submit([bases[i] for i in sel], [scalars[i] for i in sel],
+                                         [sizes[i] for i in sel], g2=g2)
+
+    @staticmethod
+    def _collect(job, count: int):
+        """Results of _submit in instance order (an empty instance is the identity)."""
+        sel, batch = job
+        out: List[Optional[tuple]] = [None] * count
+        if batch is not None:
+            try:
+                for i, v in zip(sel, batch.wait()):
+                    out[i] = v
+            finally:
+                batch.destroy()
         return out
 
 
