@@ -160,6 +160,11 @@ int zk_ctx_destroy(zk_ctx* ctx) {
         cudaStreamSynchronize(ctx->impl.copy_stream);
         cudaStreamDestroy(ctx->impl.copy_stream);
     }
+    for (cudaStream_t st : ctx->impl.side_streams) {
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+    }
+    for (cudaEvent_t ev : ctx->impl.side_events) cudaEventDestroy(ev);
     if (ctx->impl.copy_go) cudaEventDestroy(ctx->impl.copy_go);
     if (ctx->impl.copy_done) cudaEventDestroy(ctx->impl.copy_done);
     cudaStreamDestroy(ctx->impl.stream);
@@ -441,6 +446,9 @@ int zk_bases_precompute(zk_ctx* ctx, zk_bases* b, uint32_t window_bits) {
     if (b->shifted && b->shifted_c == window_bits) return ZK_OK;
     zk::affine_t* rows = nullptr;
     uint32_t windows = 0;
+    // rows of P only: rows of phi(P) as well (GLV halves over one shared bucket set) measured
+    // slower in the steady state (2^20: 234 vs 251 Mpts/s at the best window of each), their
+    // short top windows crowding a few buckets
     int rc = zk::shift_bases(&ctx->impl, b->dev, b->n, window_bits, &rows, &windows);
     if (rc != ZK_OK) return rc;
     if (b->shifted) zk::scratch_free(&ctx->impl, b->shifted);

@@ -1,4 +1,4 @@
-// msm.cu -- BN254 G1 multi-scalar multiplication (Pippenger, signed digits, CSR buckets).
+// msm.cu -- BN254 G1 / G2 multi-scalar multiplication (Pippenger, signed digits, GLV, CSR buckets).
 //
 // Result semantics: the unique affine point sum_i s_i P_i, identical to
 // crypto/msm/pippenger.py:10-64 and runtime/metal/msm.py:179-332 (metal_msm_g1_v2).
@@ -8,9 +8,12 @@
 // (:499-535), one thread per window reduce (:540-566), CPU Horner (msm.py:322-332).
 //
 // This pipeline (all on the device except the last ~W*13 point additions):
-//  1. msm_digits_kernel   scalar -> reduced scalar (zero for an infinity base) and the CSR
-//                         histogram of its W signed c-bit digits (|d| <= 2^(c-1)),
-//                         counted with warp-aggregated atomics (__match_any_sync).
+//  0. GLV (G1 and G2 bases carry phi(P) = [lambda] P behind P): every scalar is split
+//     k = k1 + k2 lambda with |k1|, |k2| < 2^127 (glv_split), so the MSM runs over 2n points
+//     with 128-bit scalars: W = ceil(128/c) windows instead of ceil(255/c), half the buckets.
+//  1. msm_digits_kernel   scalar -> reduced scalar (zero for an infinity base), its GLV
+//                         halves, and the CSR histogram of their W signed c-bit digits
+//                         (|d| <= 2^(c-1)), counted with warp-aggregated atomics (__match_any_sync).
 //  2. device scan         counters -> CSR row pointers (scan.cu).
 //  3. msm_scatter_kernel  the digits again; entry = point index | sign << 31 in the range
 //                         of its (window, |digit|) bucket (no per-entry bucket id is
@@ -19,9 +22,10 @@
 //                         even when one bucket holds 5% of all points; a segment finds
 //                         its first bucket by binary search over the row pointers);
 //                         buckets wholly inside a segment are final; a bucket that
-//                         straddles segment boundaries leaves partial sums that tree
-//                         rounds (pairs, then groups of 4 units) merge, deciding
-//                         "straddles" from the row pointers.
+//                         straddles segment boundaries leaves partial sums that one fixup
+//                         thread per bucket adds (short buckets), or tree rounds (pairs,
+//                         then groups of 4 units) merge, deciding "straddles" from the row
+//                         pointers.
 //  5. msm_bucket_blocks   per window, blocks of g buckets: sum_b b*B_b = sum_j E_j + g*WS(Y)
 //                         with Y_j the block sums and E_j = -(sum of the g-1 prefix sums).
 //  6. msm_targets_kernel  WS(Y) = sum_j Y_j + sum_k 2^k M_k with M_k the sum of the Y_j
@@ -656,23 +660,30 @@ __global__ void __launch_bounds__(128) msm_bucket_blocks2_kernel(const typename 
 // ---- 6. plain sums per (window, target) ---------------------------------------------
 // targets 0 .. plain-1: full sums of P0, P1 (, P2) over G2 entries per window;
 // target plain + k: sum of Ylast_j over j with bit k set.
+// Each target is split over `parts` CTAs (a slice of its terms each; large single bucket
+// sets of the fixed-base mode have G2 up to 2^14); out[(w * targets + tg) * parts + part].
 template <class C>
 __global__ void __launch_bounds__(C::kTargetThreads) msm_targets_kernel(const typename C::P* __restrict__ P0,
                                                                         const typename C::P* __restrict__ P1,
                                                                         const typename C::P* __restrict__ P2,
                                                                         const typename C::P* __restrict__ Ylast,
-                                                                        MsmShape sh, typename C::P* __restrict__ out) {
+                                                                        MsmShape sh, uint32_t parts,
+                                                                        typename C::P* __restrict__ out) {
     using P = typename C::P;
     __shared__ P red[C::kTargetThreads];
-    const uint32_t w = blockIdx.x / sh.targets;
-    const uint32_t tg = blockIdx.x % sh.targets;
+    const uint32_t part = blockIdx.x % parts;
+    const uint32_t wt = blockIdx.x / parts;
+    const uint32_t w = wt / sh.targets;
+    const uint32_t tg = wt % sh.targets;
     const bool bits = tg >= sh.plain;
     const P* src = bits ? Ylast : (tg == 0 ? P0 : (tg == 1 ? P1 : P2));
     src += (size_t)w * sh.G2;
     const uint32_t count = bits ? sh.G2 / 2 : sh.G2;
+    const uint32_t per = (count + parts - 1) / parts;
+    const uint32_t t0 = part * per, t1 = min(count, t0 + per);
     const uint32_t k = bits ? tg - sh.plain : 0;
     P acc = xyzz_inf<typename C::T>();
-    for (uint32_t t = threadIdx.x; t < count; t += blockDim.x) {
+    for (uint32_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
         uint32_t j = t;
         if (bits) j = ((t >> k) << (k + 1)) | (1u << k) | (t & ((1u << k) - 1));
         acc = xyzz_add(acc, xyzz_load(src + j));
@@ -684,6 +695,38 @@ __global__ void __launch_bounds__(C::kTargetThreads) msm_targets_kernel(const ty
         __syncthreads();
     }
     if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+// The parts of each target summed: one CTA of kMergeThreads per (window, target).
+static constexpr uint32_t kMergeThreads = 32;
+
+template <class C>
+__global__ void __launch_bounds__(kMergeThreads) msm_targets_merge_kernel(const typename C::P* __restrict__ in,
+                                                                          uint32_t parts,
+                                                                          typename C::P* __restrict__ out) {
+    using P = typename C::P;
+    __shared__ P red[kMergeThreads];
+    const P* src = in + (size_t)blockIdx.x * parts;
+    P acc = xyzz_inf<typename C::T>();
+    for (uint32_t t = threadIdx.x; t < parts; t += blockDim.x) acc = xyzz_add(acc, xyzz_load(src + t));
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (uint32_t off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) red[threadIdx.x] = xyzz_add(red[threadIdx.x], red[threadIdx.x + off]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+// CTAs per target: one up to 8 terms per thread; the large single bucket sets of the
+// fixed-base mode (G2 up to 2^14) in slices of about 8 terms per thread, at most 64.
+#ifndef ZK_TARGET_SLICE
+#define ZK_TARGET_SLICE 8
+#endif
+template <class C>
+static uint32_t target_parts(const MsmShape& sh) {
+    const uint32_t slice = (uint32_t)ZK_TARGET_SLICE * (uint32_t)C::kTargetThreads;
+    return std::max<uint32_t>(1, std::min<uint32_t>(64, (sh.G2 + slice - 1) / slice));
 }
 
 // ---- fixed-base precomputation ----------------------------------------------------------
@@ -746,11 +789,12 @@ int shift_bases(Ctx* c, const affine_t* bases, size_t n, uint32_t window_bits, a
     ZK_CHECK_ARG(window_bits >= 4 && window_bits <= 20, "fixed-base window_bits must be 4..20");
     ZK_CHECK_ARG(n > 0 && n < (1ull << 31), "fixed-base precomputation needs 0 < n < 2^31");
     const MsmShape sh = make_shape(window_bits);
-    ZK_CHECK_ARG((uint64_t)sh.W * n < (1ull << 31), "fixed-base rows exceed 31-bit entry indices");
+    const uint64_t nrows = sh.W;
+    ZK_CHECK_ARG(nrows * n < (1ull << 31), "fixed-base rows exceed 31-bit entry indices");
     affine_t* rows = nullptr;
     xyzz_t* tmp = nullptr;
     fe* pref = nullptr;
-    int rc = scratch_alloc(c, (size_t)sh.W * n * sizeof(affine_t), reinterpret_cast<void**>(&rows));
+    int rc = scratch_alloc(c, (size_t)nrows * n * sizeof(affine_t), reinterpret_cast<void**>(&rows));
     if (rc != ZK_OK) return rc;
     if ((rc = scratch_alloc(c, (size_t)sh.W * n * sizeof(xyzz_t), reinterpret_cast<void**>(&tmp))) != ZK_OK ||
         (rc = scratch_alloc(c, (size_t)sh.W * n * sizeof(fe), reinterpret_cast<void**>(&pref))) != ZK_OK) {
@@ -815,6 +859,7 @@ struct MsmPipeT {
     P *slot_pts_a = nullptr, *slot_pts_b = nullptr;
     uint32_t *long_list = nullptr, *long_count = nullptr;  // fixup mode
     P *buckets = nullptr, *Yb = nullptr, *Eb = nullptr, *Y2 = nullptr, *E2 = nullptr, *F2 = nullptr, *tgt = nullptr;
+    P* tgt_parts = nullptr;  // per-part target sums before the merge (null with one part)
     P* h_tgt = nullptr;  // host copy of the per-set targets (sets * targets)
     uint32_t* h_total = nullptr;
     size_t host_elems() const { return (size_t)sh.sets * sh.targets; }
@@ -889,6 +934,8 @@ static size_t pipe_layout(MsmPipeT<C>& p, char* base) {
     p.E2 = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G2 * sizeof(P)));
     p.F2 = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G2 * sizeof(P)));
     p.tgt = reinterpret_cast<P*>(take(p.host_elems() * sizeof(P)));
+    const uint32_t parts = target_parts<C>(sh);
+    p.tgt_parts = parts > 1 ? reinterpret_cast<P*>(take(p.host_elems() * parts * sizeof(P))) : nullptr;
     return off;
 }
 
@@ -967,13 +1014,22 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
         ZK_LAUNCH(c, "msm_bucket_blocks2", msm_bucket_blocks2_kernel<C>, (nb2 + 127) / 128, 128, 0, p.Yb, p.Eb, sh, p.Y2,
                   p.E2, p.F2);
         ZK_TRY_CUDA(cudaGetLastError());
-        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel<C>, sh.sets * sh.targets, target_threads, 0, p.F2, p.E2, p.Y2,
-                  p.Y2, sh, p.tgt);
+    }
+    const uint32_t parts = target_parts<C>(sh);
+    P* tout = parts > 1 ? p.tgt_parts : p.tgt;
+    if (sh.g2 > 1) {
+        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel<C>, sh.sets * sh.targets * parts, target_threads, 0, p.F2,
+                  p.E2, p.Y2, p.Y2, sh, parts, tout);
     } else {
-        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel<C>, sh.sets * sh.targets, target_threads, 0, p.Eb, p.Yb, p.Yb,
-                  p.Yb, sh, p.tgt);
+        ZK_LAUNCH(c, "msm_targets", msm_targets_kernel<C>, sh.sets * sh.targets * parts, target_threads, 0, p.Eb,
+                  p.Yb, p.Yb, p.Yb, sh, parts, tout);
     }
     ZK_TRY_CUDA(cudaGetLastError());
+    if (parts > 1) {
+        ZK_LAUNCH(c, "msm_targets_merge", msm_targets_merge_kernel<C>, sh.sets * sh.targets, kMergeThreads, 0,
+                  p.tgt_parts, parts, p.tgt);
+        ZK_TRY_CUDA(cudaGetLastError());
+    }
     ZK_TRY_CUDA(cudaMemcpyAsync(p.h_tgt, p.tgt, p.host_elems() * sizeof(P), cudaMemcpyDeviceToHost, st));
     ZK_TRY_CUDA(cudaMemcpyAsync(p.h_total, d_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     return ZK_OK;
@@ -1146,7 +1202,7 @@ static int build_pipes(Ctx* c, const MsmJob* jobs, size_t count, uint32_t window
             continue;
         }
         const bool fixed = b.shifted != nullptr && (window_bits == 0 || window_bits == b.shifted_c);
-        const bool glv = !fixed && b.glv;
+        const bool glv = !fixed && b.glv;  // fixed-base rows hold P only (plain 255-bit windows)
         const uint32_t cb = fixed ? b.shifted_c : (window_bits ? window_bits : msm_window_for(c, b.n, glv));
         groups[std::make_tuple(cb, fixed, glv)].push_back(j);
     }
@@ -1196,6 +1252,58 @@ static void set_infinity(uint8_t* out_xy, int32_t* out_is_inf, const std::vector
     }
 }
 
+// Enqueue every pipeline of a batch. With several pipelines they are spread over the
+// context stream and kSideStreams side streams (largest first, each to the stream with the
+// least work so far), forked from and joined back into the context stream, so that the
+// latency-bound stages of small pipelines overlap the accumulation of large ones. Works
+// inside a stream capture (the fork / join events make the side streams part of it).
+static constexpr int kSideStreams = 3;
+
+static int ensure_side_streams(Ctx* c) {
+    while ((int)c->side_streams.size() < kSideStreams) {
+        cudaStream_t st = nullptr;
+        ZK_TRY_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        c->side_streams.push_back(st);
+    }
+    while ((int)c->side_events.size() <= kSideStreams) {
+        cudaEvent_t ev = nullptr;
+        ZK_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        c->side_events.push_back(ev);
+    }
+    return ZK_OK;
+}
+
+template <class C>
+static int enqueue_all(Ctx* c, std::vector<MsmPipeT<C>>& pipes, int scalars_mont, bool upload) {
+    if (pipes.size() == 1) return pipe_enqueue<C>(c, pipes[0], scalars_mont, upload);
+    int rc0 = ensure_side_streams(c);  // outside a capture (msm_plan_create calls it first)
+    if (rc0 != ZK_OK) return rc0;
+    const cudaStream_t main_stream = c->stream;
+    const int nstreams = (int)std::min<size_t>(pipes.size(), kSideStreams + 1);
+    ZK_TRY_CUDA(cudaEventRecord(c->side_events[0], main_stream));
+    for (int k = 1; k < nstreams; k++) ZK_TRY_CUDA(cudaStreamWaitEvent(c->side_streams[k - 1], c->side_events[0], 0));
+    std::vector<size_t> order(pipes.size());
+    for (size_t q = 0; q < pipes.size(); q++) order[q] = q;
+    std::sort(order.begin(), order.end(),
+              [&](size_t a, size_t b) { return pipes[a].max_entries > pipes[b].max_entries; });
+    std::vector<uint64_t> load(nstreams, 0);
+    int rc = ZK_OK;
+    for (size_t q : order) {
+        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[k] += pipes[q].max_entries + 64ull * pipes[q].nbuckets;  // + fixed cost per bucket
+        c->stream = k == 0 ? main_stream : c->side_streams[k - 1];
+        rc = pipe_enqueue<C>(c, pipes[q], scalars_mont, upload);
+        c->stream = main_stream;
+        if (rc != ZK_OK) break;
+    }
+    // join (also after a failure, so that no side stream is left outside a capture)
+    for (int k = 1; k < nstreams; k++) {
+        cudaEventRecord(c->side_events[k], c->side_streams[k - 1]);
+        cudaStreamWaitEvent(main_stream, c->side_events[k], 0);
+    }
+    return rc;
+}
+
 template <class C>
 static int batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, uint8_t* out_xy,
                      int32_t* out_is_inf) {
@@ -1222,11 +1330,11 @@ static int batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont,
         pipes[q].h_tgt = host_t.data() + h;
         pipes[q].h_total = &host_total[q];
         h += pipes[q].host_elems();
-        if ((rc = pipe_enqueue<C>(c, pipes[q], scalars_mont, true)) != ZK_OK) {
-            cudaStreamSynchronize(c->stream);
-            scratch_free(c, arena);
-            return rc;
-        }
+    }
+    if ((rc = enqueue_all<C>(c, pipes, scalars_mont, true)) != ZK_OK) {
+        cudaStreamSynchronize(c->stream);
+        scratch_free(c, arena);
+        return rc;
     }
     scratch_free(c, arena);
     ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
@@ -1299,11 +1407,11 @@ static int batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mo
         pipes[q].h_tgt = host_t + h;
         pipes[q].h_total = totals + q;
         h += pipes[q].host_elems();
-        if ((rc = pipe_enqueue<C>(c, pipes[q], scalars_mont, true)) != ZK_OK) {
-            cudaStreamSynchronize(c->stream);
-            scratch_free(c, arena);
-            return rc;
-        }
+    }
+    if ((rc = enqueue_all<C>(c, pipes, scalars_mont, true)) != ZK_OK) {
+        cudaStreamSynchronize(c->stream);
+        scratch_free(c, arena);
+        return rc;
     }
     scratch_free(c, arena);  // stream-ordered: reusable only by work enqueued after this batch
     ZK_TRY_CUDA(cudaEventRecord(a->done_ev, c->stream));
@@ -1463,6 +1571,10 @@ int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, 
         const uint64_t launches_was = c->launches;
         const auto prof_was_map = c->prof;
         c->prof_on = false;
+        if (int src = ensure_side_streams(c); src != ZK_OK) {
+            c->prof_on = prof_was;
+            return fail(src);
+        }
         cudaError_t be = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
         if (be != cudaSuccess) {
             c->prof_on = prof_was;
@@ -1470,8 +1582,7 @@ int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, 
             return fail(ZK_ECUDA);
         }
         int erc = ZK_OK;
-        for (auto& p : plan->pipes)
-            if ((erc = pipe_enqueue<CurveG1>(c, p, scalars_mont, false)) != ZK_OK) break;
+        erc = enqueue_all<CurveG1>(c, plan->pipes, scalars_mont, false);
         cudaGraph_t g = nullptr;
         cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
         plan->kernels = c->launches - launches_was;
@@ -1511,12 +1622,10 @@ int msm_plan_run(Ctx* c, MsmPlan* plan, uint8_t* out_xy, int32_t* out_is_inf) {
         prof_end(c, tok);
         c->launches += plan->kernels - 1;  // prof_begin counted the graph launch as one
     } else {
-        for (auto& p : plan->pipes) {
-            int rc = pipe_enqueue<CurveG1>(c, p, plan->scalars_mont, false);
-            if (rc != ZK_OK) {
-                cudaStreamSynchronize(c->stream);
-                return rc;
-            }
+        int rc = enqueue_all<CurveG1>(c, plan->pipes, plan->scalars_mont, false);
+        if (rc != ZK_OK) {
+            cudaStreamSynchronize(c->stream);
+            return rc;
         }
     }
     ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));

@@ -81,6 +81,8 @@ struct ProfPending {
 struct Ctx {
     int device = 0;
     int num_sms = 0;
+    // the stream ZK_LAUNCH and the copies use: the context stream, pointed at a side or
+    // copy stream for the span of one enqueue (a batch pipeline, an upload) and then restored
     cudaStream_t stream = nullptr;
     std::mutex mu;
     std::map<std::string, NttPlan*> ntt_plans;
@@ -96,6 +98,10 @@ struct Ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_go = nullptr, copy_done = nullptr;
     cudaEvent_t bases_wait = nullptr;
+    // MSM batches spread their pipelines over the context stream and these (fork / join
+    // events); created on first use
+    std::vector<cudaStream_t> side_streams;
+    std::vector<cudaEvent_t> side_events;  // fork, then one join event per side stream
     uint64_t msm_entries = 0;
     uint32_t msm_window_bits = 0, msm_windows = 0;
     // tuning tables (zk_tune_*, zk_autotune_*): 0 means the built-in rule

@@ -333,6 +333,14 @@ def test_msm_glv_edge_scalars(gpu_ctx):
         assert gpu_msm(gpu_ctx, bases, s, window_bits=c) == exp, c
     st = gpu_ctx.msm_last_stats()
     assert st["window_bits"] == 20 and st["windows"] == (128 + 19) // 20
+    # the same scalars through fixed-base rows (rows of P and of phi(P), one bucket set)
+    b = gpu_ctx.bases_from_host(bases)
+    ds = gpu_ctx.to_device(s)
+    gpu_ctx.fr_to_mont(ds, ds, n)
+    for c in (4, 7, 16, 19):
+        gpu_ctx.bases_precompute(b, c)
+        assert gpu_ctx.msm_g1(b, ds, n) == exp, ("fixed", c)
+        assert gpu_ctx.msm_g1(b, ds, n - 9, offset=9) == O.affine_to_ints(O.msm_known_answer(k[9:], s[:n - 9]))
     # one scalar at a time (each half alone in its buckets)
     for v in vals[:16]:
         one = synth.ints_to_limbs([v])
