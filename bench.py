@@ -254,6 +254,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks.get("hbm_gbs") else "fallback 6800"},
         "algorithmic_work": f"{entries} CSR entries x 10 Fq mults x 272 IMAD; {entries} x 68 B",
         "whole_msm_model": msm_model(n, total_ms / args.steps, imad_tops),
+        "sort_kernels": sort_kernels(table, prof_steps, n, entries, hbm_peak),
     }
     kernels = {name: {"launches": la // prof_steps, "ms_per_step": round(ms / prof_steps, 4)}
                for name, (la, ms) in sorted(table.items())}
@@ -306,7 +307,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
     clocks = sampler.stop()
     sweep = run_gpu_msm_sweep(ctx, args, flush) if ranks.world == 1 else None
     fixed = run_gpu_fixed_base(ctx, args, flush) if ranks.world == 1 else None
-    fixed_sweep = ({f"2^{lg}": run_gpu_fixed_base(ctx, args, flush, log_n=lg, calls=6) for lg in (16, 18, 20, 22)}
+    fixed_sweep = ({f"2^{lg}": run_gpu_fixed_base(ctx, args, flush, log_n=lg) for lg in range(16, 23)}
                    if ranks.world == 1 else None)
     ntt_sweep = run_gpu_ntt_sweep(ctx, args, flush) if ranks.world == 1 else None
     batch = run_gpu_batch(ctx, args, flush) if ranks.world == 1 else None
@@ -473,6 +474,22 @@ def traffic_of(kernel: str, log_n: int):
     """DRAM bytes of one launch from the ncu capture, or None for a workload not captured."""
     t = NCU_TRAFFIC_BYTES.get((kernel, log_n))
     return None if t is None else int(t)
+
+
+def sort_kernels(table: dict, steps: int, n: int, entries: int, hbm_peak: float) -> dict:
+    """HBM view of the digit decomposition and the CSR scatter (the memory-bound stages):
+    algorithmic bytes per launch over the live kernel time. msm_digits reads the 32-byte
+    scalars and writes the two 32-byte GLV halves; msm_scatter reads the halves and writes
+    one 4-byte entry per non-zero digit."""
+    out = {}
+    for name, nbytes in (("msm_digits", n * (32 + 64)), ("msm_scatter", n * 64 + entries * 4)):
+        la, ms = table.get(name, (0, 0.0))
+        if not la:
+            continue
+        t = ms / la
+        gbs = nbytes / (t * 1e-3) / 1e9
+        out[name] = {"ms": round(t, 4), "bytes": nbytes, "GB_s": round(gbs, 1), "frac": round(gbs / hbm_peak, 4)}
+    return out
 
 
 def msm_model(n: int, ms: float, imad_tops: float) -> dict:
