@@ -65,6 +65,7 @@ static constexpr uint32_t kNone = 0xffffffffu;
 #define ZK_MSM_GROUP 4  // measured at 2^20 / 2^22: merge 0.73 / 1.36 ms with 16, 0.48 / 1.02 ms with 4
 #endif
 static constexpr uint32_t kSegment = ZK_MSM_SEGMENT;  // entries per thread in the first accumulation round
+static constexpr uint32_t kMinSegment = 8;            // ... at least, in small pipelines
 static constexpr uint32_t kFirstGroup = 2;            // units merged per thread in the first merge round
 static constexpr uint32_t kGroup = ZK_MSM_GROUP;      // units merged per thread in later rounds
 static constexpr uint32_t kBlockG = ZK_MSM_BLOCKG;    // buckets per block in the window reduction
@@ -92,6 +93,7 @@ struct MsmShape {
     uint32_t sets;     // bucket sets to reduce: inst * Wr
     uint32_t glv;      // 1: each scalar is split k = k1 + k2 lambda (halves < 2^127, see glv_split);
                        // the phi(P) half of every instance's bases sits at bases + stride
+    uint32_t seg;      // CSR entries per thread in the accumulation (kSegment, less for small pipelines)
 };
 
 // One MSM of a pipeline: sum_{i < n} scalars[i] * bases[i] (fixed-base mode: bases holds the
@@ -104,6 +106,19 @@ struct MsmInst {
     uint32_t stride;
 };
 
+// Block structure of the window reduction for level-1 blocks of g buckets and level-2
+// blocks of g2 level-1 blocks.
+static void shape_blocks(MsmShape& s, uint32_t g, uint32_t g2 = kBlockG2) {
+    s.g = std::min<uint32_t>(g, s.B);
+    s.G = s.B / s.g;
+    s.g2 = s.G >= 2 * g2 ? g2 : 1;
+    s.G2 = s.G / s.g2;
+    s.K = 0;
+    while ((1u << s.K) < s.G2) s.K++;
+    s.plain = s.g2 > 1 ? 3 : 2;
+    s.targets = s.plain + s.K;
+}
+
 static MsmShape make_shape(uint32_t c, bool glv = false) {
     MsmShape s;
     s.c = c;
@@ -111,14 +126,8 @@ static MsmShape make_shape(uint32_t c, bool glv = false) {
     // halves < 2^127
     s.W = ((glv ? 128u : 255u) + c - 1) / c;
     s.B = 1u << (c - 1);
-    s.g = std::min<uint32_t>(kBlockG, s.B);
-    s.G = s.B / s.g;
-    s.g2 = s.G >= 2 * kBlockG2 ? kBlockG2 : 1;
-    s.G2 = s.G / s.g2;
-    s.K = 0;
-    while ((1u << s.K) < s.G2) s.K++;
-    s.plain = s.g2 > 1 ? 3 : 2;
-    s.targets = s.plain + s.K;
+    shape_blocks(s, kBlockG);
+    s.seg = kSegment;
     s.shared = 0;
     s.Wr = s.W;
     s.inst = 1;
@@ -482,9 +491,9 @@ __global__ void __launch_bounds__(128, ZK_ACC_MINB) msm_accumulate_kernel(const 
     slot_keys[2 * u] = kNone;
     slot_keys[2 * u + 1] = kNone;
     const uint32_t M = *d_total;
-    const uint32_t e0 = u * kSegment;
+    const uint32_t e0 = u * sh.seg;
     if (e0 >= M) return;
-    const uint32_t e1 = min(e0 + kSegment, M);
+    const uint32_t e1 = min(e0 + sh.seg, M);
     uint32_t cur = bucket_of(row_ptr, sh.sets * sh.B, e0);
     uint32_t end = row_ptr[cur + 1];  // > e0
     const A* bases = key_bases<C>(insts, sh, cur);
@@ -561,7 +570,7 @@ static constexpr int kFixupLongThreads = 128;
 
 template <class C>
 __global__ void __launch_bounds__(128) msm_fixup_kernel(const uint32_t* __restrict__ row_ptr, uint32_t nbuckets,
-                                                        const typename C::P* __restrict__ slot_pts,
+                                                        uint32_t seg, const typename C::P* __restrict__ slot_pts,
                                                         typename C::P* __restrict__ buckets,
                                                         uint32_t* __restrict__ long_list,
                                                         uint32_t* __restrict__ long_count) {
@@ -569,7 +578,7 @@ __global__ void __launch_bounds__(128) msm_fixup_kernel(const uint32_t* __restri
     if (k >= nbuckets) return;
     const uint32_t b0 = row_ptr[k], b1 = row_ptr[k + 1];
     if (b1 == b0) return;
-    const uint32_t u0 = b0 / kSegment, u1 = (b1 - 1) / kSegment;
+    const uint32_t u0 = b0 / seg, u1 = (b1 - 1) / seg;
     if (u0 == u1) return;  // final already (written by the accumulation)
     if (u1 - u0 > kFixupMax) {
         long_list[atomicAdd(long_count, 1u)] = k;
@@ -584,6 +593,7 @@ __global__ void __launch_bounds__(128) msm_fixup_kernel(const uint32_t* __restri
 // shared-memory tree.
 template <class C>
 __global__ void __launch_bounds__(kFixupLongThreads) msm_fixup_long_kernel(const uint32_t* __restrict__ row_ptr,
+                                                                           uint32_t seg,
                                                                            const typename C::P* __restrict__ slot_pts,
                                                                            typename C::P* __restrict__ buckets,
                                                                            const uint32_t* __restrict__ long_list,
@@ -593,7 +603,7 @@ __global__ void __launch_bounds__(kFixupLongThreads) msm_fixup_long_kernel(const
     const uint32_t count = *long_count;
     for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
         const uint32_t k = long_list[item];
-        const uint32_t u0 = row_ptr[k] / kSegment, u1 = (row_ptr[k + 1] - 1) / kSegment;
+        const uint32_t u0 = row_ptr[k] / seg, u1 = (row_ptr[k + 1] - 1) / seg;
         P acc = xyzz_inf<typename C::T>();
         for (uint32_t u = u0 + threadIdx.x; u <= u1; u += blockDim.x)
             acc = xyzz_add(acc, xyzz_load(slot_pts + 2 * (size_t)u + (u == u0 ? 1 : 0)));
@@ -868,7 +878,7 @@ struct MsmPipeT {
 // Shape and limits of a pipeline over `jobs` (all with window c, fixed-base mode or not).
 template <class C>
 static int pipe_init(MsmPipeT<C>& p, uint32_t c, bool fixed, bool glv, const std::vector<MsmInst>& jobs,
-                     const std::vector<size_t>& out_index) {
+                     const std::vector<size_t>& out_index, int num_sms) {
     p.sh = make_shape(c, glv);
     if (fixed) {
         p.sh.shared = 1;
@@ -895,7 +905,23 @@ static int pipe_init(MsmPipeT<C>& p, uint32_t c, bool fixed, bool glv, const std
     ZK_CHECK_ARG(p.max_entries < (1ull << 32) - kSegment, "MSM too large for 32-bit CSR offsets");
     p.nbuckets = (uint64_t)p.sh.sets * p.sh.B;
     ZK_CHECK_ARG(p.nbuckets < (1ull << 32) - 1, "MSM batch has too many buckets for 32-bit keys");
-    p.units = (uint32_t)((p.max_entries + kSegment - 1) / kSegment);
+    // Small pipelines are latency-bound (each accumulation thread is a chain of seg additions,
+    // each reduction thread one of g or g2): shorter segments while there are fewer than about
+    // four waves of accumulation threads and buckets still span at most ~2 segments on average
+    // (more pieces cost more in the fixup than the shorter chains save), smaller blocks while
+    // there are fewer than two (level 1) or one (level 2) warps of block threads per SM.
+    // Measured on GB300 (single MSMs): 2^12 0.67 -> 0.48 ms, 2^14 0.69 -> 0.55 ms, 2^16
+    // 1.03 -> 0.88 ms, 2^18 1.89 -> 1.86 ms; 2^20 and larger unchanged.
+    const uint64_t acc_threads = (uint64_t)num_sms * 2048;
+    const uint64_t density = p.max_entries / std::max<uint64_t>(1, p.nbuckets);
+    while (p.sh.seg > kMinSegment && p.max_entries / p.sh.seg < acc_threads && p.sh.seg / 2 >= density / 2)
+        p.sh.seg /= 2;
+    const uint64_t min_threads = (uint64_t)num_sms * 64;
+    uint32_t g = kBlockG, g2 = kBlockG2;
+    while (g > 2 && p.nbuckets / g < min_threads) g /= 2;
+    while (g2 > 2 && p.nbuckets / g / g2 < min_threads / 2) g2 /= 2;
+    shape_blocks(p.sh, g, g2);
+    p.units = (uint32_t)((p.max_entries + p.sh.seg - 1) / p.sh.seg);
     return ZK_OK;
 }
 
@@ -978,13 +1004,13 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
     if (p.max_entries <= (uint64_t)p.nbuckets * kFixupDensity) {
         ZK_TRY_CUDA(cudaMemsetAsync(p.long_count, 0, 4, st));
         ZK_LAUNCH(c, "msm_fixup", msm_fixup_kernel<C>, (unsigned)((p.nbuckets + 127) / 128), 128, 0, p.row_ptr,
-                  (uint32_t)p.nbuckets, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
+                  (uint32_t)p.nbuckets, sh.seg, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
         ZK_TRY_CUDA(cudaGetLastError());
         ZK_LAUNCH(c, "msm_fixup_long", msm_fixup_long_kernel<C>, (unsigned)(c->num_sms * 2), kFixupLongThreads, 0,
-                  p.row_ptr, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
+                  p.row_ptr, sh.seg, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
         ZK_TRY_CUDA(cudaGetLastError());
     } else {
-        uint64_t span = kSegment;
+        uint64_t span = sh.seg;
         uint32_t in_units = p.units;
         uint32_t *ik = p.slot_keys_a, *ok = p.slot_keys_b;
         typename C::P *ip = p.slot_pts_a, *op = p.slot_pts_b;
@@ -1217,7 +1243,7 @@ static int build_pipes(Ctx* c, const MsmJob* jobs, size_t count, uint32_t window
         auto flush = [&]() -> int {
             if (part.empty()) return ZK_OK;
             out->emplace_back();
-            int rc = pipe_init<C>(out->back(), cb, fixed, glv, part, idx);
+            int rc = pipe_init<C>(out->back(), cb, fixed, glv, part, idx, c->num_sms);
             part.clear();
             idx.clear();
             N = 0;
