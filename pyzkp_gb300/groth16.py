@@ -191,6 +191,7 @@ class Query:
     bases: Optional[N.Bases]
     idx: Optional[N.DeviceArray]  # uint32 device indices, None when the set is the identity map
     count: int
+    rows_bytes: int = 0  # fixed-base rows of the G1 bases (zk_bases_precompute), if built
 
 
 @dataclass
@@ -214,8 +215,9 @@ class DeviceKey:
         return self.r1cs.n
 
     def device_bytes(self) -> int:
-        g1 = (self.a.count + self.b1.count + self.l.count + self.h.count) * 64
-        return g1 + self.b2.count * 128 + 4 * (self.a.count + self.b1.count + self.l.count)
+        qs = (self.a, self.b1, self.l, self.h)
+        g1 = sum(q.count for q in qs) * 128 + sum(q.rows_bytes for q in qs)  # points + GLV images, rows
+        return g1 + self.b2.count * 256 + 4 * (self.a.count + self.b1.count + self.l.count)
 
 
 def _upload_csr(ctx: N.Context, m: CSR):
@@ -264,8 +266,21 @@ def _query(ctx: N.Context, exps: np.ndarray, g2: bool = False, identity: bool = 
     return Query(bases, idx, count)
 
 
-def setup(ctx: N.Context, r1cs: R1CS, td: Trapdoors, keep_exponents: bool = False) -> DeviceKey:
-    """The proving key of protocols/groth16/setup.py:25-121 for the trapdoors `td`."""
+def _precompute(ctx: N.Context, q: Query) -> None:
+    """Fixed-base rows for a G1 query's bases (the reference's fixed_base_precompute policy for
+    proving keys, runtime/warmup.py:125-150): every later MSM on them runs in fixed-base mode."""
+    from .plugin import fixed_base_window
+
+    if q.count:
+        c = fixed_base_window(q.count)
+        ctx.bases_precompute(q.bases, c)
+        q.rows_bytes = -(-255 // c) * q.count * 64
+
+
+def setup(ctx: N.Context, r1cs: R1CS, td: Trapdoors, keep_exponents: bool = False,
+          fixed_base: bool = True) -> DeviceKey:
+    """The proving key of protocols/groth16/setup.py:25-121 for the trapdoors `td`. With
+    fixed_base, the G1 query bases also get their window-shifted rows (same proofs, faster MSMs)."""
     n, nv = r1cs.n, r1cs.n_vars
     log_n = n.bit_length() - 1
     t_tau = (pow(td.tau, n, FR_MODULUS) - 1) % FR_MODULUS
@@ -324,6 +339,9 @@ def setup(ctx: N.Context, r1cs: R1CS, td: Trapdoors, keep_exponents: bool = Fals
                     mats=(_upload_csr(ctx, r1cs.a), _upload_csr(ctx, r1cs.b), _upload_csr(ctx, r1cs.c)))
     if keep_exponents:
         key.exps = {"a": ua, "b": ub, "l": l_exp, "h": h_exp, "ic": ints_to_limbs(ic_exp)}
+    if fixed_base:
+        for q in (a_q, b1_q, l_q, h_q):
+            _precompute(ctx, q)
     ctx.sync()
     return key
 
