@@ -284,6 +284,7 @@ int zk_bases_destroy(zk_bases *b);
  * later zk_msm_g1 on these bases (with window_bits 0 or c) then sums all windows in one
  * bucket set: no per-window bucket reduction and no doubling chain. Same result.
  */
+/* G2 handles (zk_bases_g2_create) take the same call: rows of G2 points, 128 bytes each. */
 int zk_bases_precompute(zk_ctx *ctx, zk_bases *b, uint32_t window_bits);
 int zk_bases_count(const zk_bases *b, size_t *n);
 

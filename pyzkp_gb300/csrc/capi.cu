@@ -439,20 +439,27 @@ int zk_bases_create_dev(zk_ctx* ctx, const void* xy_canonical_dev, size_t n, zk_
 
 int zk_bases_precompute(zk_ctx* ctx, zk_bases* b, uint32_t window_bits) {
     CTX_OR_FAIL(ctx);
-    if (b == nullptr || b->dev == nullptr) {
-        zk::set_error("zk_bases_precompute needs G1 bases");
+    if (b == nullptr || (b->dev == nullptr && b->dev2 == nullptr)) {
+        zk::set_error("zk_bases_precompute needs a bases handle");
         return ZK_EINVAL;
     }
-    if (b->shifted && b->shifted_c == window_bits) return ZK_OK;
-    zk::affine_t* rows = nullptr;
+    if ((b->shifted || b->shifted2) && b->shifted_c == window_bits) return ZK_OK;
     uint32_t windows = 0;
-    // rows of P only: rows of phi(P) as well (GLV halves over one shared bucket set) measured
-    // slower in the steady state (2^20: 234 vs 251 Mpts/s at the best window of each), their
-    // short top windows crowding a few buckets
-    int rc = zk::shift_bases(&ctx->impl, b->dev, b->n, window_bits, &rows, &windows);
-    if (rc != ZK_OK) return rc;
-    if (b->shifted) zk::scratch_free(&ctx->impl, b->shifted);
-    b->shifted = rows;
+    int rc = ZK_OK;
+    if (b->dev2) {  // G2 bases
+        zk::affine2_t* rows = nullptr;
+        if ((rc = zk::shift_bases_g2(&ctx->impl, b->dev2, b->n, window_bits, &rows, &windows)) != ZK_OK) return rc;
+        if (b->shifted2) zk::scratch_free(&ctx->impl, b->shifted2);
+        b->shifted2 = rows;
+    } else {
+        zk::affine_t* rows = nullptr;
+        // rows of P only: rows of phi(P) as well (GLV halves over one shared bucket set) measured
+        // slower in the steady state (2^20: 234 vs 251 Mpts/s at the best window of each), their
+        // short top windows crowding a few buckets
+        if ((rc = zk::shift_bases(&ctx->impl, b->dev, b->n, window_bits, &rows, &windows)) != ZK_OK) return rc;
+        if (b->shifted) zk::scratch_free(&ctx->impl, b->shifted);
+        b->shifted = rows;
+    }
     b->shifted_c = window_bits;
     b->shifted_windows = windows;
     ZK_TRY_CUDA(cudaStreamSynchronize(ctx->impl.stream));
@@ -463,6 +470,7 @@ int zk_bases_destroy(zk_bases* b) {
     if (b == nullptr) return ZK_OK;
     cudaSetDevice(b->ctx->impl.device);
     if (b->shifted) zk::scratch_free(&b->ctx->impl, b->shifted);
+    if (b->shifted2) zk::scratch_free(&b->ctx->impl, b->shifted2);
     if (b->dev) zk::scratch_free(&b->ctx->impl, b->dev);
     if (b->dev2) zk::scratch_free(&b->ctx->impl, b->dev2);
     delete b;
@@ -600,6 +608,7 @@ static int make_jobs(size_t count, const zk_bases* const* bases, const uint64_t*
         j.n = sizes[k];
         if (g2) {
             j.bases = b->dev2 + off;
+            j.shifted = b->shifted2 ? b->shifted2 + off : nullptr;
             j.glv = true;
         } else {
             j.bases = b->dev + off;

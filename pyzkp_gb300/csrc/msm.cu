@@ -757,69 +757,97 @@ __device__ fe fe_inverse_fermat(const fe& a) {
     return r;
 }
 
-__global__ void __launch_bounds__(128) msm_shift_bases_kernel(const affine_t* __restrict__ bases, uint32_t n,
-                                                              uint32_t c, uint32_t W, affine_t* __restrict__ out,
-                                                              xyzz_t* __restrict__ tmp, fe* __restrict__ pref) {
+// Inverses of the coordinate field (the Montgomery trick's one inversion per point).
+__device__ __forceinline__ fe c_inv(const fe& a) { return fe_inverse_fermat<FqP>(a); }
+// (a0 + a1 u)^-1 = (a0 - a1 u) / (a0^2 + a1^2) in Fq2 = Fq[u] / (u^2 + 1)
+__device__ __forceinline__ fq2 c_inv(const fq2& a) {
+    const fe inv = fe_inverse_fermat<FqP>(fe_add<FqP>(fe_sqr<FqP>(a.c0), fe_sqr<FqP>(a.c1)));
+    return {fe_mul<FqP>(a.c0, inv), fe_neg<FqP>(fe_mul<FqP>(a.c1, inv))};
+}
+
+template <class C>
+__global__ void __launch_bounds__(128) msm_shift_bases_kernel(const typename C::A* __restrict__ bases, uint32_t n,
+                                                              uint32_t c, uint32_t W, typename C::A* __restrict__ out,
+                                                              typename C::P* __restrict__ tmp,
+                                                              typename C::T* __restrict__ pref) {
+    using A = typename C::A;
+    using P = typename C::P;
+    using T = typename C::T;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const affine_t p = affine_load(bases + i);
-    fe_store(&out[i].x, p.x);
-    fe_store(&out[i].y, p.y);
+    const A p = affine_load(bases + i);
+    c_store(&out[i].x, p.x);
+    c_store(&out[i].y, p.y);
     if (affine_is_inf(p)) {
+        T zero;
+        c_set_zero(zero);
         for (uint32_t j = 1; j < W; j++) {
-            fe_store(&out[(size_t)j * n + i].x, fe_zero());
-            fe_store(&out[(size_t)j * n + i].y, fe_zero());
+            c_store(&out[(size_t)j * n + i].x, zero);
+            c_store(&out[(size_t)j * n + i].y, zero);
         }
         return;
     }
-    xyzz_t q;
+    P q;
     q.X = p.x;
     q.Y = p.y;
-    q.ZZ = fe_one<FqP>();
-    q.ZZZ = fe_one<FqP>();
-    fe run = fe_one<FqP>();
+    c_set_one(q.ZZ);
+    c_set_one(q.ZZZ);
+    T run;
+    c_set_one(run);
     for (uint32_t j = 1; j < W; j++) {
         for (uint32_t d = 0; d < c; d++) q = xyzz_dbl(q);
         xyzz_store(tmp + (size_t)j * n + i, q);
-        fe_store(pref + (size_t)j * n + i, run);
-        run = fe_mul<FqP>(run, fe_mul<FqP>(q.ZZ, q.ZZZ));
+        c_store(pref + (size_t)j * n + i, run);
+        run = c_mul(run, c_mul(q.ZZ, q.ZZZ));
     }
-    fe inv = fe_inverse_fermat<FqP>(run);
+    T inv = c_inv(run);
     for (uint32_t j = W - 1; j >= 1; j--) {
-        const xyzz_t t = xyzz_load(tmp + (size_t)j * n + i);
-        const fe zz_zzz = fe_mul<FqP>(t.ZZ, t.ZZZ);
-        const fe I = fe_mul<FqP>(inv, fe_load(pref + (size_t)j * n + i));
-        inv = fe_mul<FqP>(inv, zz_zzz);
-        fe_store(&out[(size_t)j * n + i].x, fe_mul<FqP>(t.X, fe_mul<FqP>(t.ZZZ, I)));
-        fe_store(&out[(size_t)j * n + i].y, fe_mul<FqP>(t.Y, fe_mul<FqP>(t.ZZ, I)));
+        const P t = xyzz_load(tmp + (size_t)j * n + i);
+        const T zz_zzz = c_mul(t.ZZ, t.ZZZ);
+        const T I = c_mul(inv, c_load(pref + (size_t)j * n + i));
+        inv = c_mul(inv, zz_zzz);
+        c_store(&out[(size_t)j * n + i].x, c_mul(t.X, c_mul(t.ZZZ, I)));
+        c_store(&out[(size_t)j * n + i].y, c_mul(t.Y, c_mul(t.ZZ, I)));
     }
 }
 
-int shift_bases(Ctx* c, const affine_t* bases, size_t n, uint32_t window_bits, affine_t** out, uint32_t* windows) {
+template <class C>
+static int shift_bases_t(Ctx* c, const typename C::A* bases, size_t n, uint32_t window_bits, typename C::A** out,
+                         uint32_t* windows) {
+    using A = typename C::A;
     ZK_CHECK_ARG(window_bits >= 4 && window_bits <= 20, "fixed-base window_bits must be 4..20");
     ZK_CHECK_ARG(n > 0 && n < (1ull << 31), "fixed-base precomputation needs 0 < n < 2^31");
     const MsmShape sh = make_shape(window_bits);
     const uint64_t nrows = sh.W;
     ZK_CHECK_ARG(nrows * n < (1ull << 31), "fixed-base rows exceed 31-bit entry indices");
-    affine_t* rows = nullptr;
-    xyzz_t* tmp = nullptr;
-    fe* pref = nullptr;
-    int rc = scratch_alloc(c, (size_t)nrows * n * sizeof(affine_t), reinterpret_cast<void**>(&rows));
+    A* rows = nullptr;
+    typename C::P* tmp = nullptr;
+    typename C::T* pref = nullptr;
+    int rc = scratch_alloc(c, (size_t)nrows * n * sizeof(A), reinterpret_cast<void**>(&rows));
     if (rc != ZK_OK) return rc;
-    if ((rc = scratch_alloc(c, (size_t)sh.W * n * sizeof(xyzz_t), reinterpret_cast<void**>(&tmp))) != ZK_OK ||
-        (rc = scratch_alloc(c, (size_t)sh.W * n * sizeof(fe), reinterpret_cast<void**>(&pref))) != ZK_OK) {
+    if ((rc = scratch_alloc(c, (size_t)sh.W * n * sizeof(typename C::P), reinterpret_cast<void**>(&tmp))) != ZK_OK ||
+        (rc = scratch_alloc(c, (size_t)sh.W * n * sizeof(typename C::T), reinterpret_cast<void**>(&pref))) != ZK_OK) {
         scratch_free(c, rows);
         scratch_free(c, tmp);
         return rc;
     }
-    ZK_LAUNCH(c, "msm_shift_bases", msm_shift_bases_kernel, (unsigned)((n + 127) / 128), 128, 0, bases, (uint32_t)n,
-              window_bits, sh.W, rows, tmp, pref);
+    ZK_LAUNCH(c, "msm_shift_bases", msm_shift_bases_kernel<C>, (unsigned)((n + 127) / 128), 128, 0, bases,
+              (uint32_t)n, window_bits, sh.W, rows, tmp, pref);
     ZK_TRY_CUDA(cudaGetLastError());
     scratch_free(c, tmp);
     scratch_free(c, pref);
     *out = rows;
     *windows = sh.W;
     return ZK_OK;
+}
+
+int shift_bases(Ctx* c, const affine_t* bases, size_t n, uint32_t window_bits, affine_t** out, uint32_t* windows) {
+    return shift_bases_t<CurveG1>(c, bases, n, window_bits, out, windows);
+}
+
+int shift_bases_g2(Ctx* c, const affine2_t* bases, size_t n, uint32_t window_bits, affine2_t** out,
+                   uint32_t* windows) {
+    return shift_bases_t<CurveG2>(c, bases, n, window_bits, out, windows);
 }
 
 // ---- host ---------------------------------------------------------------------------
@@ -1460,10 +1488,7 @@ static int batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mo
 int msm_batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, bool g2,
                      uint8_t* out_xy, int32_t* out_is_inf, MsmAsync** out) {
     *out = nullptr;
-    if (g2) {
-        for (size_t j = 0; j < count; j++) ZK_CHECK_ARG(jobs[j].shifted == nullptr, "G2 MSMs have no fixed-base mode");
-        return batch_submit<CurveG2>(c, jobs, count, scalars_mont, window_bits, out_xy, out_is_inf, out);
-    }
+    if (g2) return batch_submit<CurveG2>(c, jobs, count, scalars_mont, window_bits, out_xy, out_is_inf, out);
     return batch_submit<CurveG1>(c, jobs, count, scalars_mont, window_bits, out_xy, out_is_inf, out);
 }
 
@@ -1497,7 +1522,6 @@ int msm_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, ui
 
 int msm_g2_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits,
                      uint8_t* out_xy, int32_t* out_is_inf) {
-    for (size_t j = 0; j < count; j++) ZK_CHECK_ARG(jobs[j].shifted == nullptr, "G2 MSMs have no fixed-base mode");
     return batch_run<CurveG2>(c, jobs, count, scalars_mont, window_bits, out_xy, out_is_inf);
 }
 

@@ -145,7 +145,7 @@ struct MsmJob {
     const fe* scalars = nullptr;
     uint64_t n = 0;
     const void* bases = nullptr;  // affine_t (G1) or affine2_t (G2) points
-    const affine_t* shifted = nullptr;
+    const void* shifted = nullptr;  // affine_t (G1) or affine2_t (G2) rows
     uint32_t shifted_c = 0;
     uint64_t stride = 0;  // points in the base set: row stride of `shifted`, offset of the GLV half
     bool glv = false;     // G1 bases whose phi(P) half sits at bases + stride (GLV split scalars)
@@ -171,6 +171,8 @@ uint64_t msm_plan_kernels(const MsmPlan* plan);
 int msm_plan_run(Ctx* c, MsmPlan* plan, uint8_t* out_xy, int32_t* out_is_inf);
 void msm_plan_destroy(Ctx* c, MsmPlan* plan);
 int shift_bases(Ctx* c, const affine_t* bases, size_t n, uint32_t window_bits, affine_t** out, uint32_t* windows);
+int shift_bases_g2(Ctx* c, const affine2_t* bases, size_t n, uint32_t window_bits, affine2_t** out,
+                   uint32_t* windows);
 
 // One transform of an NTT batch (the arguments of ntt_run).
 struct NttJob {
@@ -204,6 +206,7 @@ struct zk_bases {
     zk::affine2_t* dev2 = nullptr;  // G2: 2n Montgomery affine points over Fq2, then their GLV images
                                     // (beta^2 x, y) (null for G1 bases)
     zk::affine_t* shifted = nullptr;  // fixed-base rows [2^(c j)] P_i, j < shifted_windows, row stride n
+    zk::affine2_t* shifted2 = nullptr;  // the same rows of G2 bases
     uint32_t shifted_c = 0;
     uint32_t shifted_windows = 0;
 };

@@ -217,7 +217,8 @@ class DeviceKey:
     def device_bytes(self) -> int:
         qs = (self.a, self.b1, self.l, self.h)
         g1 = sum(q.count for q in qs) * 128 + sum(q.rows_bytes for q in qs)  # points + GLV images, rows
-        return g1 + self.b2.count * 256 + 4 * (self.a.count + self.b1.count + self.l.count)
+        g2 = self.b2.count * 256 + self.b2.rows_bytes
+        return g1 + g2 + 4 * (self.a.count + self.b1.count + self.l.count)
 
 
 def _upload_csr(ctx: N.Context, m: CSR):
@@ -266,21 +267,22 @@ def _query(ctx: N.Context, exps: np.ndarray, g2: bool = False, identity: bool = 
     return Query(bases, idx, count)
 
 
-def _precompute(ctx: N.Context, q: Query) -> None:
-    """Fixed-base rows for a G1 query's bases (the reference's fixed_base_precompute policy for
+def _precompute(ctx: N.Context, q: Query, g2: bool = False) -> None:
+    """Fixed-base rows for a query's bases (the reference's fixed_base_precompute policy for
     proving keys, runtime/warmup.py:125-150): every later MSM on them runs in fixed-base mode."""
     from .plugin import fixed_base_window
 
     if q.count:
         c = fixed_base_window(q.count)
         ctx.bases_precompute(q.bases, c)
-        q.rows_bytes = -(-255 // c) * q.count * 64
+        q.rows_bytes = -(-255 // c) * q.count * (128 if g2 else 64)
 
 
 def setup(ctx: N.Context, r1cs: R1CS, td: Trapdoors, keep_exponents: bool = False,
           fixed_base: bool = True) -> DeviceKey:
     """The proving key of protocols/groth16/setup.py:25-121 for the trapdoors `td`. With
-    fixed_base, the G1 query bases also get their window-shifted rows (same proofs, faster MSMs)."""
+    fixed_base, the query bases (G1 and G2) also get their window-shifted rows (same proofs,
+    faster MSMs)."""
     n, nv = r1cs.n, r1cs.n_vars
     log_n = n.bit_length() - 1
     t_tau = (pow(td.tau, n, FR_MODULUS) - 1) % FR_MODULUS
@@ -342,6 +344,7 @@ def setup(ctx: N.Context, r1cs: R1CS, td: Trapdoors, keep_exponents: bool = Fals
     if fixed_base:
         for q in (a_q, b1_q, l_q, h_q):
             _precompute(ctx, q)
+        _precompute(ctx, b2_q, g2=True)
     ctx.sync()
     return key
 

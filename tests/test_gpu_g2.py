@@ -106,3 +106,25 @@ def test_msm_g2_glv_edge_scalars(gpu_ctx):
     for i in range(15):  # one scalar at a time, on its own base
         one = _dev(gpu_ctx, s[i:i + 1])
         assert gpu_ctx.msm_g2(b, one, 1, offset=i) == _g2(O.g2_msm_known_answer(k[i:i + 1], s[i:i + 1])), i
+
+
+def test_msm_g2_fixed_base_rows(gpu_ctx):
+    """Window-shifted G2 rows (zk_bases_precompute on a G2 handle): the same points as the
+    plain path, for several windows, with offsets and in a batch beside plain instances."""
+    n = 1500
+    k = synth.base_dlogs(4400, n)
+    k[7] = 0  # an infinity base
+    xy = O.g2_fixed_base_mul(O.G2_GENERATOR, k)
+    s = synth.fr_uniform(4401, n)
+    exp = _g2(O.g2_msm_known_answer(k, s))
+    b = gpu_ctx.bases_g2_from_host(xy)
+    ds = _dev(gpu_ctx, s)
+    for c in (5, 10, 16):
+        gpu_ctx.bases_precompute(b, c)
+        assert gpu_ctx.msm_g2(b, ds, n) == exp, c
+        m = 333
+        assert gpu_ctx.msm_g2(b, ds, m, offset=40) == _g2(O.g2_msm_known_answer(k[40:40 + m], s[:m])), c
+    plain = gpu_ctx.bases_g2_from_host(xy[:600])
+    got = gpu_ctx.msm_g2_batch([b, plain, b], [ds, ds, ds], [n, 600, 100])
+    assert got == [exp, _g2(O.g2_msm_known_answer(k[:600], s[:600])), _g2(O.g2_msm_known_answer(k[:100], s[:100]))]
+
