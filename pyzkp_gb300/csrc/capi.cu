@@ -532,9 +532,12 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
         zk::scratch_free(c, bases);
         return rc;
     }
-    // copy stream: bases upload + in-place conversion to Montgomery form, after the allocations
+    // main stream: the scalars first, alone on the link (the digit sort waits for them); the
+    // copy stream then uploads the points and converts them (only the accumulation, after the
+    // sort, waits for those)
     const cudaStream_t main_stream = c->stream;
-    cudaError_t e = cudaEventRecord(c->copy_go, main_stream);
+    cudaError_t e = cudaMemcpyAsync(scalars, scalars_host, n * 32, cudaMemcpyHostToDevice, main_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->copy_go, main_stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->copy_go, 0);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(bases, xy_canonical_host, n * 64, cudaMemcpyHostToDevice, c->copy_stream);
@@ -545,9 +548,7 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
         c->stream = main_stream;
         e = cudaEventRecord(c->copy_done, c->copy_stream);
     }
-    // main stream: scalars, digits, sort; the accumulation waits for copy_done
-    if (e == cudaSuccess && rc == ZK_OK)
-        e = cudaMemcpyAsync(scalars, scalars_host, n * 32, cudaMemcpyHostToDevice, main_stream);
+    // main stream: digits and sort; the accumulation waits for copy_done
     if (e == cudaSuccess && rc == ZK_OK) {
         c->bases_wait = c->copy_done;
         rc = zk::msm_run(c, static_cast<const zk::affine_t*>(bases), static_cast<const zk::fe*>(scalars), n,
