@@ -649,12 +649,12 @@ __device__ __forceinline__ fe fe_mul(const fe& a, const fe& b) {
 
 template <class F>
 __device__ __forceinline__ fe2 fe_mul2(const fe& a, const fe& b, const fe& c, const fe& d) {
+#ifdef ZK_USE_MUL2
 #ifdef ZK_MUL_STYLE
     constexpr int style = ZK_MUL_STYLE;
 #else
     constexpr int style = F::MUL_STYLE;
 #endif
-#ifdef ZK_USE_MUL2
     // measured on GB300 (MSM 2^20): 179 Mpts/s with the interleaved pair, 180 without
     if constexpr (style == 3) return fe_mul2_call<F>(a, b, c, d);
 #endif
