@@ -190,6 +190,40 @@ def test_ntt_2_23_sparse_sampled_and_roundtrip(gpu_ctx):
     assert (d.download().view("<u8").reshape(n, 4) == dense).all()
 
 
+def _gather_canonical(ctx, src, idx):
+    didx = ctx.to_device(np.asarray(idx, dtype=np.uint32))
+    g = ctx.alloc(len(idx) * 32)
+    ctx.fr_gather(g, src, didx, len(idx))
+    ctx.fr_from_mont(g, g, len(idx))
+    return synth.limbs_to_ints(g.download().view("<u8").reshape(-1, 4))
+
+
+def test_ntt_2_28_maximum_size_closed_form(gpu_ctx):
+    """The largest domain (2^28, the 2-adicity of r, crypto/poly/ntt.py:9): input a_i = b^i
+    generated on the device, whose transforms have closed forms -- forward
+    sum_i (b w^k)^i = (b^n - 1) / (b w^k - 1), coset with s: the same with b s -- checked
+    exactly at sampled indices; then the inverse brings the input back (sampled)."""
+    log_n = 28
+    n = 1 << log_n
+    om = O.omega_for_size(n)
+    b, s = 0x1234567890ABCDEF1234567, 5
+    a = gpu_ctx.alloc(n * 32)
+    gpu_ctx.fr_powers(a, b, n)  # Montgomery b^i
+    ev = gpu_ctx.alloc(n * 32)
+    rng = np.random.default_rng(28)
+    idx = [0, 1, n // 2, n - 1] + [int(x) for x in rng.integers(0, n, 28)]
+    for mode, base in ((N.NTT_EVALS_FROM_COEFFS, b), (N.NTT_COSET_EVALS_FROM_COEFFS, b * s % R)):
+        gpu_ctx.ntt(mode, ev, a, n, log_n, om, s if mode == N.NTT_COSET_EVALS_FROM_COEFFS else 1)
+        got = _gather_canonical(gpu_ctx, ev, idx)
+        num = (pow(base, n, R) - 1) % R
+        for k, g in zip(idx, got):
+            assert g == num * pow((base * pow(om, k, R) - 1) % R, R - 2, R) % R, (mode, k)
+    # forward then inverse (coset pair) restores the powers
+    gpu_ctx.ntt(N.NTT_COSET_COEFFS_FROM_EVALS, ev, ev, n, log_n, om, s)
+    back = _gather_canonical(gpu_ctx, ev, idx)
+    assert back == [pow(b, k, R) for k in idx]
+
+
 def test_ntt_coset_zero_shift_and_other_shift(gpu_ctx):
     n = 64
     v = synth.fr_uniform(99, n)
@@ -281,6 +315,25 @@ def test_msm_2_20_known_answer(gpu_ctx):
     m = 1000
     exp2 = O.affine_to_ints(O.msm_known_answer(k[7:7 + m], s[:m]))
     assert gpu_ctx.msm_g1(bases, ds, m, offset=7) == exp2
+
+
+def test_msm_2_24_known_answer(gpu_ctx):
+    """A large MSM (2^24 points: 2^25 GLV halves x 8 windows = 2^28 CSR entries) against the
+    known answer; bases generated on the device."""
+    log_n = 24
+    n = 1 << log_n
+    seed = synth.seed_for(2, log_n)
+    k = synth.base_dlogs(seed, n)
+    s = synth.fr_uniform(seed, n)
+    dk = gpu_ctx.to_device(k)
+    dxy = gpu_ctx.alloc(n * 64)
+    gpu_ctx.g1_fixed_base_mul((1, 2), dk, n, dxy)
+    del dk
+    bases = gpu_ctx.bases_from_device(dxy, n)
+    del dxy
+    ds = gpu_ctx.to_device(s)
+    gpu_ctx.fr_to_mont(ds, ds, n)
+    assert gpu_ctx.msm_g1(bases, ds, n) == O.affine_to_ints(O.msm_known_answer(k, s))
 
 
 def test_msm_g1_host_one_call(gpu_ctx):
