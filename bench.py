@@ -434,7 +434,7 @@ def run_gpu_ntt(ctx, args, ranks, log_n, flush, imad_tops, hbm_peak, brief=False
 
 
 def run_gpu_ntt_sweep(ctx, args, flush, sizes=(12, 16, 20, 22)) -> dict:
-    """Config 1: the four transforms (ROOTS_/COSET_ EVALS/COEFFS, shift 5) at every size,
+    """The four transforms (ROOTS_/COSET_ EVALS/COEFFS, shift 5) at 2^12..2^22,
     device-resident Montgomery data, L2 flushed before each step (median of the steps)."""
     from pyzkp_gb300 import _native as N
     from pyzkp_gb300 import synth

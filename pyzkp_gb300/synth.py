@@ -22,9 +22,10 @@ FQ_MODULUS = 2188824287183927522224640574525727508869631115729782366268903789464
 _MASK62 = np.uint64((1 << 62) - 1)
 
 
-def seed_for(config_index: int, log_n: int) -> int:
-    """Seed convention of the measured configurations: 0xC0FFEE + 1000*config + log2(n)."""
-    return 0xC0FFEE + 1000 * int(config_index) + int(log_n)
+def seed_for(family: int, log_n: int) -> int:
+    """Seed of a synthetic input: 0xC0FFEE + 1000*family + log2(n), with the workload family
+    0 = the 4096-point MSM case, 1 = NTTs, 2 = MSM sweeps, 3 = batches, 5 = PLONK quotient."""
+    return 0xC0FFEE + 1000 * int(family) + int(log_n)
 
 
 def int_to_limbs(v: int) -> np.ndarray:

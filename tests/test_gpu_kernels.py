@@ -401,6 +401,21 @@ def test_msm_glv_edge_scalars(gpu_ctx):
         assert got == O.affine_to_ints(O.msm_known_answer(k[:1], one)), hex(v)
 
 
+def test_msm_canonical_scalars_at_or_above_r(gpu_ctx):
+    """Canonical scalars are reduced mod r first, as msm_pippenger does (s % FR_MODULUS,
+    crypto/msm/pippenger.py:28): r, r + 1, 2r - 1, 2^256 - 1 and friends give the MSM of
+    their residues."""
+    vals = [R, R + 1, 2 * R - 1, 2 * R, 3 * R + 12345, (1 << 256) - 1, (1 << 255) + 7, R - 1]
+    n = len(vals)
+    k = synth.base_dlogs(777, n)
+    bases = O.g1_fixed_base_mul(O.G1_GENERATOR, k)
+    raw = synth.ints_to_limbs(vals)
+    red = synth.ints_to_limbs([v % R for v in vals])
+    exp = O.affine_to_ints(O.msm_known_answer(k, red))
+    assert gpu_msm(gpu_ctx, bases, raw, mont=False) == exp
+    assert gpu_ctx.msm_g1_host(bases, raw, n) == exp
+
+
 def test_msm_empty_and_errors(gpu_ctx):
     bases = gpu_ctx.bases_from_host(O.g1_fixed_base_mul(O.G1_GENERATOR, synth.base_dlogs(1, 4)))
     ds = gpu_ctx.to_device(synth.fr_uniform(1, 4))
