@@ -32,6 +32,25 @@ def test_library_exports_every_declared_symbol():
         assert re.search(rf"\bT {name}\b", out), name
 
 
+def test_header_is_plain_c_and_links(tmp_path):
+    """include/zkgpu.h compiles as strict C99 and every declared entry point links against the
+    library (what a cgo / FFI binding of the reference's side would do); nothing is called."""
+    names = _header_symbols()
+    src = tmp_path / "abi.c"
+    refs = ",\n    ".join(f"(void (*)(void)){n}" for n in names)
+    src.write_text('#include "zkgpu.h"\n#include <stdio.h>\n'
+                   f"void (*const zk_all[])(void) = {{\n    {refs}\n}};\n"
+                   "int main(void) { printf(\"%d\\n\", (int)(sizeof zk_all / sizeof zk_all[0])); return 0; }\n")
+    lib_dir = os.path.dirname(N.LIB_PATH)
+    lib_name = os.path.basename(N.LIB_PATH)[3:-3]  # libX.so -> X
+    exe = tmp_path / "abi"
+    res = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                          "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe), "-L", lib_dir,
+                          f"-l{lib_name}", f"-Wl,-rpath,{lib_dir}"], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    assert len(names) > 60
+
+
 def test_null_arguments_map_to_value_error():
     L = N.load()
     with pytest.raises(ValueError):
