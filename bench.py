@@ -730,9 +730,9 @@ def run_gpu_plonk(ctx, args, flush, log_n: int = 20) -> dict:
     """The PLONK quotient step of protocols/plonk/prove.py:319-420 at n = 2^log_n, extended
     domain m = 4n: 15 coset NTTs of the n-coefficient polynomials to m evaluations (z also at
     shift * omega_n), PLONK_T_QUOTIENT_EVALS, BATCH_INV of Z_H, POINTWISE_MUL and the coset
-    iNTT of t -- as device calls, inputs resident, L2 flushed before each step. Sampled
-    quotient numerators and Z_H values are checked against the oracle formula."""
-    from oracle import oracle as O
+    iNTT of t -- as device calls, inputs resident, L2 flushed before each step. The 15
+    evaluation vectors, the numerators and Z_H are gathered at 16 indices into the private
+    key ``_samples``; the CPU baseline leg checks them (``cpu_check_plonk``) and drops the key."""
     from pyzkp_gb300 import _native as N
     from pyzkp_gb300 import synth
 
@@ -781,15 +781,10 @@ def run_gpu_plonk(ctx, args, flush, log_n: int = 20) -> dict:
         ctx.fr_gather(g, src, didx, idx.size)
         ctx.fr_from_mont(g, g, idx.size)
         got.append(synth.limbs_to_ints(g.download().view("<u8").reshape(-1, 4)))
-    ok = True
-    for s_i, i in enumerate(idx):
-        vecs = [[got[j][s_i]] for j in range(15)]
-        x = shift * pow(om_m, int(i), R) % R
-        e_num, _ = O.plonk_t_quotient_evals(vecs, n, om_m, x, shift_n, alpha, beta, gamma, k1, k2)
-        e_zh = (shift_n * pow(pow(om_m, n, R), int(i), R) - 1) % R
-        ok = ok and e_num[0] == got[15][s_i] and e_zh == got[16][s_i]
+    samples = {"idx": [int(i) for i in idx], "got": got, "n": n, "om_m": om_m, "shift": shift,
+               "shift_n": shift_n, "params": (alpha, beta, gamma, k1, k2)}
     return {"n": n, "m": m, "ms": round(ms, 3), "Melem_s_extended": round(m / (ms * 1e-3) / 1e6, 1),
-            "steps": steps, "sampled_check_ok": ok,
+            "steps": steps, "sampled_check_ok": None, "_samples": samples,
             "work": "15 coset NTTs n -> 4n (one batched call), quotient evals, batch inverse, product, coset iNTT"}
 
 
@@ -890,6 +885,26 @@ def cpu_ntt_sample(log_n: int, budget_s: float = 5.0):
     return n * runs / el / 1e6, runs, el
 
 
+def cpu_check_plonk(samples: dict) -> bool:
+    """Checks the GPU arm's gathered PLONK quotient samples: at each sampled index i the
+    numerator is the oracle formula applied to the 15 gathered evaluations at
+    x = shift * omega_m^i, and Z_H(x) = shift^n * omega_m^(n i) - 1."""
+    from oracle import oracle as O
+    from pyzkp_gb300 import synth
+
+    R = synth.FR_MODULUS
+    got, n, om_m = samples["got"], samples["n"], samples["om_m"]
+    alpha, beta, gamma, k1, k2 = samples["params"]
+    ok = True
+    for s_i, i in enumerate(samples["idx"]):
+        vecs = [[got[j][s_i]] for j in range(15)]
+        x = samples["shift"] * pow(om_m, i, R) % R
+        e_num, _ = O.plonk_t_quotient_evals(vecs, n, om_m, x, samples["shift_n"], alpha, beta, gamma, k1, k2)
+        e_zh = (samples["shift_n"] * pow(pow(om_m, n, R), i, R) - 1) % R
+        ok = ok and e_num[0] == got[15][s_i] and e_zh == got[16][s_i]
+    return ok
+
+
 def cpu_baseline(log_n: int, gpu_result) -> dict:
     """CPU baseline leg (rank 0, N=1): the oracle port timed on a bounded sample; it also
     checks the GPU arm's MSM result against the known answer [sum k_i s_i]G."""
@@ -957,8 +972,13 @@ def main() -> None:
             return
         res = run_gpu(args, ranks)
         if ranks.rank == 0:
+            plonk = res.get("plonk_quotient_2_20") or {}
+            samples = plonk.pop("_samples", None)
             if ranks.world == 1 and not args.no_cpu_baseline:
-                res["cpu_baseline"] = cpu_baseline(args.log_n, res.get("msm_result"))
+                if args.only in ("all", "msm"):
+                    res["cpu_baseline"] = cpu_baseline(args.log_n, res.get("msm_result"))
+                if samples is not None:
+                    plonk["sampled_check_ok"] = cpu_check_plonk(samples)
             print(json.dumps(res), flush=True)
     finally:
         ranks.close()
