@@ -307,6 +307,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
     ntt = run_gpu_ntt(ctx, args, ranks, 20, flush, imad_tops, hbm_peak)
     ntt22 = run_gpu_ntt(ctx, args, ranks, 22, flush, imad_tops, hbm_peak, brief=True)
     clocks = sampler.stop()
+    msm_4096 = run_gpu_msm_4096(ctx, args, flush) if ranks.world == 1 else None
     sweep = run_gpu_msm_sweep(ctx, args, flush) if ranks.world == 1 else None
     fixed = run_gpu_fixed_base(ctx, args, flush) if ranks.world == 1 else None
     fixed_sweep = ({f"2^{lg}": run_gpu_fixed_base(ctx, args, flush, log_n=lg) for lg in range(16, 23)}
@@ -346,6 +347,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
         "roofline": roofline,
         "ntt": ntt,
         "ntt_2_22": ntt22,
+        "msm_2_12": msm_4096,
         "msm_sweep": sweep,
         "msm_fixed_base_2_20": fixed,
         "msm_fixed_base_sweep": fixed_sweep,
@@ -554,6 +556,50 @@ def run_gpu_msm_sweep(ctx, args, flush, sizes=(16, 17, 18, 19, 20, 21, 22)) -> d
         out[f"2^{log_n}"] = row
         bases.free()
     return out
+
+
+def run_gpu_msm_4096(ctx, args, flush, steps: int = 50) -> dict:
+    """The 4096-point G1 MSM the reference runs on CPU (bases [k_i]G, uniform scalars, seed
+    family 0): device time with resident inputs, and end to end through zk_msm_g1_host from
+    pinned host memory. The result goes to the CPU baseline leg for the known-answer check."""
+    from pyzkp_gb300 import synth
+
+    log_n = 12
+    n = 1 << log_n
+    seed = synth.seed_for(0, log_n)
+    k, s = synth.base_dlogs(seed, n), synth.fr_uniform(seed, n)
+    dk = ctx.to_device(k)
+    xy = ctx.alloc(n * 64)
+    ctx.g1_fixed_base_mul((1, 2), dk, n, xy)
+    bases = ctx.bases_from_device(xy, n)
+    pin_xy = ctx.pinned(n * 64)
+    pin_xy.array[:] = xy.download().view(np.uint8).reshape(-1)
+    pin_s = ctx.pinned(n * 32)
+    pin_s.array[:] = s.view(np.uint8).reshape(-1)
+    ds = ctx.to_device(s)
+    ctx.fr_to_mont(ds, ds, n)
+
+    def timed(step):
+        for _ in range(max(3, args.warmup)):
+            r = step()
+        ts = []
+        for _ in range(steps):
+            ctx.memset(flush, 1)
+            ctx.timer_start()
+            step()
+            ts.append(ctx.timer_stop())
+        return statistics.median(ts), r
+
+    ms, res = timed(lambda: ctx.msm_g1(bases, ds, n))
+    e2e_ms, res_host = timed(lambda: ctx.msm_g1_host(pin_xy, pin_s, n))
+    bases.free()
+    return {"n": n, "seed": seed, "ms": round(ms, 4), "Mpts_s": round(n / (ms * 1e-3) / 1e6, 2),
+            "e2e": {"ms": round(e2e_ms, 4), "Mpts_s": round(n / (e2e_ms * 1e-3) / 1e6, 2),
+                    "h2d_bytes_per_step": n * 96, "d2h_bytes_per_step": 64 + 4,
+                    "path": "zk_msm_g1_host(pinned host affine points, pinned canonical scalars)"},
+            "steps": steps, "device_equals_host_call": res == res_host,
+            "msm_result": [hex(res[0]), hex(res[1])] if res else None,
+            "l2": "flushed (256 MB memset) before every timed step"}
 
 
 def run_gpu_fixed_base(ctx, args, flush, log_n: int = 20, calls: int = 16) -> dict:
@@ -905,6 +951,32 @@ def cpu_check_plonk(samples: dict) -> bool:
     return ok
 
 
+def cpu_msm_4096(gpu_row: dict, budget_s: float = 3.0) -> dict:
+    """The 4096-point MSM on the host: the C restatement of crypto/msm/pippenger.py with the
+    reference's window rule, timed over repeated runs, and the GPU arm's result against the
+    known answer [sum k_i s_i]G and against this Pippenger."""
+    from oracle import oracle as O
+    from pyzkp_gb300 import synth
+
+    n, seed = gpu_row["n"], gpu_row["seed"]
+    k, s = synth.base_dlogs(seed, n), synth.fr_uniform(seed, n)
+    bases = O.g1_fixed_base_mul(O.G1_GENERATOR, k)
+    w = O.msm_window_rule(n)
+    runs, t0 = 0, time.perf_counter()
+    while True:
+        got = O.msm_pippenger(bases, s, w)
+        runs += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s:
+            break
+    pip = O.affine_to_ints(got)
+    known = O.affine_to_ints(O.msm_known_answer(k, s))
+    return {"value": round(n * runs / el / 1e6, 4), "unit": "Mpts/s", "ms": round(el / runs * 1e3, 3),
+            "window_bits": w, "runs": runs,
+            "gpu_result_matches_known_answer": [hex(known[0]), hex(known[1])] == gpu_row["msm_result"],
+            "pippenger_matches_known_answer": pip == known}
+
+
 def cpu_baseline(log_n: int, gpu_result) -> dict:
     """CPU baseline leg (rank 0, N=1): the oracle port timed on a bounded sample; it also
     checks the GPU arm's MSM result against the known answer [sum k_i s_i]G."""
@@ -977,6 +1049,8 @@ def main() -> None:
             if ranks.world == 1 and not args.no_cpu_baseline:
                 if args.only in ("all", "msm"):
                     res["cpu_baseline"] = cpu_baseline(args.log_n, res.get("msm_result"))
+                if res.get("msm_2_12"):
+                    res["cpu_baseline"]["msm_2_12"] = cpu_msm_4096(res["msm_2_12"])
                 if samples is not None:
                     plonk["sampled_check_ok"] = cpu_check_plonk(samples)
             print(json.dumps(res), flush=True)
