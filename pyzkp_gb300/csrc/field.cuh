@@ -664,9 +664,332 @@ __device__ __forceinline__ fe2 fe_mul2(const fe& a, const fe& b, const fe& c, co
     return r;
 }
 
+// ---- separated forms: a 512-bit product, then one Montgomery reduction -------------------
+//
+// Splitting the product from the reduction lets a square skip the 28 repeated cross
+// products (36 instead of 64 partial products) and lets a difference of two products
+// a b - c d share one reduction. They serve the lazy Fq of the curve formulas only.
+//
+// Reduction: for T = T_lo + 2^256 T_hi, the m_i of the Montgomery rows depend on T_lo alone,
+// so (T + M p) / 2^256 = T_hi + (T_lo + M p) / 2^256; the second term is a CIOS reduction of
+// the low 8 limbs (a 9-limb window, no carry beyond it) and is at most p. With T < 4p^2
+// (a product of two values below 2p) T_hi < 0.76 p, so the result stays below 2p; with
+// T < 8p^2 (a sum of two such products) it is below 2.52 p and one conditional subtraction
+// of 2p brings it below 2p (both moduli are below 0.19 * 2^256).
+//
+// The carry flag primitives are one PTX instruction each on the device (asm volatile keeps
+// their order, so the flag flows from one to the next as in a single asm block); on the
+// host they emulate the flag, so the same code runs in a host-side check of the arithmetic.
+#ifndef __CUDA_ARCH__
+inline uint32_t& host_carry_flag() {
+    static thread_local uint32_t cc = 0;
+    return cc;
+}
+#endif
+
+__host__ __device__ __forceinline__ uint32_t u_add_cc(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm volatile("add.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+#else
+    const uint64_t s = (uint64_t)a + b;
+    host_carry_flag() = (uint32_t)(s >> 32);
+    return (uint32_t)s;
+#endif
+}
+
+__host__ __device__ __forceinline__ uint32_t u_addc_cc(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm volatile("addc.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+#else
+    const uint64_t s = (uint64_t)a + b + host_carry_flag();
+    host_carry_flag() = (uint32_t)(s >> 32);
+    return (uint32_t)s;
+#endif
+}
+
+__host__ __device__ __forceinline__ uint32_t u_addc(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm volatile("addc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+#else
+    return (uint32_t)((uint64_t)a + b + host_carry_flag());
+#endif
+}
+
+__host__ __device__ __forceinline__ uint32_t u_sub_cc(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm volatile("sub.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+#else
+    host_carry_flag() = a < b ? 1u : 0u;
+    return a - b;
+#endif
+}
+
+__host__ __device__ __forceinline__ uint32_t u_subc_cc(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm volatile("subc.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+#else
+    const uint64_t d = (uint64_t)a - b - host_carry_flag();
+    host_carry_flag() = (uint32_t)(d >> 63);
+    return (uint32_t)d;
+#endif
+}
+
+__host__ __device__ __forceinline__ uint32_t u_subc(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm volatile("subc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+#else
+    return (uint32_t)((uint64_t)a - b - host_carry_flag());
+#endif
+}
+
+__host__ __device__ __forceinline__ uint32_t lo32(uint64_t x) { return (uint32_t)x; }
+__host__ __device__ __forceinline__ uint32_t hi32(uint64_t x) { return (uint32_t)(x >> 32); }
+
+// Row I of t += a * b_I with a below 2^255: the low halves of a_j b_I into t_{I+j} (carry
+// into t_{I+8}), the high halves into t_{I+j+1}. FIRST: t_{I..I+8} are not yet written
+// (the first product's rows). Two products accumulated row by row stay below
+// 2 * 2^255 * 2^(32(I+1)) = 2^(32(I+9)), so nothing carries out of t_{I+8}.
+template <int I, bool FIRST>
+__host__ __device__ __forceinline__ void sos_row(uint32_t* t, const uint32_t* a, uint32_t bi) {
+    uint64_t p[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) p[j] = (uint64_t)a[j] * bi;
+    if constexpr (FIRST && I == 0) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) t[j] = lo32(p[j]);
+        t[1] = u_add_cc(t[1], hi32(p[0]));
+#pragma unroll
+        for (int j = 1; j < 7; j++) t[j + 1] = u_addc_cc(t[j + 1], hi32(p[j]));
+        t[8] = u_addc(0u, hi32(p[7]));
+        return;
+    }
+    t[I] = u_add_cc(t[I], lo32(p[0]));
+#pragma unroll
+    for (int j = 1; j < 8; j++) t[I + j] = u_addc_cc(t[I + j], lo32(p[j]));
+    if constexpr (FIRST) t[I + 8] = u_addc(0u, 0u);
+    else t[I + 8] = u_addc(t[I + 8], 0u);
+    t[I + 1] = u_add_cc(t[I + 1], hi32(p[0]));
+#pragma unroll
+    for (int j = 1; j < 7; j++) t[I + j + 1] = u_addc_cc(t[I + j + 1], hi32(p[j]));
+    t[I + 8] = u_addc(t[I + 8], hi32(p[7]));
+}
+
+// Row I of the cross products a_I a_j (j > I) into t_{I+j}: 7 - I products.
+template <int I>
+__host__ __device__ __forceinline__ void sqr_cross_row(uint32_t* t, const uint32_t* a) {
+    constexpr int L = 7 - I;
+    uint64_t p[8];
+#pragma unroll
+    for (int j = I + 1; j < 8; j++) p[j] = (uint64_t)a[I] * a[j];
+    if constexpr (I == 0) {
+#pragma unroll
+        for (int j = 1; j < 8; j++) t[j] = lo32(p[j]);
+        t[2] = u_add_cc(t[2], hi32(p[1]));
+#pragma unroll
+        for (int j = 2; j < 7; j++) t[j + 1] = u_addc_cc(t[j + 1], hi32(p[j]));
+        t[8] = u_addc(0u, hi32(p[7]));
+        return;
+    }
+    // low halves: t_{2I+1} .. t_{I+7}, carry into t_{I+8} (not yet written)
+    t[2 * I + 1] = u_add_cc(t[2 * I + 1], lo32(p[I + 1]));
+#pragma unroll
+    for (int j = I + 2; j < 8; j++) t[I + j] = u_addc_cc(t[I + j], lo32(p[j]));
+    t[I + 8] = u_addc(0u, 0u);
+    // high halves: t_{2I+2} .. t_{I+8}
+    if constexpr (L == 1) {
+        t[I + 8] = t[I + 8] + hi32(p[7]);
+    } else {
+        t[2 * I + 2] = u_add_cc(t[2 * I + 2], hi32(p[I + 1]));
+#pragma unroll
+        for (int j = I + 2; j < 7; j++) t[I + j + 1] = u_addc_cc(t[I + j + 1], hi32(p[j]));
+        t[I + 8] = u_addc(t[I + 8], hi32(p[7]));
+    }
+}
+
+// t[0..15] = a * a: the cross products once, doubled, plus the squares a_i^2 at limb 2i.
+__host__ __device__ __forceinline__ void sos_sqr_wide(uint32_t* t, const uint32_t* a) {
+    sqr_cross_row<0>(t, a);
+    sqr_cross_row<1>(t, a);
+    sqr_cross_row<2>(t, a);
+    sqr_cross_row<3>(t, a);
+    sqr_cross_row<4>(t, a);
+    sqr_cross_row<5>(t, a);
+    sqr_cross_row<6>(t, a);
+    // t_1 .. t_14 hold the cross sum (below a^2 / 2 < 2^511); double it into t_1 .. t_15
+    t[1] = u_add_cc(t[1], t[1]);
+#pragma unroll
+    for (int j = 2; j < 15; j++) t[j] = u_addc_cc(t[j], t[j]);
+    t[15] = u_addc(0u, 0u);
+    uint64_t d[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) d[i] = (uint64_t)a[i] * a[i];
+    t[0] = lo32(d[0]);
+    t[1] = u_add_cc(t[1], hi32(d[0]));
+#pragma unroll
+    for (int i = 1; i < 7; i++) {
+        t[2 * i] = u_addc_cc(t[2 * i], lo32(d[i]));
+        t[2 * i + 1] = u_addc_cc(t[2 * i + 1], hi32(d[i]));
+    }
+    t[14] = u_addc_cc(t[14], lo32(d[7]));
+    t[15] = u_addc(t[15], hi32(d[7]));
+}
+
+// r = T_hi + (T_lo + M p) / 2^256 for t = T (16 limbs): T * 2^-256 mod p, below T_hi + p + 1.
+template <class F>
+__host__ __device__ __forceinline__ fe sos_redc(const uint32_t* t) {
+    uint32_t w[9];
+#pragma unroll
+    for (int j = 0; j < 8; j++) w[j] = t[j];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const uint32_t m = w[0] * F::INV;
+        uint64_t q[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) q[j] = (uint64_t)m * F::P(j);
+        w[0] = u_add_cc(w[0], lo32(q[0]));
+#pragma unroll
+        for (int j = 1; j < 8; j++) w[j] = u_addc_cc(w[j], lo32(q[j]));
+        w[8] = u_addc(0u, 0u);
+        w[1] = u_add_cc(w[1], hi32(q[0]));
+#pragma unroll
+        for (int j = 1; j < 7; j++) w[j + 1] = u_addc_cc(w[j + 1], hi32(q[j]));
+        w[8] = u_addc(w[8], hi32(q[7]));
+        // w_0 == 0 now (m was chosen so); shift one limb
+#pragma unroll
+        for (int j = 0; j < 8; j++) w[j] = w[j + 1];
+    }
+    fe r;
+    r.v[0] = u_add_cc(w[0], t[8]);
+#pragma unroll
+    for (int j = 1; j < 7; j++) r.v[j] = u_addc_cc(w[j], t[j + 8]);
+    r.v[7] = u_addc(w[7], t[15]);
+    return r;
+}
+
+// 2p - c for c in [0, 2p): in (0, 2p], congruent to -c
+template <class F>
+__host__ __device__ __forceinline__ fe sos_neg2p(const fe& c) {
+    fe r;
+    r.v[0] = u_sub_cc(p2_limb<F>(0), c.v[0]);
+#pragma unroll
+    for (int j = 1; j < 7; j++) r.v[j] = u_subc_cc(p2_limb<F>(j), c.v[j]);
+    r.v[7] = u_subc(p2_limb<F>(7), c.v[7]);
+    return r;
+}
+
+// r = t - 2p if t >= 2p else t, for t < 4p (the host-and-device twin of fe_reduce_2p)
+template <class F>
+__host__ __device__ __forceinline__ fe sos_reduce_2p(const fe& t) {
+    fe s;
+    s.v[0] = u_sub_cc(t.v[0], p2_limb<F>(0));
+#pragma unroll
+    for (int j = 1; j < 8; j++) s.v[j] = u_subc_cc(t.v[j], p2_limb<F>(j));
+    const uint32_t borrow = u_subc(0u, 0u);
+    fe r;
+#pragma unroll
+    for (int j = 0; j < 8; j++) r.v[j] = borrow ? t.v[j] : s.v[j];
+    return r;
+}
+
+// a^2 * 2^-256 mod p in [0, 2p) for a in [0, 2p)
+template <class F>
+__host__ __device__ __forceinline__ fe fe_sqr_sos(const fe& a) {
+    static_assert(F::LAZY, "the separated forms keep lazy values");
+    uint32_t t[16];
+    sos_sqr_wide(t, a.v);
+    return sos_redc<F>(t);
+}
+
+// (a b + c d) * 2^-256 mod p in [0, 2p) for inputs in [0, 2p] (one reduction)
+template <class F>
+__host__ __device__ __forceinline__ fe fe_mul_add_sos(const fe& a, const fe& b, const fe& c, const fe& d) {
+    static_assert(F::LAZY, "the separated forms keep lazy values");
+    uint32_t t[16];
+    sos_row<0, true>(t, a.v, b.v[0]);
+    sos_row<0, false>(t, c.v, d.v[0]);
+    sos_row<1, true>(t, a.v, b.v[1]);
+    sos_row<1, false>(t, c.v, d.v[1]);
+    sos_row<2, true>(t, a.v, b.v[2]);
+    sos_row<2, false>(t, c.v, d.v[2]);
+    sos_row<3, true>(t, a.v, b.v[3]);
+    sos_row<3, false>(t, c.v, d.v[3]);
+    sos_row<4, true>(t, a.v, b.v[4]);
+    sos_row<4, false>(t, c.v, d.v[4]);
+    sos_row<5, true>(t, a.v, b.v[5]);
+    sos_row<5, false>(t, c.v, d.v[5]);
+    sos_row<6, true>(t, a.v, b.v[6]);
+    sos_row<6, false>(t, c.v, d.v[6]);
+    sos_row<7, true>(t, a.v, b.v[7]);
+    sos_row<7, false>(t, c.v, d.v[7]);
+    return sos_reduce_2p<F>(sos_redc<F>(t));
+}
+
+// (a b - c d) * 2^-256 mod p in [0, 2p) for inputs in [0, 2p): a b + (2p - c) d
+template <class F>
+__host__ __device__ __forceinline__ fe fe_mul_sub_sos(const fe& a, const fe& b, const fe& c, const fe& d) {
+    return fe_mul_add_sos<F>(a, b, sos_neg2p<F>(c), d);
+}
+
+template <class F>
+__device__ __noinline__ fe fe_sqr_sos_call(const fe a) {
+    return fe_sqr_sos<F>(a);
+}
+
+template <class F>
+__device__ __noinline__ fe fe_mul_add_sos_call(const fe a, const fe b, const fe c, const fe d) {
+    return fe_mul_add_sos<F>(a, b, c, d);
+}
+
+template <class F>
+__device__ __noinline__ fe fe_mul_sub_sos_call(const fe a, const fe b, const fe c, const fe d) {
+    return fe_mul_sub_sos<F>(a, b, c, d);
+}
+
+// The separated forms are used for the lazy fields with the called multiplication (style
+// 3: the curve formulas over Fq); ZK_NO_SOS keeps every product on fe_mul for comparison.
+template <class F>
+__device__ __forceinline__ constexpr bool use_sos() {
+#if defined(ZK_NO_SOS)
+    return false;
+#else
+#ifdef ZK_MUL_STYLE
+    constexpr int style = ZK_MUL_STYLE;
+#else
+    constexpr int style = F::MUL_STYLE;
+#endif
+    return F::LAZY && style == 3;
+#endif
+}
+
 template <class F>
 __device__ __forceinline__ fe fe_sqr(const fe& a) {
-    return fe_mul<F>(a, a);
+    if constexpr (use_sos<F>()) return fe_sqr_sos_call<F>(a);
+    else return fe_mul<F>(a, a);
+}
+
+// a b - c d, and a b + c d (inputs in the field's representation)
+template <class F>
+__device__ __forceinline__ fe fe_mul_sub(const fe& a, const fe& b, const fe& c, const fe& d) {
+    if constexpr (use_sos<F>()) return fe_mul_sub_sos_call<F>(a, b, c, d);
+    else return fe_sub<F>(fe_mul<F>(a, b), fe_mul<F>(c, d));
+}
+
+template <class F>
+__device__ __forceinline__ fe fe_mul_add(const fe& a, const fe& b, const fe& c, const fe& d) {
+    if constexpr (use_sos<F>()) return fe_mul_add_sos_call<F>(a, b, c, d);
+    else return fe_add<F>(fe_mul<F>(a, b), fe_mul<F>(c, d));
 }
 
 // canonical value (any 256-bit input, reduced mod p first) -> Montgomery form
