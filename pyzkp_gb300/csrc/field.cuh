@@ -614,9 +614,15 @@ __device__ __noinline__ fe fe_mul_call(const fe a, const fe b) {
 }
 
 template <class F>
+__host__ __device__ __forceinline__ fe fe_mul_sos(const fe& a, const fe& b);
+
+template <class F>
 __device__ __noinline__ fe fe_mul_wide_call(const fe a, const fe b) {
 #ifdef ZK_WIDE_ACC
     return fe_mul_acc_unrolled<F>(a, b);
+#elif defined(ZK_SOS_MUL)
+    if constexpr (F::LAZY) return fe_mul_sos<F>(a, b);
+    else return fe_mul_wide_unrolled<F>(a, b);
 #else
     return fe_mul_wide_unrolled<F>(a, b);
 #endif
@@ -909,6 +915,22 @@ __host__ __device__ __forceinline__ fe fe_sqr_sos(const fe& a) {
     static_assert(F::LAZY, "the separated forms keep lazy values");
     uint32_t t[16];
     sos_sqr_wide(t, a.v);
+    return sos_redc<F>(t);
+}
+
+// a b * 2^-256 mod p in [0, 2p) for a, b in [0, 2p): product rows, then the reduction
+template <class F>
+__host__ __device__ __forceinline__ fe fe_mul_sos(const fe& a, const fe& b) {
+    static_assert(F::LAZY, "the separated forms keep lazy values");
+    uint32_t t[16];
+    sos_row<0, true>(t, a.v, b.v[0]);
+    sos_row<1, true>(t, a.v, b.v[1]);
+    sos_row<2, true>(t, a.v, b.v[2]);
+    sos_row<3, true>(t, a.v, b.v[3]);
+    sos_row<4, true>(t, a.v, b.v[4]);
+    sos_row<5, true>(t, a.v, b.v[5]);
+    sos_row<6, true>(t, a.v, b.v[6]);
+    sos_row<7, true>(t, a.v, b.v[7]);
     return sos_redc<F>(t);
 }
 

@@ -1,4 +1,4 @@
-"""The separated Fq forms of field.cuh (square, a b + c d, a b - c d with one Montgomery
+"""The separated Fq forms of field.cuh (square, a b + c d, a b - c d, a b with one Montgomery
 reduction) built for the host and checked against Python integers: congruence with
 x * 2^-256 mod q and the lazy bound [0, 2q) on random inputs and on the edges of [0, 2q)."""
 
@@ -41,9 +41,9 @@ def test_separated_forms_match_integers(tmp_path):
     res = subprocess.run([str(exe), str(src), str(dst)], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
     raw = dst.read_bytes()
-    assert len(raw) == 96 * len(recs)
+    assert len(raw) == 128 * len(recs)
     for i, (a, b, c, d) in enumerate(recs):
-        sq, madd, msub = (int.from_bytes(raw[96 * i + 32 * k:96 * i + 32 * k + 32], "little") for k in range(3))
-        for got, want in ((sq, a * a), (madd, a * b + c * d), (msub, a * b - c * d)):
+        sq, madd, msub, mul = (int.from_bytes(raw[128 * i + 32 * k:128 * i + 32 * k + 32], "little") for k in range(4))
+        for got, want in ((sq, a * a), (madd, a * b + c * d), (msub, a * b - c * d), (mul, a * b)):
             assert got < 2 * Q, (i, a, b, c, d)
             assert got % Q == want * RINV % Q, (i, a, b, c, d)
