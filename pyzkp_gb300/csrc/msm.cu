@@ -58,9 +58,6 @@ static constexpr uint32_t kNone = 0xffffffffu;
 #ifndef ZK_MSM_BLOCKG
 #define ZK_MSM_BLOCKG 8
 #endif
-#ifndef ZK_ACC_MINB
-#define ZK_ACC_MINB 1  // minimum resident CTAs per SM asked of the accumulation kernel
-#endif
 #ifndef ZK_MSM_GROUP
 #define ZK_MSM_GROUP 4  // measured at 2^20 / 2^22: merge 0.73 / 1.36 ms with 16, 0.48 / 1.02 ms with 4
 #endif
@@ -477,7 +474,7 @@ __device__ __forceinline__ uint32_t bucket_of(const uint32_t* __restrict__ row_p
 }
 
 template <class C>
-__global__ void __launch_bounds__(128, ZK_ACC_MINB) msm_accumulate_kernel(const uint32_t* __restrict__ entries,
+__global__ void __launch_bounds__(128, C::kAccMinBlocks) msm_accumulate_kernel(const uint32_t* __restrict__ entries,
                                                              const uint32_t* __restrict__ d_total,
                                                              const uint32_t* __restrict__ row_ptr,
                                                              const MsmInst* __restrict__ insts, MsmShape sh,
