@@ -283,6 +283,9 @@ __device__ __forceinline__ void xyzz_store(XyzzT<T>* p, const XyzzT<T>& a) {
 #ifndef ZK_ACC_MINB
 #define ZK_ACC_MINB 4
 #endif
+#ifndef ZK_ACC_MINB_G2
+#define ZK_ACC_MINB_G2 1
+#endif
 struct CurveG1 {
     using T = fe;
     using A = affine_t;
@@ -296,7 +299,7 @@ struct CurveG2 {
     using A = affine2_t;
     using P = xyzz2_t;
     static constexpr int kTargetThreads = 128;  // 128 x 256-byte points of shared memory
-    static constexpr int kAccMinBlocks = 1;
+    static constexpr int kAccMinBlocks = ZK_ACC_MINB_G2;
 };
 
 }  // namespace zk
