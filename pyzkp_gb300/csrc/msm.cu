@@ -314,6 +314,10 @@ __device__ __forceinline__ uint32_t bits_at(const fe& s, uint32_t k, uint32_t c)
 }
 
 __device__ __forceinline__ void warp_aggregated_inc(uint32_t* counters, uint32_t key, bool active) {
+#ifdef ZK_SCATTER_PLAIN
+    if (active) atomicAdd(counters + key, 1u);
+    return;
+#endif
     const uint32_t live = __ballot_sync(0xffffffffu, active);
     if (!active) return;
     const uint32_t peers = __match_any_sync(live, key);
@@ -421,6 +425,10 @@ __global__ void msm_scatter_kernel(const fe* __restrict__ reduced, const MsmInst
             const uint32_t key = (set0 + (sh.shared ? 0u : w)) * sh.B + (d & 0x7fffffffu) - 1;
             // fixed-base: row w of the shifted bases; GLV: the phi(P) half for h = 1
             const uint32_t point = sh.shared ? w * stride + i : i + h * stride;
+#ifdef ZK_SCATTER_PLAIN
+            if (nz) entries[atomicAdd(cursor + key, 1u)] = point | ((d & 0x80000000u) ^ flip);
+            continue;
+#endif
             const uint32_t live = __ballot_sync(0xffffffffu, nz);
             if (nz) {
                 const uint32_t peers = __match_any_sync(live, key);
