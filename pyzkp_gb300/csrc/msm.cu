@@ -1096,7 +1096,10 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
 
 // A persistent pool of host threads for the combination step (created on first use,
 // never destroyed: its threads sleep between jobs). run() executes fn(0 .. count-1) on the
-// workers and the calling thread and returns when all are done; calls are serialised.
+// calling thread and on at most count - 1 woken workers, and returns when every task is
+// done -- not when every worker has woken: a late worker finds no task left and sleeps
+// again. Tasks are claimed from one atomic ticket (generation | count | next index), so a
+// worker can only claim a task of the run in progress; calls are serialised.
 class HostPool {
    public:
     static HostPool& get() {
@@ -1106,26 +1109,31 @@ class HostPool {
 
     void run(size_t count, const std::function<void(size_t)>& fn) {
         if (count == 0) return;
-        if (count == 1 || workers_ == 0) {
+        if (count == 1 || workers_ == 0 || count > kMaxTasks) {
             for (size_t i = 0; i < count; i++) fn(i);
             return;
         }
         std::lock_guard<std::mutex> serial(run_mu_);
+        gen_ = (gen_ + 1) & 0xffffu;
+        fn_ = &fn;
+        done_.store(0, std::memory_order_relaxed);
+        ticket_.store(gen_ << 48 | (uint64_t)count << 24, std::memory_order_release);
         {
             std::lock_guard<std::mutex> g(mu_);
-            fn_ = &fn;
-            count_ = count;
-            next_.store(0);
-            active_ = workers_;
-            gen_++;
+            wake_++;
         }
-        cv_.notify_all();
+        const size_t helpers = std::min(count - 1, workers_);
+        for (size_t i = 0; i < helpers; i++) cv_.notify_one();
         work();
-        std::unique_lock<std::mutex> g(mu_);
-        done_cv_.wait(g, [&] { return active_ == 0; });
+        if (done_.load(std::memory_order_acquire) < count) {
+            std::unique_lock<std::mutex> g(mu_);
+            done_cv_.wait(g, [&] { return done_.load(std::memory_order_acquire) >= count; });
+        }
     }
 
    private:
+    static constexpr size_t kMaxTasks = (1u << 24) - 1;
+
     HostPool() {
         const size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
         workers_ = std::min<size_t>(hw, 16) - 1;
@@ -1137,27 +1145,37 @@ class HostPool {
         for (;;) {
             {
                 std::unique_lock<std::mutex> g(mu_);
-                cv_.wait(g, [&] { return gen_ != seen; });
-                seen = gen_;
+                cv_.wait(g, [&] { return wake_ != seen; });
+                seen = wake_;
             }
             work();
-            std::lock_guard<std::mutex> g(mu_);
-            if (--active_ == 0) done_cv_.notify_one();
         }
     }
 
+    // Claim and run tasks while the ticket has some left. A successful claim of task i means
+    // the run that published the ticket is still waiting for task i, so fn_ is its function.
     void work() {
-        for (size_t i; (i = next_.fetch_add(1)) < count_;) (*fn_)(i);
+        for (;;) {
+            uint64_t cur = ticket_.load(std::memory_order_acquire);
+            const uint64_t count = (cur >> 24) & kMaxTasks, i = cur & kMaxTasks;
+            if (i >= count) return;
+            if (!ticket_.compare_exchange_weak(cur, cur + 1, std::memory_order_acq_rel)) continue;
+            (*fn_)(i);
+            if (done_.fetch_add(1, std::memory_order_acq_rel) + 1 == count) {
+                std::lock_guard<std::mutex> g(mu_);
+                done_cv_.notify_all();
+            }
+        }
     }
 
     size_t workers_ = 0;
     std::mutex run_mu_, mu_;
     std::condition_variable cv_, done_cv_;
     const std::function<void(size_t)>* fn_ = nullptr;
-    size_t count_ = 0;
-    std::atomic<size_t> next_{0};
-    size_t active_ = 0;
-    uint64_t gen_ = 0;
+    std::atomic<uint64_t> ticket_{0};
+    std::atomic<size_t> done_{0};
+    uint64_t wake_ = 0;  // under mu_
+    uint64_t gen_ = 0;   // under run_mu_
 };
 
 // Host: the sum S_w of window (or set) w of instance k from its targets:
