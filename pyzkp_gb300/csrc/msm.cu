@@ -1125,10 +1125,12 @@ class HostPool {
         const size_t helpers = std::min(count - 1, workers_);
         for (size_t i = 0; i < helpers; i++) cv_.notify_one();
         work();
-        if (done_.load(std::memory_order_acquire) < count) {
-            std::unique_lock<std::mutex> g(mu_);
-            done_cv_.wait(g, [&] { return done_.load(std::memory_order_acquire) >= count; });
-        }
+        // the tasks still running were claimed by awake workers; the wait re-checks every
+        // millisecond, so even a lost wakeup of the condition variable only costs that much
+        std::unique_lock<std::mutex> g(mu_);
+        while (done_.load(std::memory_order_acquire) < count)
+            done_cv_.wait_for(g, std::chrono::milliseconds(1),
+                              [&] { return done_.load(std::memory_order_acquire) >= count; });
     }
 
    private:
