@@ -144,17 +144,20 @@ uint32_t msm_auto_window(size_t n) {
 
 // GLV: the same rule over n scalars (2n half-scalars of 128 bits), lowered while the window
 // count stays the same (fewer buckets for the same entries: c = 14 -> 13, 12 stays).
-// Window size of the GLV split (halves of ~127 bits). Measured on GB300 for n = 2^8 .. 2^19
-// (G1, uniform scalars, every c from about log2(n) - 6 to log2(n)): the best c keeps the top
-// window well filled. A sparse top window (c = 9: 2 of its 9 bits used, c = 14: 2 of 14,
-// c = 15: 7 of 15) puts a large share of all points into a few buckets, whose pieces the
-// long-bucket fixup adds in trees of serial point additions (0.04 - 0.44 ms). Gains over the
-// earlier rule (log2(n) - 3, lowered while W stays): 2^8 -22%, 2^10 -19%, 2^12 -7%,
-// 2^13 -3.5%, 2^14 -2%, 2^17 -3%, 2^18 -5.4%.
+// Window size of the GLV split (halves of ~127 bits). Measured on GB300 for n = 2^8 .. 2^20
+// (G1, every c from about log2(n) - 6 to log2(n), uniform and witness-like scalars); the
+// table holds the c with the smallest product of the two times relative to their best.
+// A sparse top window (c = 9: 2 of its 9 bits used, c = 14: 2 of 14) puts a large share of
+// all points into a few buckets, and so do repeated small scalars (0 and 1 in witnesses);
+// the long-bucket fixup adds their pieces in trees of serial point additions (0.04 - 0.6
+// ms), which the merge rounds of larger c avoid. Against the earlier rule (log2(n) - 3,
+// lowered while W stays): uniform 2^8 -22%, 2^10 -19%, 2^12 -7%; witness-like 2^11 -10%,
+// 2^17 -27%, 2^18 -31% (uniform +3% / +6% there). From 2^19 on c = 16 stays (uniform
+// 2^19 / 2^20 best at 16, witness-like at 13 / 14).
 uint32_t msm_auto_window_glv(size_t n) {
     uint32_t lg = 0;
     while ((1ull << lg) < n) lg++;
-    static const uint8_t kMeasured[19] = {0, 0, 0, 0, 0, 0, 0, 0, 8, 8, 8, 8, 10, 13, 12, 13, 13, 16, 16};
+    static const uint8_t kMeasured[19] = {0, 0, 0, 0, 0, 0, 0, 0, 8, 8, 8, 9, 10, 11, 11, 13, 13, 13, 15};
     if (lg >= 8 && lg <= 18) return kMeasured[lg];
     uint32_t c = msm_auto_window(n);
     while (c > 4 && (128 + c - 2) / (c - 1) == (128 + c - 1) / c) c--;
