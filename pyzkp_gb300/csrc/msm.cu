@@ -585,7 +585,6 @@ static constexpr uint32_t kFixupMax = 8;
 #define ZK_FIXUP_DENSITY 96
 #endif
 static constexpr uint64_t kFixupDensity = ZK_FIXUP_DENSITY;  // CSR entries per bucket up to which the fixup is used
-static constexpr int kFixupLongThreads = 128;
 
 template <class C>
 __global__ void __launch_bounds__(128) msm_fixup_kernel(const uint32_t* __restrict__ row_ptr, uint32_t nbuckets,
@@ -611,14 +610,14 @@ __global__ void __launch_bounds__(128) msm_fixup_kernel(const uint32_t* __restri
 // One CTA per listed bucket (grid-stride over the list): strided partial sums, then a
 // shared-memory tree.
 template <class C>
-__global__ void __launch_bounds__(kFixupLongThreads) msm_fixup_long_kernel(const uint32_t* __restrict__ row_ptr,
+__global__ void __launch_bounds__(C::kFixupLongThreads) msm_fixup_long_kernel(const uint32_t* __restrict__ row_ptr,
                                                                            uint32_t seg,
                                                                            const typename C::P* __restrict__ slot_pts,
                                                                            typename C::P* __restrict__ buckets,
                                                                            const uint32_t* __restrict__ long_list,
                                                                            const uint32_t* __restrict__ long_count) {
     using P = typename C::P;
-    __shared__ P red[kFixupLongThreads];
+    __shared__ P red[C::kFixupLongThreads];
     const uint32_t count = *long_count;
     for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
         const uint32_t k = long_list[item];
@@ -1053,7 +1052,7 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
         ZK_LAUNCH(c, "msm_fixup", msm_fixup_kernel<C>, (unsigned)((p.nbuckets + 127) / 128), 128, 0, p.row_ptr,
                   (uint32_t)p.nbuckets, sh.seg, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
         ZK_TRY_CUDA(cudaGetLastError());
-        ZK_LAUNCH(c, "msm_fixup_long", msm_fixup_long_kernel<C>, (unsigned)(c->num_sms * 2), kFixupLongThreads, 0,
+        ZK_LAUNCH(c, "msm_fixup_long", msm_fixup_long_kernel<C>, (unsigned)(c->num_sms * 2), C::kFixupLongThreads, 0,
                   p.row_ptr, sh.seg, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
         ZK_TRY_CUDA(cudaGetLastError());
     } else {
