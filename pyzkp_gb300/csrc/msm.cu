@@ -622,12 +622,17 @@ __global__ void __launch_bounds__(C::kFixupLongThreads) msm_fixup_long_kernel(co
     for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
         const uint32_t k = long_list[item];
         const uint32_t u0 = row_ptr[k] / seg, u1 = (row_ptr[k + 1] - 1) / seg;
+        // the tree spans the next power of two of the pieces (at most the CTA): a bucket of 16
+        // segments takes 4 levels of serial additions, not log2(blockDim)
+        uint32_t width = 1;
+        while (width < u1 - u0 + 1 && width < blockDim.x) width <<= 1;
         P acc = xyzz_inf<typename C::T>();
-        for (uint32_t u = u0 + threadIdx.x; u <= u1; u += blockDim.x)
-            acc = xyzz_add(acc, xyzz_load(slot_pts + 2 * (size_t)u + (u == u0 ? 1 : 0)));
+        if (threadIdx.x < width)
+            for (uint32_t u = u0 + threadIdx.x; u <= u1; u += width)
+                acc = xyzz_add(acc, xyzz_load(slot_pts + 2 * (size_t)u + (u == u0 ? 1 : 0)));
         red[threadIdx.x] = acc;
         __syncthreads();
-        for (uint32_t off = blockDim.x / 2; off > 0; off >>= 1) {
+        for (uint32_t off = width / 2; off > 0; off >>= 1) {
             if (threadIdx.x < off) red[threadIdx.x] = xyzz_add(red[threadIdx.x], red[threadIdx.x + off]);
             __syncthreads();
         }
@@ -710,15 +715,20 @@ __global__ void __launch_bounds__(C::kTargetThreads) msm_targets_kernel(const ty
     const uint32_t per = (count + parts - 1) / parts;
     const uint32_t t0 = part * per, t1 = min(count, t0 + per);
     const uint32_t k = bits ? tg - sh.plain : 0;
+    // the tree spans the next power of two of this slice's terms (at most the CTA)
+    const uint32_t terms = t1 > t0 ? t1 - t0 : 0;
+    uint32_t width = 1;
+    while (width < terms && width < blockDim.x) width <<= 1;
     P acc = xyzz_inf<typename C::T>();
-    for (uint32_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-        uint32_t j = t;
-        if (bits) j = ((t >> k) << (k + 1)) | (1u << k) | (t & ((1u << k) - 1));
-        acc = xyzz_add(acc, xyzz_load(src + j));
-    }
+    if (threadIdx.x < width)
+        for (uint32_t t = t0 + threadIdx.x; t < t1; t += width) {
+            uint32_t j = t;
+            if (bits) j = ((t >> k) << (k + 1)) | (1u << k) | (t & ((1u << k) - 1));
+            acc = xyzz_add(acc, xyzz_load(src + j));
+        }
     red[threadIdx.x] = acc;
     __syncthreads();
-    for (uint32_t off = blockDim.x / 2; off > 0; off >>= 1) {
+    for (uint32_t off = width / 2; off > 0; off >>= 1) {
         if (threadIdx.x < off) red[threadIdx.x] = xyzz_add(red[threadIdx.x], red[threadIdx.x + off]);
         __syncthreads();
     }
@@ -735,11 +745,14 @@ __global__ void __launch_bounds__(kMergeThreads) msm_targets_merge_kernel(const 
     using P = typename C::P;
     __shared__ P red[kMergeThreads];
     const P* src = in + (size_t)blockIdx.x * parts;
+    uint32_t width = 1;
+    while (width < parts && width < blockDim.x) width <<= 1;
     P acc = xyzz_inf<typename C::T>();
-    for (uint32_t t = threadIdx.x; t < parts; t += blockDim.x) acc = xyzz_add(acc, xyzz_load(src + t));
+    if (threadIdx.x < width)
+        for (uint32_t t = threadIdx.x; t < parts; t += width) acc = xyzz_add(acc, xyzz_load(src + t));
     red[threadIdx.x] = acc;
     __syncthreads();
-    for (uint32_t off = blockDim.x / 2; off > 0; off >>= 1) {
+    for (uint32_t off = width / 2; off > 0; off >>= 1) {
         if (threadIdx.x < off) red[threadIdx.x] = xyzz_add(red[threadIdx.x], red[threadIdx.x + off]);
         __syncthreads();
     }
