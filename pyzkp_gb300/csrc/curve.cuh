@@ -288,11 +288,16 @@ __device__ __forceinline__ void xyzz_store(XyzzT<T>* p, const XyzzT<T>& a) {
 #endif
 // Threads of the CTA that sums one long bucket's pieces (strided partial sums, then a
 // shared-memory tree of the threads' partials); G2 points (256 B) keep it at 128 so that
-// the tree fits 32 KB of static shared memory. Measured on GB300 for G1 (witness-like
-// scalars, whose 0/1 values make one bucket of ~1600 segments): 0.51 ms with 256 threads
-// against 0.61 ms with 128, MSM 2^20 354 against 342 Mpts/s; uniform scalars unchanged.
+// the tree fits 32 KB of static shared memory. G1 runs 256 threads with two CTAs per SM
+// (128 registers, a few spilled): measured on GB300 the kernel takes 0.50 ms for the one
+// bucket of ~1600 segments that the 0/1 values of witness-like scalars make at 2^20 (MSM
+// 355 Mpts/s), against 0.54 ms with one 256-thread CTA per SM (350) and 0.66 ms with 128
+// threads (337); with ~500 long buckets of a 2^16 MSM it takes 0.080 / 0.121 / 0.084 ms.
 #ifndef ZK_FIXUP_LONG_G1
 #define ZK_FIXUP_LONG_G1 256
+#endif
+#ifndef ZK_FIXUP_LONG_MINB_G1
+#define ZK_FIXUP_LONG_MINB_G1 2
 #endif
 struct CurveG1 {
     using T = fe;
@@ -301,6 +306,7 @@ struct CurveG1 {
     static constexpr int kTargetThreads = 256;
     static constexpr int kAccMinBlocks = ZK_ACC_MINB;
     static constexpr int kFixupLongThreads = ZK_FIXUP_LONG_G1;
+    static constexpr int kFixupLongMinBlocks = ZK_FIXUP_LONG_MINB_G1;
 };
 
 struct CurveG2 {
@@ -310,6 +316,7 @@ struct CurveG2 {
     static constexpr int kTargetThreads = 128;  // 128 x 256-byte points of shared memory
     static constexpr int kAccMinBlocks = ZK_ACC_MINB_G2;
     static constexpr int kFixupLongThreads = 128;
+    static constexpr int kFixupLongMinBlocks = 1;
 };
 
 }  // namespace zk

@@ -610,7 +610,7 @@ __global__ void __launch_bounds__(128) msm_fixup_kernel(const uint32_t* __restri
 // One CTA per listed bucket (grid-stride over the list): strided partial sums, then a
 // shared-memory tree.
 template <class C>
-__global__ void __launch_bounds__(C::kFixupLongThreads) msm_fixup_long_kernel(const uint32_t* __restrict__ row_ptr,
+__global__ void __launch_bounds__(C::kFixupLongThreads, C::kFixupLongMinBlocks) msm_fixup_long_kernel(const uint32_t* __restrict__ row_ptr,
                                                                            uint32_t seg,
                                                                            const typename C::P* __restrict__ slot_pts,
                                                                            typename C::P* __restrict__ buckets,
