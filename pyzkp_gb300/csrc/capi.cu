@@ -167,6 +167,8 @@ int zk_ctx_destroy(zk_ctx* ctx) {
     for (cudaEvent_t ev : ctx->impl.side_events) cudaEventDestroy(ev);
     if (ctx->impl.copy_go) cudaEventDestroy(ctx->impl.copy_go);
     if (ctx->impl.copy_done) cudaEventDestroy(ctx->impl.copy_done);
+    for (cudaEvent_t ev : ctx->impl.chunk_ev)
+        if (ev) cudaEventDestroy(ev);
     cudaStreamDestroy(ctx->impl.stream);
     delete ctx;
     return ZK_OK;
@@ -523,6 +525,7 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
         ZK_TRY_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
         ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_go, cudaEventDisableTiming));
         ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
+        for (cudaEvent_t& ev : c->chunk_ev) ZK_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     }
     void* bases = nullptr;
     void* scalars = nullptr;
@@ -532,13 +535,23 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
         zk::scratch_free(c, bases);
         return rc;
     }
-    // main stream: the scalars first, alone on the link (the digit sort waits for them); the
-    // copy stream then uploads the points and converts them (only the accumulation, after the
-    // sort, waits for those)
+    // copy stream (after the main stream's earlier work on the scratch): the scalars first,
+    // alone on the link, in chunks whose digits the main stream sorts as each arrives (one
+    // chunk below 2^18 scalars); then the points, converted there too (only the
+    // accumulation, after the sort, waits for those)
     const cudaStream_t main_stream = c->stream;
-    cudaError_t e = cudaMemcpyAsync(scalars, scalars_host, n * 32, cudaMemcpyHostToDevice, main_stream);
-    if (e == cudaSuccess) e = cudaEventRecord(c->copy_go, main_stream);
+    const size_t nchunks = n >= ((size_t)1 << 18) ? 4 : 1;
+    c->scalar_chunks.clear();
+    cudaError_t e = cudaEventRecord(c->copy_go, main_stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->copy_go, 0);
+    for (size_t q = 0, j0 = 0; q < nchunks && e == cudaSuccess; q++) {
+        const size_t j1 = q + 1 == nchunks ? n : std::min(n, ((q + 1) * n / nchunks + 255) & ~(size_t)255);
+        e = cudaMemcpyAsync(static_cast<uint8_t*>(scalars) + j0 * 32, static_cast<const uint8_t*>(scalars_host) + j0 * 32,
+                            (j1 - j0) * 32, cudaMemcpyHostToDevice, c->copy_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(c->chunk_ev[q], c->copy_stream);
+        c->scalar_chunks.emplace_back((uint32_t)j1, c->chunk_ev[q]);
+        j0 = j1;
+    }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(bases, xy_canonical_host, n * 64, cudaMemcpyHostToDevice, c->copy_stream);
     if (e == cudaSuccess) {
@@ -555,6 +568,7 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
                          scalars_mont, window_bits, out_xy, out_is_inf, nullptr, 0, n, /*glv=*/true);
         c->bases_wait = nullptr;
     }
+    c->scalar_chunks.clear();
     // the frees are ordered on the main stream: after the copy stream is done with `bases`
     cudaStreamWaitEvent(main_stream, c->copy_done, 0);
     zk::scratch_free(c, scalars);

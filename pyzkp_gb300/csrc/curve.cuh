@@ -140,6 +140,19 @@ __device__ __forceinline__ bool affine_is_inf(const AffineT<T>& p) {
     return c_is_zero(p.x) && c_is_zero(p.y);
 }
 
+// OR of every limb of a coordinate
+__device__ __forceinline__ uint32_t c_bits_or(const fe& a) {
+    return a.v[0] | a.v[1] | a.v[2] | a.v[3] | a.v[4] | a.v[5] | a.v[6] | a.v[7];
+}
+__device__ __forceinline__ uint32_t c_bits_or(const fq2& a) { return c_bits_or(a.c0) | c_bits_or(a.c1); }
+
+// The stored form of infinity in a base array: all bits zero. Exact for stored bases: the
+// Montgomery conversion keeps 0 at 0, and no point of either curve has x = y = 0.
+template <class T>
+__device__ __forceinline__ bool affine_is_zero_bits(const AffineT<T>& p) {
+    return (c_bits_or(p.x) | c_bits_or(p.y)) == 0;
+}
+
 template <class T = fe>
 __device__ __forceinline__ XyzzT<T> xyzz_inf() {
     XyzzT<T> r;

@@ -364,13 +364,14 @@ __device__ __forceinline__ uint32_t signed_digit(const fe& s, uint32_t w, const 
     return v;
 }
 
-// Canonical scalars (reduced mod r; zero where the base is infinity) to `reduced` for the
-// scatter, and the CSR histogram of the digits.
+// Canonical scalars (reduced mod r) to `reduced` for the scatter, and the CSR histogram of
+// the digits. The bases are not read here (an infinity base is skipped where the
+// accumulation loads it), so the points may still be uploading while the digits run.
 template <class C>
-__global__ void msm_digits_kernel(const MsmInst* __restrict__ insts, const uint32_t* __restrict__ offs, uint32_t N,
-                                  int scalars_mont, MsmShape sh, fe* __restrict__ reduced,
+__global__ void msm_digits_kernel(const MsmInst* __restrict__ insts, const uint32_t* __restrict__ offs, uint32_t j0,
+                                  uint32_t N, int scalars_mont, MsmShape sh, fe* __restrict__ reduced,
                                   uint32_t* __restrict__ counts) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t j = j0 + blockIdx.x * blockDim.x + threadIdx.x;  // scalars [j0, N) in this launch
     const bool valid = j < N;
     fe s = fe_zero();
     uint32_t set0 = 0;
@@ -379,7 +380,6 @@ __global__ void msm_digits_kernel(const MsmInst* __restrict__ insts, const uint3
         const uint32_t i = j - __ldg(offs + k);
         s = fe_ldg(insts[k].scalars + i);
         s = scalars_mont ? fe_from_mont<FrP>(s) : fe_from_mont<FrP>(fe_to_mont<FrP>(s));
-        if (affine_is_inf(affine_load(static_cast<const typename C::A*>(insts[k].bases) + i))) s = fe_zero();
         set0 = k * sh.Wr;
         if (!sh.glv) fe_store(reduced + j, s);
     }
@@ -529,6 +529,7 @@ __global__ void __launch_bounds__(128, C::kAccMinBlocks) msm_accumulate_kernel(c
         }
         const uint32_t ent = entries[e];
         A p = affine_load(bases + (ent & 0x7fffffffu));
+        if (affine_is_zero_bits(p)) continue;  // an infinity base adds nothing
         if (ent >> 31) p.y = c_neg(p.y);
         acc = xyzz_madd(acc, p.x, p.y);
     }
@@ -1041,9 +1042,25 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
     ZK_TRY_CUDA(cudaMemsetAsync(p.buckets, 0, p.nbuckets * sizeof(P), st));
     const uint32_t N = (uint32_t)p.N;
     const unsigned nblk = (unsigned)((p.N + 255) / 256);
-    ZK_LAUNCH(c, "msm_digits", msm_digits_kernel<C>, nblk, 256, 0, p.d_inst, p.d_offs, N, scalars_mont, sh,
-              reinterpret_cast<fe*>(p.digits), p.row_ptr);
-    ZK_TRY_CUDA(cudaGetLastError());
+    if (!c->scalar_chunks.empty() && c->scalar_chunks.back().first == N && p.inst.size() == 1) {
+        // scalars still arriving: each chunk's digits wait for its copy only
+        uint32_t j0 = 0;
+        for (const auto& ch : c->scalar_chunks) {
+            ZK_TRY_CUDA(cudaStreamWaitEvent(st, ch.second, 0));
+            ZK_LAUNCH(c, "msm_digits", msm_digits_kernel<C>, (unsigned)((ch.first - j0 + 255) / 256), 256, 0,
+                      p.d_inst, p.d_offs, j0, ch.first, scalars_mont, sh, reinterpret_cast<fe*>(p.digits),
+                      p.row_ptr);
+            ZK_TRY_CUDA(cudaGetLastError());
+            j0 = ch.first;
+        }
+    } else {
+        // scalars still arriving on another stream, for a pipeline that does not match the
+        // chunks: wait for all of them
+        if (!c->scalar_chunks.empty()) ZK_TRY_CUDA(cudaStreamWaitEvent(st, c->scalar_chunks.back().second, 0));
+        ZK_LAUNCH(c, "msm_digits", msm_digits_kernel<C>, nblk, 256, 0, p.d_inst, p.d_offs, 0u, N, scalars_mont, sh,
+                  reinterpret_cast<fe*>(p.digits), p.row_ptr);
+        ZK_TRY_CUDA(cudaGetLastError());
+    }
     // row_ptr[0..nbuckets) := exclusive scan; row_ptr[nbuckets] := total
     int rc = device_exclusive_scan(c, p.row_ptr, p.nbuckets, p.row_ptr + p.nbuckets, p.scan_tmp);
     if (rc != ZK_OK) return rc;

@@ -98,6 +98,10 @@ struct Ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_go = nullptr, copy_done = nullptr;
     cudaEvent_t bases_wait = nullptr;
+    // ... and the scalars arrive in chunks on that stream: (end index, event recorded after
+    // its copy); a single-instance pipeline of that size runs its digits chunk by chunk
+    std::vector<std::pair<uint32_t, cudaEvent_t>> scalar_chunks;
+    cudaEvent_t chunk_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // MSM batches spread their pipelines over the context stream and these (fork / join
     // events); created on first use
     std::vector<cudaStream_t> side_streams;

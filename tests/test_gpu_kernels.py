@@ -368,6 +368,38 @@ def test_msm_g1_host_one_call(gpu_ctx):
     pin_s.free()
 
 
+def test_msm_g1_host_alternating_infinity_sets(gpu_ctx):
+    """zk_msm_g1_host at 2^20 from pinned buffers, alternating a base set whose every second
+    point is infinity with the full set (the same scratch buffers in turn): the points upload
+    on a second stream while the digits are sorted, and each result must equal the known
+    answer -- nothing before the accumulation may depend on the points' upload."""
+    n = 1 << 20
+    seed = synth.seed_for(2, 20) + 17
+    k = synth.base_dlogs(seed, n)
+    s = synth.fr_uniform(seed, n)
+    dk = gpu_ctx.to_device(k)
+    dxy = gpu_ctx.alloc(n * 64)
+    gpu_ctx.g1_fixed_base_mul((1, 2), dk, n, dxy)
+    full = dxy.download().view("<u8").reshape(n, 8)
+    half = full.copy()
+    half[1::2] = 0
+    k_half = k.copy()
+    k_half[1::2] = 0
+    exp_full = O.affine_to_ints(O.msm_known_answer(k, s))
+    exp_half = O.affine_to_ints(O.msm_known_answer(k_half, s))
+    pin_full = gpu_ctx.pinned(n * 64)
+    pin_full.array[:] = full.view(np.uint8).reshape(-1)
+    pin_half = gpu_ctx.pinned(n * 64)
+    pin_half.array[:] = half.view(np.uint8).reshape(-1)
+    pin_s = gpu_ctx.pinned(n * 32)
+    pin_s.array[:] = s.view(np.uint8).reshape(-1)
+    for _ in range(2):
+        assert gpu_ctx.msm_g1_host(pin_half, pin_s, n) == exp_half
+        assert gpu_ctx.msm_g1_host(pin_full, pin_s, n) == exp_full
+    for b in (pin_full, pin_half, pin_s):
+        b.free()
+
+
 def test_msm_glv_edge_scalars(gpu_ctx):
     """G1 MSMs split every scalar k = k1 + k2 lambda (GLV): scalars at the ends of the range,
     lambda itself, its negation and rounding midpoints, on random bases, for every window
