@@ -403,6 +403,7 @@ static int bases_from_dev_canonical(zk_ctx* ctx, const void* xy_dev, size_t n, z
     // the GLV images phi(P_i) behind them
     rc = zk::convert<zk::FqP, 1>(&ctx->impl, b->dev, xy_dev, 2 * n);
     if (rc == ZK_OK) rc = zk::glv_phi(&ctx->impl, b->dev, n);
+    if (rc == ZK_OK) rc = zk::any_infinity(&ctx->impl, b->dev, n, false, &b->has_inf);
     if (rc != ZK_OK) {
         zk::scratch_free(&ctx->impl, b->dev);
         delete b;
@@ -505,7 +506,7 @@ int zk_msm_g1(zk_ctx* ctx, const zk_bases* bases, size_t offset, const void* sca
     }
     return zk::msm_run(&ctx->impl, bases->dev + offset, static_cast<const zk::fe*>(scalars_dev), n, scalars_mont,
                        window_bits, out_xy, out_is_inf, bases->shifted ? bases->shifted + offset : nullptr,
-                       bases->shifted_c, bases->n, /*glv=*/true);
+                       bases->shifted_c, bases->n, /*glv=*/true, bases->has_inf);
 }
 
 int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scalars_host, size_t n, int scalars_mont,
@@ -632,6 +633,7 @@ static int make_jobs(size_t count, const zk_bases* const* bases, const uint64_t*
         }
         j.shifted_c = b->shifted_c;
         j.stride = b->n;
+        j.inf_points = b->has_inf;
     }
     return ZK_OK;
 }
@@ -783,6 +785,7 @@ static int bases_g2_create(zk_ctx* ctx, const void* xy_canonical, size_t n, cuda
         if (e == cudaSuccess) {
             rc = zk::convert<zk::FqP, 1>(&ctx->impl, b->dev2, b->dev2, 4 * n);
             if (rc == ZK_OK) rc = zk::glv_phi2(&ctx->impl, b->dev2, n);  // the GLV images behind them
+            if (rc == ZK_OK) rc = zk::any_infinity(&ctx->impl, b->dev2, n, true, &b->has_inf);
         } else {
             zk::set_error(std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
             rc = ZK_ECUDA;

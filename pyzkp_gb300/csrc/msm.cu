@@ -309,6 +309,46 @@ int glv_phi2(Ctx* c, affine2_t* pts, size_t n) {
     return ZK_OK;
 }
 
+template <class A>
+__global__ void any_zero_point_kernel(const A* __restrict__ pts, size_t n, uint32_t* __restrict__ flag) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const A p = affine_load(pts + i);
+        if (affine_is_zero_bits(p)) {
+            atomicOr(flag, 1u);
+            return;
+        }
+    }
+}
+
+int any_infinity(Ctx* c, const void* pts, size_t n, bool g2, bool* out) {
+    *out = false;
+    if (n == 0) return ZK_OK;
+    uint32_t* flag = nullptr;
+    int rc = scratch_alloc(c, 4, reinterpret_cast<void**>(&flag));
+    if (rc != ZK_OK) return rc;
+    uint32_t h = 0;
+    cudaError_t e = cudaMemsetAsync(flag, 0, 4, c->stream);
+    if (e == cudaSuccess) {
+        const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)c->num_sms * 8);
+        if (g2)
+            ZK_LAUNCH(c, "any_zero_point", any_zero_point_kernel<affine2_t>, blocks, 256, 0,
+                      static_cast<const affine2_t*>(pts), n, flag);
+        else
+            ZK_LAUNCH(c, "any_zero_point", any_zero_point_kernel<affine_t>, blocks, 256, 0,
+                      static_cast<const affine_t*>(pts), n, flag);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    scratch_free(c, flag);
+    if (e != cudaSuccess) {
+        set_error(std::string("any_infinity: ") + cudaGetErrorString(e));
+        return ZK_ECUDA;
+    }
+    *out = h != 0;
+    return ZK_OK;
+}
+
 int glv_phi(Ctx* c, affine_t* pts, size_t n) {
     if (n == 0) return ZK_OK;
     static const fe beta_m = glv_beta_mont(false);
@@ -495,7 +535,7 @@ __device__ __forceinline__ uint32_t bucket_of(const uint32_t* __restrict__ row_p
     return lo;
 }
 
-template <class C>
+template <class C, bool kSkipInf>
 __global__ void __launch_bounds__(128, C::kAccMinBlocks) msm_accumulate_kernel(const uint32_t* __restrict__ entries,
                                                              const uint32_t* __restrict__ d_total,
                                                              const uint32_t* __restrict__ row_ptr,
@@ -529,7 +569,8 @@ __global__ void __launch_bounds__(128, C::kAccMinBlocks) msm_accumulate_kernel(c
         }
         const uint32_t ent = entries[e];
         A p = affine_load(bases + (ent & 0x7fffffffu));
-        if (affine_is_zero_bits(p)) continue;  // an infinity base adds nothing
+        if constexpr (kSkipInf)
+            if (affine_is_zero_bits(p)) continue;  // an infinity base adds nothing
         if (ent >> 31) p.y = c_neg(p.y);
         acc = xyzz_madd(acc, p.x, p.y);
     }
@@ -919,6 +960,7 @@ struct MsmPipeT {
     uint64_t max_entries = 0;  // N * W
     uint64_t nbuckets = 0;     // sets * B
     uint32_t units = 0;        // first-round accumulation units
+    bool skip_inf = true;      // some instance's points may hold infinity: tested per entry
     std::vector<MsmInst> inst;
     std::vector<uint32_t> offs;     // inst + 1 prefix offsets
     std::vector<size_t> out_index;  // result slot of each instance
@@ -1072,8 +1114,10 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
     // accumulation rounds (the first kernel that reads the points)
     if (c->bases_wait != nullptr) ZK_TRY_CUDA(cudaStreamWaitEvent(st, c->bases_wait, 0));
     const uint32_t* d_total = p.row_ptr + p.nbuckets;
-    ZK_LAUNCH(c, "msm_accumulate", msm_accumulate_kernel<C>, (p.units + 127) / 128, 128, 0, p.entries, d_total,
-              p.row_ptr, p.d_inst, sh, p.units, p.buckets, p.slot_keys_a, p.slot_pts_a);
+    // point sets without infinity skip the per-entry test
+    auto* accumulate = p.skip_inf ? msm_accumulate_kernel<C, true> : msm_accumulate_kernel<C, false>;
+    ZK_LAUNCH(c, "msm_accumulate", accumulate, (p.units + 127) / 128, 128, 0, p.entries, d_total, p.row_ptr,
+              p.d_inst, sh, p.units, p.buckets, p.slot_keys_a, p.slot_pts_a);
     ZK_TRY_CUDA(cudaGetLastError());
     // Partial sums of straddling buckets: short buckets (up to ~3 segments on average) by one
     // fixup pass, longer ones by merge rounds (kFixupDensity).
@@ -1336,13 +1380,16 @@ static int build_pipes(Ctx* c, const MsmJob* jobs, size_t count, uint32_t window
         std::vector<MsmInst> part;
         std::vector<size_t> idx;
         uint64_t N = 0;
+        bool part_inf = false;
         auto flush = [&]() -> int {
             if (part.empty()) return ZK_OK;
             out->emplace_back();
             int rc = pipe_init<C>(out->back(), cb, fixed, glv, part, idx, c->num_sms);
+            out->back().skip_inf = part_inf;
             part.clear();
             idx.clear();
             N = 0;
+            part_inf = false;
             return rc;
         };
         for (size_t j : kv.second) {
@@ -1359,6 +1406,7 @@ static int build_pipes(Ctx* c, const MsmJob* jobs, size_t count, uint32_t window
             part.push_back(mi);
             idx.push_back(j);
             N += b.n;
+            part_inf = part_inf || b.inf_points;
         }
         int rc = flush();
         if (rc != ZK_OK) return rc;
@@ -1595,8 +1643,9 @@ int msm_g2_batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont,
 
 int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
             uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted, uint32_t shifted_c, uint64_t stride,
-            bool glv) {
+            bool glv, bool inf_points) {
     MsmJob job;
+    job.inf_points = inf_points;
     job.scalars = scalars;
     job.n = n;
     job.bases = bases;

@@ -200,7 +200,7 @@ static int time_msm(Ctx* c, const zk_bases* b, const fe* scalars, size_t n, uint
     double best = 1e30;
     for (int r = 0; r < reps + 1; r++) {
         const auto t0 = std::chrono::steady_clock::now();
-        int rc = msm_run(c, b->dev, scalars, n, 1, cbits, xy, &inf, nullptr, 0, b->n, /*glv=*/true);
+        int rc = msm_run(c, b->dev, scalars, n, 1, cbits, xy, &inf, nullptr, 0, b->n, /*glv=*/true, b->has_inf);
         if (rc != ZK_OK) return rc;
         const double t = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         if (r > 0 && t < best) best = t;  // the first call warms the pool and caches

@@ -137,7 +137,10 @@ int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log
             const uint8_t shift[32]);
 int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
             uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted = nullptr, uint32_t shifted_c = 0,
-            uint64_t stride = 0, bool glv = false);
+            uint64_t stride = 0, bool glv = false, bool inf_points = true);
+// Whether any of the n stored points (affine_t, or affine2_t when g2) is infinity (all zero);
+// synchronises the context stream.
+int any_infinity(Ctx* c, const void* pts, size_t n, bool g2, bool* out);
 // G1 bases with the GLV half: pts[n + i] = phi(pts[i]) = (beta x_i, y_i) for i < n.
 int glv_phi(Ctx* c, affine_t* pts, size_t n);
 // G2 bases with the GLV half: pts[n + i] = (beta^2 x_i, y_i) = [lambda] P_i.
@@ -153,6 +156,7 @@ struct MsmJob {
     uint32_t shifted_c = 0;
     uint64_t stride = 0;  // points in the base set: row stride of `shifted`, offset of the GLV half
     bool glv = false;     // G1 bases whose phi(P) half sits at bases + stride (GLV split scalars)
+    bool inf_points = true;  // the points may hold infinity (all zero): the accumulation tests each
 };
 struct MsmPlan;
 uint32_t msm_auto_window(size_t n);
@@ -213,6 +217,7 @@ struct zk_bases {
     zk::affine2_t* shifted2 = nullptr;  // the same rows of G2 bases
     uint32_t shifted_c = 0;
     uint32_t shifted_windows = 0;
+    bool has_inf = true;  // some point is infinity (found on the device when the set is created)
 };
 
 struct zk_batch {
