@@ -67,8 +67,10 @@ def test_msm_batch_many_base_sets_offsets_and_fixed_base(gpu_ctx):
     k2, b2 = _bases(gpu_ctx, 202, 9000, zero_at=(9,))
     k3, b3 = _bases(gpu_ctx, 203, 3000)
     gpu_ctx.bases_precompute(b3, 10)  # b3 instances run in fixed-base mode (c = 10)
+    # (b2, k2, 0, 5000) reaches b2's infinity point and shares a pipeline (same window) with
+    # the first b1 instance, whose set holds none
     spec = [(b1, k1, 0, 5000), (b2, k2, 100, 8000), (b3, k3, 0, 3000), (b1, k1, 4000, 1000), (b3, k3, 7, 2000),
-            (b2, k2, 8999, 1), (b2, k2, 0, 0)]
+            (b2, k2, 8999, 1), (b2, k2, 0, 0), (b2, k2, 0, 5000)]
     bases, offs, sizes, dev, exp = [], [], [], [], []
     for j, (b, k, off, m) in enumerate(spec):
         s = synth.fr_uniform(900 + j, m)
