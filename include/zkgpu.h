@@ -304,10 +304,11 @@ int zk_msm_g1(zk_ctx *ctx, const zk_bases *bases, size_t offset, const void *sca
  * G1 MSM from host memory in one call: the shape of metal_msm_g1 (runtime/metal/msm.py:65-143),
  * which packs and uploads the points on every call (_msm_g1, runtime/kernels/metal/kernels.py:84-120).
  * xy_canonical_host: n affine canonical points (64 bytes each, (0,0) = infinity);
- * scalars_host: n elements as for zk_msm_g1 (scalars_mont selects the form). The points
- * are uploaded and converted on a second stream while the scalars' digits are sorted;
- * the bucket accumulation waits for them. Pinned host memory (zk_host_alloc) makes both
- * copies asynchronous. Same result as zk_bases_create + zk_h2d + zk_msm_g1.
+ * scalars_host: n elements as for zk_msm_g1 (scalars_mont selects the form). On a second
+ * stream the scalars go up first (in chunks whose digits are computed as each arrives),
+ * then the points, converted there while the digits are sorted; the bucket accumulation
+ * waits for them. Pinned host memory (zk_host_alloc) makes the copies asynchronous. Same
+ * result as zk_bases_create + zk_h2d + zk_msm_g1.
  */
 int zk_msm_g1_host(zk_ctx *ctx, const void *xy_canonical_host, const void *scalars_host, size_t n,
                    int scalars_mont, uint32_t window_bits, uint8_t out_xy[64], int *out_is_inf);
