@@ -55,18 +55,29 @@ __device__ __forceinline__ fq2 c_add(const fq2& a, const fq2& b) { return {c_add
 __device__ __forceinline__ fq2 c_sub(const fq2& a, const fq2& b) { return {c_sub(a.c0, b.c0), c_sub(a.c1, b.c1)}; }
 __device__ __forceinline__ fq2 c_dbl(const fq2& a) { return {c_dbl(a.c0), c_dbl(a.c1)}; }
 __device__ __forceinline__ fq2 c_neg(const fq2& a) { return {c_neg(a.c0), c_neg(a.c1)}; }
-// (a0 + a1 u)(b0 + b1 u) = (a0 b0 - a1 b1) + (a0 b1 + a1 b0) u. Karatsuba, 3 full products
-// ((a0 + a1)(b0 + b1) - a0 b0 - a1 b1 for the u coefficient); ZK_FQ2_SCHOOLBOOK selects the
-// separated forms instead (4 partial products, 2 reductions). Measured on GB300 (G2 MSM,
-// schoolbook against Karatsuba): accumulation 12.1 / 10.5 ms at 2^20, window reduction
-// kernels about 10% faster, whole MSM 14.8 / 13.4 ms at 2^20 and 2.27 / 2.45 ms at 2^16.
+// (a0 + a1 u)(b0 + b1 u) = (a0 b0 - a1 b1) + (a0 b1 + a1 b0) u, Karatsuba: the u coefficient
+// is (a0 + a1)(b0 + b1) - a0 b0 - a1 b1. ZK_FQ2_SCHOOLBOOK selects a0 b0 - a1 b1, a0 b1 + a1 b0
+// with one reduction each instead (4 partial products): measured on GB300 against full
+// Karatsuba products, accumulation 12.1 / 10.5 ms at 2^20, whole MSM 14.8 / 13.4 ms.
 #ifdef ZK_FQ2_SCHOOLBOOK
 constexpr bool kFq2Schoolbook = true;
 #else
 constexpr bool kFq2Schoolbook = false;
 #endif
+// Default: Karatsuba with lazy reduction (fe2_mul_lazy: 3 unreduced 512-bit products, 2
+// reductions; ZK_FQ2_FULL keeps 3 full products). Measured on GB300 (G2 MSM): 2.03 / 2.45 ms
+// at 2^16, 4.55 / 5.27 ms at 2^18, 12.71 / 13.35 ms at 2^20 (accumulation -2%, window
+// reduction and fixup kernels -18 to -28%).
+#ifdef ZK_FQ2_FULL
+constexpr bool kFq2Lazy = false;
+#else
+constexpr bool kFq2Lazy = true;
+#endif
 __device__ __forceinline__ fq2 c_mul(const fq2& a, const fq2& b) {
-    if constexpr (use_sos<FqP>() && kFq2Schoolbook) {
+    if constexpr (use_sos<FqP>() && kFq2Lazy) {
+        const fe_pair r = fe2_mul_lazy_call<FqP>(a.c0, a.c1, b.c0, b.c1);
+        return {r.c0, r.c1};
+    } else if constexpr (use_sos<FqP>() && kFq2Schoolbook) {
         return {fe_mul_sub<FqP>(a.c0, b.c0, a.c1, b.c1), fe_mul_add<FqP>(a.c0, b.c1, a.c1, b.c0)};
     } else {
         const fe t0 = c_mul(a.c0, b.c0);

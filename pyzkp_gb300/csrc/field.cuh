@@ -46,6 +46,14 @@ struct FqP {
     static constexpr bool LAZY = true;
 #endif
     __host__ __device__ static constexpr uint32_t ONE(int i) { return i == 0 ? 0xc58f0d9du : i == 1 ? 0xd35d438du : i == 2 ? 0xf5c70b3du : i == 3 ? 0x0a78eb28u : i == 4 ? 0x7879462cu : i == 5 ? 0x666ea36fu : i == 6 ? 0x9a07df2fu : 0x0e0a77c1u; }
+    // 4 q^2 as 16 limbs (the offset that keeps a difference of two products below 4q^2 each
+    // non-negative)
+    __host__ __device__ static constexpr uint32_t FOUR_P_SQ(int i) {
+        constexpr uint32_t v[16] = {0x9d75a6c4u, 0xed516288u, 0x27ab0404u, 0x98081cb4u, 0xb65b2b72u, 0x29406271u,
+                                    0xe8490b21u, 0x11a27a55u, 0xd31ace34u, 0x9bb7e970u, 0x58dd5818u, 0xc02e1544u,
+                                    0x0d234872u, 0x6669bdf0u, 0xd8f2fe71u, 0x249712e1u};
+        return v[i];
+    }
     __host__ __device__ static constexpr uint32_t R2(int i) { return i == 0 ? 0x538afa89u : i == 1 ? 0xf32cfc5bu : i == 2 ? 0xd44501fbu : i == 3 ? 0xb5e71911u : i == 4 ? 0x0a417ff6u : i == 5 ? 0x47ab1effu : i == 6 ? 0xcab8351fu : 0x06d89f71u; }
 };
 
@@ -962,6 +970,83 @@ __host__ __device__ __forceinline__ fe fe_mul_add_sos(const fe& a, const fe& b, 
 template <class F>
 __host__ __device__ __forceinline__ fe fe_mul_sub_sos(const fe& a, const fe& b, const fe& c, const fe& d) {
     return fe_mul_add_sos<F>(a, b, sos_neg2p<F>(c), d);
+}
+
+// Fq2 product with lazy reduction (Karatsuba): T0 = a0 b0, T1 = a1 b1, T2 = (a0 + a1)(b0 + b1)
+// as 512-bit products, c0 = redc(T0 + (4q^2 - T1)), c1 = redc(T2 - T0 - T1) = redc(a0 b1 + a1 b0):
+// 3 products and 2 reductions instead of 3 full products. Inputs in [0, 2q): the sums a0 + a1
+// stay below 4q < 2^256 unreduced (one product row stays inside its 9 limbs for any 256-bit
+// operand), both arguments of the reductions are below 8q^2, results in [0, 2q).
+struct fe_pair {
+    fe c0, c1;
+};
+
+template <class F>
+__host__ __device__ __forceinline__ fe_pair fe2_mul_lazy(const fe& a0, const fe& a1, const fe& b0, const fe& b1) {
+    static_assert(F::LAZY, "the separated forms keep lazy values");
+    uint32_t t0[16], t1[16];
+    sos_row<0, true>(t0, a0.v, b0.v[0]);
+    sos_row<1, true>(t0, a0.v, b0.v[1]);
+    sos_row<2, true>(t0, a0.v, b0.v[2]);
+    sos_row<3, true>(t0, a0.v, b0.v[3]);
+    sos_row<4, true>(t0, a0.v, b0.v[4]);
+    sos_row<5, true>(t0, a0.v, b0.v[5]);
+    sos_row<6, true>(t0, a0.v, b0.v[6]);
+    sos_row<7, true>(t0, a0.v, b0.v[7]);
+    sos_row<0, true>(t1, a1.v, b1.v[0]);
+    sos_row<1, true>(t1, a1.v, b1.v[1]);
+    sos_row<2, true>(t1, a1.v, b1.v[2]);
+    sos_row<3, true>(t1, a1.v, b1.v[3]);
+    sos_row<4, true>(t1, a1.v, b1.v[4]);
+    sos_row<5, true>(t1, a1.v, b1.v[5]);
+    sos_row<6, true>(t1, a1.v, b1.v[6]);
+    sos_row<7, true>(t1, a1.v, b1.v[7]);
+    // u = T0 + (4q^2 - T1) in (0, 8q^2); s = T0 + T1 (below 8q^2)
+    uint32_t u[16], s[16];
+    u[0] = u_sub_cc(F::FOUR_P_SQ(0), t1[0]);
+#pragma unroll
+    for (int j = 1; j < 15; j++) u[j] = u_subc_cc(F::FOUR_P_SQ(j), t1[j]);
+    u[15] = u_subc(F::FOUR_P_SQ(15), t1[15]);
+    u[0] = u_add_cc(u[0], t0[0]);
+#pragma unroll
+    for (int j = 1; j < 15; j++) u[j] = u_addc_cc(u[j], t0[j]);
+    u[15] = u_addc(u[15], t0[15]);
+    s[0] = u_add_cc(t0[0], t1[0]);
+#pragma unroll
+    for (int j = 1; j < 15; j++) s[j] = u_addc_cc(t0[j], t1[j]);
+    s[15] = u_addc(t0[15], t1[15]);
+    fe_pair r;
+    r.c0 = sos_reduce_2p<F>(sos_redc<F>(u));
+    // T2 - s with a0 + a1, b0 + b1 as plain 256-bit sums
+    fe sa, sb;
+    sa.v[0] = u_add_cc(a0.v[0], a1.v[0]);
+#pragma unroll
+    for (int j = 1; j < 7; j++) sa.v[j] = u_addc_cc(a0.v[j], a1.v[j]);
+    sa.v[7] = u_addc(a0.v[7], a1.v[7]);
+    sb.v[0] = u_add_cc(b0.v[0], b1.v[0]);
+#pragma unroll
+    for (int j = 1; j < 7; j++) sb.v[j] = u_addc_cc(b0.v[j], b1.v[j]);
+    sb.v[7] = u_addc(b0.v[7], b1.v[7]);
+    uint32_t t2[16];
+    sos_row<0, true>(t2, sa.v, sb.v[0]);
+    sos_row<1, true>(t2, sa.v, sb.v[1]);
+    sos_row<2, true>(t2, sa.v, sb.v[2]);
+    sos_row<3, true>(t2, sa.v, sb.v[3]);
+    sos_row<4, true>(t2, sa.v, sb.v[4]);
+    sos_row<5, true>(t2, sa.v, sb.v[5]);
+    sos_row<6, true>(t2, sa.v, sb.v[6]);
+    sos_row<7, true>(t2, sa.v, sb.v[7]);
+    t2[0] = u_sub_cc(t2[0], s[0]);
+#pragma unroll
+    for (int j = 1; j < 15; j++) t2[j] = u_subc_cc(t2[j], s[j]);
+    t2[15] = u_subc(t2[15], s[15]);
+    r.c1 = sos_reduce_2p<F>(sos_redc<F>(t2));
+    return r;
+}
+
+template <class F>
+__device__ __noinline__ fe_pair fe2_mul_lazy_call(const fe a0, const fe a1, const fe b0, const fe b1) {
+    return fe2_mul_lazy<F>(a0, a1, b0, b1);
 }
 
 template <class F>

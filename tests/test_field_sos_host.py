@@ -1,6 +1,7 @@
 """The separated Fq forms of field.cuh (square, a b + c d, a b - c d, a b with one Montgomery
-reduction) built for the host and checked against Python integers: congruence with
-x * 2^-256 mod q and the lazy bound [0, 2q) on random inputs and on the edges of [0, 2q)."""
+reduction, and the lazily reduced Fq2 product) built for the host and checked against Python
+integers: congruence with x * 2^-256 mod q and the lazy bound [0, 2q) on random inputs and
+on the edges of [0, 2q)."""
 
 import os
 import random
@@ -41,9 +42,11 @@ def test_separated_forms_match_integers(tmp_path):
     res = subprocess.run([str(exe), str(src), str(dst)], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
     raw = dst.read_bytes()
-    assert len(raw) == 128 * len(recs)
+    assert len(raw) == 192 * len(recs)
     for i, (a, b, c, d) in enumerate(recs):
-        sq, madd, msub, mul = (int.from_bytes(raw[128 * i + 32 * k:128 * i + 32 * k + 32], "little") for k in range(4))
-        for got, want in ((sq, a * a), (madd, a * b + c * d), (msub, a * b - c * d), (mul, a * b)):
+        sq, madd, msub, mul, f0, f1 = (int.from_bytes(raw[192 * i + 32 * k:192 * i + 32 * k + 32], "little")
+                                       for k in range(6))
+        for got, want in ((sq, a * a), (madd, a * b + c * d), (msub, a * b - c * d), (mul, a * b),
+                          (f0, a * c - b * d), (f1, a * d + b * c)):
             assert got < 2 * Q, (i, a, b, c, d)
             assert got % Q == want * RINV % Q, (i, a, b, c, d)
