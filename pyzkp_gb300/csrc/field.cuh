@@ -67,6 +67,12 @@ struct FrLazyP : FrP {
 #endif
 };
 
+// Fr with one non-inlined copy of the product, for kernels whose loop bodies hold many
+// products (inlined, they overflow the instruction cache).
+struct FrCallP : FrP {
+    static constexpr int MUL_STYLE = 3;
+};
+
 // One field element: 8 little-endian 32-bit limbs (32 bytes, 32-byte aligned in memory).
 struct __align__(16) fe {
     uint32_t v[8];

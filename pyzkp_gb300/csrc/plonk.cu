@@ -40,15 +40,6 @@ __device__ fe fe_pow_fermat_inv(const fe& a) {
     return r;
 }
 
-__device__ __forceinline__ fe fr_pow_u64(fe base, uint64_t e) {
-    fe acc = fe_one<FrP>();
-    for (; e; e >>= 1) {
-        if (e & 1) acc = fe_mul<FrP>(acc, base);
-        base = fe_mul<FrP>(base, base);
-    }
-    return acc;
-}
-
 // out must not alias in: the backward pass reads in[] again (out holds the prefixes).
 __global__ void fr_batch_inv_kernel(fe* __restrict__ out, const fe* __restrict__ in, size_t n) {
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -73,6 +64,18 @@ __global__ void fr_batch_inv_kernel(fe* __restrict__ out, const fe* __restrict__
     }
 }
 
+// The quotient kernel holds ~23 products per element: Fr with the non-inlined product
+using FrQ = FrCallP;
+
+__device__ __forceinline__ fe fr_pow_q(fe base, uint64_t e) {
+    fe acc = fe_one<FrQ>();
+    for (; e; e >>= 1) {
+        if (e & 1) acc = fe_mul<FrQ>(acc, base);
+        base = fe_mul<FrQ>(base, base);
+    }
+    return acc;
+}
+
 struct QuotientIn {
     const fe* v[15];  // a b c z pi ql qr qm qo qc s1 s2 s3 zshift l1 (Montgomery)
 };
@@ -87,30 +90,30 @@ __global__ void plonk_quotient_kernel(QuotientIn in, QuotientK K, size_t m, fe* 
     const size_t i0 = t * kQChunk;
     if (i0 >= m) return;
     const size_t i1 = i0 + kQChunk < m ? i0 + kQChunk : m;
-    fe x = fe_mul<FrP>(K.shift, fr_pow_u64(K.omega_m, i0));
-    fe un = fr_pow_u64(K.u, i0);
+    fe x = fe_mul<FrQ>(K.shift, fr_pow_q(K.omega_m, i0));
+    fe un = fr_pow_q(K.u, i0);
     for (size_t i = i0; i < i1; i++) {
         const fe a = fe_ldg(in.v[0] + i), b = fe_ldg(in.v[1] + i), c = fe_ldg(in.v[2] + i);
         const fe z = fe_ldg(in.v[3] + i);
-        fe gate = fe_add<FrP>(fe_mul<FrP>(fe_ldg(in.v[5] + i), a), fe_mul<FrP>(fe_ldg(in.v[6] + i), b));
-        gate = fe_add<FrP>(gate, fe_mul<FrP>(fe_mul<FrP>(fe_ldg(in.v[7] + i), a), b));
-        gate = fe_add<FrP>(gate, fe_mul<FrP>(fe_ldg(in.v[8] + i), c));
-        gate = fe_add<FrP>(gate, fe_add<FrP>(fe_ldg(in.v[9] + i), fe_ldg(in.v[4] + i)));
-        const fe t1 = fe_add<FrP>(fe_add<FrP>(a, fe_mul<FrP>(K.beta, x)), K.gamma);
-        const fe t2 = fe_add<FrP>(fe_add<FrP>(b, fe_mul<FrP>(K.beta_k1, x)), K.gamma);
-        const fe t3 = fe_add<FrP>(fe_add<FrP>(c, fe_mul<FrP>(K.beta_k2, x)), K.gamma);
-        const fe left = fe_mul<FrP>(fe_mul<FrP>(fe_mul<FrP>(t1, t2), t3), z);
-        const fe u1 = fe_add<FrP>(fe_add<FrP>(a, fe_mul<FrP>(K.beta, fe_ldg(in.v[10] + i))), K.gamma);
-        const fe u2 = fe_add<FrP>(fe_add<FrP>(b, fe_mul<FrP>(K.beta, fe_ldg(in.v[11] + i))), K.gamma);
-        const fe u3 = fe_add<FrP>(fe_add<FrP>(c, fe_mul<FrP>(K.beta, fe_ldg(in.v[12] + i))), K.gamma);
-        const fe right = fe_mul<FrP>(fe_mul<FrP>(fe_mul<FrP>(u1, u2), u3), fe_ldg(in.v[13] + i));
-        const fe perm = fe_sub<FrP>(left, right);
-        const fe boundary = fe_mul<FrP>(fe_sub<FrP>(z, K.one), fe_ldg(in.v[14] + i));
-        const fe v = fe_add<FrP>(gate, fe_add<FrP>(fe_mul<FrP>(K.alpha, perm), fe_mul<FrP>(K.alpha2, boundary)));
+        fe gate = fe_add<FrQ>(fe_mul<FrQ>(fe_ldg(in.v[5] + i), a), fe_mul<FrQ>(fe_ldg(in.v[6] + i), b));
+        gate = fe_add<FrQ>(gate, fe_mul<FrQ>(fe_mul<FrQ>(fe_ldg(in.v[7] + i), a), b));
+        gate = fe_add<FrQ>(gate, fe_mul<FrQ>(fe_ldg(in.v[8] + i), c));
+        gate = fe_add<FrQ>(gate, fe_add<FrQ>(fe_ldg(in.v[9] + i), fe_ldg(in.v[4] + i)));
+        const fe t1 = fe_add<FrQ>(fe_add<FrQ>(a, fe_mul<FrQ>(K.beta, x)), K.gamma);
+        const fe t2 = fe_add<FrQ>(fe_add<FrQ>(b, fe_mul<FrQ>(K.beta_k1, x)), K.gamma);
+        const fe t3 = fe_add<FrQ>(fe_add<FrQ>(c, fe_mul<FrQ>(K.beta_k2, x)), K.gamma);
+        const fe left = fe_mul<FrQ>(fe_mul<FrQ>(fe_mul<FrQ>(t1, t2), t3), z);
+        const fe u1 = fe_add<FrQ>(fe_add<FrQ>(a, fe_mul<FrQ>(K.beta, fe_ldg(in.v[10] + i))), K.gamma);
+        const fe u2 = fe_add<FrQ>(fe_add<FrQ>(b, fe_mul<FrQ>(K.beta, fe_ldg(in.v[11] + i))), K.gamma);
+        const fe u3 = fe_add<FrQ>(fe_add<FrQ>(c, fe_mul<FrQ>(K.beta, fe_ldg(in.v[12] + i))), K.gamma);
+        const fe right = fe_mul<FrQ>(fe_mul<FrQ>(fe_mul<FrQ>(u1, u2), u3), fe_ldg(in.v[13] + i));
+        const fe perm = fe_sub<FrQ>(left, right);
+        const fe boundary = fe_mul<FrQ>(fe_sub<FrQ>(z, K.one), fe_ldg(in.v[14] + i));
+        const fe v = fe_add<FrQ>(gate, fe_add<FrQ>(fe_mul<FrQ>(K.alpha, perm), fe_mul<FrQ>(K.alpha2, boundary)));
         fe_store(num + i, v);
-        fe_store(zh + i, fe_sub<FrP>(fe_mul<FrP>(K.shift_n, un), K.one));
-        un = fe_mul<FrP>(un, K.u);
-        x = fe_mul<FrP>(x, K.omega_m);
+        fe_store(zh + i, fe_sub<FrQ>(fe_mul<FrQ>(K.shift_n, un), K.one));
+        un = fe_mul<FrQ>(un, K.u);
+        x = fe_mul<FrQ>(x, K.omega_m);
     }
 }
 
