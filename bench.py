@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--log-n", type=int, default=LOG_N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "msm", "ntt", "batch", "serve", "plonk"],
+    ap.add_argument("--only", default="all", choices=["all", "msm", "ntt", "batch", "serve", "plonk", "g2"],
                     help="msm / ntt: only that kernel family, no e2e (short commands for profiling)")
     return ap.parse_args()
 
@@ -176,6 +176,8 @@ def run_gpu(args, ranks: Ranks) -> dict:
         return {"serve": run_gpu_serve(ctx, args)}
     if args.only == "plonk":
         return {"plonk_quotient_2_20": run_gpu_plonk(ctx, args, ctx.alloc(FLUSH_BYTES))}
+    if args.only == "g2":
+        return {"msm_g2": run_gpu_g2(ctx, args, ctx.alloc(FLUSH_BYTES))}
     if args.only == "ntt":
         flush = ctx.alloc(FLUSH_BYTES)
         peaks = load_peaks()
@@ -308,6 +310,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
     ntt22 = run_gpu_ntt(ctx, args, ranks, 22, flush, imad_tops, hbm_peak, brief=True)
     clocks = sampler.stop()
     msm_4096 = run_gpu_msm_4096(ctx, args, flush) if ranks.world == 1 else None
+    g2 = run_gpu_g2(ctx, args, flush) if ranks.world == 1 else None
     sweep = run_gpu_msm_sweep(ctx, args, flush) if ranks.world == 1 else None
     fixed = run_gpu_fixed_base(ctx, args, flush) if ranks.world == 1 else None
     fixed_sweep = ({f"2^{lg}": run_gpu_fixed_base(ctx, args, flush, log_n=lg) for lg in range(16, 23)}
@@ -348,6 +351,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
         "ntt": ntt,
         "ntt_2_22": ntt22,
         "msm_2_12": msm_4096,
+        "msm_g2": g2,
         "msm_sweep": sweep,
         "msm_fixed_base_2_20": fixed,
         "msm_fixed_base_sweep": fixed_sweep,
@@ -600,6 +604,43 @@ def run_gpu_msm_4096(ctx, args, flush, steps: int = 50) -> dict:
             "steps": steps, "device_equals_host_call": res == res_host,
             "msm_result": [hex(res[0]), hex(res[1])] if res else None,
             "l2": "flushed (256 MB memset) before every timed step"}
+
+
+def run_gpu_g2(ctx, args, flush, sizes=(16, 18, 20)) -> dict:
+    """G2 MSMs (the group of the Groth16 B query): bases [k_i]G2 from the device fixed-base
+    multiplication, uniform scalars, GLV split, L2 flushed before each timed call. The result
+    of the largest size goes to the CPU baseline leg for the known-answer check."""
+    from pyzkp_gb300 import synth
+    from pyzkp_gb300.groth16 import G2_GEN
+
+    out = {}
+    steps = max(3, min(args.steps, 10))
+    for lg in sizes:
+        n = 1 << lg
+        seed = synth.seed_for(6, lg)
+        dk = ctx.to_device(synth.base_dlogs(seed, n))
+        xy = ctx.alloc(n * 128)
+        ctx.g2_fixed_base_mul(G2_GEN, dk, n, xy)
+        bases = ctx.bases_g2_from_device(xy, n)
+        del dk, xy
+        ds = ctx.to_device(synth.fr_uniform(seed, n))
+        ctx.fr_to_mont(ds, ds, n)
+        for _ in range(2):
+            res = ctx.msm_g2(bases, ds, n)
+        ts = []
+        for _ in range(steps):
+            ctx.memset(flush, 1)
+            ctx.timer_start()
+            ctx.msm_g2(bases, ds, n)
+            ts.append(ctx.timer_stop())
+        ms = statistics.median(ts)
+        row = {"n": n, "seed": seed, "ms": round(ms, 3), "Mpts_s": round(n / (ms * 1e-3) / 1e6, 2),
+               "window_bits": ctx.msm_last_stats()["window_bits"]}
+        if lg == max(sizes):
+            row["msm_result"] = None if res is None else [hex(v) for v in (res[0][0], res[0][1], res[1][0], res[1][1])]
+        out[f"2^{lg}"] = row
+        bases.free()
+    return out
 
 
 def run_gpu_fixed_base(ctx, args, flush, log_n: int = 20, calls: int = 16) -> dict:
@@ -977,6 +1018,17 @@ def cpu_msm_4096(gpu_row: dict, budget_s: float = 3.0) -> dict:
             "pippenger_matches_known_answer": pip == known}
 
 
+def cpu_check_g2(row: dict) -> bool:
+    """The GPU arm's G2 MSM result against the known answer [sum k_i s_i]G2."""
+    from oracle import oracle as O
+    from pyzkp_gb300 import synth
+
+    n, seed = row["n"], row["seed"]
+    k, s = synth.base_dlogs(seed, n), synth.fr_uniform(seed, n)
+    known = synth.limbs_to_ints(O.g2_mul(O.G2_GENERATOR, O.fr_dot(k, s)).reshape(4, 4))
+    return row.get("msm_result") == [hex(v) for v in known]
+
+
 def cpu_baseline(log_n: int, gpu_result) -> dict:
     """CPU baseline leg (rank 0, N=1): the oracle port timed on a bounded sample; it also
     checks the GPU arm's MSM result against the known answer [sum k_i s_i]G."""
@@ -1051,6 +1103,12 @@ def main() -> None:
                     res["cpu_baseline"] = cpu_baseline(args.log_n, res.get("msm_result"))
                 if res.get("msm_2_12"):
                     res["cpu_baseline"]["msm_2_12"] = cpu_msm_4096(res["msm_2_12"])
+                g2 = res.get("msm_g2") or {}
+                big = max(g2, key=lambda key: g2[key]["n"]) if g2 else None
+                if big and "cpu_baseline" in res:
+                    res["cpu_baseline"]["g2_result_matches_known_answer"] = cpu_check_g2(g2[big])
+                elif big:
+                    res["g2_result_matches_known_answer"] = cpu_check_g2(g2[big])
                 if samples is not None:
                     plonk["sampled_check_ok"] = cpu_check_plonk(samples)
             print(json.dumps(res), flush=True)

@@ -24,7 +24,8 @@ _MASK62 = np.uint64((1 << 62) - 1)
 
 def seed_for(family: int, log_n: int) -> int:
     """Seed of a synthetic input: 0xC0FFEE + 1000*family + log2(n), with the workload family
-    0 = the 4096-point MSM case, 1 = NTTs, 2 = MSM sweeps, 3 = batches, 5 = PLONK quotient."""
+    0 = the 4096-point MSM case, 1 = NTTs, 2 = MSM sweeps, 3 = batches, 5 = PLONK quotient,
+    6 = G2 MSMs."""
     return 0xC0FFEE + 1000 * int(family) + int(log_n)
 
 
