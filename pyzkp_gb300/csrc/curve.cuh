@@ -320,6 +320,11 @@ __device__ __forceinline__ void xyzz_store(XyzzT<T>* p, const XyzzT<T>& a) {
 #ifndef ZK_FIXUP_LONG_G1
 #define ZK_FIXUP_LONG_G1 256
 #endif
+// Minimum resident 128-thread CTAs per SM asked of the G1 merge and fixup kernels (G2 keeps
+// 1: its points need the registers).
+#ifndef ZK_RED_MINB
+#define ZK_RED_MINB 1
+#endif
 #ifndef ZK_FIXUP_LONG_MINB_G1
 #define ZK_FIXUP_LONG_MINB_G1 2
 #endif
@@ -331,6 +336,7 @@ struct CurveG1 {
     static constexpr int kAccMinBlocks = ZK_ACC_MINB;
     static constexpr int kFixupLongThreads = ZK_FIXUP_LONG_G1;
     static constexpr int kFixupLongMinBlocks = ZK_FIXUP_LONG_MINB_G1;
+    static constexpr int kRedMinBlocks = ZK_RED_MINB;
 };
 
 struct CurveG2 {
@@ -341,6 +347,7 @@ struct CurveG2 {
     static constexpr int kAccMinBlocks = ZK_ACC_MINB_G2;
     static constexpr int kFixupLongThreads = 128;
     static constexpr int kFixupLongMinBlocks = 1;
+    static constexpr int kRedMinBlocks = 1;
 };
 
 }  // namespace zk

@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(128, C::kAccMinBlocks) msm_accumulate_kernel(c
 // the group sizes so far). The first merge round uses pairs: most straddling buckets
 // cross exactly one segment boundary, so that round carries nearly all the work.
 template <class C>
-__global__ void __launch_bounds__(128) msm_merge_kernel(const uint32_t* __restrict__ in_keys,
+__global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_merge_kernel(const uint32_t* __restrict__ in_keys,
                                                         const typename C::P* __restrict__ in_pts, uint32_t in_units,
                                                         uint32_t group, const uint32_t* __restrict__ d_total,
                                                         const uint32_t* __restrict__ row_ptr, uint64_t span,
@@ -629,7 +629,7 @@ static constexpr uint32_t kFixupMax = 8;
 static constexpr uint64_t kFixupDensity = ZK_FIXUP_DENSITY;  // CSR entries per bucket up to which the fixup is used
 
 template <class C>
-__global__ void __launch_bounds__(128) msm_fixup_kernel(const uint32_t* __restrict__ row_ptr, uint32_t nbuckets,
+__global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_fixup_kernel(const uint32_t* __restrict__ row_ptr, uint32_t nbuckets,
                                                         uint32_t seg, const typename C::P* __restrict__ slot_pts,
                                                         typename C::P* __restrict__ buckets,
                                                         uint32_t* __restrict__ long_list,
