@@ -169,6 +169,7 @@ int zk_ctx_destroy(zk_ctx* ctx) {
     if (ctx->impl.copy_done) cudaEventDestroy(ctx->impl.copy_done);
     for (cudaEvent_t ev : ctx->impl.chunk_ev)
         if (ev) cudaEventDestroy(ev);
+    if (ctx->impl.inf_flag_dev) cudaFree(ctx->impl.inf_flag_dev);
     cudaStreamDestroy(ctx->impl.stream);
     delete ctx;
     return ZK_OK;
@@ -527,6 +528,7 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
         ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_go, cudaEventDisableTiming));
         ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
         for (cudaEvent_t& ev : c->chunk_ev) ZK_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        ZK_TRY_CUDA(cudaMalloc(reinterpret_cast<void**>(&c->inf_flag_dev), 4));
     }
     void* bases = nullptr;
     void* scalars = nullptr;
@@ -555,18 +557,24 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
     }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(bases, xy_canonical_host, n * 64, cudaMemcpyHostToDevice, c->copy_stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->inf_flag_dev, 0, 4, c->copy_stream);
     if (e == cudaSuccess) {
-        c->stream = c->copy_stream;  // the conversion and GLV kernels are launched on the copy stream
-        rc = zk::convert<zk::FqP, 1>(c, bases, bases, 2 * n);
+        // on the copy stream: mark infinity points, then convert and add the GLV images
+        c->stream = c->copy_stream;
+        rc = zk::mark_infinity(c, bases, n, false, c->inf_flag_dev);
+        if (rc == ZK_OK) rc = zk::convert<zk::FqP, 1>(c, bases, bases, 2 * n);
         if (rc == ZK_OK) rc = zk::glv_phi(c, static_cast<zk::affine_t*>(bases), n);
         c->stream = main_stream;
         e = cudaEventRecord(c->copy_done, c->copy_stream);
     }
-    // main stream: digits and sort; the accumulation waits for copy_done
+    // main stream: digits and sort; the accumulation waits for copy_done (and with it for
+    // the infinity flag)
     if (e == cudaSuccess && rc == ZK_OK) {
         c->bases_wait = c->copy_done;
+        c->inf_flag = c->inf_flag_dev;
         rc = zk::msm_run(c, static_cast<const zk::affine_t*>(bases), static_cast<const zk::fe*>(scalars), n,
                          scalars_mont, window_bits, out_xy, out_is_inf, nullptr, 0, n, /*glv=*/true);
+        c->inf_flag = nullptr;
         c->bases_wait = nullptr;
     }
     c->scalar_chunks.clear();

@@ -320,6 +320,19 @@ __global__ void any_zero_point_kernel(const A* __restrict__ pts, size_t n, uint3
     }
 }
 
+int mark_infinity(Ctx* c, const void* pts, size_t n, bool g2, uint32_t* flag) {
+    if (n == 0) return ZK_OK;
+    const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)c->num_sms * 8);
+    if (g2)
+        ZK_LAUNCH(c, "any_zero_point", any_zero_point_kernel<affine2_t>, blocks, 256, 0,
+                  static_cast<const affine2_t*>(pts), n, flag);
+    else
+        ZK_LAUNCH(c, "any_zero_point", any_zero_point_kernel<affine_t>, blocks, 256, 0,
+                  static_cast<const affine_t*>(pts), n, flag);
+    ZK_TRY_CUDA(cudaGetLastError());
+    return ZK_OK;
+}
+
 int any_infinity(Ctx* c, const void* pts, size_t n, bool g2, bool* out) {
     *out = false;
     if (n == 0) return ZK_OK;
@@ -329,14 +342,11 @@ int any_infinity(Ctx* c, const void* pts, size_t n, bool g2, bool* out) {
     uint32_t h = 0;
     cudaError_t e = cudaMemsetAsync(flag, 0, 4, c->stream);
     if (e == cudaSuccess) {
-        const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)c->num_sms * 8);
-        if (g2)
-            ZK_LAUNCH(c, "any_zero_point", any_zero_point_kernel<affine2_t>, blocks, 256, 0,
-                      static_cast<const affine2_t*>(pts), n, flag);
-        else
-            ZK_LAUNCH(c, "any_zero_point", any_zero_point_kernel<affine_t>, blocks, 256, 0,
-                      static_cast<const affine_t*>(pts), n, flag);
-        e = cudaGetLastError();
+        rc = mark_infinity(c, pts, n, g2, flag);
+        if (rc != ZK_OK) {
+            scratch_free(c, flag);
+            return rc;
+        }
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -542,11 +552,14 @@ __global__ void __launch_bounds__(128, C::kAccMinBlocks) msm_accumulate_kernel(c
                                                              const MsmInst* __restrict__ insts, MsmShape sh,
                                                              uint32_t units, typename C::P* __restrict__ buckets,
                                                              uint32_t* __restrict__ slot_keys,
-                                                             typename C::P* __restrict__ slot_pts) {
+                                                             typename C::P* __restrict__ slot_pts,
+                                                             const uint32_t* __restrict__ inf_flag) {
     using P = typename C::P;
     using A = typename C::A;
     const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= units) return;
+    // kSkipInf: the points may hold infinity; a flag (when given) says whether they do
+    const bool test_inf = kSkipInf && (inf_flag == nullptr || *inf_flag != 0);
     slot_keys[2 * u] = kNone;
     slot_keys[2 * u + 1] = kNone;
     const uint32_t M = *d_total;
@@ -570,7 +583,7 @@ __global__ void __launch_bounds__(128, C::kAccMinBlocks) msm_accumulate_kernel(c
         const uint32_t ent = entries[e];
         A p = affine_load(bases + (ent & 0x7fffffffu));
         if constexpr (kSkipInf)
-            if (affine_is_zero_bits(p)) continue;  // an infinity base adds nothing
+            if (test_inf && affine_is_zero_bits(p)) continue;  // an infinity base adds nothing
         if (ent >> 31) p.y = c_neg(p.y);
         acc = xyzz_madd(acc, p.x, p.y);
     }
@@ -1117,7 +1130,7 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
     // point sets without infinity skip the per-entry test
     auto* accumulate = p.skip_inf ? msm_accumulate_kernel<C, true> : msm_accumulate_kernel<C, false>;
     ZK_LAUNCH(c, "msm_accumulate", accumulate, (p.units + 127) / 128, 128, 0, p.entries, d_total, p.row_ptr,
-              p.d_inst, sh, p.units, p.buckets, p.slot_keys_a, p.slot_pts_a);
+              p.d_inst, sh, p.units, p.buckets, p.slot_keys_a, p.slot_pts_a, p.skip_inf ? c->inf_flag : nullptr);
     ZK_TRY_CUDA(cudaGetLastError());
     // Partial sums of straddling buckets: short buckets (up to ~3 segments on average) by one
     // fixup pass, longer ones by merge rounds (kFixupDensity).

@@ -102,6 +102,10 @@ struct Ctx {
     // its copy); a single-instance pipeline of that size runs its digits chunk by chunk
     std::vector<std::pair<uint32_t, cudaEvent_t>> scalar_chunks;
     cudaEvent_t chunk_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // ... and a device word set there when some uploaded point is infinity: while `inf_flag`
+    // is set, accumulations that test for infinity do so only if the word is non-zero
+    uint32_t* inf_flag_dev = nullptr;
+    const uint32_t* inf_flag = nullptr;
     // MSM batches spread their pipelines over the context stream and these (fork / join
     // events); created on first use
     std::vector<cudaStream_t> side_streams;
@@ -141,6 +145,8 @@ int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scal
 // Whether any of the n stored points (affine_t, or affine2_t when g2) is infinity (all zero);
 // synchronises the context stream.
 int any_infinity(Ctx* c, const void* pts, size_t n, bool g2, bool* out);
+// The same on the context stream without waiting: ORs 1 into *flag if a point is infinity.
+int mark_infinity(Ctx* c, const void* pts, size_t n, bool g2, uint32_t* flag);
 // G1 bases with the GLV half: pts[n + i] = phi(pts[i]) = (beta x_i, y_i) for i < n.
 int glv_phi(Ctx* c, affine_t* pts, size_t n);
 // G2 bases with the GLV half: pts[n + i] = (beta^2 x_i, y_i) = [lambda] P_i.
