@@ -15,8 +15,9 @@
 //         - (a + beta s1 + gamma)(b + beta s2 + gamma)(c + beta s3 + gamma) z(omega x)
 //   num_i = gate + alpha perm + alpha^2 (z - 1) L1
 //   zh_i  = shift_n u^i - 1
-// One thread per chunk of kQChunk consecutive points, the powers of omega_m and u carried
-// from the chunk start (computed by square-and-multiply).
+// One thread per kQChunk points, 32 apart (a warp covers 32 * kQChunk consecutive points, so
+// its loads are contiguous), the powers of omega_m and u carried from the thread's first
+// point (computed by square-and-multiply) in steps of omega_m^32 and u^32.
 #include <cstring>
 
 #include "zk_internal.cuh"
@@ -82,17 +83,20 @@ struct QuotientIn {
 
 struct QuotientK {  // Montgomery constants
     fe omega_m, u, shift, shift_n, alpha, alpha2, beta, gamma, beta_k1, beta_k2, one;
+    fe omega_step, u_step;  // omega_m^32, u^32: a lane's step
 };
 
 __global__ void plonk_quotient_kernel(QuotientIn in, QuotientK K, size_t m, fe* __restrict__ num,
                                       fe* __restrict__ zh) {
+    // a warp covers 32 * kQChunk consecutive points, lane l the points base + l + 32 k (each
+    // load of the warp reads 32 consecutive elements)
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t i0 = t * kQChunk;
+    const size_t lane = t & 31;
+    const size_t i0 = (t - lane) * kQChunk + lane;
     if (i0 >= m) return;
-    const size_t i1 = i0 + kQChunk < m ? i0 + kQChunk : m;
     fe x = fe_mul<FrQ>(K.shift, fr_pow_q(K.omega_m, i0));
     fe un = fr_pow_q(K.u, i0);
-    for (size_t i = i0; i < i1; i++) {
+    for (size_t i = i0, k = 0; k < kQChunk && i < m; k++, i += 32) {
         const fe a = fe_ldg(in.v[0] + i), b = fe_ldg(in.v[1] + i), c = fe_ldg(in.v[2] + i);
         const fe z = fe_ldg(in.v[3] + i);
         fe gate = fe_add<FrQ>(fe_mul<FrQ>(fe_ldg(in.v[5] + i), a), fe_mul<FrQ>(fe_ldg(in.v[6] + i), b));
@@ -112,8 +116,8 @@ __global__ void plonk_quotient_kernel(QuotientIn in, QuotientK K, size_t m, fe* 
         const fe v = fe_add<FrQ>(gate, fe_add<FrQ>(fe_mul<FrQ>(K.alpha, perm), fe_mul<FrQ>(K.alpha2, boundary)));
         fe_store(num + i, v);
         fe_store(zh + i, fe_sub<FrQ>(fe_mul<FrQ>(K.shift_n, un), K.one));
-        un = fe_mul<FrQ>(un, K.u);
-        x = fe_mul<FrQ>(x, K.omega_m);
+        un = fe_mul<FrQ>(un, K.u_step);
+        x = fe_mul<FrQ>(x, K.omega_step);
     }
 }
 
@@ -211,6 +215,8 @@ int zk_plonk_quotient_evals(zk_ctx* ctx, const void* const* inputs, size_t m, ui
     K.beta_k1 = zk::mont_of(zkh::mul(F, bm, zkh::to_mont(F, kk1)));
     K.beta_k2 = zk::mont_of(zkh::mul(F, bm, zkh::to_mont(F, kk2)));
     K.one = zk::mont_of(zkh::one(F));
+    K.omega_step = zk::mont_of(zkh::pow_u64(F, zkh::to_mont(F, om), 32));
+    K.u_step = zk::mont_of(zkh::pow_u64(F, zkh::pow_u64(F, zkh::to_mont(F, om), n), 32));
     zk::Ctx* c = &ctx->impl;
     const size_t chunks = (m + zk::kQChunk - 1) / zk::kQChunk;
     ZK_LAUNCH(c, "plonk_quotient", zk::plonk_quotient_kernel, (unsigned)((chunks + 127) / 128), 128, 0, in, K, m,
