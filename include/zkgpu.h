@@ -260,8 +260,10 @@ int zk_autotune_load(zk_ctx *ctx, const char *path);
  * static device array of the library (2 MiB + 128 KiB per device that loads it,
  * held until exit), so n <= 2^16 (log_n <= 16, larger sizes give ZK_EINVAL). Every
  * call on a device shares that array: calls that overlap on the GPU race and must be
- * serialised by the caller. The first call on each device sets up the array's device
- * address; make that first call before any stream capture.
+ * serialised by the caller. Each call rebuilds its tables on the device from values its
+ * kernel launch carries, so the GPU reads no host memory of the library. The first call
+ * on each device sets up the array's device address; make that first call before any
+ * stream capture.
  */
 int zk_ntt_noalloc(zk_ctx *ctx, int mode, void *out_dev, const void *in_dev, size_t in_len, uint32_t log_n,
                    const uint8_t omega[32], const uint8_t shift[32]);

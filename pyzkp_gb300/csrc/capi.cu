@@ -523,13 +523,14 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
         return ZK_OK;
     }
     Ctx* c = &ctx->impl;
-    if (c->copy_stream == nullptr) {
-        ZK_TRY_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-        ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_go, cudaEventDisableTiming));
-        ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
-        for (cudaEvent_t& ev : c->chunk_ev) ZK_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-        ZK_TRY_CUDA(cudaMalloc(reinterpret_cast<void**>(&c->inf_flag_dev), 4));
-    }
+    // each lazily created resource under its own check: a failure part way leaves the rest
+    // to be created by the next call
+    if (c->copy_stream == nullptr) ZK_TRY_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    if (c->copy_go == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_go, cudaEventDisableTiming));
+    if (c->copy_done == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
+    for (cudaEvent_t& ev : c->chunk_ev)
+        if (ev == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    if (c->inf_flag_dev == nullptr) ZK_TRY_CUDA(cudaMalloc(reinterpret_cast<void**>(&c->inf_flag_dev), 4));
     void* bases = nullptr;
     void* scalars = nullptr;
     int rc = zk::scratch_alloc(c, 2 * n * sizeof(zk::affine_t), &bases);

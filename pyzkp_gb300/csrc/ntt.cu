@@ -718,10 +718,13 @@ void ntt_plan_destroy(Ctx* c, NttBatchPlan* plan) {
 // static device array of fixed size. Limits and rules:
 //   * n <= 2^16 (kNoAllocMaxLogN); larger sizes are rejected with ZK_EINVAL;
 //   * the array is shared by every call on a device and keeps the last call's
-//     contents; nothing in it has to start at zero (each call uploads its tables and
-//     its first pass writes every element the second pass reads), but calls that
-//     overlap on the GPU (different streams, or different contexts of one device)
-//     race on it and must be serialised by the caller;
+//     contents; nothing in it has to start at zero (each call rebuilds its tables on
+//     the device and its first pass writes every element the second pass reads), but
+//     calls that overlap on the GPU (different streams, or different contexts of one
+//     device) race on it and must be serialised by the caller;
+//   * the tables are computed on the device by a kernel that receives their generators
+//     by value (no host buffer is read by the GPU, so nothing on the host outlives the
+//     call);
 //   * the first call on each device does the set-up (cudaGetSymbolAddress of the
 //     array, the kernel's shared-memory attribute), so that first call should come
 //     before any stream capture;
@@ -760,17 +763,49 @@ static int noalloc_setup(int device, fe** out) {
     return ZK_OK;
 }
 
-// Host staging of the tables (fixed size, reused; guarded by g_noalloc_stage_mu).
-static std::mutex g_noalloc_stage_mu;
-static zkh::F4 g_noalloc_stage[kNoAllocTableElems];
+// The tables as segments: table[off + i] = start * base^i for i < count (Montgomery),
+// built on the device from these values, which the launch carries by value.
+static constexpr int kNoAllocMaxSegs = 10;
+struct NoAllocTableSpec {
+    uint32_t nseg;
+    uint32_t off[kNoAllocMaxSegs];
+    uint32_t count[kNoAllocMaxSegs];
+    fe start[kNoAllocMaxSegs];
+    fe base[kNoAllocMaxSegs];
+};
 
-static void stage_powers(const zkh::F4& base, size_t count, size_t* pos, const zkh::F4* scale = nullptr) {
-    const zkh::Field& F = zkh::fr();
-    zkh::F4 cur = scale ? *scale : zkh::one(F);
-    for (size_t i = 0; i < count; i++) {
-        g_noalloc_stage[(*pos)++] = cur;
-        cur = zkh::mul(F, cur, base);
+__global__ void ntt_noalloc_tables_kernel(fe* __restrict__ tables, NoAllocTableSpec S) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t s = 0; s < S.nseg; s++) {
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < S.count[s]; i += stride) {
+            fe acc = S.start[s];
+            fe b = S.base[s];
+            for (uint32_t e = i; e != 0; e >>= 1) {  // square-and-multiply, exponent i < 2^10
+                if (e & 1) acc = fe_mul<FrP>(acc, b);
+                if (e > 1) b = fe_mul<FrP>(b, b);
+            }
+            fe_store(tables + S.off[s] + i, acc);
+        }
     }
+}
+
+static fe to_fe(const zkh::F4& x) {
+    fe r;
+    std::memcpy(r.v, x.v, 32);
+    return r;
+}
+
+// Appends the segment start * base^i, i < count, at *pos; false when the spec is full.
+static bool add_segment(NoAllocTableSpec* S, size_t* pos, const zkh::F4& base, size_t count,
+                        const zkh::F4* start = nullptr) {
+    if (S->nseg >= (uint32_t)kNoAllocMaxSegs) return false;
+    const uint32_t k = S->nseg++;
+    S->off[k] = (uint32_t)*pos;
+    S->count[k] = (uint32_t)count;
+    S->start[k] = to_fe(start ? *start : zkh::one(zkh::fr()));
+    S->base[k] = to_fe(base);
+    *pos += count;
+    return true;
 }
 
 static int ntt_run_noalloc(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log_n,
@@ -805,26 +840,27 @@ static int ntt_run_noalloc(Ctx* c, int mode, fe* out, const fe* in, size_t in_le
     const uint64_t hi_count = (n >> plan.s_bits) + 1;
     const zkh::F4 w = inverse ? zkh::inv(F, om) : om;
 
-    std::lock_guard<std::mutex> g(g_noalloc_stage_mu);
+    NoAllocTableSpec spec{};
+    bool ok = true;
     size_t pos = 0;
-    size_t off_lo = pos;
-    stage_powers(w, lo_count, &pos);
-    size_t off_hi = pos;
-    stage_powers(zkh::pow_u64(F, w, lo_count), hi_count, &pos);
+    const size_t off_lo = pos;
+    ok = ok && add_segment(&spec, &pos, w, lo_count);
+    const size_t off_hi = pos;
+    ok = ok && add_segment(&spec, &pos, zkh::pow_u64(F, w, lo_count), hi_count);
     size_t off_radix[4] = {0, 0, 0, 0};
     for (int p = 0; p < plan.npass; p++) {
         off_radix[p] = pos;
         const uint32_t lr = plan.pass_log_r[p];
-        stage_powers(zkh::pow_u64(F, w, n >> lr), std::max<uint64_t>(1, (1ull << lr) / 2), &pos);
+        ok = ok && add_segment(&spec, &pos, zkh::pow_u64(F, w, n >> lr), std::max<uint64_t>(1, (1ull << lr) / 2));
     }
     size_t off_pre_lo = 0, off_pre_hi = 0, off_post_lo = 0, off_post_hi = 0;
     bool has_pre = false, has_post = false, post_const = false;
     if (mode == ZK_NTT_COSET_EVALS_FROM_COEFFS) {
         has_pre = true;
         off_pre_lo = pos;
-        stage_powers(sh, lo_count, &pos);
+        ok = ok && add_segment(&spec, &pos, sh, lo_count);
         off_pre_hi = pos;
-        stage_powers(zkh::pow_u64(F, sh, lo_count), hi_count, &pos);
+        ok = ok && add_segment(&spec, &pos, zkh::pow_u64(F, sh, lo_count), hi_count);
     }
     if (inverse) {
         has_post = true;
@@ -833,21 +869,20 @@ static int ntt_run_noalloc(Ctx* c, int mode, fe* out, const fe* in, size_t in_le
         off_post_lo = pos;
         if (mode == ZK_NTT_COEFFS_FROM_EVALS) {
             post_const = true;
-            g_noalloc_stage[pos++] = ninv;
+            ok = ok && add_segment(&spec, &pos, zkh::one(F), 1, &ninv);
         } else {
             zkh::F4 is = zkh::is_zero(sh) ? sh : zkh::inv(F, sh);
-            stage_powers(is, lo_count, &pos, &ninv);
+            ok = ok && add_segment(&spec, &pos, is, lo_count, &ninv);
             off_post_hi = pos;
-            stage_powers(zkh::pow_u64(F, is, lo_count), hi_count, &pos);
+            ok = ok && add_segment(&spec, &pos, zkh::pow_u64(F, is, lo_count), hi_count);
         }
     }
-    if (pos > kNoAllocTableElems) {
+    if (!ok || pos > kNoAllocTableElems) {
         set_error("zk_ntt_noalloc: table layout exceeds the static scratch");
         return ZK_EINVAL;
     }
-    // pageable source: the copy is staged before cudaMemcpyAsync returns, so the host
-    // staging area may be reused by the next call
-    ZK_TRY_CUDA(cudaMemcpyAsync(tables, g_noalloc_stage, pos * 32, cudaMemcpyHostToDevice, c->stream));
+    ZK_LAUNCH(c, "ntt_noalloc_tables", ntt_noalloc_tables_kernel, 8, 256, 0, tables, spec);
+    ZK_TRY_CUDA(cudaGetLastError());
 
     const uint32_t valid = (uint32_t)(in_len < n ? in_len : n);
     NttPassParams P{};

@@ -229,8 +229,8 @@ def _g1_point(res):
 
 # ------------------------------------------------------------------------------ context
 def _ir_for(registry) -> Any:
-    """The module holding OpType / Device / Backend / DType / Buffer of ``registry``'s runtime:
-    the reference's ``runtime.ir`` or this package's mirror."""
+    """The module holding OpType / Device / Backend / DType / Buffer of ``registry``'s runtime
+    (the reference's ``runtime.ir`` for ``runtime.kernels.registry.KernelRegistry``)."""
     modname = type(registry).__module__
     if modname.endswith(".kernels.registry"):
         return importlib.import_module(modname[: -len(".kernels.registry")] + ".ir")
@@ -268,14 +268,14 @@ def _shared_runtime(device: int = 0) -> GpuRuntime:
 
 
 def _default_ir():
+    """The reference's ``runtime.ir`` (its IR types); the plugin has no runtime of its own."""
     if "runtime.ir" in sys.modules:
         return sys.modules["runtime.ir"]
     try:
         return importlib.import_module("runtime.ir")
-    except ImportError:
-        from pyzkp_gb300 import runtime_mirror
-
-        return runtime_mirror
+    except ImportError as e:
+        raise ImportError("pyZKP's runtime (runtime.ir) is not importable: put the reference on sys.path, "
+                          "or pass its runtime.ir module as ir=") from e
 
 
 # ------------------------------------------------------------------------------ helpers
@@ -324,7 +324,7 @@ def _log2_exact(n: int) -> int:
 
 # ------------------------------------------------------------------------------ registration
 def register_gb300_kernels(registry, *, ir: Any = None) -> None:
-    """Register the GB300 KernelFns into ``registry`` (the reference's KernelRegistry or the mirror)."""
+    """Register the GB300 KernelFns into ``registry`` (the reference's ``KernelRegistry``)."""
     ir = ir or _ir_for(registry)
     OpType, Device, Backend, DType, Buffer = ir.OpType, ir.Device, ir.Backend, ir.DType, ir.Buffer
     METAL, BM = Device.METAL, Backend.METAL

@@ -1,7 +1,7 @@
 """Generate golden vectors by running the unmodified reference (fzybravery/pyZKP).
 
-Run in a container that has the reference checked out (default path
-``/root/reference``, override with ``PYZKP_REFERENCE``):
+Needs the reference: ``PYZKP_REFERENCE`` (a checkout or install directory) or the pip
+install in ``baseline/_ref`` (tests/reference_env.py finds it):
 
     python tests/golden/make_golden.py
 
@@ -32,12 +32,12 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("PYZKP_REFERENCE", "/root/reference")
-
-sys.dont_write_bytecode = True
 sys.path.insert(0, REPO)
-sys.path.insert(0, os.path.join(REPO, "oracle", "py_ecc_shim"))
-sys.path.insert(0, REF)
+sys.path.insert(0, os.path.join(REPO, "tests"))
+
+import reference_env  # noqa: E402
+
+reference_env.add_to_path()
 
 import numpy as np  # noqa: E402
 

@@ -1,7 +1,7 @@
 """Generate Groth16 golden vectors by running the unmodified reference (fzybravery/pyZKP).
 
-Run in a container that has the reference checked out (default path
-``/root/reference``, override with ``PYZKP_REFERENCE``):
+Needs the reference: ``PYZKP_REFERENCE`` (a checkout or install directory) or the pip
+install in ``baseline/_ref`` (tests/reference_env.py finds it):
 
     python tests/golden/make_groth16_golden.py
 
@@ -28,11 +28,11 @@ from dataclasses import dataclass
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("PYZKP_REFERENCE", "/root/reference")
+sys.path.insert(0, os.path.join(REPO, "tests"))
 
-sys.dont_write_bytecode = True
-sys.path.insert(0, os.path.join(REPO, "oracle", "py_ecc_shim"))
-sys.path.insert(0, REF)
+import reference_env  # noqa: E402
+
+reference_env.add_to_path()
 
 import importlib  # noqa: E402
 

@@ -1,12 +1,14 @@
-"""GPU tests of the drop-in KernelFns (pyzkp_gb300.plugin) through the executor.
+"""GPU tests of the drop-in KernelFns (pyzkp_gb300.plugin) through the reference's own runtime.
 
 They follow the reference's Metal tests (tests/correctness/metal/test_runtime_metal_*.py):
-register the transfer kernels and the device kernels, build a Graph with
-TO_DEVICE -> op -> FROM_DEVICE, run it with RuntimeConfig(backend=METAL), and
-compare with the reference's CPU result -- here the committed golden vectors made
-by running the reference (tests/golden/make_golden.py) or exact Python arithmetic.
-The runtime types come from pyzkp_gb300.runtime_mirror (the reference is not on the
-GPU machine); py_ecc is the test-only stand-in under oracle/py_ecc_shim.
+register the reference's CPU kernels and the GB300 kernels into the reference's
+``KernelRegistry``, build a ``Graph`` with TO_DEVICE -> op -> FROM_DEVICE, run it with the
+reference's ``Executor`` under ``RuntimeConfig(backend=METAL)`` (``plugin.install()`` makes
+that config create a GB300 context), and compare with the reference's CPU result -- the
+committed golden vectors made by running the reference (tests/golden/make_golden.py,
+make_plonk_golden.py) or exact Python arithmetic. The reference comes from
+``PYZKP_REFERENCE`` or ``baseline/_ref`` (tests/reference_env.py); py_ecc is the test-only
+stand-in under oracle/py_ecc_shim.
 """
 
 import json
@@ -15,17 +17,19 @@ import sys
 
 import pytest
 
+import reference_env
+
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle", "py_ecc_shim"))
+R = reference_env.runtime()
 
 from py_ecc import optimized_bn128 as bn  # noqa: E402
 
 from oracle import oracle as O  # noqa: E402
 from pyzkp_gb300 import plugin, synth  # noqa: E402
-from pyzkp_gb300 import runtime_mirror as R  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 FR = synth.FR_MODULUS
+plugin.install()
 
 
 def _golden(name):
@@ -34,7 +38,9 @@ def _golden(name):
 
 
 def _exe():
+    """A registry set up the way the reference's provers do it (protocols/groth16/prove.py:56-62)."""
     reg = R.KernelRegistry()
+    R.register_cpu_kernels(reg, backend=R.Backend.METAL)
     plugin.register_gb300_kernels(reg)
     return R.Executor(registry=reg), reg
 
@@ -214,7 +220,7 @@ def test_kzg_batch_commit_and_msm_batch():
 def test_pool_reuse_with_gb300_runtime():
     # tests/correctness/metal/test_runtime_metal_pool.py against GB300 memory
     pool = R.MemoryPool()
-    rt = plugin.GpuContext.create_default(ir=R).metal
+    rt = plugin.GpuContext.create_default(ir=R.ir).metal
     b1 = pool.alloc_metal(rt, 1024)
     b2 = pool.alloc_metal(rt, 1024)
     assert pool.metal_stats.alloc_calls == 2 and pool.metal_stats.in_use == 2
@@ -356,14 +362,7 @@ def test_batch_inv_op_zero_maps_to_zero():
     assert got == [pow(v, FR - 2, FR) if v else 0 for v in vals]
 
 
-def test_plonk_t_quotient_evals_op_matches_cpu_kernel():
-    m, n = 64, 16
-    om = O.omega_for_size(m)
-    vecs = [synth.limbs_to_ints(synth.fr_uniform(910 + j, m)) for j in range(15)]
-    attrs = {"n": n, "m": m, "omega_m": om, "shift": 7, "shift_n": pow(7, n, FR), "alpha": 11111, "beta": 22222,
-             "gamma": 33333, "k1": 2, "k2": 3}
-    exp_num, exp_zh = O.plonk_t_quotient_evals(vecs, n, om, 7, pow(7, n, FR), 11111, 22222, 33333, 2, 3)
-    exe, _ = _exe()
+def _plonk_quotient_graph(vecs, attrs, exe):
     g = R.Graph()
     names = [f"v{j}" for j in range(15)]
     for name, v in zip(names, vecs):
@@ -372,6 +371,29 @@ def test_plonk_t_quotient_evals_op_matches_cpu_kernel():
     g.add_node(op=R.OpType.BATCH_INV, inputs=["zh"], outputs=["inv_zh"])
     g.add_node(op=R.OpType.POINTWISE_MUL, inputs=["num", "inv_zh"], outputs=["t"])
     exe.run(g, runtime_config=_cfg(), keep=["num", "zh", "t"])
-    assert list(g.buffers["num"].data) == exp_num
-    assert list(g.buffers["zh"].data) == exp_zh
-    assert list(g.buffers["t"].data) == [x * pow(z, FR - 2, FR) % FR if z else 0 for x, z in zip(exp_num, exp_zh)]
+    return [list(g.buffers[k].data) for k in ("num", "zh", "t")]
+
+
+def _fr_sha(vals):
+    import hashlib
+
+    return hashlib.sha256(b"".join(int(v).to_bytes(32, "little") for v in vals)).hexdigest()
+
+
+def test_plonk_t_quotient_evals_op_matches_reference_golden():
+    """PLONK_T_QUOTIENT_EVALS against the reference's own _plonk_t_quotient_evals
+    (runtime/kernels/cpu/kernels.py:607-693) on its committed outputs: m = 2^6 .. 2^10, 2^12,
+    a ragged m = 100 and a shift_n that is not shift^n, every element compared (SHA-256 of
+    the whole vector, plus sampled values); then BATCH_INV and POINTWISE_MUL as in
+    protocols/plonk/prove.py:412-414."""
+    exe, _ = _exe()
+    for rec in _golden("plonk_reference.json")["quotient"]:
+        m = rec["m"]
+        vecs = [synth.limbs_to_ints(synth.fr_uniform(rec["seed"] + j, m)) for j in range(15)]
+        attrs = {k: (v if isinstance(v, int) else int(v, 16)) for k, v in rec["attrs"].items()}
+        num, zh, t = _plonk_quotient_graph(vecs, attrs, exe)
+        assert _fr_sha(num) == rec["num_sha256"], m
+        assert _fr_sha(zh) == rec["zh_sha256"], m
+        for i, v in rec["num_at"].items():
+            assert num[int(i)] == int(v, 16), (m, i)
+        assert t == [x * pow(z, FR - 2, FR) % FR if z else 0 for x, z in zip(num, zh)]

@@ -135,3 +135,31 @@ def test_oracle_g2_matches_shim_and_known_answer():
     assert not bases[7].any()
     s = synth.fr_witness_like(32, 200)
     assert (O.g2_msm(bases, s) == O.g2_msm_known_answer(k, s)).all()
+
+
+PLONK_INPUTS = 15
+
+
+def plonk_quotient_case_inputs(rec):
+    """The 15 input vectors and the attrs of a ``plonk_reference.json`` quotient record."""
+    m = rec["m"]
+    vecs = [synth.limbs_to_ints(synth.fr_uniform(rec["seed"] + j, m)) for j in range(PLONK_INPUTS)]
+    attrs = {k: (v if isinstance(v, int) else int(v, 16)) for k, v in rec["attrs"].items()}
+    return vecs, attrs
+
+
+def _fr_sha(vals):
+    return hashlib.sha256(b"".join(int(v).to_bytes(32, "little") for v in vals)).hexdigest()
+
+
+def test_plonk_quotient_oracle_matches_reference_golden():
+    """oracle/oracle.py's restatement of _plonk_t_quotient_evals (runtime/kernels/cpu/kernels.py:607-693)
+    reproduces the reference's own outputs (tests/golden/make_plonk_golden.py)."""
+    for rec in _golden("plonk_reference.json")["quotient"]:
+        vecs, a = plonk_quotient_case_inputs(rec)
+        num, zh = O.plonk_t_quotient_evals(vecs, a["n"], a["omega_m"], a["shift"], a["shift_n"], a["alpha"],
+                                           a["beta"], a["gamma"], a["k1"], a["k2"])
+        assert _fr_sha(num) == rec["num_sha256"], rec["m"]
+        assert _fr_sha(zh) == rec["zh_sha256"], rec["m"]
+        for i, v in rec["num_at"].items():
+            assert num[int(i)] == int(v, 16)
