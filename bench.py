@@ -173,7 +173,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
         flush = ctx.alloc(FLUSH_BYTES)
         return {"batch": run_gpu_batch(ctx, args, flush)}
     if args.only == "serve":
-        return {"serve": run_gpu_serve(ctx, args)}
+        return {"groth16_serve": run_gpu_serve(ctx, args)}
     if args.only == "plonk":
         return {"plonk_quotient_2_20": run_gpu_plonk(ctx, args, ctx.alloc(FLUSH_BYTES))}
     if args.only == "g2":
@@ -875,54 +875,103 @@ def run_gpu_plonk(ctx, args, flush, log_n: int = 20) -> dict:
             "work": "15 coset NTTs n -> 4n (one batched call), quotient evals, batch inverse, product, coset iNTT"}
 
 
+_SERVE_VERIFY_JOBS: list = []
+
+
 def run_gpu_serve(ctx, args, requests: int = 200, grid=tuple(x / 2 for x in range(20, 37))) -> dict:
     """Groth16 proof serving: Poisson arrivals, request sizes m = round(2^U), U ~ Uniform[10, 18],
     snapped to resident circuits at U on a 0.5 grid (a circuit needs its own proving key);
     synthetic diagonal R1CS (x_i y_i = z_i), keys from a fast own setup. Continuous batching
-    against the plain one-at-a-time prover on the same traces; proofs must agree bit for bit."""
+    (three slot contexts, the first at the most urgent stream priority for small requests)
+    against batch-at-a-time and the plain one-at-a-time prover on the same traces; the proofs
+    of every mode must agree bit for bit, and every continuous-mode proof is verified with the
+    reference's verification equation by the CPU leg (off the timed path)."""
     from pyzkp_gb300 import groth16 as G
     from pyzkp_gb300 import serve
 
     t0 = time.perf_counter()
-    keys, wits, sizes = {}, {}, {}
+    keys, wits, sizes, pubs = {}, {}, {}, {}
     for i, u in enumerate(grid):
         m = int(round(2 ** u))
         keys[i] = G.setup(ctx, G.diagonal_r1cs(m), G.Trapdoors.seeded(0x5E7 + i))
-        wits[i], _ = G.diagonal_witness(ctx, m, 0xA11CE + i)
+        wits[i], pubs[i] = G.diagonal_witness(ctx, m, 0xA11CE + i)
         sizes[i] = m
     setup_s = time.perf_counter() - t0
     prover = G.Prover(ctx)
-    svc = serve.ProverService(prover, keys, wits, budget_bytes=48 << 30, max_batch=64)
+    svc = serve.ProverService(prover, keys, wits, budget_bytes=48 << 30, max_batch=64, slots=3)
     weights = [0.5] + [1.0] * (len(grid) - 2) + [0.5]
-    # warm-up, then the closed-loop capacity of one full batch and of one-at-a-time proving
-    warm = serve.poisson_trace(1e9, len(grid), list(keys), seed=1)
-    svc.run(warm, batched=True)
+    svc.warm()
+    # closed-loop capacity: a burst of requests all present at t = 0
     closed = serve.poisson_trace(1e9, 64, list(keys), seed=2, weights=weights)
-    t1 = time.perf_counter()
-    svc.run(closed, batched=True)
-    cap_batched = len(closed) / (time.perf_counter() - t1)
-    t1 = time.perf_counter()
-    svc.run(closed[:16], batched=False)
-    cap_plain = 16 / (time.perf_counter() - t1)
+    cap = {}
+    for mode, tr in (("continuous", closed), ("batch", closed), ("plain", closed[:16])):
+        t1 = time.perf_counter()
+        res = svc.run(tr, mode)
+        cap[mode] = len(tr) / (time.perf_counter() - t1)
+        if mode == "continuous":
+            cap_proofs = res.proofs
     sweep = []
     exact = True
+    verify_jobs = []
+
+    def collect(trace, res):
+        for a, p in zip(trace, res.proofs):
+            if p is not None:
+                k = keys[a.key_id]
+                vk = (k.vk.alpha_g1, k.vk.beta_g2, k.vk.gamma_g2, k.vk.delta_g2, k.vk.ic)
+                verify_jobs.append((a.key_id, vk, pubs[a.key_id], (p.a, p.b, p.c)))
+
+    collect(closed, type("R", (), {"proofs": cap_proofs})())
     for frac in (0.25, 0.5, 0.9):
-        rate = frac * cap_batched
+        rate = frac * cap["continuous"]
         tr = serve.poisson_trace(rate, requests, list(keys), seed=int(frac * 1000), weights=weights)
-        rb = svc.run(tr, batched=True)
-        rp = svc.run(tr, batched=False)
-        exact = exact and rb.proofs == rp.proofs
-        sweep.append({"rate_per_s": round(rate, 1), "batched": rb.summary(), "plain": rp.summary()})
+        rc = svc.run(tr, "continuous")
+        rb = svc.run(tr, "batch")
+        rp = svc.run(tr, "plain")
+        exact = exact and rc.proofs == rp.proofs and rb.proofs == rp.proofs and all(p is not None for p in rc.proofs)
+        collect(tr, rc)
+        sweep.append({"rate_per_s": round(rate, 1), "continuous": rc.summary(), "batch": rb.summary(),
+                      "plain": rp.summary()})
+    svc.close()
+    _SERVE_VERIFY_JOBS[:] = verify_jobs
     mean_m = sum(w * sizes[i] for i, w in zip(sorted(sizes), weights)) / sum(weights)
     return {
         "workload": "Groth16 prove, diagonal R1CS, m = round(2^U), U ~ U[10,18] on a 0.5 grid, Poisson arrivals",
         "circuits": len(grid), "constraints": [sizes[i] for i in sorted(sizes)], "mean_constraints": round(mean_m),
         "setup_s": round(setup_s, 2), "key_bytes": sum(k.device_bytes() for k in keys.values()),
-        "capacity_batched_proofs_s": round(cap_batched, 1), "capacity_plain_proofs_s": round(cap_plain, 1),
-        "sweep": sweep, "bit_exact_batched_vs_plain": exact,
+        "capacity_proofs_s": {k: round(v, 1) for k, v in cap.items()},
+        "capacity_continuous_over_plain": round(cap["continuous"] / cap["plain"], 2),
+        "capacity_batch_over_plain": round(cap["batch"] / cap["plain"], 2),
+        "sweep": sweep, "bit_exact_all_modes": exact,
+        "proofs_total": len(verify_jobs), "proofs_verified": None,
         "note": "latency = completion - arrival on the wall clock; proof assembly (5 host scalar "
-                "multiplications per proof) runs on host threads",
+                "multiplications per proof) runs on host threads; proofs_verified is filled by the CPU leg",
     }
+
+
+def _verify_chunk(jobs):
+    from oracle import groth16_verify as V
+
+    return V.verify_many(jobs)
+
+
+def cpu_verify_serve(jobs) -> dict:
+    """Every served proof through the reference's verification equation (protocols/groth16/
+    verify.py:11-23) with the stand-in pairing, in a spawned process pool (off the timed path)."""
+    import multiprocessing as mp
+
+    if not jobs:
+        return {"proofs_verified": 0, "proofs_total": 0}
+    t0 = time.perf_counter()
+    workers = max(1, min(16, (os.cpu_count() or 2) - 1))
+    # chunks grouped by key so that each worker builds few verifiers
+    jobs = sorted(jobs, key=lambda j: j[0])
+    chunks = [jobs[i::workers * 2] for i in range(workers * 2)]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        res = [ok for part in pool.map(_verify_chunk, chunks) for ok in part]
+    return {"proofs_verified": int(sum(res)), "proofs_total": len(res), "verify_s": round(time.perf_counter() - t0, 1),
+            "verifier": "reference verification equation (protocols/groth16/verify.py:11-23), py_ecc stand-in "
+                        f"pairing, {workers} host processes"}
 
 
 def load_peaks() -> dict:
@@ -1111,6 +1160,8 @@ def main() -> None:
                     res["g2_result_matches_known_answer"] = cpu_check_g2(g2[big])
                 if samples is not None:
                     plonk["sampled_check_ok"] = cpu_check_plonk(samples)
+                if res.get("groth16_serve") and _SERVE_VERIFY_JOBS:
+                    res["groth16_serve"].update(cpu_verify_serve(_SERVE_VERIFY_JOBS))
             print(json.dumps(res), flush=True)
     finally:
         ranks.close()

@@ -51,6 +51,12 @@ int zk_version(void);
  * (runtime/metal/runtime.py:493-629, runtime/context.py:42-47).
  */
 int zk_ctx_create(int device, zk_ctx **out);
+/* The same with a CUDA stream priority for the context's streams (lower = more urgent;
+ * clamped into zk_stream_priority_range). A serving loop gives its short requests a more
+ * urgent context, so that their kernels are scheduled ahead of a long batch's. No
+ * counterpart in the reference (its Metal command queue has no priorities). */
+int zk_ctx_create_prio(int device, int priority, zk_ctx **out);
+int zk_stream_priority_range(int *least, int *greatest);
 int zk_ctx_destroy(zk_ctx *ctx);
 /* Block until all work queued on the context stream has finished. */
 int zk_ctx_sync(zk_ctx *ctx);
@@ -92,6 +98,20 @@ int zk_free(zk_ctx *ctx, void *dptr);
 /* Copies on the context stream; both block until the copy is complete. */
 int zk_h2d(zk_ctx *ctx, void *dst_dev, const void *src_host, size_t bytes);
 int zk_d2h(zk_ctx *ctx, void *dst_host, const void *src_dev, size_t bytes);
+/* The same copies without waiting: they return once enqueued on the context stream. The
+ * host buffer must stay valid -- and, for zk_d2h_async, unread -- until the stream has
+ * passed the copy (a fence, zk_ctx_sync or a blocking call); page-locked memory
+ * (zk_host_alloc) lets the copy overlap other work. */
+int zk_h2d_async(zk_ctx *ctx, void *dst_dev, const void *src_host, size_t bytes);
+int zk_d2h_async(zk_ctx *ctx, void *dst_host, const void *src_dev, size_t bytes);
+/* Fence: a point on the context stream after everything enqueued so far.
+ * zk_fence_wait returns ZK_OK once the device has passed it, ZK_ETIMEOUT if timeout_ms
+ * (>= 0; 0 = just ask) passes first; a negative timeout waits without a limit. No
+ * counterpart in the reference (its Metal ops wait for completion inside every op). */
+typedef struct zk_fence zk_fence;
+int zk_fence_record(zk_ctx *ctx, zk_fence **out);
+int zk_fence_wait(zk_fence *f, int timeout_ms);
+int zk_fence_destroy(zk_fence *f);
 /* Device-to-device copy on the context stream (asynchronous). */
 int zk_d2d(zk_ctx *ctx, void *dst_dev, const void *src_dev, size_t bytes);
 /* Fill bytes of device memory (asynchronous on the context stream). */
@@ -179,6 +199,9 @@ int zk_ntt_plan_destroy(zk_ntt_plan *plan);
  *                       R1CS rows A w, B w, C w of eval_r1cs_vectors.
  *   zk_fr_r1cs_check    *bad = #{i : a[i] b[i] != c[i]}: zero iff A B - C vanishes on the
  *                       domain, i.e. the remainder of qap.py:94-95 is empty.
+ *   zk_fr_r1cs_check_async  the same count added to the uint64 at bad_dev (device memory,
+ *                       zeroed by the caller) without waiting: a serving loop reads it
+ *                       with the request's other results and fails only that request.
  *   zk_fr_qap_quotient  out[i] = (a[i] b[i] - c[i]) * zinv (zinv canonical): on the coset
  *                       shift * <omega>, zinv = (shift^n - 1)^-1 divides by X^n - 1.
  *   zk_fr_gather        out[i] = in[idx[i]] (idx uint32 device).
@@ -192,6 +215,7 @@ int zk_ntt_plan_destroy(zk_ntt_plan *plan);
 int zk_fr_spmv(zk_ctx *ctx, uint32_t nrows, const uint32_t *row_ptr_dev, const uint32_t *cols_dev,
                const void *coeffs_dev, const void *x_dev, void *out_dev);
 int zk_fr_r1cs_check(zk_ctx *ctx, const void *a, const void *b, const void *c, size_t n, uint64_t *bad);
+int zk_fr_r1cs_check_async(zk_ctx *ctx, const void *a, const void *b, const void *c, size_t n, void *bad_dev);
 int zk_fr_qap_quotient(zk_ctx *ctx, void *out, const void *a, const void *b, const void *c, size_t n,
                        const uint8_t zinv[32]);
 int zk_fr_gather(zk_ctx *ctx, void *out, const void *in, const uint32_t *idx_dev, size_t n);
@@ -232,11 +256,12 @@ int zk_host_g2_add(const uint8_t p[128], const uint8_t q[128], uint8_t out[128])
 /*
  * Tuning tables of a context (0 = the built-in rule). MSM: window bits for MSMs whose
  * ceil(log2 n) is log_n (the reference's fixed rule is max(4, min(16, bitlen(n) - 2)),
- * runtime/kernels/cpu/kernels.py:553-571; this library's default is clamp(log2 n - 3,
- * 4, 16)). NTT: radix bits of each pass for 2^log_n (1..4 passes of 1..11 bits summing
+ * runtime/kernels/cpu/kernels.py:553-571; this library's default is a measured table per
+ * size). NTT: radix bits of each pass for 2^log_n (1..4 passes of 1..11 bits summing
  * to log_n; default: the fewest passes, as equal as possible). zk_tune_get_* report the
- * effective choice. zk_autotune_msm / zk_autotune_ntt time the candidates on the device
- * and keep the fastest (best_ms: its time); zk_autotune_save / _load write and read the
+ * effective choice. zk_autotune_msm / zk_autotune_ntt time the built-in choice and the
+ * candidates on the device and keep a candidate only if it beats the built-in choice by
+ * more than 3% (else the entry stays 0; best_ms: the kept choice's time); zk_autotune_save / _load write and read the
  * tables as JSON ({"msm_window": {"20": 17}, "ntt_split": {"20": [10, 10]}}). Tuning
  * changes timings only, never results. No reference counterpart.
  */

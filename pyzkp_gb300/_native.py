@@ -41,7 +41,8 @@ EXPORTED_SYMBOLS = (
     "zk_msm_g2", "zk_msm_g2_batch", "zk_g2_fixed_base_mul", "zk_fr_spmv", "zk_fr_r1cs_check",
     "zk_fr_qap_quotient", "zk_fr_gather", "zk_fr_scale", "zk_fr_powers", "zk_fr_div_xn_minus_1", "zk_host_g1_mul",
     "zk_host_g1_add", "zk_host_g2_mul", "zk_host_g2_add", "zk_fr_add", "zk_bases_g2_create_dev", "zk_fr_batch_inv",
-    "zk_plonk_quotient_evals",
+    "zk_plonk_quotient_evals", "zk_ctx_create_prio", "zk_stream_priority_range", "zk_h2d_async", "zk_d2h_async",
+    "zk_fence_record", "zk_fence_wait", "zk_fence_destroy", "zk_fr_r1cs_check_async",
 )
 
 _lib: Optional[ctypes.CDLL] = None
@@ -137,6 +138,14 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_g2_fixed_base_mul": ([P, P, P, S, P], I),
             "zk_fr_spmv": ([P, U32, P, P, P, P, P], I),
             "zk_fr_r1cs_check": ([P, P, P, P, S, ctypes.POINTER(ctypes.c_uint64)], I),
+            "zk_fr_r1cs_check_async": ([P, P, P, P, S, P], I),
+            "zk_ctx_create_prio": ([I, I, PP], I),
+            "zk_stream_priority_range": ([ctypes.POINTER(I), ctypes.POINTER(I)], I),
+            "zk_h2d_async": ([P, P, P, S], I),
+            "zk_d2h_async": ([P, P, P, S], I),
+            "zk_fence_record": ([P, PP], I),
+            "zk_fence_wait": ([P, I], I),
+            "zk_fence_destroy": ([P], I),
             "zk_fr_qap_quotient": ([P, P, P, P, P, S, P], I),
             "zk_fr_gather": ([P, P, P, P, S], I),
             "zk_fr_scale": ([P, P, P, P, S], I),
@@ -274,6 +283,23 @@ class PinnedBuffer:
             self.free()
         except Exception:
             pass
+
+
+class PinnedArray(np.ndarray):
+    """A numpy array in page-locked host memory; it keeps its ``PinnedBuffer`` alive."""
+
+    def __array_finalize__(self, obj) -> None:
+        self._pin = getattr(obj, "_pin", None)
+
+
+def pinned_copy(a: np.ndarray) -> PinnedArray:
+    """A C-contiguous copy of ``a`` in page-locked host memory."""
+    a = np.ascontiguousarray(a)
+    buf = PinnedBuffer(a.nbytes)
+    out = buf.array.view(a.dtype).reshape(a.shape).view(PinnedArray)
+    out[...] = a
+    out._pin = buf
+    return out
 
 
 class Bases:
@@ -430,15 +456,73 @@ class MsmPlan:
             pass
 
 
-class Context:
-    """One GPU, one stream (zk_ctx)."""
+class Fence:
+    """A point on a context's stream (zk_fence): ``done()`` asks, ``wait()`` blocks."""
 
-    def __init__(self, device: int = 0) -> None:
+    def __init__(self, handle) -> None:
+        self.handle = handle
+
+    def wait(self, timeout_ms: int = -1) -> None:
+        check(load().zk_fence_wait(self.handle, int(timeout_ms)), "zk_fence_wait")
+
+    def done(self) -> bool:
+        try:
+            self.wait(0)
+            return True
+        except TimeoutError:
+            return False
+
+    def destroy(self) -> None:
+        if self.handle is not None:
+            load().zk_fence_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def stream_priority_range():
+    """(least, greatest) CUDA stream priorities of the device (greatest = most urgent)."""
+    lo, hi = ctypes.c_int(), ctypes.c_int()
+    check(load().zk_stream_priority_range(ctypes.byref(lo), ctypes.byref(hi)), "zk_stream_priority_range")
+    return int(lo.value), int(hi.value)
+
+
+class Context:
+    """One GPU, one stream (zk_ctx); ``priority`` sets the CUDA priority of its streams."""
+
+    def __init__(self, device: int = 0, priority: Optional[int] = None) -> None:
         L = load()
         h = ctypes.c_void_p()
-        check(L.zk_ctx_create(int(device), ctypes.byref(h)), "zk_ctx_create")
+        if priority is None:
+            check(L.zk_ctx_create(int(device), ctypes.byref(h)), "zk_ctx_create")
+        else:
+            check(L.zk_ctx_create_prio(int(device), int(priority), ctypes.byref(h)), "zk_ctx_create_prio")
         self.handle = h.value
         self.device = device
+        self.priority = priority
+
+    def fence(self) -> Fence:
+        h = ctypes.c_void_p()
+        check(load().zk_fence_record(self.handle, ctypes.byref(h)), "zk_fence_record")
+        return Fence(h.value)
+
+    def h2d_async(self, dst, src: np.ndarray, nbytes: Optional[int] = None) -> None:
+        """Enqueue a host-to-device copy; ``src`` must stay unchanged until the stream passes it."""
+        if not src.flags.c_contiguous:
+            raise ValueError("h2d_async needs a C-contiguous host array")
+        nb = src.nbytes if nbytes is None else int(nbytes)
+        check(load().zk_h2d_async(self.handle, getattr(dst, "ptr", dst), src.ctypes.data, nb), "zk_h2d_async")
+
+    def d2h_async(self, dst: np.ndarray, src, nbytes: Optional[int] = None) -> None:
+        """Enqueue a device-to-host copy; ``dst`` is valid once the stream has passed it."""
+        if not dst.flags.c_contiguous:
+            raise ValueError("d2h_async needs a C-contiguous host array")
+        nb = dst.nbytes if nbytes is None else int(nbytes)
+        check(load().zk_d2h_async(self.handle, dst.ctypes.data, getattr(src, "ptr", src), nb), "zk_d2h_async")
 
     def close(self) -> None:
         if self.handle is not None:
@@ -771,6 +855,12 @@ class Context:
         check(load().zk_fr_r1cs_check(self.handle, getattr(a, "ptr", a), getattr(b, "ptr", b), getattr(c, "ptr", c),
                                       int(n), ctypes.byref(bad)), "zk_fr_r1cs_check")
         return int(bad.value)
+
+    def fr_r1cs_check_async(self, a, b, c, n: int, bad_dev) -> None:
+        """Adds #{i : a[i] b[i] != c[i]} to the uint64 at ``bad_dev`` (device) without waiting."""
+        check(load().zk_fr_r1cs_check_async(self.handle, getattr(a, "ptr", a), getattr(b, "ptr", b),
+                                            getattr(c, "ptr", c), int(n), getattr(bad_dev, "ptr", bad_dev)),
+              "zk_fr_r1cs_check_async")
 
     def fr_qap_quotient(self, out, a, b, c, n: int, zinv: int) -> None:
         check(load().zk_fr_qap_quotient(self.handle, getattr(out, "ptr", out), getattr(a, "ptr", a),

@@ -1,7 +1,10 @@
 // capi.cu -- extern "C" entry points declared in include/zkgpu.h.
+#include <chrono>
 #include <cstring>
 #include <iterator>
+#include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "zk_internal.cuh"
@@ -25,6 +28,29 @@ int scratch_alloc(Ctx* c, size_t bytes, void** p) {
 
 void scratch_free(Ctx* c, void* p) {
     if (p) cudaFreeAsync(p, c->stream);
+}
+
+int pinned_take(Ctx* c, size_t bytes, void** p, size_t* got) {
+    {
+        std::lock_guard<std::mutex> g(c->pinned_mu);
+        auto it = c->pinned_free.lower_bound(bytes);
+        // reuse a block of up to 4x the size asked for; a larger one stays for larger asks
+        if (it != c->pinned_free.end() && it->first <= 4 * bytes + 4096) {
+            *p = it->second;
+            *got = it->first;
+            c->pinned_free.erase(it);
+            return ZK_OK;
+        }
+    }
+    ZK_TRY_CUDA(cudaMallocHost(p, bytes ? bytes : 16));
+    *got = bytes ? bytes : 16;
+    return ZK_OK;
+}
+
+void pinned_give(Ctx* c, void* p, size_t bytes) {
+    if (p == nullptr) return;
+    std::lock_guard<std::mutex> g(c->pinned_mu);
+    c->pinned_free.emplace(bytes, p);
 }
 
 static cudaEvent_t take_event(Ctx* c) {
@@ -113,7 +139,7 @@ const char* zk_last_error(void) { return zk::g_last_error.c_str(); }
 
 int zk_version(void) { return 1; }
 
-int zk_ctx_create(int device, zk_ctx** out) {
+int zk_ctx_create_prio(int device, int priority, zk_ctx** out) {
     if (out == nullptr) {
         zk::set_error("null output pointer");
         return ZK_EINVAL;
@@ -130,17 +156,34 @@ int zk_ctx_create(int device, zk_ctx** out) {
         return ZK_EINVAL;
     }
     ZK_TRY_CUDA(cudaSetDevice(device));
-    zk_ctx* c = new zk_ctx();
+    int least = 0, greatest = 0;
+    ZK_TRY_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    // clamp into the device's range (greatest is the most urgent, numerically smallest)
+    if (priority > least) priority = least;
+    if (priority < greatest) priority = greatest;
+    std::unique_ptr<zk_ctx> c(new zk_ctx());
     c->impl.device = device;
+    c->impl.priority = priority;
     ZK_TRY_CUDA(cudaDeviceGetAttribute(&c->impl.num_sms, cudaDevAttrMultiProcessorCount, device));
-    ZK_TRY_CUDA(cudaStreamCreateWithFlags(&c->impl.stream, cudaStreamNonBlocking));
+    ZK_TRY_CUDA(cudaStreamCreateWithPriority(&c->impl.stream, cudaStreamNonBlocking, priority));
     // keep freed stream-ordered allocations cached in the device pool
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
         uint64_t threshold = UINT64_MAX;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
     }
-    *out = c;
+    *out = c.release();
+    return ZK_OK;
+}
+
+int zk_ctx_create(int device, zk_ctx** out) { return zk_ctx_create_prio(device, 0, out); }
+
+int zk_stream_priority_range(int* least, int* greatest) {
+    if (least == nullptr || greatest == nullptr) {
+        zk::set_error("null output pointer");
+        return ZK_EINVAL;
+    }
+    ZK_TRY_CUDA(cudaDeviceGetStreamPriorityRange(least, greatest));
     return ZK_OK;
 }
 
@@ -170,6 +213,7 @@ int zk_ctx_destroy(zk_ctx* ctx) {
     for (cudaEvent_t ev : ctx->impl.chunk_ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->impl.inf_flag_dev) cudaFree(ctx->impl.inf_flag_dev);
+    for (auto& kv : ctx->impl.pinned_free) cudaFreeHost(kv.second);
     cudaStreamDestroy(ctx->impl.stream);
     delete ctx;
     return ZK_OK;
@@ -330,6 +374,82 @@ int zk_d2h(zk_ctx* ctx, void* dst_host, const void* src_dev, size_t bytes) {
     if (bytes == 0) return ZK_OK;
     ZK_TRY_CUDA(cudaMemcpyAsync(dst_host, src_dev, bytes, cudaMemcpyDeviceToHost, ctx->impl.stream));
     ZK_TRY_CUDA(cudaStreamSynchronize(ctx->impl.stream));
+    return ZK_OK;
+}
+
+int zk_h2d_async(zk_ctx* ctx, void* dst_dev, const void* src_host, size_t bytes) {
+    CTX_OR_FAIL(ctx);
+    if (bytes == 0) return ZK_OK;
+    if (dst_dev == nullptr || src_host == nullptr) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    ZK_TRY_CUDA(cudaMemcpyAsync(dst_dev, src_host, bytes, cudaMemcpyHostToDevice, ctx->impl.stream));
+    return ZK_OK;
+}
+
+int zk_d2h_async(zk_ctx* ctx, void* dst_host, const void* src_dev, size_t bytes) {
+    CTX_OR_FAIL(ctx);
+    if (bytes == 0) return ZK_OK;
+    if (dst_host == nullptr || src_dev == nullptr) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    ZK_TRY_CUDA(cudaMemcpyAsync(dst_host, src_dev, bytes, cudaMemcpyDeviceToHost, ctx->impl.stream));
+    return ZK_OK;
+}
+
+int zk_fence_record(zk_ctx* ctx, zk_fence** out) {
+    CTX_OR_FAIL(ctx);
+    if (out == nullptr) {
+        zk::set_error("null output pointer");
+        return ZK_EINVAL;
+    }
+    *out = nullptr;
+    std::unique_ptr<zk_fence> f(new zk_fence());
+    f->device = ctx->impl.device;
+    ZK_TRY_CUDA(cudaEventCreateWithFlags(&f->ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(f->ev, ctx->impl.stream);
+    if (e != cudaSuccess) {
+        cudaEventDestroy(f->ev);
+        zk::set_error(std::string("cudaEventRecord: ") + cudaGetErrorString(e));
+        return ZK_ECUDA;
+    }
+    *out = f.release();
+    return ZK_OK;
+}
+
+int zk_fence_wait(zk_fence* f, int timeout_ms) {
+    if (f == nullptr) {
+        zk::set_error("null zk_fence");
+        return ZK_EINVAL;
+    }
+    cudaSetDevice(f->device);
+    if (timeout_ms < 0) {
+        ZK_TRY_CUDA(cudaEventSynchronize(f->ev));
+        return ZK_OK;
+    }
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
+    for (;;) {
+        const cudaError_t e = cudaEventQuery(f->ev);
+        if (e == cudaSuccess) return ZK_OK;
+        if (e != cudaErrorNotReady) {
+            zk::set_error(std::string("zk_fence_wait: ") + cudaGetErrorString(e));
+            return ZK_ECUDA;
+        }
+        if (std::chrono::steady_clock::now() >= deadline) {
+            zk::set_error("zk_fence_wait: the fence has not passed yet");
+            return ZK_ETIMEOUT;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
+int zk_fence_destroy(zk_fence* f) {
+    if (f == nullptr) return ZK_OK;
+    cudaSetDevice(f->device);
+    cudaEventDestroy(f->ev);
+    delete f;
     return ZK_OK;
 }
 
@@ -525,7 +645,8 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
     Ctx* c = &ctx->impl;
     // each lazily created resource under its own check: a failure part way leaves the rest
     // to be created by the next call
-    if (c->copy_stream == nullptr) ZK_TRY_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    if (c->copy_stream == nullptr)
+        ZK_TRY_CUDA(cudaStreamCreateWithPriority(&c->copy_stream, cudaStreamNonBlocking, c->priority));
     if (c->copy_go == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_go, cudaEventDisableTiming));
     if (c->copy_done == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
     for (cudaEvent_t& ev : c->chunk_ev)

@@ -1445,7 +1445,7 @@ static constexpr int kSideStreams = 3;
 static int ensure_side_streams(Ctx* c) {
     while ((int)c->side_streams.size() < kSideStreams) {
         cudaStream_t st = nullptr;
-        ZK_TRY_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        ZK_TRY_CUDA(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, c->priority));
         c->side_streams.push_back(st);
     }
     while ((int)c->side_events.size() <= kSideStreams) {
@@ -1529,7 +1529,9 @@ static int batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont,
 // thread waits for the device, combines the windows on the host and signals completion ----
 struct MsmAsync {
     cudaEvent_t done_ev = nullptr;
-    void* pinned = nullptr;  // per-set targets and entry totals of every pipeline
+    Ctx* ctx = nullptr;
+    void* pinned = nullptr;  // per-set targets and entry totals of every pipeline (from ctx's pool)
+    size_t pinned_bytes = 0;
     std::thread worker;
     std::mutex mu;
     std::condition_variable cv;
@@ -1539,7 +1541,7 @@ struct MsmAsync {
     virtual ~MsmAsync() {
         if (worker.joinable()) worker.join();
         if (done_ev) cudaEventDestroy(done_ev);
-        if (pinned) cudaFreeHost(pinned);
+        if (pinned) pinned_give(ctx, pinned, pinned_bytes);
     }
     void finish(int code, const std::string& err) {
         std::lock_guard<std::mutex> g(mu);
@@ -1578,7 +1580,8 @@ static int batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mo
     }
     // pinned host targets: the device-to-host copies stay asynchronous
     const size_t host_bytes = host_elems * sizeof(typename C::P) + pipes.size() * sizeof(uint32_t);
-    ZK_TRY_CUDA(cudaMallocHost(&a->pinned, host_bytes));
+    a->ctx = c;
+    if ((rc = pinned_take(c, host_bytes, &a->pinned, &a->pinned_bytes)) != ZK_OK) return rc;
     ZK_TRY_CUDA(cudaEventCreateWithFlags(&a->done_ev, cudaEventDisableTiming));
     char* arena = nullptr;
     if ((rc = scratch_alloc(c, bytes, reinterpret_cast<void**>(&arena))) != ZK_OK) return rc;

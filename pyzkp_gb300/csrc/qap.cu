@@ -230,6 +230,21 @@ int zk_fr_r1cs_check(zk_ctx* ctx, const void* a, const void* b, const void* c, s
                          static_cast<const fe*>(c), n, bad);
 }
 
+int zk_fr_r1cs_check_async(zk_ctx* ctx, const void* a, const void* b, const void* c, size_t n, void* bad_dev) {
+    QAP_CTX(ctx);
+    if (bad_dev == nullptr || (n && (!a || !b || !c))) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    if (n == 0) return ZK_OK;
+    zk::Ctx* cc = &ctx->impl;
+    ZK_LAUNCH(cc, "fr_r1cs_check", zk::fr_r1cs_check_kernel, zk::grid_of(n, 256, cc->num_sms), 256, 0,
+              static_cast<const fe*>(a), static_cast<const fe*>(b), static_cast<const fe*>(c), n,
+              static_cast<unsigned long long*>(bad_dev));
+    ZK_TRY_CUDA(cudaGetLastError());
+    return ZK_OK;
+}
+
 int zk_fr_qap_quotient(zk_ctx* ctx, void* out, const void* a, const void* b, const void* c, size_t n,
                        const uint8_t zinv[32]) {
     QAP_CTX(ctx);

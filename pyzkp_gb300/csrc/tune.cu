@@ -18,6 +18,11 @@
 
 namespace zk {
 
+// A tuned choice replaces the built-in one only when it is faster by this fraction: the
+// candidates are timed alone, one call each, and a smaller gain is within run-to-run noise
+// (and may not carry over to batched use).
+static constexpr double kTuneMargin = 0.03;
+
 static uint32_t ceil_log2(size_t n) {
     uint32_t lg = 0;
     while ((1ull << lg) < n) lg++;
@@ -352,21 +357,27 @@ int zk_autotune_msm(zk_ctx* ctx, const zk_bases* bases, const void* scalars_dev,
     }
     const size_t n = (size_t)1 << log_n;
     const uint32_t rule = zk::msm_auto_window_glv(n);
+    // the built-in window is timed first and kept unless another beats it by kTuneMargin
+    double rule_ms = 0;
+    int rc0 = zk::time_msm(&ctx->impl, bases, static_cast<const zk::fe*>(scalars_dev), n, rule, reps < 1 ? 1 : reps,
+                           &rule_ms);
+    if (rc0 != ZK_OK) return rc0;
     uint32_t best_c = rule;
-    double best = 1e30;
+    double best = rule_ms;
     for (int d = -2; d <= 2; d++) {
         const int cb = (int)rule + d;
-        if (cb < 4 || cb > 20) continue;
+        if (d == 0 || cb < 4 || cb > 20) continue;
         double ms = 0;
         int rc = zk::time_msm(&ctx->impl, bases, static_cast<const zk::fe*>(scalars_dev), n, (uint32_t)cb,
                               reps < 1 ? 1 : reps, &ms);
         if (rc != ZK_OK) return rc;
-        if (ms < best) {
+        if (ms < best && ms < rule_ms * (1.0 - zk::kTuneMargin)) {
             best = ms;
             best_c = (uint32_t)cb;
         }
     }
-    ctx->impl.tune_msm_window[zk::ceil_log2(n)] = (uint8_t)best_c;
+    // 0 = the built-in rule (so a later change of the rule is not masked by a stored copy)
+    ctx->impl.tune_msm_window[zk::ceil_log2(n)] = best_c == rule ? 0 : (uint8_t)best_c;
     if (best_window) *best_window = best_c;
     if (best_ms) *best_ms = best;
     return ZK_OK;
@@ -406,9 +417,23 @@ int zk_autotune_ntt(zk_ctx* ctx, void* data_dev, uint32_t log_n, int reps, uint3
     }
     uint8_t saved[4];
     std::memcpy(saved, c->tune_ntt_split[log_n], 4);
-    double best = 1e30;
-    std::vector<uint32_t> best_split;
+    // the built-in split is timed first and kept unless a candidate beats it by kTuneMargin
+    {
+        std::lock_guard<std::mutex> g(c->mu);
+        std::memset(c->tune_ntt_split[log_n], 0, 4);
+    }
+    double rule_ms = 0;
+    int rc0 = zk::time_ntt(c, static_cast<zk::fe*>(data_dev), log_n, reps < 1 ? 1 : reps, &rule_ms);
+    if (rc0 != ZK_OK) {
+        std::memcpy(c->tune_ntt_split[log_n], saved, 4);
+        return rc0;
+    }
+    uint32_t rule_np = 0, rule_bits[4] = {0, 0, 0, 0};
+    zk::get_split(c, log_n, &rule_np, rule_bits);
+    double best = rule_ms;
+    std::vector<uint32_t> best_split;  // empty: the built-in split
     for (const auto& cand : cands) {
+        if (cand.size() == rule_np && std::equal(cand.begin(), cand.end(), rule_bits)) continue;
         int rc = zk::set_split(c, log_n, (uint32_t)cand.size(), cand.data());
         double ms = 0;
         if (rc == ZK_OK) rc = zk::time_ntt(c, static_cast<zk::fe*>(data_dev), log_n, reps < 1 ? 1 : reps, &ms);
@@ -416,17 +441,17 @@ int zk_autotune_ntt(zk_ctx* ctx, void* data_dev, uint32_t log_n, int reps, uint3
             std::memcpy(c->tune_ntt_split[log_n], saved, 4);
             return rc;
         }
-        if (ms < best) {
+        if (ms < best && ms < rule_ms * (1.0 - zk::kTuneMargin)) {
             best = ms;
             best_split = cand;
         }
     }
     if (best_split.empty()) {
-        std::memcpy(c->tune_ntt_split[log_n], saved, 4);
-        zk::set_error("zk_autotune_ntt: no candidate split");
-        return ZK_EINVAL;
+        std::lock_guard<std::mutex> g(c->mu);
+        std::memset(c->tune_ntt_split[log_n], 0, 4);
+    } else {
+        zk::set_split(c, log_n, (uint32_t)best_split.size(), best_split.data());
     }
-    zk::set_split(c, log_n, (uint32_t)best_split.size(), best_split.data());
     if (npass && bits) zk::get_split(c, log_n, npass, bits);
     if (best_ms) *best_ms = best;
     return ZK_OK;

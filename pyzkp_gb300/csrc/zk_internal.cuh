@@ -81,6 +81,7 @@ struct ProfPending {
 struct Ctx {
     int device = 0;
     int num_sms = 0;
+    int priority = 0;  // CUDA stream priority of the context stream and its side / copy streams
     // the stream ZK_LAUNCH and the copies use: the context stream, pointed at a side or
     // copy stream for the span of one enqueue (a batch pipeline, an upload) and then restored
     cudaStream_t stream = nullptr;
@@ -115,7 +116,16 @@ struct Ctx {
     // tuning tables (zk_tune_*, zk_autotune_*): 0 means the built-in rule
     uint8_t tune_msm_window[32] = {};    // MSM window bits by ceil(log2 n)
     uint8_t tune_ntt_split[29][4] = {};  // NTT radix bits per pass by log2 n
+    // page-locked result buffers of asynchronous MSM batches, kept for reuse: allocating
+    // and freeing page-locked memory per batch can wait for the whole device
+    std::mutex pinned_mu;
+    std::multimap<size_t, void*> pinned_free;  // size -> block
 };
+
+// A page-locked block of at least `bytes` from the context's free list (else a new one of
+// exactly `bytes`; *got = its size); pinned_give returns it. Both are thread-safe.
+int pinned_take(Ctx* c, size_t bytes, void** p, size_t* got);
+void pinned_give(Ctx* c, void* p, size_t bytes);
 
 int prof_begin(Ctx* c, const char* name);
 void prof_end(Ctx* c, int token);
@@ -209,6 +219,11 @@ void ntt_plan_destroy(Ctx* c, NttBatchPlan* plan);
 
 struct zk_ctx {
     zk::Ctx impl;
+};
+
+struct zk_fence {
+    int device = 0;
+    cudaEvent_t ev = nullptr;
 };
 
 struct zk_bases {

@@ -384,38 +384,167 @@ class Request:
     s: int
 
 
+class PendingProofs:
+    """Requests whose device work is enqueued (``Prover.submit``). ``done()`` asks whether the
+    device has finished it; ``results()`` waits and returns, per request in order, its Proof
+    or the exception that failed that request alone (an unsatisfied witness or a bad
+    argument fails its own request, never the others of the batch).
+
+    ``results()`` = ``finish_device()`` (on the thread that uses the context: collects the
+    MSM values and releases the device buffers) + ``finish_host()`` (the proof assembly,
+    host-only, any thread)."""
+
+    def __init__(self, prover: "Prover", ctx: N.Context, live, errors, g1_job, g2_job, bad_host, fence,
+                 buffers) -> None:
+        self._prover, self._ctx = prover, ctx
+        self._live, self._errors = live, errors
+        self._g1_job, self._g2_job = g1_job, g2_job
+        self._bad_host, self._fence, self._buffers = bad_host, fence, buffers
+        self._g1 = self._g2 = self._bad = None
+        self._device_done = False
+        self._results: Optional[list] = None
+
+    def __len__(self) -> int:
+        return len(self._errors)
+
+    def done(self) -> bool:
+        return self._device_done or self._fence.done()
+
+    def finish_device(self) -> None:
+        if self._device_done:
+            return
+        try:
+            self._fence.wait()
+            self._g1 = Prover._collect(self._g1_job, 4 * len(self._live))
+            self._g2 = Prover._collect(self._g2_job, len(self._live))
+            if self._bad_host is not None:
+                self._bad = self._bad_host.array[:8 * len(self._live)].view(np.uint64).copy()
+        finally:
+            for b in self._buffers:
+                b.free()
+            self._buffers = []
+            self._fence.destroy()
+            if self._bad_host is not None:
+                self._prover._give_pinned(self._bad_host)
+                self._bad_host = None
+            self._device_done = True
+
+    def finish_host(self) -> list:
+        if self._results is not None:
+            return self._results
+        g1, g2, bad = self._g1, self._g2, self._bad
+        out = list(self._errors)
+
+        def one(i):
+            q = self._live[i][0]
+            if bad is not None and int(bad[i]) != 0:
+                return ValueError("witness does not satisfy R1CS (non-zero remainder)")
+            a_lin, b_lin_g1, l_acc, h_acc = g1[4 * i:4 * i + 4]
+            try:
+                return assemble(q.key, a_lin, b_lin_g1, g2[i], l_acc, h_acc, q.r, q.s)
+            except Exception as e:  # noqa: BLE001 -- the request's own failure
+                return e
+
+        # host scalar multiplications release the GIL inside the library: assemble in parallel
+        n = len(self._live)
+        proofs = list(Prover._pool().map(one, range(n))) if n > 1 else [one(i) for i in range(n)]
+        for (_, _, _, slot), pr in zip(self._live, proofs):
+            out[slot] = pr
+        self._results = out
+        return out
+
+    def results(self) -> list:
+        self.finish_device()
+        return self.finish_host()
+
+
+def pin_witness(witness: np.ndarray) -> np.ndarray:
+    """A page-locked copy of a witness (canonical uint64[n_vars, 4]): ``Prover.submit`` then
+    uploads it without waiting for earlier device work."""
+    return N.pinned_copy(np.ascontiguousarray(witness, dtype=np.uint64).reshape(-1, 4))
+
+
 class Prover:
     """Groth16 proofs on the device, one at a time or a batch per call (prove / prove_batch of
-    protocols/groth16/prove.py with the randomness passed in)."""
+    protocols/groth16/prove.py with the randomness passed in), or asynchronously (``submit``)."""
 
     def __init__(self, ctx: N.Context) -> None:
+        import threading
+
         self.ctx = ctx
+        self._pinned: List[N.PinnedBuffer] = []  # small page-locked buffers for reuse
+        self._pinned_lock = threading.Lock()
+
+    def _take_pinned(self, nbytes: int) -> N.PinnedBuffer:
+        """A page-locked buffer of at least nbytes (allocating page-locked memory per batch can
+        wait for the whole device, so buffers are kept and reused)."""
+        with self._pinned_lock:
+            for i, b in enumerate(self._pinned):
+                if b.nbytes >= nbytes:
+                    return self._pinned.pop(i)
+        return N.PinnedBuffer(max(nbytes, 4096))
+
+    def _give_pinned(self, buf: N.PinnedBuffer) -> None:
+        with self._pinned_lock:
+            self._pinned.append(buf)
 
     def prove(self, key: DeviceKey, witness: np.ndarray, r: int, s: int) -> Proof:
         return self.prove_batch([Request(key, witness, r, s)])[0]
 
     def prove_batch(self, reqs: Sequence[Request]) -> List[Proof]:
-        ctx = self.ctx
-        live = []
-        for q in reqs:
+        """All proofs of ``reqs``; raises the first request's error (as the reference's
+        prove_batch raises for an unsatisfied witness, qap.py:98-99)."""
+        res = self.submit(reqs).results()
+        for r in res:
+            if isinstance(r, Exception):
+                raise r
+        return res
+
+    def submit(self, reqs: Sequence[Request], ctx: Optional[N.Context] = None) -> PendingProofs:
+        """Enqueue the device work of ``reqs`` on ``ctx`` (default: the prover's context) and
+        return at once: R1CS rows A w, B w, C w, the satisfiability count (read back with the
+        results, so that nothing here waits for the device), the QAP transforms, the MSM
+        scalar gathers, and one asynchronous G1 and one G2 MSM batch. Witnesses made by
+        ``pin_witness`` are uploaded without waiting; others with a blocking copy."""
+        ctx = ctx or self.ctx
+        live, errors, buffers = [], [None] * len(reqs), []
+        for slot, q in enumerate(reqs):
             k = q.key
-            w = np.ascontiguousarray(q.witness, dtype=np.uint64).reshape(-1, 4)
+            w = q.witness
+            pinned = (isinstance(w, N.PinnedArray) and w.flags.c_contiguous and w.dtype == np.uint64
+                      and w.ndim == 2 and w.shape[1] == 4)
+            if not pinned:
+                w = np.ascontiguousarray(w, dtype=np.uint64).reshape(-1, 4)
             if w.shape[0] != k.r1cs.n_vars:
-                raise ValueError("witness length mismatch")
+                errors[slot] = ValueError("witness length mismatch")
+                continue
             n = k.n
-            wd = ctx.to_device(w)
+            wd = ctx.alloc(w.shape[0] * 32)
+            buffers.append(wd)
+            if pinned:
+                ctx.h2d_async(wd, w)
+            else:
+                wd.upload(w)
             ctx.fr_to_mont(wd, wd, w.shape[0])
             ev = [ctx.alloc(n * 32) for _ in range(3)]
+            buffers.extend(ev)
             for mat, out in zip(k.mats, ev):
                 ctx.fr_spmv(n, mat[0], mat[1], mat[2], wd, out)
-            live.append((q, wd, ev))
-        # the remainder of (A B - C) / (X^n - 1) is empty iff A B == C on the domain
-        for q, _, ev in live:
-            if ctx.fr_r1cs_check(ev[0], ev[1], ev[2], q.key.n):
-                raise ValueError("witness does not satisfy R1CS (non-zero remainder)")
+            live.append((q, wd, ev, slot))
+        if not live:
+            return PendingProofs(self, ctx, [], errors, ([], None), ([], None), None, ctx.fence(), buffers)
+        # the remainder of (A B - C) / (X^n - 1) is empty iff A B == C on the domain: one
+        # counter per request, read back with the results
+        bad_dev = ctx.alloc(8 * len(live))
+        buffers.append(bad_dev)
+        ctx.memset(bad_dev, 0)
+        for i, (q, _, ev, _) in enumerate(live):
+            ctx.fr_r1cs_check_async(ev[0], ev[1], ev[2], q.key.n, bad_dev.ptr + 8 * i)
+        bad_host = self._take_pinned(8 * len(live))
+        ctx.d2h_async(bad_host.array[:8 * len(live)], bad_dev)
         # H = coset_iNTT((A B - C)(5 w^i) / (5^n - 1)), every transform in place, batched
         jobs1, jobs2, jobs3 = [], [], []
-        for q, _, ev in live:
+        for q, _, ev, _ in live:
             n = q.key.n
             lg, om = n.bit_length() - 1, omega_for_size(n)
             for e in ev:
@@ -424,22 +553,22 @@ class Prover:
             jobs3.append((MODE_COSET_COEFFS, ev[0], ev[0], n, lg, om, COSET_SHIFT))
         ctx.ntt_batch(jobs1)
         ctx.ntt_batch(jobs2)
-        for q, _, ev in live:
+        for q, _, ev, _ in live:
             n = q.key.n
             zinv = pow((pow(COSET_SHIFT, n, FR_MODULUS) - 1) % FR_MODULUS, FR_MODULUS - 2, FR_MODULUS)
             ctx.fr_qap_quotient(ev[0], ev[0], ev[1], ev[2], n, zinv)
         ctx.ntt_batch(jobs3)
         # MSM scalars: w gathered by each resident base set's index list; h = ev[0][:n-1]
-        g1_bases, g1_sc, g1_n, g2_bases, g2_sc, g2_n, keep = [], [], [], [], [], [], []
-        for q, wd, ev in live:
+        g1_bases, g1_sc, g1_n, g2_bases, g2_sc, g2_n = [], [], [], [], [], []
+        for q, wd, ev, _ in live:
             k = q.key
             sc = {}
             for name, qu in (("a", k.a), ("b", k.b1), ("l", k.l)):
                 d = ctx.alloc(max(1, qu.count) * 32)
+                buffers.append(d)
                 if qu.count:
                     ctx.fr_gather(d, wd, qu.idx, qu.count)
                 sc[name] = d
-            keep.append(sc)
             for qu, d in ((k.a, sc["a"]), (k.b1, sc["b"]), (k.l, sc["l"]), (k.h, ev[0])):
                 g1_bases.append(qu.bases)
                 g1_sc.append(d)
@@ -450,18 +579,7 @@ class Prover:
         # both batches in flight: the G1 windows are combined on the host while the G2 MSMs run
         g1_job = self._submit(ctx, g1_bases, g1_sc, g1_n, g2=False)
         g2_job = self._submit(ctx, g2_bases, g2_sc, g2_n, g2=True)
-        g1 = self._collect(g1_job, len(g1_n))
-        g2 = self._collect(g2_job, len(g2_n))
-
-        def one(i):
-            q = live[i][0]
-            a_lin, b_lin_g1, l_acc, h_acc = g1[4 * i:4 * i + 4]
-            return assemble(q.key, a_lin, b_lin_g1, g2[i], l_acc, h_acc, q.r, q.s)
-
-        # host scalar multiplications release the GIL inside the library: assemble in parallel
-        if len(live) > 1:
-            return list(self._pool().map(one, range(len(live))))
-        return [one(0)] if live else []
+        return PendingProofs(self, ctx, live, errors, g1_job, g2_job, bad_host, ctx.fence(), buffers)
 
     _executor = None
 
@@ -510,4 +628,5 @@ def assemble(key: DeviceKey, a_lin, b_lin_g1, b_lin_g2, l_acc, h_acc, r: int, s:
 
 
 __all__ = ["R1CS", "CSR", "diagonal_r1cs", "diagonal_witness", "Trapdoors", "VerifyingKey", "Proof", "DeviceKey",
-           "setup", "query_points", "Request", "Prover", "assemble", "omega_for_size", "int_to_limbs"]
+           "setup", "query_points", "Request", "Prover", "PendingProofs", "pin_witness", "assemble", "omega_for_size",
+           "int_to_limbs"]

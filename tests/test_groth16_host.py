@@ -3,7 +3,6 @@
 
 import json
 import os
-import sys
 
 import numpy as np
 import pytest
@@ -14,7 +13,6 @@ from pyzkp_gb300 import serve, synth
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 R = synth.FR_MODULUS
-REF = os.environ.get("PYZKP_REFERENCE", "/root/reference")
 
 
 def test_host_curve_ops_match_oracle():
@@ -68,10 +66,9 @@ def test_r1cs_from_golden_rows_matches_reference_layout():
 
 @pytest.mark.reference
 def test_r1cs_from_reference_compile_r1cs():
-    if not os.path.isdir(REF):
-        pytest.skip("reference checkout not present")
-    sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle", "py_ecc_shim"))
-    sys.path.insert(0, REF)
+    import reference_env
+
+    reference_env.require()
     from frontend.api import compile_circuit
     from frontend.circuit.schema import public, secret
     from protocols.groth16.r1cs import compile_r1cs
@@ -103,7 +100,7 @@ def test_poisson_trace_and_percentiles():
     assert tr[0].t == 0.0 and (gaps >= 0).all() and abs(gaps.mean() - 0.01) < 0.001
     counts = np.bincount([a.key_id for a in tr], minlength=6)[3:]
     assert abs(counts[1] / len(tr) - 0.5) < 0.05
-    res = serve.TraceResult(proofs=[None] * 4, latency_s=[0.004, 0.001, 0.003, 0.002], makespan_s=2.0,
-                            batches=[1, 3])
+    res = serve.TraceResult(proofs=["p"] * 4, errors=[None] * 4, latency_s=[0.004, 0.001, 0.003, 0.002],
+                            makespan_s=2.0, batches=[1, 3])
     s = res.summary()
     assert s["p50_ms"] in (2.0, 3.0) and s["p99_ms"] == 4.0 and s["proofs_per_s"] == 2.0 and s["mean_batch"] == 2
