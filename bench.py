@@ -32,6 +32,7 @@ import os
 import statistics
 import subprocess
 import sys
+from typing import Optional
 import tempfile
 import time
 
@@ -1067,6 +1068,65 @@ def cpu_msm_4096(gpu_row: dict, budget_s: float = 3.0) -> dict:
             "pippenger_matches_known_answer": pip == known}
 
 
+def cpu_reference_python(gpu_4096: Optional[dict], msm_logs=(12, 16), ntt_logs=(16, 20)) -> Optional[dict]:
+    """The reference's own Python CPU path (crypto/msm/pippenger.py:msm_pippenger with the
+    window rule of runtime/kernels/cpu/kernels.py:_msm_g1_impl, crypto/poly/ntt.py:ntt), run
+    unmodified from the pip install in baseline/_ref with the py_ecc stand-in, single-threaded
+    (it is pure Python), on the same seeds as the GPU arm. The 4096-point result is compared
+    with the GPU's. None when the reference is not installed next to the repository."""
+    import importlib
+
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    try:
+        import reference_env
+
+        reference_env.add_to_path()
+        pip = importlib.import_module("crypto.msm.pippenger")
+        rntt = importlib.import_module("crypto.poly.ntt")
+    except ImportError:
+        return None
+    from oracle import oracle as O
+    from py_ecc import optimized_bn128 as bn
+    from pyzkp_gb300 import synth
+
+    out = {"kind": "reference", "cores": 1, "host_cpus": os.cpu_count(),
+           "source": "unmodified reference (baseline/_ref) + py_ecc stand-in, one Python thread"}
+    msm = {}
+    for lg in msm_logs:
+        n = 1 << lg
+        seed = synth.seed_for(0 if lg == 12 else 2, lg)
+        xy = O.g1_fixed_base_mul(O.G1_GENERATOR, synth.base_dlogs(seed, n))
+        pts = [(bn.FQ(x), bn.FQ(y), bn.FQ(1)) for x, y in (O.affine_to_ints(row) for row in xy)]
+        sc = synth.limbs_to_ints(synth.fr_uniform(seed, n))
+        w = max(4, min(16, n.bit_length() - 2))
+        t0 = time.perf_counter()
+        res = bn.normalize(pip.msm_pippenger(pts, sc, w))
+        el = time.perf_counter() - t0
+        row = {"Mpts_s": round(n / el / 1e6, 6), "s": round(el, 2), "window_bits": w}
+        if lg == 12 and gpu_4096 is not None:
+            row["gpu_result_equal"] = [hex(int(res[0])), hex(int(res[1]))] == gpu_4096.get("msm_result")
+        msm[f"2^{lg}"] = row
+    big = msm.get(f"2^{max(msm_logs)}")
+    if big:
+        # 2^20 not run: n / (n at the largest size run) times its time, and windows 254/w scaled
+        lg = max(msm_logs)
+        w20, w_big = 16, big["window_bits"]
+        est = big["s"] * (1 << (20 - lg)) * (-(-254 // w20)) / (-(-254 // w_big))
+        msm["2^20"] = {"Mpts_s": round((1 << 20) / est / 1e6, 6), "s": round(est, 1),
+                       "extrapolated": f"from 2^{lg}: x n, x windows (ceil(254/16) / ceil(254/{w_big}))"}
+    nt = {}
+    for lg in ntt_logs:
+        n = 1 << lg
+        v = synth.limbs_to_ints(synth.fr_uniform(synth.seed_for(1, lg), n))
+        t0 = time.perf_counter()
+        rntt.ntt(v, rntt.omega_for_size(n))
+        el = time.perf_counter() - t0
+        nt[f"2^{lg}"] = {"Melem_s": round(n / el / 1e6, 4), "s": round(el, 2)}
+    out["msm"] = msm
+    out["ntt_forward"] = nt
+    return out
+
+
 def cpu_check_g2(row: dict) -> bool:
     """The GPU arm's G2 MSM result against the known answer [sum k_i s_i]G2."""
     from oracle import oracle as O
@@ -1160,6 +1220,8 @@ def main() -> None:
                     res["g2_result_matches_known_answer"] = cpu_check_g2(g2[big])
                 if samples is not None:
                     plonk["sampled_check_ok"] = cpu_check_plonk(samples)
+                if args.only == "all" and "cpu_baseline" in res:
+                    res["cpu_baseline"]["reference_python"] = cpu_reference_python(res.get("msm_2_12"))
                 if res.get("groth16_serve") and _SERVE_VERIFY_JOBS:
                     res["groth16_serve"].update(cpu_verify_serve(_SERVE_VERIFY_JOBS))
             print(json.dumps(res), flush=True)
