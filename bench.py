@@ -786,6 +786,34 @@ def run_gpu_batch(ctx, args, flush, count: int = 64, lo: int = 10, hi: int = 20)
     ok_plan = snapshot() == ref_n
     nplan_launches = nplan.launches()
     nplan.free()
+    # the work-queue form: every pass of every transform in one persistent launch
+    nplan = ctx.ntt_plan(jobs, use_graph=True, queue=True)
+    t_nqueue = timed(nplan.run)
+    ctx.ntt_queue_status()
+    ok_queue = snapshot() == ref_n
+    nqueue_launches = nplan.launches()
+    nplan.free()
+    # small transforms only (2^10..2^14), where launch latency weighs most
+    small_logs = [int(round(u)) for u in rng.uniform(lo, 14, size=count)]
+    small_bufs = []
+    for j, lg in enumerate(small_logs):
+        a = ctx.to_device(synth.fr_uniform(seed + 300 + j, 1 << lg))
+        ctx.fr_to_mont(a, a, 1 << lg)
+        small_bufs.append((a, ctx.alloc((1 << lg) * 32)))
+    small_jobs = [(2, o, a, 1 << lg, lg, ntt_omega(1 << lg), 5) for (a, o), lg in zip(small_bufs, small_logs)]
+    small = {"elements": sum(1 << lg for lg in small_logs)}
+    small_ref = None
+    for name, q in (("plan_graph", False), ("plan_graph_queue", True)):
+        sp = ctx.ntt_plan(small_jobs, use_graph=True, queue=q)
+        small[name + "_ms"] = round(timed(sp.run), 4)
+        ctx.ntt_queue_status()
+        ctx.sync()
+        h = [hashlib.sha256(o.download((1 << lg) * 32).tobytes()).hexdigest()
+             for (_, o, _, _, lg, _, _) in small_jobs]
+        small_ref = small_ref or h
+        small["bit_exact"] = small.get("bit_exact", True) and h == small_ref
+        sp.free()
+    del small_bufs, small_jobs
     t0 = time.perf_counter()
     splits = {}
     scratch = ctx.alloc((1 << hi) * 32)
@@ -802,13 +830,16 @@ def run_gpu_batch(ctx, args, flush, count: int = 64, lo: int = 10, hi: int = 20)
     out["ntt"] = {
         "mode": "coset forward, shift 5", "elements": elems,
         "plain_ms": round(t_nplain, 3), "batch_ms": round(t_nbatch, 3), "plan_graph_ms": round(t_nplan, 3),
-        "plan_graph_tuned_ms": round(t_ntuned, 3),
+        "plan_graph_tuned_ms": round(t_ntuned, 3), "plan_graph_queue_ms": round(t_nqueue, 3),
         "plain_Melem_s": round(elems / (t_nplain * 1e-3) / 1e6, 1),
         "batch_Melem_s": round(elems / (t_nbatch * 1e-3) / 1e6, 1),
         "plan_graph_Melem_s": round(elems / (t_nplan * 1e-3) / 1e6, 1),
         "plan_graph_tuned_Melem_s": round(elems / (t_ntuned * 1e-3) / 1e6, 1),
-        "graph_kernels": nplan_launches, "tuned_splits": {f"2^{k}": v for k, v in splits.items()},
-        "autotune_s": round(ntune_s, 2), "bit_exact_vs_plain": ok_batch and ok_plan and ok_tuned,
+        "plan_graph_queue_Melem_s": round(elems / (t_nqueue * 1e-3) / 1e6, 1),
+        "graph_kernels": nplan_launches, "queue_graph_kernels": nqueue_launches,
+        "tuned_splits": {f"2^{k}": v for k, v in splits.items()},
+        "autotune_s": round(ntune_s, 2), "bit_exact_vs_plain": ok_batch and ok_plan and ok_tuned and ok_queue,
+        "small_2_10_to_2_14": small,
     }
     bases.free()
     return out
@@ -905,7 +936,7 @@ def run_gpu_serve(ctx, args, requests: int = 200, grid=tuple(x / 2 for x in rang
     # closed-loop capacity: a burst of requests all present at t = 0
     closed = serve.poisson_trace(1e9, 64, list(keys), seed=2, weights=weights)
     cap = {}
-    for mode, tr in (("continuous", closed), ("batch", closed), ("plain", closed[:16])):
+    for mode, tr in (("continuous", closed), ("batch", closed), ("plain", closed)):
         t1 = time.perf_counter()
         res = svc.run(tr, mode)
         cap[mode] = len(tr) / (time.perf_counter() - t1)

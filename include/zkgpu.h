@@ -178,10 +178,39 @@ int zk_ntt_batch(zk_ctx *ctx, size_t count, const int *modes, void *const *outs,
                  const uint64_t *in_lens, const uint32_t *log_ns, const uint8_t *omegas, const uint8_t *shifts);
 
 /*
- * NTT batch plan: the descriptors and scratch of a zk_ntt_batch with fixed buffers,
- * prepared once; with use_graph = 1 a run is one CUDA graph launch. zk_ntt_plan_run
- * is asynchronous on the context stream; the buffers must outlive the plan.
+ * Work-queue form of a batch (north_star's "(instance, pass, tile) items"; no reference
+ * counterpart, the reference runs one op at a time): every pass of every transform in ONE
+ * persistent launch. Items are (transform, pass, tile), queued pass level by pass level
+ * with the largest transforms first; each CTA takes the next item from a device ticket,
+ * and an item of pass p > 0 waits (on the device) until its own transform's pass p - 1 has
+ * finished, so a transform's next pass starts while other transforms are still in the
+ * previous one. Every wait is bounded (2 s): a wait that runs out stops that launch early,
+ * and zk_ntt_queue_status reports it.
+ *   zk_ntt_batch_set_queue  on != 0: zk_ntt_batch on this context uses the queue form
+ *                           (default off: one launch per pass level).
+ *   zk_ntt_queue_status     synchronises the context stream; ZK_OK, or ZK_ETIMEOUT if a
+ *                           work-queue launch of this context gave up since the last call
+ *                           (its outputs are then incomplete).
+ *   zk_ntt_queue_selftest   for tests of the bound: one work-queue launch of a 2^12
+ *                           transform whose second pass waits for a first-pass tile that
+ *                           does not exist, with a wait limit of limit_us (1..10^7 us);
+ *                           returns ZK_ETIMEOUT with *entry_out = 1 + the queue entry whose
+ *                           wait ran out first (the second pass, or a third one waiting on
+ *                           it), the context staying usable; else ZK_OK or an error.
  */
+int zk_ntt_batch_set_queue(zk_ctx *ctx, int on);
+int zk_ntt_queue_status(zk_ctx *ctx);
+int zk_ntt_queue_selftest(zk_ctx *ctx, uint64_t limit_us, uint32_t *entry_out);
+
+/*
+ * NTT batch plan: the descriptors and scratch of a zk_ntt_batch with fixed buffers,
+ * prepared once. flags (the use_graph argument): ZK_NTT_PLAN_GRAPH (1) makes a run one
+ * CUDA graph launch; ZK_NTT_PLAN_QUEUE (2) runs the batch in its work-queue form (one
+ * persistent launch, see zk_ntt_batch_set_queue). zk_ntt_plan_run is asynchronous on the
+ * context stream; the buffers must outlive the plan.
+ */
+#define ZK_NTT_PLAN_GRAPH 1
+#define ZK_NTT_PLAN_QUEUE 2
 typedef struct zk_ntt_plan zk_ntt_plan;
 int zk_ntt_plan_create(zk_ctx *ctx, size_t count, const int *modes, void *const *outs, const void *const *ins,
                        const uint64_t *in_lens, const uint32_t *log_ns, const uint8_t *omegas, const uint8_t *shifts,

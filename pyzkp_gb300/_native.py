@@ -20,6 +20,8 @@ LIB_PATH = os.environ.get("ZKGPU_LIB") or os.path.join(HERE, "_lib", "libzkgpu.s
 
 ZK_OK, ZK_EINVAL, ZK_ECUDA, ZK_ENOMEM, ZK_ENODEV, ZK_ETIMEOUT = 0, 1, 2, 3, 4, 5
 
+NTT_PLAN_GRAPH, NTT_PLAN_QUEUE = 1, 2
+
 NTT_EVALS_FROM_COEFFS = 0
 NTT_COEFFS_FROM_EVALS = 1
 NTT_COSET_EVALS_FROM_COEFFS = 2
@@ -43,6 +45,7 @@ EXPORTED_SYMBOLS = (
     "zk_host_g1_add", "zk_host_g2_mul", "zk_host_g2_add", "zk_fr_add", "zk_bases_g2_create_dev", "zk_fr_batch_inv",
     "zk_plonk_quotient_evals", "zk_ctx_create_prio", "zk_stream_priority_range", "zk_h2d_async", "zk_d2h_async",
     "zk_fence_record", "zk_fence_wait", "zk_fence_destroy", "zk_fr_r1cs_check_async",
+    "zk_ntt_batch_set_queue", "zk_ntt_queue_status", "zk_ntt_queue_selftest",
 )
 
 _lib: Optional[ctypes.CDLL] = None
@@ -118,6 +121,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_ntt_batch": ([P, S, P, PP, PP, P, P, P, P], I),
             "zk_ntt_plan_create": ([P, S, P, PP, PP, P, P, P, P, I, PP], I),
             "zk_ntt_plan_run": ([P], I),
+            "zk_ntt_batch_set_queue": ([P, I], I),
+            "zk_ntt_queue_status": ([P], I),
+            "zk_ntt_queue_selftest": ([P, ctypes.c_uint64, ctypes.POINTER(U32)], I),
             "zk_ntt_plan_launches": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
             "zk_ntt_plan_destroy": ([P], I),
             "zk_tune_set_msm_window": ([P, U32, U32], I),
@@ -795,13 +801,33 @@ class Context:
         check(load().zk_ntt_batch(self.handle, count, modes.ctypes.data, outs, ins, lens.ctypes.data,
                                   logs.ctypes.data, om.ctypes.data, sh.ctypes.data), "zk_ntt_batch")
 
-    def ntt_plan(self, jobs, *, use_graph: bool = True) -> "NttPlan":
+    def ntt_plan(self, jobs, *, use_graph: bool = True, queue: bool = False) -> "NttPlan":
+        """A prepared batch; ``queue``: its work-queue form (one persistent launch)."""
         count, modes, outs, ins, lens, logs, om, sh = self._ntt_args(jobs)
         h = ctypes.c_void_p()
+        flags = (NTT_PLAN_GRAPH if use_graph else 0) | (NTT_PLAN_QUEUE if queue else 0)
         check(load().zk_ntt_plan_create(self.handle, count, modes.ctypes.data, outs, ins, lens.ctypes.data,
-                                        logs.ctypes.data, om.ctypes.data, sh.ctypes.data, 1 if use_graph else 0,
+                                        logs.ctypes.data, om.ctypes.data, sh.ctypes.data, flags,
                                         ctypes.byref(h)), "zk_ntt_plan_create")
         return NttPlan(self, h.value, [j[1] for j in jobs] + [j[2] for j in jobs])
+
+    def ntt_batch_set_queue(self, on: bool) -> None:
+        """ntt_batch in its work-queue form (one persistent launch) when on."""
+        check(load().zk_ntt_batch_set_queue(self.handle, 1 if on else 0), "zk_ntt_batch_set_queue")
+
+    def ntt_queue_status(self) -> None:
+        """Waits for the context stream; raises TimeoutError if a work-queue launch gave up."""
+        check(load().zk_ntt_queue_status(self.handle), "zk_ntt_queue_status")
+
+    def ntt_queue_selftest(self, limit_us: int) -> int:
+        """Runs a work-queue launch whose wait cannot succeed (zk_ntt_queue_selftest); returns
+        1 + the queue entry whose wait ran out. Raises if the launch did not time out."""
+        e = ctypes.c_uint32()
+        rc = load().zk_ntt_queue_selftest(self.handle, int(limit_us), ctypes.byref(e))
+        if rc != ZK_ETIMEOUT:
+            check(rc, "zk_ntt_queue_selftest")
+            raise ZkError("zk_ntt_queue_selftest: the wait did not run out")
+        return int(e.value)
 
     # ---- tuning
     def tune_set_msm_window(self, log_n: int, window_bits: int) -> None:

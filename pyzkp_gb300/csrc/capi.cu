@@ -213,6 +213,7 @@ int zk_ctx_destroy(zk_ctx* ctx) {
     for (cudaEvent_t ev : ctx->impl.chunk_ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->impl.inf_flag_dev) cudaFree(ctx->impl.inf_flag_dev);
+    if (ctx->impl.ntt_queue_err) cudaFree(ctx->impl.ntt_queue_err);
     for (auto& kv : ctx->impl.pinned_free) cudaFreeHost(kv.second);
     cudaStreamDestroy(ctx->impl.stream);
     delete ctx;
@@ -1017,11 +1018,36 @@ int zk_ntt_plan_create(zk_ctx* ctx, size_t count, const int* modes, void* const*
     std::vector<zk::NttJob> jobs;
     int rc = make_ntt_jobs(count, modes, outs, ins, in_lens, log_ns, omegas, shifts, &jobs);
     if (rc != ZK_OK) return rc;
+    if (use_graph & ~(ZK_NTT_PLAN_GRAPH | ZK_NTT_PLAN_QUEUE)) {
+        zk::set_error("unknown NTT plan flags");
+        return ZK_EINVAL;
+    }
     zk::NttBatchPlan* impl = nullptr;
-    rc = zk::ntt_plan_create(&ctx->impl, jobs.data(), count, use_graph != 0, &impl);
+    rc = zk::ntt_plan_create(&ctx->impl, jobs.data(), count, (use_graph & ZK_NTT_PLAN_GRAPH) != 0,
+                             (use_graph & ZK_NTT_PLAN_QUEUE) != 0, &impl);
     if (rc != ZK_OK) return rc;
     *out = new zk_ntt_plan{ctx, impl};
     return ZK_OK;
+}
+
+int zk_ntt_batch_set_queue(zk_ctx* ctx, int on) {
+    CTX_OR_FAIL(ctx);
+    ctx->impl.ntt_queue = on != 0;
+    return ZK_OK;
+}
+
+int zk_ntt_queue_status(zk_ctx* ctx) {
+    CTX_OR_FAIL(ctx);
+    return zk::ntt_queue_status(&ctx->impl);
+}
+
+int zk_ntt_queue_selftest(zk_ctx* ctx, uint64_t limit_us, uint32_t* entry_out) {
+    CTX_OR_FAIL(ctx);
+    if (entry_out == nullptr || limit_us == 0 || limit_us > 10000000ull) {
+        zk::set_error("zk_ntt_queue_selftest: limit_us must be in [1, 10^7] and entry_out non-null");
+        return ZK_EINVAL;
+    }
+    return zk::ntt_queue_selftest(&ctx->impl, limit_us * 1000ull, entry_out);
 }
 
 int zk_ntt_plan_run(zk_ntt_plan* plan) {

@@ -91,8 +91,28 @@ __device__ __forceinline__ void smem_put(uint4* s_lo, uint4* s_hi, uint32_t i, c
     s_hi[i] = make_uint4(v.v[4], v.v[5], v.v[6], v.v[7]);
 }
 
-// One CTA's tile `tile` of one pass (shared by the single-transform and the batch kernel).
-__device__ __forceinline__ void ntt_pass_body(const NttPassParams& P, uint32_t tile, uint4* smem) {
+// A 32-byte element through L2 only (ld.global.cg): for data that other CTAs wrote earlier
+// in the same launch, which the non-coherent read-only path is not guaranteed to see.
+__device__ __forceinline__ fe fe_ldcg(const fe* p) {
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+    uint4 lo = __ldcg(q), hi = __ldcg(q + 1);
+    fe r;
+    r.v[0] = lo.x;
+    r.v[1] = lo.y;
+    r.v[2] = lo.z;
+    r.v[3] = lo.w;
+    r.v[4] = hi.x;
+    r.v[5] = hi.y;
+    r.v[6] = hi.z;
+    r.v[7] = hi.w;
+    return r;
+}
+
+// One CTA's tile `tile` of one pass (shared by the single-transform, the batch and the
+// queue kernel). l2_in: the pass input was written earlier in the same launch (a runtime
+// flag rather than a template argument: one copy of the body in the queue kernel).
+__device__ __forceinline__ void ntt_pass_body(const NttPassParams& P, uint32_t tile, uint4* smem,
+                                              bool l2_in = false) {
     const uint32_t log_r = P.log_r, log_t = P.log_t;
     const uint32_t R = 1u << log_r, T = 1u << log_t, E = R << log_t;
     uint4* s_lo = smem;
@@ -107,7 +127,7 @@ __device__ __forceinline__ void ntt_pass_body(const NttPassParams& P, uint32_t t
         const uint32_t m = idx >> log_t, t = idx & (T - 1);
         const uint32_t col = c0 + t;
         const uint32_t g = col + (m << stride_log);
-        fe v = g < P.in_len ? fe_ldg(P.in + g) : fe_zero();
+        fe v = g < P.in_len ? (l2_in ? fe_ldcg(P.in + g) : fe_ldg(P.in + g)) : fe_zero();
         if (P.pre_lo != nullptr && g < P.in_len) v = fe_mul<FrN>(v, lookup2(P.pre_lo, P.pre_hi, g, P.s_bits));
         if (P.log_l != 0) {
             const uint32_t e = (m * (col & l_mask)) << tw_shift;
@@ -187,6 +207,123 @@ __global__ void __launch_bounds__(kNttThreads, 3) ntt_pass_batch_kernel(const Nt
     }
     __syncthreads();
     ntt_pass_body(sP, s_tile, smem);
+}
+
+// ---- persistent launch from a device work queue --------------------------------------------
+// The queue is the list of (transform, pass) entries in queue order; entry e owns the items
+// [first, first + tiles), one per tile of that pass. Every CTA of one launch takes items from
+// a ticket counter until the queue is empty. An item of pass p > 0 waits until `need` tiles of
+// the transform's pass p - 1 (entry `dep`) have finished: entries are ordered pass level by
+// pass level (the largest transforms first within a level), so every item waited on was
+// taken earlier by a running CTA, whose own dependencies were taken earlier still -- the
+// earliest unfinished item never waits, and the launch cannot deadlock whatever the number
+// of resident CTAs. A transform's pass p + 1 starts as soon as its own pass p is done, while
+// other transforms are still in pass p (no launch boundary between levels).
+struct NttQueueEntry {
+    NttPassParams P;
+    uint32_t first;  // first item of the entry in queue order
+    uint32_t tiles;  // items (CTAs of the pass)
+    int32_t dep;     // entry of the transform's previous pass, -1 for a first pass
+    uint32_t need;   // finished items of `dep` to wait for (its tiles)
+};
+
+// Queue state words, zeroed before each launch: the ticket, the status, then one finished-item
+// counter per entry. Status 0: every item ran; otherwise 1 + the entry whose wait ran out.
+static constexpr uint32_t kQueueTicket = 0, kQueueStatus = 1, kQueueDone = 2;
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Entries whose first items are cached in shared memory for the item lookup (more entries:
+// the lookup reads the global table).
+static constexpr uint32_t kQueueSmemEntries = 1024;
+static constexpr uint32_t kNone32 = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t queue_ticket(uint32_t* state, uint32_t nitems) {
+    volatile uint32_t* vstate = state;
+    return vstate[kQueueStatus] != 0 ? nitems : atomicAdd(state + kQueueTicket, 1u);
+}
+
+__global__ void __launch_bounds__(kNttThreads, 3) ntt_queue_kernel(const NttQueueEntry* __restrict__ entries,
+                                                                  uint32_t nentries, uint32_t nitems,
+                                                                  uint32_t* state,
+                                                                  const uint64_t* __restrict__ limit,
+                                                                  uint32_t* sticky) {
+    extern __shared__ uint4 smem[];
+    __shared__ NttQueueEntry sE;
+    __shared__ uint32_t s_first[kQueueSmemEntries];
+    __shared__ uint32_t s_next, s_item, s_entry, s_tile, s_stop;
+    volatile uint32_t* vstate = state;
+    const bool cached = nentries <= kQueueSmemEntries;
+    if (cached)
+        for (uint32_t e = threadIdx.x; e < nentries; e += blockDim.x) s_first[e] = entries[e].first;
+    if (threadIdx.x == 0) s_next = queue_ticket(state, nitems);
+    __syncthreads();
+    uint32_t finished = kNone32;  // warp 1, lane 0: the entry of the tile this CTA just finished
+    for (;;) {
+        if (threadIdx.x < 32) {  // warp 0: find the next item's entry, copy it, wait for its dependency
+            const uint32_t item = s_next;
+            uint32_t e = 0;
+            if (threadIdx.x == 0 && item < nitems) {
+                uint32_t lo = 0, hi = nentries;  // the entry holding `item`: largest e with first <= item
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if ((cached ? s_first[mid] : entries[mid].first) <= item) lo = mid;
+                    else hi = mid;
+                }
+                e = lo;
+            }
+            e = __shfl_sync(0xffffffffu, e, 0);
+            constexpr uint32_t kWords = sizeof(NttQueueEntry) / 4;
+            static_assert(kWords <= 32 && sizeof(NttQueueEntry) % 4 == 0, "queue entry copy by one warp");
+            if (item < nitems && threadIdx.x < kWords)
+                reinterpret_cast<uint32_t*>(&sE)[threadIdx.x] =
+                    reinterpret_cast<const uint32_t*>(entries + e)[threadIdx.x];
+            __syncwarp();
+            if (threadIdx.x == 0) {
+                s_item = item;
+                s_entry = e;
+                s_stop = 0;
+                if (item < nitems) {
+                    s_tile = item - sE.first;
+                    if (sE.dep >= 0) {
+                        const uint32_t dep = (uint32_t)sE.dep, need = sE.need;
+                        const uint64_t t0 = global_ns();
+                        uint32_t ns = 32;
+                        while (vstate[kQueueDone + dep] < need) {
+                            // bounded: give up when the limit passes or another CTA gave up
+                            if (vstate[kQueueStatus] != 0 || global_ns() - t0 > *limit) {
+                                if (atomicCAS(state + kQueueStatus, 0u, e + 1u) == 0u) atomicCAS(sticky, 0u, e + 1u);
+                                s_stop = 1;
+                                break;
+                            }
+                            __nanosleep(ns);
+                            if (ns < 1024) ns <<= 1;
+                        }
+                        __threadfence();  // acquire: the previous pass's outputs before our loads
+                    }
+                }
+            }
+        } else if (threadIdx.x == 32 && finished != kNone32) {
+            // warp 1 publishes the finished tile while warp 0 looks up the next item
+            __threadfence();  // release: the tile's outputs (ordered by the barrier) before the counter
+            atomicAdd(state + kQueueDone + finished, 1u);
+        }
+        __syncthreads();
+        if (s_item >= nitems || s_stop) return;
+        if (threadIdx.x == 32) finished = s_entry;
+        // the next item's ticket now: its latency hides behind this tile. The item is taken
+        // only after this one's dependency is met, which keeps the earliest unfinished item
+        // always runnable.
+        uint32_t nxt = 0;
+        if (threadIdx.x == 0) nxt = queue_ticket(state, nitems);
+        ntt_pass_body(sE.P, s_tile, smem, sE.dep >= 0);
+        __syncthreads();  // every store of the tile issued; sE and s_tile free again
+        if (threadIdx.x == 0) s_next = nxt;
+    }
 }
 
 // full[e] = lo[e mod 2^s] hi[e >> s] for e < n: a two-level table flattened into one
@@ -374,6 +511,8 @@ static int set_smem_attr(int device) {
                                          (2 << kTileLogElems) * 16));
         ZK_TRY_CUDA(cudaFuncSetAttribute(ntt_pass_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (2 << kTileLogElems) * 16));
+        ZK_TRY_CUDA(cudaFuncSetAttribute(ntt_queue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (2 << kTileLogElems) * 16));
         done[device] = true;
     }
     return ZK_OK;
@@ -512,6 +651,13 @@ struct NttBatch {
     std::vector<size_t> items_at, first_at;  // byte offsets inside desc
     char* desc = nullptr;
     fe* scratch = nullptr;
+    // queue form (one persistent launch): entries in queue order, then the wait limit (ns)
+    // and the state words (ticket, status, finished items per entry), all inside desc
+    bool queue = false;
+    std::vector<NttQueueEntry> qentries;
+    uint32_t qitems = 0, qsmem = 32, qgrid = 0;
+    size_t queue_at = 0, limit_at = 0, state_at = 0;
+    uint64_t limit_ns = 2000000000ull;
 };
 
 static int batch_prepare(Ctx* c, const NttJob* jobs, size_t count, NttBatch* b) {
@@ -577,6 +723,55 @@ static int batch_layout(const NttJob* jobs, size_t count, NttBatch* b, Ctx* c) {
         b->first_at[L] = off;
         off += b->first[L].size() * 4;
     }
+    if (b->queue) {
+        // every CTA that can be resident at once, and no more CTAs than items
+        b->qsmem = 32;
+        uint64_t items = 0;
+        for (size_t j = 0; j < count; j++)
+            for (const PassLaunch& pl : b->jobs[j]) {
+                b->qsmem = std::max(b->qsmem, pl.smem);
+                items += pl.blocks;
+            }
+        int per_sm = 0;
+        ZK_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ntt_queue_kernel, kNttThreads, b->qsmem));
+        b->qgrid = (uint32_t)std::min<uint64_t>(items, (uint64_t)std::max(1, per_sm) * c->num_sms);
+        // Queue order: pass level by pass level, the largest transforms first within a level,
+        // so that the first items of the next level belong to the transforms whose previous
+        // pass began earliest; every entry follows the entry it waits for. (Measured on
+        // GB300: queueing a transform's next pass two waves after its previous one, to read
+        // its intermediate from L2, was slower: 64 mixed transforms 3.11 against 2.98 ms,
+        // 64 small ones 0.165 against 0.12 ms -- its items wait on unfinished passes.)
+        std::vector<size_t> order(count);
+        for (size_t j = 0; j < count; j++) order[j] = j;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](size_t a, size_t z) { return jobs[a].log_n > jobs[z].log_n; });
+        std::vector<int32_t> prev(count, -1);
+        b->qentries.clear();
+        b->qitems = 0;
+        for (size_t L = 0; L < b->items.size(); L++) {
+            for (size_t j : order) {
+                if (L >= b->jobs[j].size()) continue;
+                const PassLaunch& pl = b->jobs[j][L];
+                NttQueueEntry e{};
+                e.P = pl.P;
+                e.first = b->qitems;
+                e.tiles = pl.blocks;
+                e.dep = prev[j];
+                e.need = L ? b->jobs[j][L - 1].blocks : 0u;
+                prev[j] = (int32_t)b->qentries.size();
+                b->qentries.push_back(e);
+                b->qitems += pl.blocks;
+            }
+        }
+        off = (off + 255) & ~(size_t)255;
+        b->queue_at = off;
+        off += b->qentries.size() * sizeof(NttQueueEntry);
+        off = (off + 255) & ~(size_t)255;
+        b->limit_at = off;
+        off += 8;
+        b->state_at = off;
+        off += (kQueueDone + b->qentries.size()) * 4;
+    }
     b->desc_bytes = off ? off : 16;
     return ZK_OK;
 }
@@ -588,10 +783,25 @@ static int batch_upload(Ctx* c, NttBatch* b) {
         ZK_TRY_CUDA(cudaMemcpyAsync(b->desc + b->first_at[L], b->first[L].data(), b->first[L].size() * 4,
                                     cudaMemcpyHostToDevice, c->stream));
     }
+    if (b->queue) {
+        ZK_TRY_CUDA(cudaMemcpyAsync(b->desc + b->queue_at, b->qentries.data(),
+                                    b->qentries.size() * sizeof(NttQueueEntry), cudaMemcpyHostToDevice, c->stream));
+        ZK_TRY_CUDA(cudaMemcpyAsync(b->desc + b->limit_at, &b->limit_ns, 8, cudaMemcpyHostToDevice, c->stream));
+    }
     return ZK_OK;
 }
 
 static int batch_enqueue(Ctx* c, const NttBatch* b) {
+    if (b->queue) {
+        if (b->qitems == 0) return ZK_OK;
+        uint32_t* state = reinterpret_cast<uint32_t*>(b->desc + b->state_at);
+        ZK_TRY_CUDA(cudaMemsetAsync(state, 0, (kQueueDone + b->qentries.size()) * 4, c->stream));
+        ZK_LAUNCH(c, "ntt_queue", ntt_queue_kernel, b->qgrid, kNttThreads, b->qsmem,
+                  reinterpret_cast<const NttQueueEntry*>(b->desc + b->queue_at), (uint32_t)b->qentries.size(),
+                  b->qitems, state, reinterpret_cast<const uint64_t*>(b->desc + b->limit_at), c->ntt_queue_err);
+        ZK_TRY_CUDA(cudaGetLastError());
+        return ZK_OK;
+    }
     for (size_t L = 0; L < b->items.size(); L++) {
         if (b->blocks[L] == 0) continue;
         ZK_LAUNCH(c, "ntt_pass_batch", ntt_pass_batch_kernel, b->blocks[L], b->threads[L], b->smem[L],
@@ -602,12 +812,36 @@ static int batch_enqueue(Ctx* c, const NttBatch* b) {
     return ZK_OK;
 }
 
+// The context's work-queue error word (allocated once, before any capture can need it).
+static int ensure_queue_word(Ctx* c) {
+    std::lock_guard<std::mutex> g(c->mu);
+    if (c->ntt_queue_err == nullptr) {
+        ZK_TRY_CUDA(cudaMalloc(reinterpret_cast<void**>(&c->ntt_queue_err), 4));
+        ZK_TRY_CUDA(cudaMemsetAsync(c->ntt_queue_err, 0, 4, c->stream));
+    }
+    return ZK_OK;
+}
+
+int ntt_queue_status(Ctx* c) {
+    if (c->ntt_queue_err == nullptr) return ZK_OK;
+    ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
+    uint32_t v = 0;
+    ZK_TRY_CUDA(cudaMemcpy(&v, c->ntt_queue_err, 4, cudaMemcpyDeviceToHost));
+    if (v == 0) return ZK_OK;
+    ZK_TRY_CUDA(cudaMemset(c->ntt_queue_err, 0, 4));
+    set_error("NTT work queue: the wait of queue entry " + std::to_string(v - 1) +
+              " for its previous pass ran out; that launch stopped early and its outputs are incomplete");
+    return ZK_ETIMEOUT;
+}
+
 int ntt_batch_run(Ctx* c, const NttJob* jobs, size_t count) {
     if (count == 0) return ZK_OK;
     NttBatch b;
+    b.queue = c->ntt_queue;
     int rc = batch_prepare(c, jobs, count, &b);
     if (rc != ZK_OK) return rc;
     if ((rc = set_smem_attr(c->device)) != ZK_OK) return rc;
+    if (b.queue && (rc = ensure_queue_word(c)) != ZK_OK) return rc;
     if ((rc = batch_layout(jobs, count, &b, c)) != ZK_OK) return rc;  // sizes only
     char* arena = nullptr;
     const size_t scratch_bytes = ((b.scratch_elems * 32) + 255) & ~(size_t)255;
@@ -627,12 +861,14 @@ struct NttBatchPlan {
     uint64_t kernels = 0;
 };
 
-int ntt_plan_create(Ctx* c, const NttJob* jobs, size_t count, bool graph, NttBatchPlan** out) {
+int ntt_plan_create(Ctx* c, const NttJob* jobs, size_t count, bool graph, bool queue, NttBatchPlan** out) {
     std::unique_ptr<NttBatchPlan> plan(new NttBatchPlan());
     NttBatch& b = plan->b;
+    b.queue = queue;
     int rc = batch_prepare(c, jobs, count, &b);
     if (rc != ZK_OK) return rc;
     if ((rc = set_smem_attr(c->device)) != ZK_OK) return rc;
+    if (queue && (rc = ensure_queue_word(c)) != ZK_OK) return rc;
     if ((rc = batch_layout(jobs, count, &b, c)) != ZK_OK) return rc;
     const size_t scratch_bytes = ((b.scratch_elems * 32) + 255) & ~(size_t)255;
     ZK_TRY_CUDA(cudaMalloc(reinterpret_cast<void**>(&plan->arena), scratch_bytes + b.desc_bytes));
@@ -695,6 +931,73 @@ int ntt_plan_run(Ctx* c, NttBatchPlan* plan) {
 }
 
 uint64_t ntt_plan_kernels(const NttBatchPlan* plan) { return plan->kernels; }
+
+int ntt_queue_selftest(Ctx* c, uint64_t limit_ns, uint32_t* entry_out) {
+    // one 2^12 transform (two passes, or three under a tuned split) on zeroed buffers: the
+    // second pass's items wait for one first-pass tile more than the queue holds, so their
+    // waits run out (and a third pass's, waiting on the second, too)
+    const uint32_t log_n = 12;
+    static const uint8_t one[32] = {1};
+    uint8_t omega[32];
+    {
+        // omega = 5^((r - 1) / 2^12): a primitive 2^12-th root of unity (5 generates Fr^*)
+        const zkh::Field& F = zkh::fr();
+        uint64_t e[4];
+        std::memcpy(e, F.p, 32);
+        e[0] -= 1;  // r - 1 (r is odd)
+        for (uint32_t i = 0; i < log_n; i++)
+            for (int k = 0; k < 4; k++) e[k] = (e[k] >> 1) | (k < 3 ? e[k + 1] << 63 : 0);
+        const zkh::F4 om = zkh::pow(F, zkh::to_mont(F, zkh::F4{{5, 0, 0, 0}}), e);
+        const zkh::F4 canon = zkh::from_mont(F, om);
+        std::memcpy(omega, canon.v, 32);
+    }
+    fe* buf = nullptr;
+    const size_t n = (size_t)1 << log_n;
+    ZK_TRY_CUDA(cudaMalloc(reinterpret_cast<void**>(&buf), n * 32 * 2));
+    auto done = [&](int rc) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(buf);
+        return rc;
+    };
+    if (cudaMemsetAsync(buf, 0, n * 32 * 2, c->stream) != cudaSuccess) return done(ZK_ECUDA);
+    NttJob J;
+    J.mode = ZK_NTT_EVALS_FROM_COEFFS;
+    J.out = buf + n;
+    J.in = buf;
+    J.in_len = n;
+    J.log_n = log_n;
+    J.omega = omega;
+    J.shift = one;
+    NttBatchPlan* plan = nullptr;
+    int rc = ntt_plan_create(c, &J, 1, false, true, &plan);
+    if (rc != ZK_OK) return done(rc);
+    NttBatch& b = plan->b;
+    rc = ZK_EINVAL;
+    if (b.qentries.size() >= 2 && b.qentries[1].dep == 0) {
+        b.qentries[1].need = b.qentries[0].tiles + 1;  // one tile more than pass 1 has
+        b.limit_ns = limit_ns;
+        rc = batch_upload(c, &b);
+        if (rc == ZK_OK) rc = batch_enqueue(c, &b);
+    } else {
+        set_error("NTT queue self-test: unexpected plan shape");
+    }
+    uint32_t st = 0;
+    if (rc == ZK_OK) {
+        cudaError_t e = cudaMemcpyAsync(&st, b.desc + b.state_at + 4 * kQueueStatus, 4, cudaMemcpyDeviceToHost,
+                                        c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            set_error(std::string("NTT queue self-test: ") + cudaGetErrorString(e));
+            rc = ZK_ECUDA;
+        }
+    }
+    ntt_plan_destroy(c, plan);
+    if (rc != ZK_OK) return done(rc);
+    *entry_out = st;
+    // the sticky context record is the self-test's own: clear it
+    cudaMemsetAsync(c->ntt_queue_err, 0, 4, c->stream);
+    return done(st == 0 ? ZK_OK : ZK_ETIMEOUT);
+}
 
 void ntt_plan_destroy(Ctx* c, NttBatchPlan* plan) {
     if (plan == nullptr) return;

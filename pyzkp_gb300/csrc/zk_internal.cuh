@@ -88,6 +88,10 @@ struct Ctx {
     std::mutex mu;
     std::map<std::string, NttPlan*> ntt_plans;
     size_t ntt_full_table_bytes = 0;  // device bytes held by full (one-load) NTT tables
+    // zk_ntt_batch as one persistent launch from a device work queue (zk_ntt_batch_set_queue),
+    // and the device word where such launches record a wait that ran out (zk_ntt_queue_status)
+    bool ntt_queue = false;
+    uint32_t* ntt_queue_err = nullptr;
     uint64_t launches = 0;
     bool prof_on = false;
     std::map<std::string, ProfEntry> prof;
@@ -210,7 +214,13 @@ struct NttJob {
 };
 struct NttBatchPlan;
 int ntt_batch_run(Ctx* c, const NttJob* jobs, size_t count);
-int ntt_plan_create(Ctx* c, const NttJob* jobs, size_t count, bool graph, NttBatchPlan** out);
+int ntt_plan_create(Ctx* c, const NttJob* jobs, size_t count, bool graph, bool queue, NttBatchPlan** out);
+// ZK_OK, or ZK_ETIMEOUT when a work-queue launch since the last call gave up waiting
+// (synchronises the context stream; clears the record)
+int ntt_queue_status(Ctx* c);
+// A work-queue launch whose second pass waits for one more first-pass tile than exist, with
+// the given wait limit: returns its status (ZK_ETIMEOUT expected), for tests of the limit.
+int ntt_queue_selftest(Ctx* c, uint64_t limit_ns, uint32_t* entry_out);
 int ntt_plan_run(Ctx* c, NttBatchPlan* plan);
 uint64_t ntt_plan_kernels(const NttBatchPlan* plan);
 void ntt_plan_destroy(Ctx* c, NttBatchPlan* plan);

@@ -192,6 +192,74 @@ def test_ntt_plan_replays_with_new_inputs(gpu_ctx, use_graph):
     plan.free()
 
 
+def test_ntt_batch_work_queue_matches_oracle(gpu_ctx):
+    """The work-queue form (one persistent launch) gives the per-transform results, in place and
+    out of place, including 3-pass transforms (tuned split) whose middle pass reads data other
+    CTAs wrote earlier in the same launch."""
+    spec = NTT_SPEC + [(2, 14, 1 << 14, 5, True), (1, 15, 1 << 15, 1, False)]
+    try:
+        gpu_ctx.tune_set_ntt_split(14, [5, 5, 4])
+        gpu_ctx.tune_set_ntt_split(15, [4, 6, 5])
+        gpu_ctx.ntt_batch_set_queue(True)
+        for rep in range(2):
+            jobs, inputs, outs = _ntt_jobs(gpu_ctx, spec, 3300 + 50 * rep)
+            gpu_ctx.ntt_batch(jobs)
+            gpu_ctx.ntt_queue_status()
+            for (mode, log_n, in_len, shift, _), v, d in zip(spec, inputs, outs):
+                got = _download(gpu_ctx, d, 1 << log_n)
+                assert (got == _oracle_ntt(mode, v, log_n, shift)).all(), (rep, mode, log_n, in_len)
+    finally:
+        gpu_ctx.ntt_batch_set_queue(False)
+        gpu_ctx.tune_set_ntt_split(14, [])
+        gpu_ctx.tune_set_ntt_split(15, [])
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_ntt_queue_plan_replays_and_counts_one_kernel(gpu_ctx, use_graph):
+    spec = [s for s in NTT_SPEC if not s[4]]
+    jobs, _, outs = _ntt_jobs(gpu_ctx, spec, 3400)
+    plan = gpu_ctx.ntt_plan(jobs, use_graph=use_graph, queue=True)
+    if use_graph:
+        assert plan.launches() == 1  # the whole batch is one kernel
+    for rep in range(3):
+        inputs = []
+        for j, (mode, log_n, in_len, shift, _) in enumerate(spec):
+            v = synth.fr_uniform(4400 + 100 * rep + j, in_len)
+            if in_len:
+                jobs[j][2].upload(v)
+                gpu_ctx.fr_to_mont(jobs[j][2], jobs[j][2], in_len)
+            inputs.append(v)
+        plan.run()
+        gpu_ctx.ntt_queue_status()
+        for (mode, log_n, in_len, shift, _), v, d in zip(spec, inputs, outs):
+            got = _download(gpu_ctx, d, 1 << log_n)
+            assert (got == _oracle_ntt(mode, v, log_n, shift)).all(), (rep, mode, log_n)
+    plan.free()
+
+
+def test_ntt_queue_wait_limit_runs_out_and_context_survives(gpu_ctx):
+    """A wait that can never succeed (a second pass waiting for one first-pass tile more than
+    exist) gives up at its limit: the launch returns, the status names the waiting entry, and
+    the context runs the next transform correctly."""
+    import time
+
+    t = time.perf_counter()
+    entry = gpu_ctx.ntt_queue_selftest(20000)  # 20 ms limit
+    assert time.perf_counter() - t < 5.0
+    assert entry in (2, 3)  # 1 + queue entry 1 (the second pass), or 2 under a 3-pass split
+    gpu_ctx.ntt_queue_status()  # the self-test's record is its own: nothing left over
+    v = synth.fr_uniform(3500, 1 << 12)
+    d = gpu_ctx.to_device(v)
+    gpu_ctx.fr_to_mont(d, d, 1 << 12)
+    gpu_ctx.ntt_batch_set_queue(True)
+    try:
+        gpu_ctx.ntt_batch([(0, d, d, 1 << 12, 12, _omega(12), 1)])
+        gpu_ctx.ntt_queue_status()
+    finally:
+        gpu_ctx.ntt_batch_set_queue(False)
+    assert (_download(gpu_ctx, d, 1 << 12) == _oracle_ntt(0, v, 12, 1)).all()
+
+
 def test_ntt_tuned_splits_in_place_and_json(gpu_ctx, tmp_path):
     """A tuned radix split changes timing only: 3-pass in-place transforms, tuning file round trip."""
     try:
