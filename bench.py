@@ -490,18 +490,32 @@ def traffic_of(kernel: str, log_n: int):
 
 
 def sort_kernels(table: dict, steps: int, n: int, entries: int, hbm_peak: float) -> dict:
-    """HBM view of the digit decomposition and the CSR scatter (the memory-bound stages):
-    algorithmic bytes per launch over the live kernel time. msm_digits reads the 32-byte
-    scalars and writes the two 32-byte GLV halves; msm_scatter reads the halves and writes
-    one 4-byte entry per non-zero digit."""
+    """HBM view of the CSR sort (the memory-bound stages): algorithmic bytes per launch over
+    the live kernel time. Tiled sort: msm_codes reads the 32-byte scalars and writes one
+    4-byte code per (point, window); msm_hist reads the codes; msm_scatter_tiles reads them
+    again and writes one 4-byte entry each (its per-tile counters are not counted). Atomic
+    sort (bucket sets over 2^15): msm_digits reads the scalars and writes the two 32-byte
+    GLV halves; msm_scatter reads the halves and writes the entries. `stage`: every sort
+    kernel together (scan and per-tile counter passes included) against the stage's own
+    minimum, the scalars in and the entries out."""
     out = {}
-    for name, nbytes in (("msm_digits", n * (32 + 64)), ("msm_scatter", n * 64 + entries * 4)):
+    for name, nbytes in (("msm_codes", n * 32 + entries * 4), ("msm_hist", entries * 4),
+                         ("msm_scatter_tiles", entries * 8), ("msm_digits", n * (32 + 64)),
+                         ("msm_scatter", n * 64 + entries * 4)):
         la, ms = table.get(name, (0, 0.0))
         if not la:
             continue
         t = ms / la
         gbs = nbytes / (t * 1e-3) / 1e9
         out[name] = {"ms": round(t, 4), "bytes": nbytes, "GB_s": round(gbs, 1), "frac": round(gbs / hbm_peak, 4)}
+    names = ("msm_codes", "msm_hist", "msm_hist_total", "msm_hist_offsets", "msm_scatter_tiles", "msm_digits",
+             "msm_scatter", "scan_tiles", "scan_add")
+    t = sum(table[k][1] / steps for k in names if k in table and table[k][0])
+    if t > 0:
+        nbytes = n * 32 + entries * 4
+        gbs = nbytes / (t * 1e-3) / 1e9
+        out["stage"] = {"ms": round(t, 4), "bytes": nbytes, "GB_s": round(gbs, 1), "frac": round(gbs / hbm_peak, 4),
+                        "kernels": [k for k in names if k in table and table[k][0]]}
     return out
 
 
@@ -942,6 +956,41 @@ def run_gpu_serve(ctx, args, requests: int = 200, grid=tuple(x / 2 for x in rang
         cap[mode] = len(tr) / (time.perf_counter() - t1)
         if mode == "continuous":
             cap_proofs = res.proofs
+    # The accumulation floor of the burst: its CSR entries (fixed-base mode: ceil(255 / c)
+    # per point and query) times the accumulation kernel's time per entry, measured on one
+    # large MSM of the largest resident key (G1 l-query, G2 b-query). No mode can prove the
+    # burst faster than this, so plain_time / floor bounds the batched / plain ratio.
+    from pyzkp_gb300 import synth
+    from pyzkp_gb300.plugin import fixed_base_window
+
+    def _entries(q):
+        return q.count * -(-255 // fixed_base_window(q.count)) if q.count else 0
+
+    e_g1 = sum(_entries(q) for a in closed for q in (keys[a.key_id].a, keys[a.key_id].b1, keys[a.key_id].l,
+                                                      keys[a.key_id].h))
+    e_g2 = sum(_entries(keys[a.key_id].b2) for a in closed)
+    big = keys[max(keys, key=lambda i: sizes[i])]
+    per_entry = {}
+    for name, q, fn in (("g1", big.l, ctx.msm_g1), ("g2", big.b2, ctx.msm_g2)):
+        sc = ctx.to_device(synth.fr_uniform(77, q.count))
+        ctx.fr_to_mont(sc, sc, q.count)
+        fn(q.bases, sc, q.count)
+        ctx.sync()
+        ctx.prof_reset()
+        ctx.prof_enable(True)
+        fn(q.bases, sc, q.count)
+        ctx.sync()
+        tab = ctx.prof_table()
+        ctx.prof_enable(False)
+        per_entry[name] = tab["msm_accumulate"][1] / ctx.msm_last_stats()["entries"]
+        del sc
+    floor_ms = e_g1 * per_entry["g1"] + e_g2 * per_entry["g2"]
+    plain_ms = len(closed) / cap["plain"] * 1e3
+    floor = {"g1_entries": e_g1, "g2_entries": e_g2,
+             "ns_per_entry": {k: round(v * 1e6, 3) for k, v in per_entry.items()},
+             "burst_ms": round(floor_ms, 2), "plain_burst_ms": round(plain_ms, 2),
+             "continuous_burst_ms": round(len(closed) / cap["continuous"] * 1e3, 2),
+             "max_ratio_over_plain": round(plain_ms / floor_ms, 2)}
     sweep = []
     exact = True
     verify_jobs = []
@@ -974,6 +1023,7 @@ def run_gpu_serve(ctx, args, requests: int = 200, grid=tuple(x / 2 for x in rang
         "capacity_proofs_s": {k: round(v, 1) for k, v in cap.items()},
         "capacity_continuous_over_plain": round(cap["continuous"] / cap["plain"], 2),
         "capacity_batch_over_plain": round(cap["batch"] / cap["plain"], 2),
+        "accumulation_floor": floor,
         "sweep": sweep, "bit_exact_all_modes": exact,
         "proofs_total": len(verify_jobs), "proofs_verified": None,
         "note": "latency = completion - arrival on the wall clock; proof assembly (5 host scalar "

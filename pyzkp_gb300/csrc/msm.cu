@@ -508,6 +508,147 @@ __global__ void msm_scatter_kernel(const fe* __restrict__ reduced, const MsmInst
     }
 }
 
+// ---- 2-3 (tiled form). CSR sort without global atomics ----------------------------------
+// Used when a bucket set fits shared memory (B <= kTiledMaxB). The entries of bucket set s
+// (instance k = s / Wr) are enumerated in a fixed order: position set_base[s] + idx with
+// idx = i * halves + h (point i, GLV half h) for window sets, idx = w * n_k + i for the one
+// shared set of the fixed-base mode. Each set's positions are cut into tiles of `te`
+// entries, numbered from set_tile0[s]:
+//   codes     one 32-bit code per position: |d| - 1 | sign << 31, kNoCode for a zero digit
+//             (digits computed once, from the canonical scalars);
+//   hist      per tile, its bucket counts in shared memory -> M[tile][b] (no global atomics);
+//   totals    per (set, b), the sum over the set's tiles -> row_ptr, then the exclusive scan;
+//   offsets   M[tile][b] := row_ptr + the counts of the set's earlier tiles;
+//   scatter   per tile, shared-memory cursors from M: entries land in tile order within each
+//             bucket (the order inside a tile is that of the shared-memory atomics).
+static constexpr uint32_t kNoCode = 0xffffffffu;
+static constexpr uint32_t kTiledMaxB = 1u << 15;  // 128 KB of shared-memory counters
+static constexpr uint32_t kTiledThreads = 1024;
+
+template <class C>
+__global__ void msm_codes_kernel(const MsmInst* __restrict__ insts, const uint32_t* __restrict__ offs, uint32_t j0,
+                                 uint32_t N, int scalars_mont, MsmShape sh, const uint32_t* __restrict__ set_base,
+                                 uint32_t* __restrict__ codes) {
+    const uint32_t j = j0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    const uint32_t k = find_inst(offs, sh.inst, j);
+    const uint32_t i = j - __ldg(offs + k);
+    fe s = fe_ldg(insts[k].scalars + i);
+    s = scalars_mont ? fe_from_mont<FrP>(s) : fe_from_mont<FrP>(fe_to_mont<FrP>(s));
+    const uint32_t set0 = k * sh.Wr;
+    if (sh.glv) {
+        fe h[2];
+        glv_split(s, h[0], h[1]);
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) {
+            const uint32_t flip = h[hh].v[7] & 0x80000000u;  // the half is negative
+            h[hh].v[7] &= 0x7fffffffu;
+            uint32_t carry = 0;
+            for (uint32_t w = 0; w < sh.W; w++) {
+                const uint32_t d = signed_digit(h[hh], w, sh, carry);
+                const uint32_t code = d ? (((d & 0x7fffffffu) - 1) | ((d & 0x80000000u) ^ flip)) : kNoCode;
+                codes[__ldg(set_base + set0 + w) + 2 * i + hh] = code;
+            }
+        }
+        return;
+    }
+    const uint32_t nk = insts[k].n;
+    uint32_t carry = 0;
+    for (uint32_t w = 0; w < sh.W; w++) {
+        const uint32_t d = signed_digit(s, w, sh, carry);
+        const uint32_t code = d ? (((d & 0x7fffffffu) - 1) | (d & 0x80000000u)) : kNoCode;
+        const uint32_t pos = sh.shared ? __ldg(set_base + set0) + w * nk + i : __ldg(set_base + set0 + w) + i;
+        codes[pos] = code;
+    }
+}
+
+// The set of tile t: the largest s with set_tile0[s] <= t.
+__device__ __forceinline__ uint32_t set_of_tile(const uint32_t* __restrict__ set_tile0, uint32_t sets, uint32_t t) {
+    uint32_t lo = 0, hi = sets;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(set_tile0 + mid) <= t) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(kTiledThreads) msm_hist_kernel(const uint32_t* __restrict__ codes,
+                                                                 const uint32_t* __restrict__ set_base,
+                                                                 const uint32_t* __restrict__ set_tile0,
+                                                                 uint32_t sets, uint32_t te, uint32_t B,
+                                                                 uint32_t* __restrict__ M) {
+    extern __shared__ uint32_t hist[];
+    const uint32_t t = blockIdx.x;
+    const uint32_t s = set_of_tile(set_tile0, sets, t);
+    const uint32_t e0 = set_base[s] + (t - set_tile0[s]) * te;
+    const uint32_t e1 = min(e0 + te, set_base[s + 1]);
+    for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const uint32_t code = __ldg(codes + e);
+        if (code != kNoCode) atomicAdd(hist + (code & 0x7fffffffu), 1u);
+    }
+    __syncthreads();
+    uint32_t* out = M + (size_t)t * B;
+    for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) out[b] = hist[b];
+}
+
+// row_ptr[s B + b] = the count of bucket b of set s over the set's tiles.
+__global__ void msm_hist_total_kernel(const uint32_t* __restrict__ M, const uint32_t* __restrict__ set_tile0,
+                                      uint32_t sets, uint32_t B, uint32_t* __restrict__ row_ptr) {
+    const uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= (uint64_t)sets * B) return;
+    const uint32_t s = (uint32_t)(x / B), b = (uint32_t)(x % B);
+    uint32_t sum = 0;
+    for (uint32_t t = set_tile0[s]; t < set_tile0[s + 1]; t++) sum += M[(size_t)t * B + b];
+    row_ptr[x] = sum;
+}
+
+// M[t][b] := the first position of tile t's entries of bucket b (row_ptr: scanned).
+__global__ void msm_hist_offsets_kernel(uint32_t* __restrict__ M, const uint32_t* __restrict__ set_tile0,
+                                        uint32_t sets, uint32_t B, const uint32_t* __restrict__ row_ptr) {
+    const uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= (uint64_t)sets * B) return;
+    const uint32_t s = (uint32_t)(x / B), b = (uint32_t)(x % B);
+    uint32_t base = row_ptr[x];
+    for (uint32_t t = set_tile0[s]; t < set_tile0[s + 1]; t++) {
+        const uint32_t v = M[(size_t)t * B + b];
+        M[(size_t)t * B + b] = base;
+        base += v;
+    }
+}
+
+__global__ void __launch_bounds__(kTiledThreads) msm_scatter_tiles_kernel(const uint32_t* __restrict__ codes,
+                                                                          const uint32_t* __restrict__ set_base,
+                                                                          const uint32_t* __restrict__ set_tile0,
+                                                                          uint32_t te, MsmShape sh,
+                                                                          const MsmInst* __restrict__ insts,
+                                                                          const uint32_t* __restrict__ M,
+                                                                          uint32_t* __restrict__ entries) {
+    extern __shared__ uint32_t cursor[];
+    const uint32_t t = blockIdx.x;
+    const uint32_t s = set_of_tile(set_tile0, sh.sets, t);
+    const uint32_t sb = set_base[s];
+    const uint32_t e0 = sb + (t - set_tile0[s]) * te;
+    const uint32_t e1 = min(e0 + te, set_base[s + 1]);
+    const uint32_t* in = M + (size_t)t * sh.B;
+    for (uint32_t b = threadIdx.x; b < sh.B; b += blockDim.x) cursor[b] = in[b];
+    const uint32_t k = s / sh.Wr;
+    const uint32_t nk = insts[k].n, stride = insts[k].stride;
+    __syncthreads();
+    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const uint32_t code = __ldg(codes + e);
+        if (code == kNoCode) continue;
+        const uint32_t idx = e - sb;
+        // fixed-base: row w of the shifted bases; GLV: the phi(P) half for h = 1
+        const uint32_t point = sh.shared ? (idx / nk) * stride + idx % nk
+                                         : (sh.glv ? (idx >> 1) + (idx & 1) * stride : idx);
+        const uint32_t pos = atomicAdd(cursor + (code & 0x7fffffffu), 1u);
+        entries[pos] = point | (code & 0x80000000u);
+    }
+}
+
 // ---- 4. accumulation ------------------------------------------------------------
 // Emit the accumulated sum of `key` over entry range [e0, e1): final if the bucket
 // lies inside the range, else into the unit's first (bucket began earlier) or last
@@ -985,6 +1126,11 @@ struct MsmPipeT {
     uint32_t *long_list = nullptr, *long_count = nullptr;  // fixup mode
     P *buckets = nullptr, *Yb = nullptr, *Eb = nullptr, *Y2 = nullptr, *E2 = nullptr, *F2 = nullptr, *tgt = nullptr;
     P* tgt_parts = nullptr;  // per-part target sums before the merge (null with one part)
+    // tiled CSR sort (B <= kTiledMaxB): set positions, tiles and per-tile bucket counts
+    bool tiled = false;
+    uint32_t te = 0, tiles = 0;
+    std::vector<uint32_t> set_base_h, set_tile0_h;  // sets + 1 entries each
+    uint32_t *set_base = nullptr, *set_tile0 = nullptr, *tile_hist = nullptr;
     P* h_tgt = nullptr;  // host copy of the per-set targets (sets * targets)
     uint32_t* h_total = nullptr;
     size_t host_elems() const { return (size_t)sh.sets * sh.targets; }
@@ -1037,6 +1183,32 @@ static int pipe_init(MsmPipeT<C>& p, uint32_t c, bool fixed, bool glv, const std
     while (g2 > 2 && p.nbuckets / g / g2 < min_threads / 2) g2 /= 2;
     shape_blocks(p.sh, g, g2);
     p.units = (uint32_t)((p.max_entries + p.sh.seg - 1) / p.sh.seg);
+    // tiled sort when a set's counters fit shared memory: set s = k Wr + w holds n_k halves
+    // entries per window (n_k W in the fixed-base mode's one set), cut into tiles of at least
+    // max(8192, 2B) entries (per-tile counters: at most twice the entry count in bytes) and
+    // at most 64 tiles per set
+    p.tiled = p.sh.B <= kTiledMaxB;
+    if (p.tiled) {
+        const uint32_t halves = glv ? 2u : 1u;
+        uint64_t largest = 0;
+        for (const MsmInst& mi : jobs) largest = std::max<uint64_t>(largest, (uint64_t)mi.n * (fixed ? p.sh.W : halves));
+        p.te = (uint32_t)std::max<uint64_t>(std::max<uint64_t>(8192u, 2ull * p.sh.B), ((largest + 63) / 64 + 1023) & ~1023ull);
+        p.set_base_h.assign(p.sh.sets + 1, 0);
+        p.set_tile0_h.assign(p.sh.sets + 1, 0);
+        uint64_t pos = 0, tiles = 0;
+        for (uint32_t k = 0; k < p.sh.inst; k++)
+            for (uint32_t w = 0; w < p.sh.Wr; w++) {
+                const uint64_t size = (uint64_t)jobs[k].n * (fixed ? p.sh.W : halves);
+                p.set_base_h[k * p.sh.Wr + w] = (uint32_t)pos;
+                p.set_tile0_h[k * p.sh.Wr + w] = (uint32_t)tiles;
+                pos += size;
+                tiles += (size + p.te - 1) / p.te;
+            }
+        ZK_CHECK_ARG(pos == p.max_entries && tiles < (1ull << 31), "MSM sort layout");
+        p.set_base_h[p.sh.sets] = (uint32_t)pos;
+        p.set_tile0_h[p.sh.sets] = (uint32_t)tiles;
+        p.tiles = (uint32_t)tiles;
+    }
     return ZK_OK;
 }
 
@@ -1077,26 +1249,53 @@ static size_t pipe_layout(MsmPipeT<C>& p, char* base) {
     p.tgt = reinterpret_cast<P*>(take(p.host_elems() * sizeof(P)));
     const uint32_t parts = target_parts<C>(sh);
     p.tgt_parts = parts > 1 ? reinterpret_cast<P*>(take(p.host_elems() * parts * sizeof(P))) : nullptr;
+    if (p.tiled) {
+        p.set_base = reinterpret_cast<uint32_t*>(take(p.set_base_h.size() * 4));
+        p.set_tile0 = reinterpret_cast<uint32_t*>(take(p.set_tile0_h.size() * 4));
+        p.tile_hist = reinterpret_cast<uint32_t*>(take((size_t)p.tiles * sh.B * 4));
+    }
     return off;
 }
 
-// Enqueue the device part of a pipeline on the context stream, ending with the copies of
-// the targets and the entry count to p.h_tgt / p.h_total. Allocates nothing, so it can be
-// captured into a CUDA graph (the instance descriptors are uploaded only if `upload`).
+// Dynamic shared memory of the tiled sort kernels (set once per device).
+static int set_sort_smem_attr(int device) {
+    static std::mutex mu;
+    static bool done[64] = {};
+    ZK_CHECK_ARG(device >= 0 && device < 64, "device index out of range");
+    std::lock_guard<std::mutex> g(mu);
+    if (!done[device]) {
+        ZK_TRY_CUDA(cudaFuncSetAttribute(msm_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledMaxB * 4));
+        ZK_TRY_CUDA(cudaFuncSetAttribute(msm_scatter_tiles_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kTiledMaxB * 4));
+        done[device] = true;
+    }
+    return ZK_OK;
+}
+
+// The pipeline's descriptors to the device: instances, scalar offsets, sort layout.
 template <class C>
-static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
-    using P = typename C::P;
+static int pipe_upload(Ctx* c, MsmPipeT<C>& p) {
+    cudaStream_t st = c->stream;
+    ZK_TRY_CUDA(cudaMemcpyAsync(p.d_inst, p.inst.data(), p.inst.size() * sizeof(MsmInst), cudaMemcpyHostToDevice, st));
+    ZK_TRY_CUDA(cudaMemcpyAsync(p.d_offs, p.offs.data(), p.offs.size() * 4, cudaMemcpyHostToDevice, st));
+    if (p.tiled) {
+        ZK_TRY_CUDA(cudaMemcpyAsync(p.set_base, p.set_base_h.data(), p.set_base_h.size() * 4, cudaMemcpyHostToDevice,
+                                    st));
+        ZK_TRY_CUDA(cudaMemcpyAsync(p.set_tile0, p.set_tile0_h.data(), p.set_tile0_h.size() * 4,
+                                    cudaMemcpyHostToDevice, st));
+    }
+    return ZK_OK;
+}
+
+// The CSR sort with global atomics (bucket sets larger than shared memory): digits and a
+// warp-aggregated histogram, the scan, then the digits again and a scatter through cursors.
+template <class C>
+static int enqueue_atomic_sort(Ctx* c, MsmPipeT<C>& p, int scalars_mont) {
     cudaStream_t st = c->stream;
     const MsmShape& sh = p.sh;
-    if (upload) {
-        ZK_TRY_CUDA(cudaMemcpyAsync(p.d_inst, p.inst.data(), p.inst.size() * sizeof(MsmInst),
-                                    cudaMemcpyHostToDevice, st));
-        ZK_TRY_CUDA(cudaMemcpyAsync(p.d_offs, p.offs.data(), p.offs.size() * 4, cudaMemcpyHostToDevice, st));
-    }
-    ZK_TRY_CUDA(cudaMemsetAsync(p.row_ptr, 0, (p.nbuckets + 1) * 4, st));
-    ZK_TRY_CUDA(cudaMemsetAsync(p.buckets, 0, p.nbuckets * sizeof(P), st));
     const uint32_t N = (uint32_t)p.N;
     const unsigned nblk = (unsigned)((p.N + 255) / 256);
+    ZK_TRY_CUDA(cudaMemsetAsync(p.row_ptr, 0, (p.nbuckets + 1) * 4, st));
     if (!c->scalar_chunks.empty() && c->scalar_chunks.back().first == N && p.inst.size() == 1) {
         // scalars still arriving: each chunk's digits wait for its copy only
         uint32_t j0 = 0;
@@ -1123,6 +1322,73 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
     ZK_LAUNCH(c, "msm_scatter", msm_scatter_kernel, nblk, 256, 0, reinterpret_cast<const fe*>(p.digits), p.d_inst,
               p.d_offs, N, sh, p.cursor, p.entries);
     ZK_TRY_CUDA(cudaGetLastError());
+    return ZK_OK;
+}
+
+// The tiled CSR sort of a pipeline (codes, per-tile counts, totals, scan, offsets, scatter).
+template <class C>
+static int enqueue_tiled_sort(Ctx* c, MsmPipeT<C>& p, int scalars_mont) {
+    cudaStream_t st = c->stream;
+    const MsmShape& sh = p.sh;
+    const uint32_t N = (uint32_t)p.N;
+    int rc = set_sort_smem_attr(c->device);
+    if (rc != ZK_OK) return rc;
+    uint32_t* codes = p.digits;
+    if (!c->scalar_chunks.empty() && c->scalar_chunks.back().first == N && p.inst.size() == 1) {
+        // scalars still arriving: each chunk's codes wait for its copy only
+        uint32_t j0 = 0;
+        for (const auto& ch : c->scalar_chunks) {
+            ZK_TRY_CUDA(cudaStreamWaitEvent(st, ch.second, 0));
+            ZK_LAUNCH(c, "msm_codes", msm_codes_kernel<C>, (unsigned)((ch.first - j0 + 255) / 256), 256, 0, p.d_inst,
+                      p.d_offs, j0, ch.first, scalars_mont, sh, p.set_base, codes);
+            ZK_TRY_CUDA(cudaGetLastError());
+            j0 = ch.first;
+        }
+    } else {
+        if (!c->scalar_chunks.empty()) ZK_TRY_CUDA(cudaStreamWaitEvent(st, c->scalar_chunks.back().second, 0));
+        ZK_LAUNCH(c, "msm_codes", msm_codes_kernel<C>, (unsigned)((p.N + 255) / 256), 256, 0, p.d_inst, p.d_offs, 0u,
+                  N, scalars_mont, sh, p.set_base, codes);
+        ZK_TRY_CUDA(cudaGetLastError());
+    }
+    const size_t smem = (size_t)sh.B * 4;
+    ZK_LAUNCH(c, "msm_hist", msm_hist_kernel, p.tiles, kTiledThreads, smem, codes, p.set_base, p.set_tile0, sh.sets,
+              p.te, sh.B, p.tile_hist);
+    ZK_TRY_CUDA(cudaGetLastError());
+    const unsigned nb = (unsigned)((p.nbuckets + 255) / 256);
+    ZK_LAUNCH(c, "msm_hist_total", msm_hist_total_kernel, nb, 256, 0, p.tile_hist, p.set_tile0, sh.sets, sh.B,
+              p.row_ptr);
+    ZK_TRY_CUDA(cudaGetLastError());
+    // row_ptr[0..nbuckets) := exclusive scan; row_ptr[nbuckets] := total
+    rc = device_exclusive_scan(c, p.row_ptr, p.nbuckets, p.row_ptr + p.nbuckets, p.scan_tmp);
+    if (rc != ZK_OK) return rc;
+    ZK_LAUNCH(c, "msm_hist_offsets", msm_hist_offsets_kernel, nb, 256, 0, p.tile_hist, p.set_tile0, sh.sets, sh.B,
+              p.row_ptr);
+    ZK_TRY_CUDA(cudaGetLastError());
+    ZK_LAUNCH(c, "msm_scatter_tiles", msm_scatter_tiles_kernel, p.tiles, kTiledThreads, smem, codes, p.set_base,
+              p.set_tile0, p.te, sh, p.d_inst, p.tile_hist, p.entries);
+    ZK_TRY_CUDA(cudaGetLastError());
+    return ZK_OK;
+}
+
+// Enqueue the device part of a pipeline on the context stream, ending with the copies of
+// the targets and the entry count to p.h_tgt / p.h_total. Allocates nothing, so it can be
+// captured into a CUDA graph (the instance descriptors are uploaded only if `upload`).
+template <class C>
+static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
+    using P = typename C::P;
+    cudaStream_t st = c->stream;
+    const MsmShape& sh = p.sh;
+    if (upload) {
+        int rc = pipe_upload(c, p);
+        if (rc != ZK_OK) return rc;
+    }
+    ZK_TRY_CUDA(cudaMemsetAsync(p.buckets, 0, p.nbuckets * sizeof(P), st));
+    const uint32_t N = (uint32_t)p.N;
+    const unsigned nblk = (unsigned)((p.N + 255) / 256);
+    {
+        int rc = p.tiled ? enqueue_tiled_sort<C>(c, p, scalars_mont) : enqueue_atomic_sort<C>(c, p, scalars_mont);
+        if (rc != ZK_OK) return rc;
+    }
 
     // accumulation rounds (the first kernel that reads the points)
     if (c->bases_wait != nullptr) ZK_TRY_CUDA(cudaStreamWaitEvent(st, c->bases_wait, 0));
@@ -1398,6 +1664,8 @@ static int build_pipes(Ctx* c, const MsmJob* jobs, size_t count, uint32_t window
             if (part.empty()) return ZK_OK;
             out->emplace_back();
             int rc = pipe_init<C>(out->back(), cb, fixed, glv, part, idx, c->num_sms);
+            // the sort kernels' shared-memory limit, set here and not inside a graph capture
+            if (rc == ZK_OK && out->back().tiled) rc = set_sort_smem_attr(c->device);
             out->back().skip_inf = part_inf;
             part.clear();
             idx.clear();
@@ -1735,13 +2003,8 @@ int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, 
         hp += p.host_elems() * sizeof(xyzz_t);
         p.h_total = reinterpret_cast<uint32_t*>(hp);
         hp += 16;
-        cudaError_t e1 = cudaMemcpyAsync(p.d_inst, p.inst.data(), p.inst.size() * sizeof(MsmInst),
-                                         cudaMemcpyHostToDevice, c->stream);
-        cudaError_t e2 = cudaMemcpyAsync(p.d_offs, p.offs.data(), p.offs.size() * 4, cudaMemcpyHostToDevice, c->stream);
-        if (e1 != cudaSuccess || e2 != cudaSuccess) {
-            set_error(std::string("plan descriptor upload: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
-            return fail(ZK_ECUDA);
-        }
+        const int urc = pipe_upload(c, p);
+        if (urc != ZK_OK) return fail(urc);
     }
     cudaError_t se = cudaStreamSynchronize(c->stream);
     if (se != cudaSuccess) {
