@@ -19,6 +19,7 @@
 // its loads are contiguous), the powers of omega_m and u carried from the thread's first
 // point (computed by square-and-multiply) in steps of omega_m^32 and u^32.
 #include <cstring>
+#include <vector>
 
 #include "zk_internal.cuh"
 
@@ -68,15 +69,6 @@ __global__ void fr_batch_inv_kernel(fe* __restrict__ out, const fe* __restrict__
 // The quotient kernel holds ~23 products per element: Fr with the non-inlined product
 using FrQ = FrCallP;
 
-__device__ __forceinline__ fe fr_pow_q(fe base, uint64_t e) {
-    fe acc = fe_one<FrQ>();
-    for (; e; e >>= 1) {
-        if (e & 1) acc = fe_mul<FrQ>(acc, base);
-        base = fe_mul<FrQ>(base, base);
-    }
-    return acc;
-}
-
 struct QuotientIn {
     const fe* v[15];  // a b c z pi ql qr qm qo qc s1 s2 s3 zshift l1 (Montgomery)
 };
@@ -86,16 +78,27 @@ struct QuotientK {  // Montgomery constants
     fe omega_step, u_step;  // omega_m^32, u^32: a lane's step
 };
 
-__global__ void plonk_quotient_kernel(QuotientIn in, QuotientK K, size_t m, fe* __restrict__ num,
-                                      fe* __restrict__ zh) {
+// Starting powers of a lane, from tables (Montgomery): with i0 = 512 g + l (warp g, lane l),
+// v^i0 = v^l * v^(512 (g mod 64)) * v^(32768 (g / 64)) for v = omega_m and v = u:
+//   pw[l], pw[32 + l]              omega_m^l, u^l                        (l < 32)
+//   pw[64 + j], pw[128 + j]        omega_m^(512 j), u^(512 j)           (j < 64)
+//   pw[192 + h], pw[192 + H + h]   omega_m^(32768 h), u^(32768 h)       (h < H)
+// 4 products per thread instead of ~2 log2(i0) by square-and-multiply for each of the two.
+static constexpr uint32_t kQWarpPoints = 32 * kQChunk;
+
+__global__ void plonk_quotient_kernel(QuotientIn in, QuotientK K, size_t m, const fe* __restrict__ pw, uint32_t H,
+                                      fe* __restrict__ num, fe* __restrict__ zh) {
     // a warp covers 32 * kQChunk consecutive points, lane l the points base + l + 32 k (each
     // load of the warp reads 32 consecutive elements)
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t lane = t & 31;
     const size_t i0 = (t - lane) * kQChunk + lane;
     if (i0 >= m) return;
-    fe x = fe_mul<FrQ>(K.shift, fr_pow_q(K.omega_m, i0));
-    fe un = fr_pow_q(K.u, i0);
+    const size_t g = i0 / kQWarpPoints;
+    const uint32_t glo = (uint32_t)(g & 63), ghi = (uint32_t)(g >> 6);
+    fe x = fe_mul<FrQ>(fe_mul<FrQ>(fe_ldg(pw + lane), fe_ldg(pw + 64 + glo)), fe_ldg(pw + 192 + ghi));
+    x = fe_mul<FrQ>(K.shift, x);
+    fe un = fe_mul<FrQ>(fe_mul<FrQ>(fe_ldg(pw + 32 + lane), fe_ldg(pw + 128 + glo)), fe_ldg(pw + 192 + H + ghi));
     for (size_t i = i0, k = 0; k < kQChunk && i < m; k++, i += 32) {
         const fe a = fe_ldg(in.v[0] + i), b = fe_ldg(in.v[1] + i), c = fe_ldg(in.v[2] + i);
         const fe z = fe_ldg(in.v[3] + i);
@@ -218,10 +221,39 @@ int zk_plonk_quotient_evals(zk_ctx* ctx, const void* const* inputs, size_t m, ui
     K.omega_step = zk::mont_of(zkh::pow_u64(F, zkh::to_mont(F, om), 32));
     K.u_step = zk::mont_of(zkh::pow_u64(F, zkh::pow_u64(F, zkh::to_mont(F, om), n), 32));
     zk::Ctx* c = &ctx->impl;
+    // the starting-power tables of the kernel (see plonk_quotient_kernel)
+    const uint64_t warps = (m + zk::kQWarpPoints - 1) / zk::kQWarpPoints;
+    const uint32_t H = (uint32_t)((warps + 63) / 64);
+    std::vector<zkh::F4> pw(192 + 2 * (size_t)H);
+    const zkh::F4 om_m = zkh::to_mont(F, om);
+    const zkh::F4 u_m = zkh::pow_u64(F, om_m, n);
+    struct Run {
+        size_t at;
+        zkh::F4 base;
+        size_t count;
+    };
+    const Run runs[6] = {{0, om_m, 32},
+                         {32, u_m, 32},
+                         {64, zkh::pow_u64(F, om_m, zk::kQWarpPoints), 64},
+                         {128, zkh::pow_u64(F, u_m, zk::kQWarpPoints), 64},
+                         {192, zkh::pow_u64(F, om_m, 64ull * zk::kQWarpPoints), H},
+                         {192 + (size_t)H, zkh::pow_u64(F, u_m, 64ull * zk::kQWarpPoints), H}};
+    for (const Run& r : runs) {
+        zkh::F4 cur = zkh::one(F);
+        for (size_t i = 0; i < r.count; i++) {
+            pw[r.at + i] = cur;
+            cur = zkh::mul(F, cur, r.base);
+        }
+    }
+    void* d_pw = nullptr;
+    int rc = zk::scratch_alloc(c, pw.size() * 32, &d_pw);
+    if (rc != ZK_OK) return rc;
+    ZK_TRY_CUDA(cudaMemcpyAsync(d_pw, pw.data(), pw.size() * 32, cudaMemcpyHostToDevice, c->stream));
     const size_t chunks = (m + zk::kQChunk - 1) / zk::kQChunk;
     ZK_LAUNCH(c, "plonk_quotient", zk::plonk_quotient_kernel, (unsigned)((chunks + 127) / 128), 128, 0, in, K, m,
-              static_cast<fe*>(num_out), static_cast<fe*>(zh_out));
+              static_cast<const fe*>(d_pw), H, static_cast<fe*>(num_out), static_cast<fe*>(zh_out));
     ZK_TRY_CUDA(cudaGetLastError());
+    zk::scratch_free(c, d_pw);
     return ZK_OK;
 }
 

@@ -397,3 +397,21 @@ def test_plonk_t_quotient_evals_op_matches_reference_golden():
         for i, v in rec["num_at"].items():
             assert num[int(i)] == int(v, 16), (m, i)
         assert t == [x * pow(z, FR - 2, FR) % FR if z else 0 for x, z in zip(num, zh)]
+
+
+def test_plonk_t_quotient_evals_many_warps_every_element():
+    """The quotient op past one warp table row: m = 70000 points (137 warps of 512 points, so
+    the starting powers use warp-table indices up to 136 = 2 * 64 + 8) and a ragged last warp,
+    every element against the oracle's restatement of _plonk_t_quotient_evals
+    (runtime/kernels/cpu/kernels.py:607-693), itself pinned to the reference's outputs."""
+    exe, _ = _exe()
+    m, n = 70000, 1 << 14
+    omega_m = O.omega_for_size(1 << 17)
+    attrs = {"n": n, "m": m, "omega_m": omega_m, "shift": 5, "shift_n": pow(5, n, FR), "alpha": 0x1234567,
+             "beta": 0xABCDEF, "gamma": 0x7654321, "k1": 7, "k2": 13}
+    vecs = [synth.limbs_to_ints(synth.fr_uniform(9700 + j, m)) for j in range(15)]
+    num, zh, _ = _plonk_quotient_graph(vecs, attrs, exe)
+    e_num, e_zh = O.plonk_t_quotient_evals(vecs, n, omega_m, 5, attrs["shift_n"], attrs["alpha"], attrs["beta"],
+                                           attrs["gamma"], 7, 13)
+    assert zh == e_zh
+    assert num == e_num
