@@ -524,6 +524,7 @@ __global__ void msm_scatter_kernel(const fe* __restrict__ reduced, const MsmInst
 static constexpr uint32_t kNoCode = 0xffffffffu;
 static constexpr uint32_t kTiledMaxB = 1u << 15;  // 128 KB of shared-memory counters
 static constexpr uint32_t kTiledThreads = 1024;
+static constexpr uint32_t kSortBatch = 8;  // codes loaded per thread before they are counted / placed
 
 template <class C>
 __global__ void msm_codes_kernel(const MsmInst* __restrict__ insts, const uint32_t* __restrict__ offs, uint32_t j0,
@@ -585,9 +586,17 @@ __global__ void __launch_bounds__(kTiledThreads) msm_hist_kernel(const uint32_t*
     const uint32_t e1 = min(e0 + te, set_base[s + 1]);
     for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) hist[b] = 0;
     __syncthreads();
-    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const uint32_t code = __ldg(codes + e);
-        if (code != kNoCode) atomicAdd(hist + (code & 0x7fffffffu), 1u);
+    // kSortBatch codes in flight per thread before their counters are bumped
+    for (uint32_t base = e0 + threadIdx.x; base < e1; base += blockDim.x * kSortBatch) {
+        uint32_t code[kSortBatch];
+#pragma unroll
+        for (uint32_t q = 0; q < kSortBatch; q++) {
+            const uint32_t e = base + q * blockDim.x;
+            code[q] = e < e1 ? __ldg(codes + e) : kNoCode;
+        }
+#pragma unroll
+        for (uint32_t q = 0; q < kSortBatch; q++)
+            if (code[q] != kNoCode) atomicAdd(hist + (code[q] & 0x7fffffffu), 1u);
     }
     __syncthreads();
     uint32_t* out = M + (size_t)t * B;
@@ -633,19 +642,27 @@ __global__ void __launch_bounds__(kTiledThreads) msm_scatter_tiles_kernel(const 
     const uint32_t e0 = sb + (t - set_tile0[s]) * te;
     const uint32_t e1 = min(e0 + te, set_base[s + 1]);
     const uint32_t* in = M + (size_t)t * sh.B;
-    for (uint32_t b = threadIdx.x; b < sh.B; b += blockDim.x) cursor[b] = in[b];
+    for (uint32_t b = threadIdx.x; b < sh.B; b += blockDim.x) cursor[b] = __ldcs(in + b);
     const uint32_t k = s / sh.Wr;
     const uint32_t nk = insts[k].n, stride = insts[k].stride;
     __syncthreads();
-    for (uint32_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-        const uint32_t code = __ldg(codes + e);
-        if (code == kNoCode) continue;
-        const uint32_t idx = e - sb;
-        // fixed-base: row w of the shifted bases; GLV: the phi(P) half for h = 1
-        const uint32_t point = sh.shared ? (idx / nk) * stride + idx % nk
-                                         : (sh.glv ? (idx >> 1) + (idx & 1) * stride : idx);
-        const uint32_t pos = atomicAdd(cursor + (code & 0x7fffffffu), 1u);
-        entries[pos] = point | (code & 0x80000000u);
+    for (uint32_t base = e0 + threadIdx.x; base < e1; base += blockDim.x * kSortBatch) {
+        uint32_t code[kSortBatch];
+#pragma unroll
+        for (uint32_t q = 0; q < kSortBatch; q++) {  // the codes' last use: streamed, evict first
+            const uint32_t e = base + q * blockDim.x;
+            code[q] = e < e1 ? __ldcs(codes + e) : kNoCode;
+        }
+#pragma unroll
+        for (uint32_t q = 0; q < kSortBatch; q++) {
+            if (code[q] == kNoCode) continue;
+            const uint32_t idx = base + q * blockDim.x - sb;
+            // fixed-base: row w of the shifted bases; GLV: the phi(P) half for h = 1
+            const uint32_t point = sh.shared ? (idx / nk) * stride + idx % nk
+                                             : (sh.glv ? (idx >> 1) + (idx & 1) * stride : idx);
+            const uint32_t pos = atomicAdd(cursor + (code[q] & 0x7fffffffu), 1u);
+            entries[pos] = point | (code[q] & 0x80000000u);
+        }
     }
 }
 
