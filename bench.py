@@ -743,6 +743,30 @@ def run_gpu_batch(ctx, args, flush, count: int = 64, lo: int = 10, hi: int = 20)
     t_plan = timed(plan.run)
     plan_launches = plan.launches()
     plan.free()
+    # the work-queue form: the sorts, then every pipeline's later stages in one launch
+    qplan = ctx.msm_plan(bases, msm_sizes, use_graph=True, queue=True)
+    for j, m in enumerate(msm_sizes):
+        ctx.d2d(qplan.slot(j), N.DeviceArray(ctx, m * 32, ptr=ptrs[j], owned=False), m * 32)
+    got_queue = qplan.run()
+    t_queue = timed(qplan.run)
+    queue_launches = qplan.launches()
+    qplan.free()
+    # small instances only (2^10..2^14), where launch latency weighs most
+    small_sizes = [int(round(2 ** u)) for u in rng.uniform(lo, 14, size=count)]
+    small = {"points": sum(small_sizes)}
+    small_src = ctx.to_device(synth.fr_uniform(seed + 2, max(small_sizes)))
+    ctx.fr_to_mont(small_src, small_src, max(small_sizes))
+    small_ref = None
+    for name, q in (("plan_graph", False), ("plan_graph_queue", True)):
+        sp = ctx.msm_plan(bases, small_sizes, use_graph=True, queue=q)
+        for j, m in enumerate(small_sizes):
+            ctx.d2d(sp.slot(j), small_src, m * 32)
+        r = sp.run()
+        small[name + "_ms"] = round(timed(sp.run), 4)
+        small[name + "_kernels"] = sp.launches()
+        small_ref = small_ref or r
+        small["bit_exact"] = small.get("bit_exact", True) and r == small_ref
+        sp.free()
     # autotuned windows for every size class of the batch (best of c in rule +- 2)
     t0 = time.perf_counter()
     tuned = {}
@@ -759,14 +783,17 @@ def run_gpu_batch(ctx, args, flush, count: int = 64, lo: int = 10, hi: int = 20)
     plan.free()
     out["msm"] = {
         "plain_ms": round(t_plain, 3), "batch_ms": round(t_batch, 3), "plan_graph_ms": round(t_plan, 3),
-        "plan_graph_tuned_ms": round(t_tuned, 3),
+        "plan_graph_tuned_ms": round(t_tuned, 3), "plan_graph_queue_ms": round(t_queue, 3),
         "plain_Mpts_s": round(total / (t_plain * 1e-3) / 1e6, 2),
         "batch_Mpts_s": round(total / (t_batch * 1e-3) / 1e6, 2),
         "plan_graph_Mpts_s": round(total / (t_plan * 1e-3) / 1e6, 2),
         "plan_graph_tuned_Mpts_s": round(total / (t_tuned * 1e-3) / 1e6, 2),
-        "graph_kernels": plan_launches, "tuned_windows": {f"2^{k}": v for k, v in tuned.items()},
+        "plan_graph_queue_Mpts_s": round(total / (t_queue * 1e-3) / 1e6, 2),
+        "graph_kernels": plan_launches, "queue_graph_kernels": queue_launches,
+        "tuned_windows": {f"2^{k}": v for k, v in tuned.items()},
         "autotune_s": round(tune_s, 2),
-        "bit_exact_vs_plain": got == ref and got_plan == ref and got_tuned == ref,
+        "bit_exact_vs_plain": got == ref and got_plan == ref and got_tuned == ref and got_queue == ref,
+        "small_2_10_to_2_14": small,
     }
     for lg in tuned:
         ctx.tune_set_msm_window(lg, 0)

@@ -427,15 +427,36 @@ int zk_batch_wait(zk_batch *batch, int timeout_ms);
 int zk_batch_destroy(zk_batch *batch);
 
 /*
+ * Work-queue form of MSM batches (north_star's "(instance, window, bucket-range) items";
+ * no reference counterpart): after each pipeline's CSR sort, ONE persistent launch runs
+ * every pipeline's later stages -- the accumulation over (instance set, window, bucket
+ * range) units, the straddling-piece fixup or merge rounds, the two levels of the window
+ * reduction and the per-window target sums -- as items of a device queue, each waiting
+ * (bounded, 2 s) until its pipeline's previous stage has published all its items.
+ *   zk_msm_batch_set_queue   on != 0: zk_msm_g1_batch / zk_msm_g2_batch and their
+ *                            asynchronous forms on this context use it (default off).
+ *   zk_msm_queue_test_limit  for tests of the bound: the next work-queue launch of this
+ *                            context gets a wait limit of limit_us (1..10^7 us) and its first
+ *                            waiting item waits for one item more than exist, so the launch
+ *                            stops early and that call returns ZK_ETIMEOUT (the context stays
+ *                            usable; the setting is used once).
+ */
+int zk_msm_batch_set_queue(zk_ctx *ctx, int on);
+int zk_msm_queue_test_limit(zk_ctx *ctx, uint64_t limit_us);
+
+/*
  * Batch plan: a zk_msm_g1_batch with fixed shapes, prepared once and run many times
  * (serving, repeated commitments). The plan owns one scalar slot per instance
  * (zk_msm_plan_scalars: device address of sizes[k] elements, filled by the caller by
  * zk_h2d or by a kernel such as zk_ntt writing into it), all scratch and pinned result
- * buffers, so a run allocates nothing. With use_graph = 1 the device work of a run is
- * captured once as a CUDA graph and each run is one graph launch. The bases handles
- * must outlive the plan. No reference counterpart (the reference rebuilds its batch per
- * call).
+ * buffers, so a run allocates nothing. flags (the use_graph argument): ZK_MSM_PLAN_GRAPH
+ * (1) captures the device work of a run once as a CUDA graph, each run then one graph
+ * launch; ZK_MSM_PLAN_QUEUE (2) runs the plan in the work-queue form above (a run whose
+ * queue gave up returns ZK_ETIMEOUT). The bases handles must outlive the plan. No
+ * reference counterpart (the reference rebuilds its batch per call).
  */
+#define ZK_MSM_PLAN_GRAPH 1
+#define ZK_MSM_PLAN_QUEUE 2
 typedef struct zk_msm_plan zk_msm_plan;
 int zk_msm_plan_create(zk_ctx *ctx, size_t count, const zk_bases *const *bases, const uint64_t *offsets,
                        const uint64_t *sizes, int scalars_mont, uint32_t window_bits, int use_graph,

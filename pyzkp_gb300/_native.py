@@ -21,6 +21,7 @@ LIB_PATH = os.environ.get("ZKGPU_LIB") or os.path.join(HERE, "_lib", "libzkgpu.s
 ZK_OK, ZK_EINVAL, ZK_ECUDA, ZK_ENOMEM, ZK_ENODEV, ZK_ETIMEOUT = 0, 1, 2, 3, 4, 5
 
 NTT_PLAN_GRAPH, NTT_PLAN_QUEUE = 1, 2
+MSM_PLAN_GRAPH, MSM_PLAN_QUEUE = 1, 2
 
 NTT_EVALS_FROM_COEFFS = 0
 NTT_COEFFS_FROM_EVALS = 1
@@ -45,7 +46,8 @@ EXPORTED_SYMBOLS = (
     "zk_host_g1_add", "zk_host_g2_mul", "zk_host_g2_add", "zk_fr_add", "zk_bases_g2_create_dev", "zk_fr_batch_inv",
     "zk_plonk_quotient_evals", "zk_ctx_create_prio", "zk_stream_priority_range", "zk_h2d_async", "zk_d2h_async",
     "zk_fence_record", "zk_fence_wait", "zk_fence_destroy", "zk_fr_r1cs_check_async",
-    "zk_ntt_batch_set_queue", "zk_ntt_queue_status", "zk_ntt_queue_selftest",
+    "zk_ntt_batch_set_queue", "zk_ntt_queue_status", "zk_ntt_queue_selftest", "zk_msm_batch_set_queue",
+    "zk_msm_queue_test_limit",
 )
 
 _lib: Optional[ctypes.CDLL] = None
@@ -122,6 +124,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_ntt_plan_create": ([P, S, P, PP, PP, P, P, P, P, I, PP], I),
             "zk_ntt_plan_run": ([P], I),
             "zk_ntt_batch_set_queue": ([P, I], I),
+            "zk_msm_batch_set_queue": ([P, I], I),
+            "zk_msm_queue_test_limit": ([P, ctypes.c_uint64], I),
             "zk_ntt_queue_status": ([P], I),
             "zk_ntt_queue_selftest": ([P, ctypes.c_uint64, ctypes.POINTER(U32)], I),
             "zk_ntt_plan_launches": ([P, ctypes.POINTER(ctypes.c_uint64)], I),
@@ -768,7 +772,8 @@ class Context:
         return _points_from(out[:count], inf[:count])
 
     def msm_plan(self, bases, sizes, *, offsets=None, scalars_mont: bool = True, window_bits: int = 0,
-                 use_graph: bool = True) -> "MsmPlan":
+                 use_graph: bool = True, queue: bool = False) -> "MsmPlan":
+        """A prepared G1 batch; ``queue``: its work-queue form (sorts, then one persistent launch)."""
         count = len(sizes)
         if isinstance(bases, Bases):
             bases = [bases] * count
@@ -778,7 +783,8 @@ class Context:
         h = ctypes.c_void_p()
         check(load().zk_msm_plan_create(self.handle, count, bh, None if off is None else off.ctypes.data,
                                         sz.ctypes.data, 1 if scalars_mont else 0, int(window_bits),
-                                        1 if use_graph else 0, ctypes.byref(h)), "zk_msm_plan_create")
+                                        (MSM_PLAN_GRAPH if use_graph else 0) | (MSM_PLAN_QUEUE if queue else 0),
+                                        ctypes.byref(h)), "zk_msm_plan_create")
         return MsmPlan(self, h.value, [int(x) for x in sizes], list(bases))
 
     @staticmethod
@@ -810,6 +816,15 @@ class Context:
                                         logs.ctypes.data, om.ctypes.data, sh.ctypes.data, flags,
                                         ctypes.byref(h)), "zk_ntt_plan_create")
         return NttPlan(self, h.value, [j[1] for j in jobs] + [j[2] for j in jobs])
+
+    def msm_batch_set_queue(self, on: bool) -> None:
+        """G1 MSM batches (and their asynchronous form) in the work-queue form when on."""
+        check(load().zk_msm_batch_set_queue(self.handle, 1 if on else 0), "zk_msm_batch_set_queue")
+
+    def msm_queue_test_limit(self, limit_us: int) -> None:
+        """Arms the next MSM work-queue launch with a wait that cannot succeed and this limit
+        (zk_msm_queue_test_limit): that call then raises TimeoutError."""
+        check(load().zk_msm_queue_test_limit(self.handle, int(limit_us)), "zk_msm_queue_test_limit")
 
     def ntt_batch_set_queue(self, on: bool) -> None:
         """ntt_batch in its work-queue form (one persistent launch) when on."""

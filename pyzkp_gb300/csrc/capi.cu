@@ -844,10 +844,31 @@ int zk_msm_plan_create(zk_ctx* ctx, size_t count, const zk_bases* const* bases, 
     std::vector<zk::MsmJob> jobs;
     int rc = make_jobs(count, bases, offsets, nullptr, sizes, &jobs);
     if (rc != ZK_OK) return rc;
+    if (use_graph & ~(ZK_MSM_PLAN_GRAPH | ZK_MSM_PLAN_QUEUE)) {
+        zk::set_error("unknown MSM plan flags");
+        return ZK_EINVAL;
+    }
     zk::MsmPlan* impl = nullptr;
-    rc = zk::msm_plan_create(&ctx->impl, jobs.data(), count, scalars_mont, window_bits, use_graph != 0, &impl);
+    rc = zk::msm_plan_create(&ctx->impl, jobs.data(), count, scalars_mont, window_bits,
+                             (use_graph & ZK_MSM_PLAN_GRAPH) != 0, (use_graph & ZK_MSM_PLAN_QUEUE) != 0, &impl);
     if (rc != ZK_OK) return rc;
     *out = new zk_msm_plan{ctx, impl};
+    return ZK_OK;
+}
+
+int zk_msm_batch_set_queue(zk_ctx* ctx, int on) {
+    CTX_OR_FAIL(ctx);
+    ctx->impl.msm_queue = on != 0;
+    return ZK_OK;
+}
+
+int zk_msm_queue_test_limit(zk_ctx* ctx, uint64_t limit_us) {
+    CTX_OR_FAIL(ctx);
+    if (limit_us == 0 || limit_us > 10000000ull) {
+        zk::set_error("zk_msm_queue_test_limit: limit_us must be in [1, 10^7]");
+        return ZK_EINVAL;
+    }
+    ctx->impl.msm_queue_test_limit_ns = limit_us * 1000ull;
     return ZK_OK;
 }
 

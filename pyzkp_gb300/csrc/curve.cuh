@@ -292,6 +292,27 @@ __device__ __forceinline__ XyzzT<T> xyzz_load(const XyzzT<T>* p) {
     return r;
 }
 
+// The same through L2 only (points written earlier in the same launch by other CTAs).
+__device__ __forceinline__ fe c_ldcg(const fe* p) { return fe_ldcg(p); }
+__device__ __forceinline__ fq2 c_ldcg(const fq2* p) { return {fe_ldcg(&p->c0), fe_ldcg(&p->c1)}; }
+
+template <class T>
+__device__ __forceinline__ XyzzT<T> xyzz_ldcg(const XyzzT<T>* p) {
+    XyzzT<T> r;
+    r.X = c_ldcg(&p->X);
+    r.Y = c_ldcg(&p->Y);
+    r.ZZ = c_ldcg(&p->ZZ);
+    r.ZZZ = c_ldcg(&p->ZZZ);
+    return r;
+}
+
+// xyzz_load, or xyzz_ldcg when kL2 (inputs produced in the same launch)
+template <bool kL2, class T>
+__device__ __forceinline__ XyzzT<T> xyzz_get(const XyzzT<T>* p) {
+    if constexpr (kL2) return xyzz_ldcg(p);
+    else return xyzz_load(p);
+}
+
 template <class T>
 __device__ __forceinline__ void xyzz_store(XyzzT<T>* p, const XyzzT<T>& a) {
     c_store(&p->X, a.X);

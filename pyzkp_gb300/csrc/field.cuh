@@ -1178,6 +1178,23 @@ __device__ __forceinline__ fe fe_ldg(const fe* p) {
     return r;
 }
 
+// A 32-byte element through L2 only (ld.global.cg): for data that other CTAs wrote earlier
+// in the same launch, which the non-coherent read-only path is not guaranteed to see.
+__device__ __forceinline__ fe fe_ldcg(const fe* p) {
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+    uint4 lo = __ldcg(q), hi = __ldcg(q + 1);
+    fe r;
+    r.v[0] = lo.x;
+    r.v[1] = lo.y;
+    r.v[2] = lo.z;
+    r.v[3] = lo.w;
+    r.v[4] = hi.x;
+    r.v[5] = hi.y;
+    r.v[6] = hi.z;
+    r.v[7] = hi.w;
+    return r;
+}
+
 __device__ __forceinline__ void fe_store(fe* p, const fe& a) {
     uint4* q = reinterpret_cast<uint4*>(p);
     q[0] = make_uint4(a.v[0], a.v[1], a.v[2], a.v[3]);

@@ -42,6 +42,7 @@
 #include <string>
 #include <thread>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "zk_internal.cuh"
@@ -667,6 +668,11 @@ __global__ void __launch_bounds__(kTiledThreads) msm_scatter_tiles_kernel(const 
 }
 
 // ---- 4. accumulation ------------------------------------------------------------
+// Each stage below is a device body (one thread's unit, bucket or block; or one CTA's
+// target / long bucket) called by its own kernel and by the persistent queue kernel
+// (msm_queue_kernel). kL2: the body's point inputs were written earlier in the same launch
+// (queue kernel), so they are read through L2 only.
+
 // Emit the accumulated sum of `key` over entry range [e0, e1): final if the bucket
 // lies inside the range, else into the unit's first (bucket began earlier) or last
 // (bucket continues later) slot.
@@ -703,24 +709,16 @@ __device__ __forceinline__ uint32_t bucket_of(const uint32_t* __restrict__ row_p
     return lo;
 }
 
+// Unit u: the CSR entries [u seg, (u + 1) seg) (M = total entries), bucket by bucket.
 template <class C, bool kSkipInf>
-__global__ void __launch_bounds__(128, C::kAccMinBlocks) msm_accumulate_kernel(const uint32_t* __restrict__ entries,
-                                                             const uint32_t* __restrict__ d_total,
-                                                             const uint32_t* __restrict__ row_ptr,
-                                                             const MsmInst* __restrict__ insts, MsmShape sh,
-                                                             uint32_t units, typename C::P* __restrict__ buckets,
-                                                             uint32_t* __restrict__ slot_keys,
-                                                             typename C::P* __restrict__ slot_pts,
-                                                             const uint32_t* __restrict__ inf_flag) {
+__device__ __forceinline__ void acc_unit(const uint32_t* __restrict__ entries, uint32_t M,
+                                         const uint32_t* __restrict__ row_ptr, const MsmInst* __restrict__ insts,
+                                         const MsmShape& sh, uint32_t u, typename C::P* buckets, uint32_t* slot_keys,
+                                         typename C::P* slot_pts, bool test_inf) {
     using P = typename C::P;
     using A = typename C::A;
-    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= units) return;
-    // kSkipInf: the points may hold infinity; a flag (when given) says whether they do
-    const bool test_inf = kSkipInf && (inf_flag == nullptr || *inf_flag != 0);
     slot_keys[2 * u] = kNone;
     slot_keys[2 * u + 1] = kNone;
-    const uint32_t M = *d_total;
     const uint32_t e0 = u * sh.seg;
     if (e0 >= M) return;
     const uint32_t e1 = min(e0 + sh.seg, M);
@@ -748,10 +746,54 @@ __global__ void __launch_bounds__(128, C::kAccMinBlocks) msm_accumulate_kernel(c
     emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
 }
 
+template <class C, bool kSkipInf>
+__global__ void __launch_bounds__(128, C::kAccMinBlocks) msm_accumulate_kernel(const uint32_t* __restrict__ entries,
+                                                             const uint32_t* __restrict__ d_total,
+                                                             const uint32_t* __restrict__ row_ptr,
+                                                             const MsmInst* __restrict__ insts, MsmShape sh,
+                                                             uint32_t units, typename C::P* __restrict__ buckets,
+                                                             uint32_t* __restrict__ slot_keys,
+                                                             typename C::P* __restrict__ slot_pts,
+                                                             const uint32_t* __restrict__ inf_flag) {
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= units) return;
+    // kSkipInf: the points may hold infinity; a flag (when given) says whether they do
+    const bool test_inf = kSkipInf && (inf_flag == nullptr || *inf_flag != 0);
+    acc_unit<C, kSkipInf>(entries, *d_total, row_ptr, insts, sh, u, buckets, slot_keys, slot_pts, test_inf);
+}
+
 // Round r >= 2: unit u merges the slots of units [u*group, (u+1)*group) of the previous
 // round, covering entries [u * span, (u+1) * span) (span = kSegment times the product of
 // the group sizes so far). The first merge round uses pairs: most straddling buckets
 // cross exactly one segment boundary, so that round carries nearly all the work.
+template <class C, bool kL2>
+__device__ __forceinline__ void merge_unit(const uint32_t* in_keys, const typename C::P* in_pts, uint32_t in_units,
+                                           uint32_t group, uint64_t M, const uint32_t* __restrict__ row_ptr,
+                                           uint64_t span, uint32_t u, typename C::P* buckets, uint32_t* slot_keys,
+                                           typename C::P* slot_pts) {
+    slot_keys[2 * u] = kNone;
+    slot_keys[2 * u + 1] = kNone;
+    const uint64_t e0l = (uint64_t)u * span;
+    if (e0l >= M) return;
+    const uint32_t e0 = (uint32_t)e0l;
+    const uint32_t e1 = (uint32_t)min(e0l + span, M);
+    const uint32_t s0 = 2 * u * group;
+    const uint32_t s1 = min(2 * (u + 1) * group, 2 * in_units);
+    uint32_t cur = kNone;
+    typename C::P acc = xyzz_inf<typename C::T>();
+    for (uint32_t s = s0; s < s1; s++) {
+        const uint32_t k = kL2 ? __ldcg(in_keys + s) : in_keys[s];
+        if (k == kNone) continue;
+        if (k != cur) {
+            if (cur != kNone) emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
+            cur = k;
+            acc = xyzz_inf<typename C::T>();
+        }
+        acc = xyzz_add(acc, xyzz_get<kL2>(in_pts + s));
+    }
+    if (cur != kNone) emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
+}
+
 template <class C>
 __global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_merge_kernel(const uint32_t* __restrict__ in_keys,
                                                         const typename C::P* __restrict__ in_pts, uint32_t in_units,
@@ -762,28 +804,7 @@ __global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_merge_kernel(const 
                                                         typename C::P* __restrict__ slot_pts) {
     const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= units) return;
-    slot_keys[2 * u] = kNone;
-    slot_keys[2 * u + 1] = kNone;
-    const uint64_t M = *d_total;
-    const uint64_t e0l = (uint64_t)u * span;
-    if (e0l >= M) return;
-    const uint32_t e0 = (uint32_t)e0l;
-    const uint32_t e1 = (uint32_t)min(e0l + span, M);
-    const uint32_t s0 = 2 * u * group;
-    const uint32_t s1 = min(2 * (u + 1) * group, 2 * in_units);
-    uint32_t cur = kNone;
-    typename C::P acc = xyzz_inf<typename C::T>();
-    for (uint32_t s = s0; s < s1; s++) {
-        const uint32_t k = in_keys[s];
-        if (k == kNone) continue;
-        if (k != cur) {
-            if (cur != kNone) emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
-            cur = k;
-            acc = xyzz_inf<typename C::T>();
-        }
-        acc = xyzz_add(acc, xyzz_load(in_pts + s));
-    }
-    if (cur != kNone) emit_piece(cur, acc, e0, e1, row_ptr, buckets, slot_keys, slot_pts, u);
+    merge_unit<C, false>(in_keys, in_pts, in_units, group, *d_total, row_ptr, span, u, buckets, slot_keys, slot_pts);
 }
 
 // Fixup instead of merge rounds (when buckets are short): a bucket k whose entries
@@ -799,14 +820,10 @@ static constexpr uint32_t kFixupMax = 8;
 #endif
 static constexpr uint64_t kFixupDensity = ZK_FIXUP_DENSITY;  // CSR entries per bucket up to which the fixup is used
 
-template <class C>
-__global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_fixup_kernel(const uint32_t* __restrict__ row_ptr, uint32_t nbuckets,
-                                                        uint32_t seg, const typename C::P* __restrict__ slot_pts,
-                                                        typename C::P* __restrict__ buckets,
-                                                        uint32_t* __restrict__ long_list,
-                                                        uint32_t* __restrict__ long_count) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nbuckets) return;
+template <class C, bool kL2>
+__device__ __forceinline__ void fixup_bucket(const uint32_t* __restrict__ row_ptr, uint32_t seg,
+                                             const typename C::P* slot_pts, typename C::P* buckets,
+                                             uint32_t* long_list, uint32_t* long_count, uint32_t k) {
     const uint32_t b0 = row_ptr[k], b1 = row_ptr[k + 1];
     if (b1 == b0) return;
     const uint32_t u0 = b0 / seg, u1 = (b1 - 1) / seg;
@@ -815,25 +832,33 @@ __global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_fixup_kernel(const 
         long_list[atomicAdd(long_count, 1u)] = k;
         return;
     }
-    typename C::P acc = xyzz_load(slot_pts + 2 * (size_t)u0 + 1);
-    for (uint32_t u = u0 + 1; u <= u1; u++) acc = xyzz_add(acc, xyzz_load(slot_pts + 2 * (size_t)u));
+    typename C::P acc = xyzz_get<kL2>(slot_pts + 2 * (size_t)u0 + 1);
+    for (uint32_t u = u0 + 1; u <= u1; u++) acc = xyzz_add(acc, xyzz_get<kL2>(slot_pts + 2 * (size_t)u));
     xyzz_store(buckets + k, acc);
 }
 
-// One CTA per listed bucket (grid-stride over the list): strided partial sums, then a
-// shared-memory tree.
 template <class C>
-__global__ void __launch_bounds__(C::kFixupLongThreads, C::kFixupLongMinBlocks) msm_fixup_long_kernel(const uint32_t* __restrict__ row_ptr,
-                                                                           uint32_t seg,
-                                                                           const typename C::P* __restrict__ slot_pts,
-                                                                           typename C::P* __restrict__ buckets,
-                                                                           const uint32_t* __restrict__ long_list,
-                                                                           const uint32_t* __restrict__ long_count) {
+__global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_fixup_kernel(const uint32_t* __restrict__ row_ptr, uint32_t nbuckets,
+                                                        uint32_t seg, const typename C::P* __restrict__ slot_pts,
+                                                        typename C::P* __restrict__ buckets,
+                                                        uint32_t* __restrict__ long_list,
+                                                        uint32_t* __restrict__ long_count) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nbuckets) return;
+    fixup_bucket<C, false>(row_ptr, seg, slot_pts, buckets, long_list, long_count, k);
+}
+
+// One CTA per listed bucket (items item0, item0 + stride, ...): strided partial sums, then a
+// shared-memory tree over `red` (blockDim points).
+template <class C, bool kL2>
+__device__ __forceinline__ void fixup_long_cta(const uint32_t* __restrict__ row_ptr, uint32_t seg,
+                                               const typename C::P* slot_pts, typename C::P* buckets,
+                                               const uint32_t* long_list, const uint32_t* long_count,
+                                               typename C::P* red, uint32_t item0, uint32_t stride) {
     using P = typename C::P;
-    __shared__ P red[C::kFixupLongThreads];
-    const uint32_t count = *long_count;
-    for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
-        const uint32_t k = long_list[item];
+    const uint32_t count = kL2 ? __ldcg(long_count) : *long_count;
+    for (uint32_t item = item0; item < count; item += stride) {
+        const uint32_t k = kL2 ? __ldcg(long_list + item) : long_list[item];
         const uint32_t u0 = row_ptr[k] / seg, u1 = (row_ptr[k + 1] - 1) / seg;
         // the tree spans the next power of two of the pieces (at most the CTA): a bucket of 16
         // segments takes 4 levels of serial additions, not log2(blockDim)
@@ -842,7 +867,7 @@ __global__ void __launch_bounds__(C::kFixupLongThreads, C::kFixupLongMinBlocks) 
         P acc = xyzz_inf<typename C::T>();
         if (threadIdx.x < width)
             for (uint32_t u = u0 + threadIdx.x; u <= u1; u += width)
-                acc = xyzz_add(acc, xyzz_load(slot_pts + 2 * (size_t)u + (u == u0 ? 1 : 0)));
+                acc = xyzz_add(acc, xyzz_get<kL2>(slot_pts + 2 * (size_t)u + (u == u0 ? 1 : 0)));
         red[threadIdx.x] = acc;
         __syncthreads();
         for (uint32_t off = width / 2; off > 0; off >>= 1) {
@@ -854,6 +879,17 @@ __global__ void __launch_bounds__(C::kFixupLongThreads, C::kFixupLongMinBlocks) 
     }
 }
 
+template <class C>
+__global__ void __launch_bounds__(C::kFixupLongThreads, C::kFixupLongMinBlocks) msm_fixup_long_kernel(const uint32_t* __restrict__ row_ptr,
+                                                                           uint32_t seg,
+                                                                           const typename C::P* __restrict__ slot_pts,
+                                                                           typename C::P* __restrict__ buckets,
+                                                                           const uint32_t* __restrict__ long_list,
+                                                                           const uint32_t* __restrict__ long_count) {
+    __shared__ typename C::P red[C::kFixupLongThreads];
+    fixup_long_cta<C, false>(row_ptr, seg, slot_pts, buckets, long_list, long_count, red, blockIdx.x, gridDim.x);
+}
+
 // ---- 5. window reduction ----------------------------------------------------------------
 // For points X_1..X_N with weights, WS(X) = sum_b b X_b. Blocks of g: X_{(j-1)g+u}, u = 1..g:
 // WS(X) = sum_j E_j + g WS(Y), Y_j = block sum, E_j = -(s_1 + ... + s_{g-1}) with s_u the
@@ -861,46 +897,58 @@ __global__ void __launch_bounds__(C::kFixupLongThreads, C::kFixupLongMinBlocks) 
 // twice (buckets -> Y1, E1 -> Y2, E2, F2 = block sums of E1), then WS(Y2) by plain sums:
 // WS(Y2) = sum_j Y2_j + sum_k 2^k M_k, M_k = sum of Y2_j with bit k of (j - 1) set.
 // Level 1: block j of window w holds buckets b = j*g + 1 .. j*g + g (stored at index b - 1).
-template <class C>
-__global__ void __launch_bounds__(128) msm_bucket_blocks_kernel(const typename C::P* __restrict__ buckets,
-                                                                MsmShape sh, typename C::P* __restrict__ Y,
-                                                                typename C::P* __restrict__ E) {
+template <class C, bool kL2>
+__device__ __forceinline__ void blocks_thread(const typename C::P* buckets, const MsmShape& sh, typename C::P* Y,
+                                              typename C::P* E, uint32_t t) {
     using P = typename C::P;
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= sh.sets * sh.G) return;
     const P* b = buckets + (size_t)t * sh.g;
     P s = xyzz_inf<typename C::T>();
     P e = xyzz_inf<typename C::T>();
     for (uint32_t u = 0; u < sh.g; u++) {
-        s = xyzz_add(s, xyzz_load(b + u));
+        s = xyzz_add(s, xyzz_get<kL2>(b + u));
         if (u + 1 < sh.g) e = xyzz_add(e, s);
     }
     xyzz_store(Y + t, s);
     xyzz_store(E + t, xyzz_neg(e));
 }
 
+template <class C>
+__global__ void __launch_bounds__(128) msm_bucket_blocks_kernel(const typename C::P* __restrict__ buckets,
+                                                                MsmShape sh, typename C::P* __restrict__ Y,
+                                                                typename C::P* __restrict__ E) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= sh.sets * sh.G) return;
+    blocks_thread<C, false>(buckets, sh, Y, E, t);
+}
+
 // Level 2 over (Y1, E1): Y2, E2 as above on Y1, and F2 = plain block sums of E1.
+template <class C, bool kL2>
+__device__ __forceinline__ void blocks2_thread(const typename C::P* Y1, const typename C::P* E1, const MsmShape& sh,
+                                               typename C::P* Y2, typename C::P* E2, typename C::P* F2, uint32_t t) {
+    using P = typename C::P;
+    const size_t base = (size_t)t * sh.g2;
+    P s = xyzz_inf<typename C::T>();
+    P e = xyzz_inf<typename C::T>();
+    P f = xyzz_inf<typename C::T>();
+    for (uint32_t u = 0; u < sh.g2; u++) {
+        s = xyzz_add(s, xyzz_get<kL2>(Y1 + base + u));
+        if (u + 1 < sh.g2) e = xyzz_add(e, s);
+        f = xyzz_add(f, xyzz_get<kL2>(E1 + base + u));
+    }
+    xyzz_store(Y2 + t, s);
+    xyzz_store(E2 + t, xyzz_neg(e));
+    xyzz_store(F2 + t, f);
+}
+
 template <class C>
 __global__ void __launch_bounds__(128) msm_bucket_blocks2_kernel(const typename C::P* __restrict__ Y1,
                                                                  const typename C::P* __restrict__ E1, MsmShape sh,
                                                                  typename C::P* __restrict__ Y2,
                                                                  typename C::P* __restrict__ E2,
                                                                  typename C::P* __restrict__ F2) {
-    using P = typename C::P;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= sh.sets * sh.G2) return;
-    const size_t base = (size_t)t * sh.g2;
-    P s = xyzz_inf<typename C::T>();
-    P e = xyzz_inf<typename C::T>();
-    P f = xyzz_inf<typename C::T>();
-    for (uint32_t u = 0; u < sh.g2; u++) {
-        s = xyzz_add(s, xyzz_load(Y1 + base + u));
-        if (u + 1 < sh.g2) e = xyzz_add(e, s);
-        f = xyzz_add(f, xyzz_load(E1 + base + u));
-    }
-    xyzz_store(Y2 + t, s);
-    xyzz_store(E2 + t, xyzz_neg(e));
-    xyzz_store(F2 + t, f);
+    blocks2_thread<C, false>(Y1, E1, sh, Y2, E2, F2, t);
 }
 
 // ---- 6. plain sums per (window, target) ---------------------------------------------
@@ -908,17 +956,14 @@ __global__ void __launch_bounds__(128) msm_bucket_blocks2_kernel(const typename 
 // target plain + k: sum of Ylast_j over j with bit k set.
 // Each target is split over `parts` CTAs (a slice of its terms each; large single bucket
 // sets of the fixed-base mode have G2 up to 2^14); out[(w * targets + tg) * parts + part].
-template <class C>
-__global__ void __launch_bounds__(C::kTargetThreads) msm_targets_kernel(const typename C::P* __restrict__ P0,
-                                                                        const typename C::P* __restrict__ P1,
-                                                                        const typename C::P* __restrict__ P2,
-                                                                        const typename C::P* __restrict__ Ylast,
-                                                                        MsmShape sh, uint32_t parts,
-                                                                        typename C::P* __restrict__ out) {
+// `blk` is the CTA's index in that order; `red` holds blockDim points.
+template <class C, bool kL2>
+__device__ __forceinline__ void targets_cta(const typename C::P* P0, const typename C::P* P1, const typename C::P* P2,
+                                            const typename C::P* Ylast, const MsmShape& sh, uint32_t parts,
+                                            typename C::P* out, typename C::P* red, uint32_t blk) {
     using P = typename C::P;
-    __shared__ P red[C::kTargetThreads];
-    const uint32_t part = blockIdx.x % parts;
-    const uint32_t wt = blockIdx.x / parts;
+    const uint32_t part = blk % parts;
+    const uint32_t wt = blk / parts;
     const uint32_t w = wt / sh.targets;
     const uint32_t tg = wt % sh.targets;
     const bool bits = tg >= sh.plain;
@@ -937,7 +982,7 @@ __global__ void __launch_bounds__(C::kTargetThreads) msm_targets_kernel(const ty
         for (uint32_t t = t0 + threadIdx.x; t < t1; t += width) {
             uint32_t j = t;
             if (bits) j = ((t >> k) << (k + 1)) | (1u << k) | (t & ((1u << k) - 1));
-            acc = xyzz_add(acc, xyzz_load(src + j));
+            acc = xyzz_add(acc, xyzz_get<kL2>(src + j));
         }
     red[threadIdx.x] = acc;
     __syncthreads();
@@ -945,31 +990,206 @@ __global__ void __launch_bounds__(C::kTargetThreads) msm_targets_kernel(const ty
         if (threadIdx.x < off) red[threadIdx.x] = xyzz_add(red[threadIdx.x], red[threadIdx.x + off]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+    if (threadIdx.x == 0) out[blk] = red[0];
+}
+
+template <class C>
+__global__ void __launch_bounds__(C::kTargetThreads) msm_targets_kernel(const typename C::P* __restrict__ P0,
+                                                                        const typename C::P* __restrict__ P1,
+                                                                        const typename C::P* __restrict__ P2,
+                                                                        const typename C::P* __restrict__ Ylast,
+                                                                        MsmShape sh, uint32_t parts,
+                                                                        typename C::P* __restrict__ out) {
+    __shared__ typename C::P red[C::kTargetThreads];
+    targets_cta<C, false>(P0, P1, P2, Ylast, sh, parts, out, red, blockIdx.x);
 }
 
 // The parts of each target summed: one CTA of kMergeThreads per (window, target).
 static constexpr uint32_t kMergeThreads = 32;
 
-template <class C>
-__global__ void __launch_bounds__(kMergeThreads) msm_targets_merge_kernel(const typename C::P* __restrict__ in,
-                                                                          uint32_t parts,
-                                                                          typename C::P* __restrict__ out) {
+template <class C, bool kL2>
+__device__ __forceinline__ void targets_merge_cta(const typename C::P* in, uint32_t parts, typename C::P* out,
+                                                  typename C::P* red, uint32_t blk) {
     using P = typename C::P;
-    __shared__ P red[kMergeThreads];
-    const P* src = in + (size_t)blockIdx.x * parts;
+    const P* src = in + (size_t)blk * parts;
     uint32_t width = 1;
     while (width < parts && width < blockDim.x) width <<= 1;
     P acc = xyzz_inf<typename C::T>();
     if (threadIdx.x < width)
-        for (uint32_t t = threadIdx.x; t < parts; t += width) acc = xyzz_add(acc, xyzz_load(src + t));
+        for (uint32_t t = threadIdx.x; t < parts; t += width) acc = xyzz_add(acc, xyzz_get<kL2>(src + t));
     red[threadIdx.x] = acc;
     __syncthreads();
     for (uint32_t off = width / 2; off > 0; off >>= 1) {
         if (threadIdx.x < off) red[threadIdx.x] = xyzz_add(red[threadIdx.x], red[threadIdx.x + off]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+    if (threadIdx.x == 0) out[blk] = red[0];
+}
+
+template <class C>
+__global__ void __launch_bounds__(kMergeThreads) msm_targets_merge_kernel(const typename C::P* __restrict__ in,
+                                                                          uint32_t parts,
+                                                                          typename C::P* __restrict__ out) {
+    __shared__ typename C::P red[kMergeThreads];
+    targets_merge_cta<C, false>(in, parts, out, red, blockIdx.x);
+}
+
+// ---- persistent form of the post-sort stages (work queue) ----------------------------------
+// All pipelines of a batch, after their sorts, in ONE launch: the queue lists (pipeline,
+// stage) entries, each owning one item per CTA-sized piece of the stage -- 128 accumulation
+// units (entry ranges of one instance's window sets), 128 merge units, 128 buckets of the
+// fixup, a share of the long-bucket list, 128 level-1 / level-2 blocks, one (set, target,
+// part) or one (set, target) merge. Entries go stage by stage (largest pipelines first within
+// a stage); an item waits until its pipeline's previous stage has published all its items.
+// The same ticket discipline as the NTT queue keeps it deadlock-free for any number of
+// resident CTAs (the earliest unfinished item never waits), and every wait is bounded.
+enum : uint32_t { kQAcc = 0, kQMerge, kQFix, kQFixLong, kQBlk1, kQBlk2, kQTgt, kQTMerge };
+
+template <class C>
+struct MsmQPipe {
+    using P = typename C::P;
+    const uint32_t* entries;
+    const uint32_t* row_ptr;
+    const uint32_t* d_total;
+    const MsmInst* insts;
+    const uint32_t* inf_flag;
+    P* buckets;
+    uint32_t* slot_keys[2];
+    P* slot_pts[2];
+    uint32_t* long_list;
+    uint32_t* long_count;
+    P *Yb, *Eb, *Y2, *E2, *F2, *tgt_out, *tgt;
+    MsmShape sh;
+    uint32_t units, nbuckets, parts, skip_inf;
+};
+
+struct MsmQEntry {
+    uint32_t pipe, stage, first, items;
+    int32_t dep;     // entry of the pipeline's previous stage, -1 for the accumulation
+    uint32_t need;   // its items
+    uint32_t in_units, out_units, group, src;  // merge rounds: units in / out, group, slots read (0: a, 1: b)
+    uint64_t span;
+};
+
+static constexpr uint32_t kMsmQThreads = 128;
+
+template <class C>
+__global__ void __launch_bounds__(kMsmQThreads, 2) msm_queue_kernel(const MsmQPipe<C>* __restrict__ pipes,
+                                                                   const MsmQEntry* __restrict__ entries,
+                                                                   uint32_t nentries, uint32_t nitems,
+                                                                   uint32_t* state,
+                                                                   const uint64_t* __restrict__ limit,
+                                                                   uint32_t* sticky) {
+    using P = typename C::P;
+    __shared__ P red[kMsmQThreads];
+    __shared__ MsmQEntry sE;
+    __shared__ MsmQPipe<C> sQ;
+    __shared__ uint32_t s_next, s_item, s_entry, s_tile, s_stop;
+    volatile uint32_t* vstate = state;
+    if (threadIdx.x == 0) s_next = queue_ticket(state, nitems);
+    __syncthreads();
+    uint32_t finished = kNone;  // warp 1, lane 0: the entry of the item this CTA just finished
+    for (;;) {
+        if (threadIdx.x < 32) {  // warp 0: find the next item's entry, copy it and its pipeline, wait
+            const uint32_t item = s_next;
+            uint32_t e = 0;
+            if (threadIdx.x == 0 && item < nitems) {
+                uint32_t lo = 0, hi = nentries;  // the entry holding `item`: largest e with first <= item
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (entries[mid].first <= item) lo = mid;
+                    else hi = mid;
+                }
+                e = lo;
+            }
+            e = __shfl_sync(0xffffffffu, e, 0);
+            if (item < nitems) {
+                constexpr uint32_t kEw = sizeof(MsmQEntry) / 4, kPw = sizeof(MsmQPipe<C>) / 4;
+                static_assert(sizeof(MsmQEntry) % 4 == 0 && sizeof(MsmQPipe<C>) % 4 == 0, "word copies");
+                for (uint32_t w = threadIdx.x; w < kEw; w += 32)
+                    reinterpret_cast<uint32_t*>(&sE)[w] = reinterpret_cast<const uint32_t*>(entries + e)[w];
+                __syncwarp();
+                const uint32_t pq = sE.pipe;
+                for (uint32_t w = threadIdx.x; w < kPw; w += 32)
+                    reinterpret_cast<uint32_t*>(&sQ)[w] = reinterpret_cast<const uint32_t*>(pipes + pq)[w];
+            }
+            __syncwarp();
+            if (threadIdx.x == 0) {
+                s_item = item;
+                s_entry = e;
+                s_stop = 0;
+                if (item < nitems) {
+                    s_tile = item - sE.first;
+                    if (sE.dep >= 0) {
+                        const uint32_t dep = (uint32_t)sE.dep, need = sE.need;
+                        const uint64_t t0 = global_ns();
+                        uint32_t ns = 32;
+                        while (vstate[kQueueDone + dep] < need) {
+                            // bounded: give up when the limit passes or another CTA gave up
+                            if (vstate[kQueueStatus] != 0 || global_ns() - t0 > *limit) {
+                                if (atomicCAS(state + kQueueStatus, 0u, e + 1u) == 0u) atomicCAS(sticky, 0u, e + 1u);
+                                s_stop = 1;
+                                break;
+                            }
+                            __nanosleep(ns);
+                            if (ns < 1024) ns <<= 1;
+                        }
+                        __threadfence();  // acquire: the previous stage's outputs before our loads
+                    }
+                }
+            }
+        } else if (threadIdx.x == 32 && finished != kNone) {
+            // warp 1 publishes the finished item while warp 0 looks up the next one
+            __threadfence();  // release: the item's outputs (ordered by the barrier) before the counter
+            atomicAdd(state + kQueueDone + finished, 1u);
+        }
+        __syncthreads();
+        if (s_item >= nitems || s_stop) return;
+        if (threadIdx.x == 32) finished = s_entry;
+        uint32_t nxt = 0;
+        if (threadIdx.x == 0) nxt = queue_ticket(state, nitems);
+        const MsmQPipe<C>& q = sQ;
+        const uint32_t b = s_tile;
+        const uint32_t i = b * kMsmQThreads + threadIdx.x;  // the thread's unit / bucket / block
+        switch (sE.stage) {
+            case kQAcc:
+                if (i < q.units) {
+                    const bool test_inf = q.skip_inf && (q.inf_flag == nullptr || *q.inf_flag != 0);
+                    acc_unit<C, true>(q.entries, *q.d_total, q.row_ptr, q.insts, q.sh, i, q.buckets, q.slot_keys[0],
+                                      q.slot_pts[0], test_inf);
+                }
+                break;
+            case kQMerge:
+                if (i < sE.out_units)
+                    merge_unit<C, true>(q.slot_keys[sE.src], q.slot_pts[sE.src], sE.in_units, sE.group, *q.d_total,
+                                        q.row_ptr, sE.span, i, q.buckets, q.slot_keys[1 - sE.src],
+                                        q.slot_pts[1 - sE.src]);
+                break;
+            case kQFix:
+                if (i < q.nbuckets)
+                    fixup_bucket<C, true>(q.row_ptr, q.sh.seg, q.slot_pts[0], q.buckets, q.long_list, q.long_count, i);
+                break;
+            case kQFixLong:
+                fixup_long_cta<C, true>(q.row_ptr, q.sh.seg, q.slot_pts[0], q.buckets, q.long_list, q.long_count, red,
+                                        b, sE.items);
+                break;
+            case kQBlk1:
+                if (i < q.sh.sets * q.sh.G) blocks_thread<C, true>(q.buckets, q.sh, q.Yb, q.Eb, i);
+                break;
+            case kQBlk2:
+                if (i < q.sh.sets * q.sh.G2) blocks2_thread<C, true>(q.Yb, q.Eb, q.sh, q.Y2, q.E2, q.F2, i);
+                break;
+            case kQTgt:
+                if (q.sh.g2 > 1) targets_cta<C, true>(q.F2, q.E2, q.Y2, q.Y2, q.sh, q.parts, q.tgt_out, red, b);
+                else targets_cta<C, true>(q.Eb, q.Yb, q.Yb, q.Yb, q.sh, q.parts, q.tgt_out, red, b);
+                break;
+            case kQTMerge:
+                targets_merge_cta<C, true>(q.tgt_out, q.parts, q.tgt, red, b);
+                break;
+        }
+        __syncthreads();  // every store of the item issued; sE, sQ and red free again
+        if (threadIdx.x == 0) s_next = nxt;
+    }
 }
 
 // CTAs per target: one up to 8 terms per thread; the large single bucket sets of the
@@ -1387,26 +1607,35 @@ static int enqueue_tiled_sort(Ctx* c, MsmPipeT<C>& p, int scalars_mont) {
     return ZK_OK;
 }
 
-// Enqueue the device part of a pipeline on the context stream, ending with the copies of
-// the targets and the entry count to p.h_tgt / p.h_total. Allocates nothing, so it can be
-// captured into a CUDA graph (the instance descriptors are uploaded only if `upload`).
+// The descriptors (if `upload`), the cleared buckets and the CSR sort of a pipeline.
 template <class C>
-static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
+static int pipe_enqueue_sort(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
     using P = typename C::P;
-    cudaStream_t st = c->stream;
-    const MsmShape& sh = p.sh;
     if (upload) {
         int rc = pipe_upload(c, p);
         if (rc != ZK_OK) return rc;
     }
-    ZK_TRY_CUDA(cudaMemsetAsync(p.buckets, 0, p.nbuckets * sizeof(P), st));
-    const uint32_t N = (uint32_t)p.N;
-    const unsigned nblk = (unsigned)((p.N + 255) / 256);
-    {
-        int rc = p.tiled ? enqueue_tiled_sort<C>(c, p, scalars_mont) : enqueue_atomic_sort<C>(c, p, scalars_mont);
-        if (rc != ZK_OK) return rc;
-    }
+    ZK_TRY_CUDA(cudaMemsetAsync(p.buckets, 0, p.nbuckets * sizeof(P), c->stream));
+    return p.tiled ? enqueue_tiled_sort<C>(c, p, scalars_mont) : enqueue_atomic_sort<C>(c, p, scalars_mont);
+}
 
+// The copies of the targets and the entry count to p.h_tgt / p.h_total.
+template <class C>
+static int pipe_enqueue_copies(Ctx* c, MsmPipeT<C>& p) {
+    using P = typename C::P;
+    ZK_TRY_CUDA(cudaMemcpyAsync(p.h_tgt, p.tgt, p.host_elems() * sizeof(P), cudaMemcpyDeviceToHost, c->stream));
+    ZK_TRY_CUDA(cudaMemcpyAsync(p.h_total, p.row_ptr + p.nbuckets, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                c->stream));
+    return ZK_OK;
+}
+
+// Accumulation, straddling pieces and window reduction of a sorted pipeline, one launch per
+// stage.
+template <class C>
+static int pipe_enqueue_reduce(Ctx* c, MsmPipeT<C>& p) {
+    using P = typename C::P;
+    cudaStream_t st = c->stream;
+    const MsmShape& sh = p.sh;
     // accumulation rounds (the first kernel that reads the points)
     if (c->bases_wait != nullptr) ZK_TRY_CUDA(cudaStreamWaitEvent(st, c->bases_wait, 0));
     const uint32_t* d_total = p.row_ptr + p.nbuckets;
@@ -1472,9 +1701,18 @@ static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
                   p.tgt_parts, parts, p.tgt);
         ZK_TRY_CUDA(cudaGetLastError());
     }
-    ZK_TRY_CUDA(cudaMemcpyAsync(p.h_tgt, p.tgt, p.host_elems() * sizeof(P), cudaMemcpyDeviceToHost, st));
-    ZK_TRY_CUDA(cudaMemcpyAsync(p.h_total, d_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     return ZK_OK;
+}
+
+// Enqueue the device part of a pipeline on the context stream, ending with the copies of
+// the targets and the entry count to p.h_tgt / p.h_total. Allocates nothing, so it can be
+// captured into a CUDA graph (the instance descriptors are uploaded only if `upload`).
+template <class C>
+static int pipe_enqueue(Ctx* c, MsmPipeT<C>& p, int scalars_mont, bool upload) {
+    int rc = pipe_enqueue_sort<C>(c, p, scalars_mont, upload);
+    if (rc == ZK_OK) rc = pipe_enqueue_reduce<C>(c, p);
+    if (rc == ZK_OK) rc = pipe_enqueue_copies<C>(c, p);
+    return rc;
 }
 
 // A persistent pool of host threads for the combination step (created on first use,
@@ -1741,9 +1979,232 @@ static int ensure_side_streams(Ctx* c) {
     return ZK_OK;
 }
 
+// ---- host side of the MSM work queue ---------------------------------------------------
+// G1 only: the G2 stages together need more than 255 registers (the kernel spills ~5 KB per
+// thread), so G2 batches keep one launch per stage.
 template <class C>
-static int enqueue_all(Ctx* c, std::vector<MsmPipeT<C>>& pipes, int scalars_mont, bool upload) {
-    if (pipes.size() == 1) return pipe_enqueue<C>(c, pipes[0], scalars_mont, upload);
+constexpr bool kQueueForm = std::is_same<C, CurveG1>::value;
+
+template <class C>
+struct MsmQueueT {
+    std::vector<MsmQPipe<C>> qp;
+    std::vector<MsmQEntry> qe;
+    std::vector<uint32_t> fixup_mode;  // per pipeline: 1 when its straddling pieces use the fixup
+    uint32_t nitems = 0, grid = 0;
+    uint64_t limit_ns = 2000000000ull;  // 2 s per wait
+    size_t pipes_at = 0, entries_at = 0, limit_at = 0, state_at = 0, bytes = 0;
+    char* dev = nullptr;
+    uint32_t* h_status = nullptr;  // host word receiving the launch's status word
+};
+
+// The queue's entries in stage order (largest pipelines first within a stage) and its device
+// layout, from the pipelines' shapes. A test limit armed on the context (zk_msm_queue_test_limit)
+// makes the first waiting entry wait for one item more than its dependency has.
+template <class C>
+static int queue_plan(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, MsmQueueT<C>& q) {
+    const size_t np = pipes.size();
+    std::vector<size_t> order(np);
+    for (size_t k = 0; k < np; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return pipes[a].max_entries > pipes[b].max_entries; });
+    // each pipeline's stages as (slot, entry); slots: 0 accumulation, 1..R merge rounds, then
+    // fixup, long fixup, level 1, level 2, targets, target merge
+    std::vector<std::vector<std::pair<uint32_t, MsmQEntry>>> st(np);
+    uint32_t rmax = 0;
+    q.fixup_mode.assign(np, 0);
+    const uint32_t long_items = std::max<uint32_t>(8, (uint32_t)(2 * c->num_sms / std::max<size_t>(1, np)));
+    auto add = [](std::vector<std::pair<uint32_t, MsmQEntry>>& v, uint32_t slot, uint32_t stage, uint64_t items) {
+        MsmQEntry e{};
+        e.stage = stage;
+        e.items = (uint32_t)items;
+        v.push_back({slot, e});
+        return &v.back().second;
+    };
+    for (size_t k = 0; k < np; k++) {
+        const MsmPipeT<C>& p = pipes[k];
+        const MsmShape& sh = p.sh;
+        add(st[k], 0, kQAcc, (p.units + kMsmQThreads - 1) / kMsmQThreads);
+        if (p.max_entries <= (uint64_t)p.nbuckets * kFixupDensity) {
+            q.fixup_mode[k] = 1;
+        } else {
+            uint64_t span = sh.seg;
+            uint32_t in_units = p.units, group = kFirstGroup, src = 0, r = 0;
+            while (in_units > 1) {
+                const uint32_t out_units = (in_units + group - 1) / group;
+                span *= group;
+                MsmQEntry* e = add(st[k], 1 + r, kQMerge, (out_units + kMsmQThreads - 1) / kMsmQThreads);
+                e->in_units = in_units;
+                e->out_units = out_units;
+                e->group = group;
+                e->src = src;
+                e->span = span;
+                src ^= 1;
+                in_units = out_units;
+                group = kGroup;
+                r++;
+            }
+            rmax = std::max(rmax, r);
+        }
+    }
+    for (size_t k = 0; k < np; k++) {
+        const MsmPipeT<C>& p = pipes[k];
+        const MsmShape& sh = p.sh;
+        const uint32_t base = 1 + rmax;
+        if (q.fixup_mode[k]) {
+            add(st[k], base, kQFix, (p.nbuckets + kMsmQThreads - 1) / kMsmQThreads);
+            add(st[k], base + 1, kQFixLong, long_items);
+        }
+        add(st[k], base + 2, kQBlk1, ((uint64_t)sh.sets * sh.G + kMsmQThreads - 1) / kMsmQThreads);
+        if (sh.g2 > 1) add(st[k], base + 3, kQBlk2, ((uint64_t)sh.sets * sh.G2 + kMsmQThreads - 1) / kMsmQThreads);
+        const uint32_t parts = target_parts<C>(sh);
+        add(st[k], base + 4, kQTgt, (uint64_t)sh.sets * sh.targets * parts);
+        if (parts > 1) add(st[k], base + 5, kQTMerge, (uint64_t)sh.sets * sh.targets);
+    }
+    q.qe.clear();
+    q.nitems = 0;
+    std::vector<int32_t> prev(np, -1);
+    std::vector<size_t> pos(np, 0);
+    bool armed = c->msm_queue_test_limit_ns != 0;
+    auto emit = [&](size_t k) {
+        MsmQEntry e = st[k][pos[k]++].second;
+        e.pipe = (uint32_t)k;
+        e.first = q.nitems;
+        e.dep = prev[k];
+        e.need = prev[k] >= 0 ? q.qe[prev[k]].items : 0;
+        if (armed && e.dep >= 0) {  // the test: a wait that nothing can satisfy
+            e.need += 1;
+            armed = false;
+        }
+        prev[k] = (int32_t)q.qe.size();
+        q.qe.push_back(e);
+        q.nitems += e.items;
+    };
+    // Order: stage by stage, the largest pipelines first within a stage -- no item waits on a
+    // stage that began late. (Measured on GB300: every smaller pipeline's whole chain first,
+    // meant to hide its latency-bound stages behind the largest accumulation, was slower --
+    // 64 instances of 2^10..2^14 5.31 against 4.59 ms -- its items wait on their own
+    // previous stages.)
+    for (uint32_t slot = 0; slot <= 6 + rmax; slot++)
+        for (size_t k : order)
+            if (pos[k] < st[k].size() && st[k][pos[k]].first == slot) emit(k);
+    ZK_CHECK_ARG(q.nitems < (1u << 31), "MSM work queue too long");
+    if (c->msm_queue_test_limit_ns != 0) {
+        q.limit_ns = c->msm_queue_test_limit_ns;
+        c->msm_queue_test_limit_ns = 0;  // one-shot
+    }
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        off = (off + 255) & ~(size_t)255;
+        const size_t r = off;
+        off += bytes;
+        return r;
+    };
+    q.pipes_at = take(np * sizeof(MsmQPipe<C>));
+    q.entries_at = take(q.qe.size() * sizeof(MsmQEntry));
+    q.limit_at = take(8);
+    q.state_at = take((kQueueDone + q.qe.size()) * 4);
+    q.bytes = (off + 255) & ~(size_t)255;
+    int per_sm = 0;
+    if constexpr (kQueueForm<C>)
+        ZK_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, msm_queue_kernel<C>, kMsmQThreads, 0));
+    q.grid = (uint32_t)std::min<uint64_t>(q.nitems, (uint64_t)std::max(1, per_sm) * c->num_sms);
+    return ZK_OK;
+}
+
+// Device pointers of the laid-out pipelines into the queue, and the queue to the device at
+// `dev` (not inside a capture).
+template <class C>
+static int queue_fill(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, MsmQueueT<C>& q, char* dev) {
+    q.dev = dev;
+    q.qp.assign(pipes.size(), MsmQPipe<C>{});
+    for (size_t k = 0; k < pipes.size(); k++) {
+        const MsmPipeT<C>& p = pipes[k];
+        MsmQPipe<C>& d = q.qp[k];
+        d.entries = p.entries;
+        d.row_ptr = p.row_ptr;
+        d.d_total = p.row_ptr + p.nbuckets;
+        d.insts = p.d_inst;
+        d.inf_flag = p.skip_inf ? c->inf_flag : nullptr;
+        d.buckets = p.buckets;
+        d.slot_keys[0] = p.slot_keys_a;
+        d.slot_keys[1] = p.slot_keys_b;
+        d.slot_pts[0] = p.slot_pts_a;
+        d.slot_pts[1] = p.slot_pts_b;
+        d.long_list = p.long_list;
+        d.long_count = p.long_count;
+        d.Yb = p.Yb;
+        d.Eb = p.Eb;
+        d.Y2 = p.Y2;
+        d.E2 = p.E2;
+        d.F2 = p.F2;
+        d.parts = target_parts<C>(p.sh);
+        d.tgt_out = d.parts > 1 ? p.tgt_parts : p.tgt;
+        d.tgt = p.tgt;
+        d.sh = p.sh;
+        d.units = p.units;
+        d.nbuckets = (uint32_t)p.nbuckets;
+        d.skip_inf = p.skip_inf ? 1u : 0u;
+    }
+    ZK_TRY_CUDA(cudaMemcpyAsync(dev + q.pipes_at, q.qp.data(), q.qp.size() * sizeof(MsmQPipe<C>),
+                                cudaMemcpyHostToDevice, c->stream));
+    ZK_TRY_CUDA(cudaMemcpyAsync(dev + q.entries_at, q.qe.data(), q.qe.size() * sizeof(MsmQEntry),
+                                cudaMemcpyHostToDevice, c->stream));
+    ZK_TRY_CUDA(cudaMemcpyAsync(dev + q.limit_at, &q.limit_ns, 8, cudaMemcpyHostToDevice, c->stream));
+    return ZK_OK;
+}
+
+// The launch on the context stream: cleared state words, the persistent kernel, its status
+// word to q.h_status (stream-ordered: read it after the stream has passed the launch).
+template <class C>
+static int queue_launch(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, MsmQueueT<C>& q) {
+    uint32_t* state = reinterpret_cast<uint32_t*>(q.dev + q.state_at);
+    ZK_TRY_CUDA(cudaMemsetAsync(state, 0, (kQueueDone + q.qe.size()) * 4, c->stream));
+    for (size_t k = 0; k < pipes.size(); k++)
+        if (q.fixup_mode[k]) ZK_TRY_CUDA(cudaMemsetAsync(pipes[k].long_count, 0, 4, c->stream));
+    if (c->bases_wait != nullptr) ZK_TRY_CUDA(cudaStreamWaitEvent(c->stream, c->bases_wait, 0));
+    if constexpr (kQueueForm<C>) {
+        ZK_LAUNCH(c, "msm_queue", msm_queue_kernel<C>, q.grid, kMsmQThreads, 0,
+                  reinterpret_cast<const MsmQPipe<C>*>(q.dev + q.pipes_at),
+                  reinterpret_cast<const MsmQEntry*>(q.dev + q.entries_at), (uint32_t)q.qe.size(), q.nitems, state,
+                  reinterpret_cast<const uint64_t*>(q.dev + q.limit_at), state + kQueueStatus);
+        ZK_TRY_CUDA(cudaGetLastError());
+    }
+    ZK_TRY_CUDA(cudaMemcpyAsync(q.h_status, state + kQueueStatus, 4, cudaMemcpyDeviceToHost, c->stream));
+    return ZK_OK;
+}
+
+static std::string queue_message(uint32_t status) {
+    return "MSM work queue: the wait of queue entry " + std::to_string(status - 1) +
+           " for its pipeline's previous stage ran out; the launch stopped early";
+}
+
+// ZK_OK, or ZK_ETIMEOUT when the finished launch reported a wait that ran out.
+static int queue_check(uint32_t status) {
+    if (status == 0) return ZK_OK;
+    set_error(queue_message(status));
+    return ZK_ETIMEOUT;
+}
+
+// Enqueue every pipeline of a batch. Without a queue each pipeline runs all its stages on one
+// of the context stream and the side streams; with a queue (`q`, prepared by queue_plan and
+// queue_fill) the sorts run on those streams and then ONE persistent launch runs every
+// pipeline's accumulation and reductions.
+template <class C>
+static int enqueue_all(Ctx* c, std::vector<MsmPipeT<C>>& pipes, int scalars_mont, bool upload,
+                       MsmQueueT<C>* q = nullptr) {
+    auto part = [&](MsmPipeT<C>& p) {
+        return q ? pipe_enqueue_sort<C>(c, p, scalars_mont, upload) : pipe_enqueue<C>(c, p, scalars_mont, upload);
+    };
+    auto finish = [&]() {
+        if (q == nullptr) return ZK_OK;
+        int rc = queue_launch<C>(c, pipes, *q);
+        for (size_t k = 0; rc == ZK_OK && k < pipes.size(); k++) rc = pipe_enqueue_copies<C>(c, pipes[k]);
+        return rc;
+    };
+    if (pipes.size() == 1) {
+        int rc = part(pipes[0]);
+        return rc == ZK_OK ? finish() : rc;
+    }
     int rc0 = ensure_side_streams(c);  // outside a capture (msm_plan_create calls it first)
     if (rc0 != ZK_OK) return rc0;
     const cudaStream_t main_stream = c->stream;
@@ -1751,16 +2212,16 @@ static int enqueue_all(Ctx* c, std::vector<MsmPipeT<C>>& pipes, int scalars_mont
     ZK_TRY_CUDA(cudaEventRecord(c->side_events[0], main_stream));
     for (int k = 1; k < nstreams; k++) ZK_TRY_CUDA(cudaStreamWaitEvent(c->side_streams[k - 1], c->side_events[0], 0));
     std::vector<size_t> order(pipes.size());
-    for (size_t q = 0; q < pipes.size(); q++) order[q] = q;
+    for (size_t k = 0; k < pipes.size(); k++) order[k] = k;
     std::sort(order.begin(), order.end(),
               [&](size_t a, size_t b) { return pipes[a].max_entries > pipes[b].max_entries; });
     std::vector<uint64_t> load(nstreams, 0);
     int rc = ZK_OK;
-    for (size_t q : order) {
-        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        load[k] += pipes[q].max_entries + 64ull * pipes[q].nbuckets;  // + fixed cost per bucket
-        c->stream = k == 0 ? main_stream : c->side_streams[k - 1];
-        rc = pipe_enqueue<C>(c, pipes[q], scalars_mont, upload);
+    for (size_t k : order) {
+        const int s = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[s] += pipes[k].max_entries + 64ull * pipes[k].nbuckets;  // + fixed cost per bucket
+        c->stream = s == 0 ? main_stream : c->side_streams[s - 1];
+        rc = part(pipes[k]);
         c->stream = main_stream;
         if (rc != ZK_OK) break;
     }
@@ -1769,7 +2230,7 @@ static int enqueue_all(Ctx* c, std::vector<MsmPipeT<C>>& pipes, int scalars_mont
         cudaEventRecord(c->side_events[k], c->side_streams[k - 1]);
         cudaStreamWaitEvent(main_stream, c->side_events[k], 0);
     }
-    return rc;
+    return rc == ZK_OK ? finish() : rc;
 }
 
 template <class C>
@@ -1788,6 +2249,16 @@ static int batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont,
         bytes += (pipe_layout(pipes[q], nullptr) + 255) & ~(size_t)255;
         host_elems += pipes[q].host_elems();
     }
+    // the work-queue form (zk_msm_batch_set_queue): its descriptors after the pipelines
+    std::unique_ptr<MsmQueueT<C>> queue;
+    uint32_t queue_status = 0;
+    const size_t queue_at = bytes;
+    if (c->msm_queue && kQueueForm<C>) {
+        queue.reset(new MsmQueueT<C>());
+        if ((rc = queue_plan<C>(c, pipes, *queue)) != ZK_OK) return rc;
+        bytes += queue->bytes;
+        queue->h_status = &queue_status;
+    }
     char* arena = nullptr;
     if ((rc = scratch_alloc(c, bytes, reinterpret_cast<void**>(&arena))) != ZK_OK) return rc;
     std::vector<typename C::P> host_t(host_elems);
@@ -1799,13 +2270,19 @@ static int batch_run(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont,
         pipes[q].h_total = &host_total[q];
         h += pipes[q].host_elems();
     }
-    if ((rc = enqueue_all<C>(c, pipes, scalars_mont, true)) != ZK_OK) {
+    if (queue) {
+        for (auto& p : pipes)
+            if ((rc = pipe_upload(c, p)) != ZK_OK) break;
+        if (rc == ZK_OK) rc = queue_fill<C>(c, pipes, *queue, arena + queue_at);
+    }
+    if (rc != ZK_OK || (rc = enqueue_all<C>(c, pipes, scalars_mont, !queue, queue.get())) != ZK_OK) {
         cudaStreamSynchronize(c->stream);
         scratch_free(c, arena);
         return rc;
     }
     scratch_free(c, arena);
     ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
+    if (queue && (rc = queue_check(queue_status)) != ZK_OK) return rc;
     combine_all<C>(c, pipes, out_xy, out_is_inf);
     return ZK_OK;
 }
@@ -1840,6 +2317,7 @@ struct MsmAsync {
 template <class C>
 struct MsmAsyncT : MsmAsync {
     std::vector<MsmPipeT<C>> pipes;
+    std::unique_ptr<MsmQueueT<C>> queue;  // work-queue form, when the context asks for it
 };
 
 template <class C>
@@ -1863,8 +2341,15 @@ static int batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mo
         bytes += (pipe_layout(pipes[q], nullptr) + 255) & ~(size_t)255;
         host_elems += pipes[q].host_elems();
     }
-    // pinned host targets: the device-to-host copies stay asynchronous
-    const size_t host_bytes = host_elems * sizeof(typename C::P) + pipes.size() * sizeof(uint32_t);
+    const size_t queue_at = bytes;
+    if (c->msm_queue && kQueueForm<C>) {
+        a->queue.reset(new MsmQueueT<C>());
+        if ((rc = queue_plan<C>(c, pipes, *a->queue)) != ZK_OK) return rc;
+        bytes += a->queue->bytes;
+    }
+    // pinned host targets (then the entry totals and the queue status): the device-to-host
+    // copies stay asynchronous
+    const size_t host_bytes = host_elems * sizeof(typename C::P) + (pipes.size() + 1) * sizeof(uint32_t);
     a->ctx = c;
     if ((rc = pinned_take(c, host_bytes, &a->pinned, &a->pinned_bytes)) != ZK_OK) return rc;
     ZK_TRY_CUDA(cudaEventCreateWithFlags(&a->done_ev, cudaEventDisableTiming));
@@ -1879,7 +2364,14 @@ static int batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mo
         pipes[q].h_total = totals + q;
         h += pipes[q].host_elems();
     }
-    if ((rc = enqueue_all<C>(c, pipes, scalars_mont, true)) != ZK_OK) {
+    if (a->queue) {
+        a->queue->h_status = totals + pipes.size();
+        *a->queue->h_status = 0;
+        for (auto& p : pipes)
+            if ((rc = pipe_upload(c, p)) != ZK_OK) break;
+        if (rc == ZK_OK) rc = queue_fill<C>(c, pipes, *a->queue, arena + queue_at);
+    }
+    if (rc != ZK_OK || (rc = enqueue_all<C>(c, pipes, scalars_mont, !a->queue, a->queue.get())) != ZK_OK) {
         cudaStreamSynchronize(c->stream);
         scratch_free(c, arena);
         return rc;
@@ -1893,6 +2385,10 @@ static int batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mo
         const cudaError_t e = cudaEventSynchronize(raw->done_ev);
         if (e != cudaSuccess) {
             raw->finish(ZK_ECUDA, std::string("asynchronous MSM batch: ") + cudaGetErrorString(e));
+            return;
+        }
+        if (raw->queue && *raw->queue->h_status != 0) {
+            raw->finish(ZK_ETIMEOUT, queue_message(*raw->queue->h_status));
             return;
         }
         combine_all<C>(c, raw->pipes, out_xy, out_is_inf, /*record=*/false);
@@ -1972,15 +2468,20 @@ struct MsmPlan {
     void* host = nullptr;  // pinned: targets and totals of every pipeline
     cudaGraphExec_t exec = nullptr;
     uint64_t kernels = 0;  // kernel launches per run
+    std::unique_ptr<MsmQueueT<CurveG1>> queue;  // work-queue form
 };
 
 int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, bool graph,
-                    MsmPlan** out) {
+                    bool queue, MsmPlan** out) {
     std::unique_ptr<MsmPlan> plan(new MsmPlan());
     plan->count = count;
     plan->scalars_mont = scalars_mont;
     int rc = build_pipes<CurveG1>(c, jobs, count, window_bits, &plan->pipes, &plan->empty);
     if (rc != ZK_OK) return rc;
+    if (queue && !plan->pipes.empty()) {
+        plan->queue.reset(new MsmQueueT<CurveG1>());
+        if ((rc = queue_plan<CurveG1>(c, plan->pipes, *plan->queue)) != ZK_OK) return rc;
+    }
     // arena: scalar slots, then every pipeline's scratch
     std::vector<size_t> slot_at(count, 0);
     size_t bytes = 0;
@@ -1994,6 +2495,11 @@ int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, 
         at[q] = bytes;
         bytes += (pipe_layout(plan->pipes[q], nullptr) + 255) & ~(size_t)255;
         host_bytes += plan->pipes[q].host_elems() * sizeof(xyzz_t) + 16;
+    }
+    const size_t queue_at = bytes;
+    if (plan->queue) {
+        bytes += plan->queue->bytes;
+        host_bytes += 16;  // the queue's status word
     }
     ZK_TRY_CUDA(cudaMalloc(reinterpret_cast<void**>(&plan->arena), bytes ? bytes : 16));
     cudaError_t he = cudaMallocHost(&plan->host, host_bytes ? host_bytes : 16);
@@ -2023,6 +2529,12 @@ int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, 
         const int urc = pipe_upload(c, p);
         if (urc != ZK_OK) return fail(urc);
     }
+    if (plan->queue) {
+        plan->queue->h_status = reinterpret_cast<uint32_t*>(hp);
+        *plan->queue->h_status = 0;
+        const int qrc = queue_fill<CurveG1>(c, plan->pipes, *plan->queue, plan->arena + queue_at);
+        if (qrc != ZK_OK) return fail(qrc);
+    }
     cudaError_t se = cudaStreamSynchronize(c->stream);
     if (se != cudaSuccess) {
         set_error(std::string("plan set-up: ") + cudaGetErrorString(se));
@@ -2045,7 +2557,7 @@ int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, 
             return fail(ZK_ECUDA);
         }
         int erc = ZK_OK;
-        erc = enqueue_all<CurveG1>(c, plan->pipes, scalars_mont, false);
+        erc = enqueue_all<CurveG1>(c, plan->pipes, scalars_mont, false, plan->queue.get());
         cudaGraph_t g = nullptr;
         cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
         plan->kernels = c->launches - launches_was;
@@ -2085,13 +2597,17 @@ int msm_plan_run(Ctx* c, MsmPlan* plan, uint8_t* out_xy, int32_t* out_is_inf) {
         prof_end(c, tok);
         c->launches += plan->kernels - 1;  // prof_begin counted the graph launch as one
     } else {
-        int rc = enqueue_all<CurveG1>(c, plan->pipes, plan->scalars_mont, false);
+        int rc = enqueue_all<CurveG1>(c, plan->pipes, plan->scalars_mont, false, plan->queue.get());
         if (rc != ZK_OK) {
             cudaStreamSynchronize(c->stream);
             return rc;
         }
     }
     ZK_TRY_CUDA(cudaStreamSynchronize(c->stream));
+    if (plan->queue) {
+        const int qrc = queue_check(*plan->queue->h_status);
+        if (qrc != ZK_OK) return qrc;
+    }
     combine_all<CurveG1>(c, plan->pipes, out_xy, out_is_inf);
     return ZK_OK;
 }

@@ -91,23 +91,6 @@ __device__ __forceinline__ void smem_put(uint4* s_lo, uint4* s_hi, uint32_t i, c
     s_hi[i] = make_uint4(v.v[4], v.v[5], v.v[6], v.v[7]);
 }
 
-// A 32-byte element through L2 only (ld.global.cg): for data that other CTAs wrote earlier
-// in the same launch, which the non-coherent read-only path is not guaranteed to see.
-__device__ __forceinline__ fe fe_ldcg(const fe* p) {
-    const uint4* q = reinterpret_cast<const uint4*>(p);
-    uint4 lo = __ldcg(q), hi = __ldcg(q + 1);
-    fe r;
-    r.v[0] = lo.x;
-    r.v[1] = lo.y;
-    r.v[2] = lo.z;
-    r.v[3] = lo.w;
-    r.v[4] = hi.x;
-    r.v[5] = hi.y;
-    r.v[6] = hi.z;
-    r.v[7] = hi.w;
-    return r;
-}
-
 // One CTA's tile `tile` of one pass (shared by the single-transform, the batch and the
 // queue kernel). l2_in: the pass input was written earlier in the same launch (a runtime
 // flag rather than a template argument: one copy of the body in the queue kernel).
@@ -227,25 +210,12 @@ struct NttQueueEntry {
     uint32_t need;   // finished items of `dep` to wait for (its tiles)
 };
 
-// Queue state words, zeroed before each launch: the ticket, the status, then one finished-item
-// counter per entry. Status 0: every item ran; otherwise 1 + the entry whose wait ran out.
-static constexpr uint32_t kQueueTicket = 0, kQueueStatus = 1, kQueueDone = 2;
-
-__device__ __forceinline__ uint64_t global_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 // Entries whose first items are cached in shared memory for the item lookup (more entries:
 // the lookup reads the global table).
 static constexpr uint32_t kQueueSmemEntries = 1024;
 static constexpr uint32_t kNone32 = 0xffffffffu;
 
-__device__ __forceinline__ uint32_t queue_ticket(uint32_t* state, uint32_t nitems) {
-    volatile uint32_t* vstate = state;
-    return vstate[kQueueStatus] != 0 ? nitems : atomicAdd(state + kQueueTicket, 1u);
-}
 
 __global__ void __launch_bounds__(kNttThreads, 3) ntt_queue_kernel(const NttQueueEntry* __restrict__ entries,
                                                                   uint32_t nentries, uint32_t nitems,

@@ -394,9 +394,13 @@ int zk_autotune_ntt(zk_ctx* ctx, void* data_dev, uint32_t log_n, int reps, uint3
         return ZK_EINVAL;
     }
     zk::Ctx* c = &ctx->impl;
+    // Splits with the fewest passes only: a split with one pass more (e.g. 6 + 6 + 6 bits at
+    // 2^18) could win alone by a few percent with its smaller tiles, but in a batch, where
+    // other transforms fill the GPU anyway, it only adds a pass level and a round trip
+    // through HBM (64 coset NTTs of 2^10..2^20 on GB300: tuned 2.96 against 2.87 ms).
     const uint32_t min_np = (log_n + 10) / 11;
     std::vector<std::vector<uint32_t>> cands;
-    for (uint32_t np = min_np; np <= std::min<uint32_t>(min_np + 1, 4); np++) {
+    for (uint32_t np = min_np; np <= min_np; np++) {
         if (np > log_n) break;
         // all compositions of log_n into np parts of 1..11 bits, max - min <= 2
         std::vector<uint32_t> part(np, 1);

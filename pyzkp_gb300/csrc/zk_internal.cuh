@@ -92,6 +92,11 @@ struct Ctx {
     // and the device word where such launches record a wait that ran out (zk_ntt_queue_status)
     bool ntt_queue = false;
     uint32_t* ntt_queue_err = nullptr;
+    // MSM batches as sorts + one persistent launch of every pipeline's later stages
+    // (zk_msm_batch_set_queue); a one-shot test limit for the next queue's waits
+    // (zk_msm_queue_test_limit: its first waiting entry then waits for an item too many)
+    bool msm_queue = false;
+    uint64_t msm_queue_test_limit_ns = 0;
     uint64_t launches = 0;
     bool prof_on = false;
     std::map<std::string, ProfEntry> prof;
@@ -137,6 +142,23 @@ int prof_resolve(Ctx* c);
 // Host-side work inside a library call, recorded in the same table when profiling is on
 // (not counted as a kernel launch).
 void prof_host(Ctx* c, const char* name, double ms);
+
+// Work queues of the persistent kernels (ntt_queue_kernel, msm_queue_kernel): state words,
+// zeroed before each launch -- the ticket, the status, then one finished-item counter per
+// queue entry. Status 0: every item ran; otherwise 1 + the entry whose wait ran out.
+static constexpr uint32_t kQueueTicket = 0, kQueueStatus = 1, kQueueDone = 2;
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The next item of a queue (nitems once a wait has run out somewhere: the launch winds down).
+__device__ __forceinline__ uint32_t queue_ticket(uint32_t* state, uint32_t nitems) {
+    volatile uint32_t* vstate = state;
+    return vstate[kQueueStatus] != 0 ? nitems : atomicAdd(state + kQueueTicket, 1u);
+}
 
 // Launch `kernel` on the context stream with launch accounting.
 #define ZK_LAUNCH(ctxp, name, kernel, grid, block, smem, ...)                 \
@@ -193,7 +215,7 @@ int msm_batch_submit(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont,
 int msm_batch_wait(MsmAsync* a, int timeout_ms);
 void msm_batch_release(MsmAsync* a);
 int msm_plan_create(Ctx* c, const MsmJob* jobs, size_t count, int scalars_mont, uint32_t window_bits, bool graph,
-                    MsmPlan** out);
+                    bool queue, MsmPlan** out);
 int msm_plan_slot(MsmPlan* plan, size_t index, void** dev);
 uint64_t msm_plan_kernels(const MsmPlan* plan);
 int msm_plan_run(Ctx* c, MsmPlan* plan, uint8_t* out_xy, int32_t* out_is_inf);

@@ -123,6 +123,82 @@ def test_msm_batch_log_uniform_64(gpu_ctx):
         assert gpu_ctx.msm_g1(b, dev[j], sizes[j]) == got[j]
 
 
+# ----------------------------------------------------------------- MSM work queue (one launch)
+def test_msm_work_queue_matches_known_answers(gpu_ctx):
+    """The work-queue form (sorts, then every pipeline's later stages in one persistent launch)
+    gives the same points: mixed sizes with infinity bases, witness-like scalars (hot buckets
+    and long-bucket fixups), several base sets with offsets and a fixed-base set, the merge-round
+    mode (window 8 at 2^16: ~1000 entries per bucket), single MSMs, and the asynchronous form."""
+    k, b = _bases(gpu_ctx, 1101, 1 << 16, zero_at=(0, 17))
+    k3, b3 = _bases(gpu_ctx, 1103, 3000)
+    gpu_ctx.bases_precompute(b3, 10)
+    sizes = [0, 1, 2, 5, 63, 64, 65, 1000, 4096, 777, (1 << 12) + 3, 20000, 1 << 16, 3]
+    scal = [synth.fr_witness_like(1200 + j, m) if j % 3 == 0 else synth.fr_uniform(1200 + j, m)
+            for j, m in enumerate(sizes)]
+    dev = [_upload(gpu_ctx, s) for s in scal]
+    exp = [_expect(k[:m], s) for m, s in zip(sizes, scal)]
+    s3 = synth.fr_uniform(1300, 2000)
+    d3 = _upload(gpu_ctx, s3)
+    e3 = _expect(k3[7:2007], s3)
+    try:
+        gpu_ctx.msm_batch_set_queue(True)
+        for rep in range(2):
+            assert gpu_ctx.msm_g1_batch(b, dev, sizes) == exp, rep
+        assert gpu_ctx.msm_g1_batch(b, dev, sizes, window_bits=9) == exp
+        assert gpu_ctx.msm_g1_batch([b, b3, b], [dev[12], d3, dev[8]], [sizes[12], 2000, sizes[8]],
+                                    offsets=[0, 7, 0]) == [exp[12], e3, exp[8]]
+        # merge rounds instead of the fixup
+        assert gpu_ctx.msm_g1_batch(b, [dev[12]], [sizes[12]], window_bits=8) == [exp[12]]
+        assert gpu_ctx.msm_g1(b, dev[11], sizes[11]) == exp[11]
+        job = gpu_ctx.msm_batch_submit(b, dev, sizes)
+        try:
+            assert job.wait() == exp
+        finally:
+            job.destroy()
+    finally:
+        gpu_ctx.msm_batch_set_queue(False)
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_msm_queue_plan_replays(gpu_ctx, use_graph):
+    n = 1 << 14
+    k, b = _bases(gpu_ctx, 1401, n)
+    rng = np.random.default_rng(17)
+    sizes = [int(round(2 ** u)) for u in rng.uniform(6, 14, size=24)] + [0, n]
+    plan = gpu_ctx.msm_plan(b, sizes, use_graph=use_graph, queue=True)
+    for rep in range(2):
+        scal = [synth.fr_uniform(1500 + 100 * rep + j, m) for j, m in enumerate(sizes)]
+        for j, s in enumerate(scal):
+            if s.shape[0]:
+                slot = plan.slot(j)
+                slot.upload(s)
+                gpu_ctx.fr_to_mont(slot, slot, s.shape[0])
+        assert plan.run() == [_expect(k[:m], s) for m, s in zip(sizes, scal)], rep
+    plan.free()
+
+
+def test_msm_queue_wait_limit_runs_out_and_context_survives(gpu_ctx):
+    """A wait that can never succeed (the first waiting item of the queue waits for one item
+    more than its dependency has) gives up at its limit: the call raises TimeoutError within
+    the limit's order of magnitude and the context's next MSM is correct."""
+    import time
+
+    k, b = _bases(gpu_ctx, 1601, 5000)
+    s = synth.fr_uniform(1602, 5000)
+    d = _upload(gpu_ctx, s)
+    try:
+        gpu_ctx.msm_batch_set_queue(True)
+        gpu_ctx.msm_queue_test_limit(20000)  # 20 ms
+        t = time.perf_counter()
+        with pytest.raises(TimeoutError):
+            gpu_ctx.msm_g1_batch(b, [d], [5000])
+        assert time.perf_counter() - t < 5.0
+        assert gpu_ctx.msm_g1_batch(b, [d], [5000]) == [_expect(k, s)]  # the limit was used once
+    finally:
+        gpu_ctx.msm_batch_set_queue(False)
+    assert gpu_ctx.msm_g1(b, d, 5000) == _expect(k, s)
+
+
 # ---------------------------------------------------------------------------- NTT batches
 def _omega(log_n: int) -> int:
     return O.omega_for_size(1 << log_n)
