@@ -622,10 +622,18 @@ __global__ void msm_hist_offsets_kernel(uint32_t* __restrict__ M, const uint32_t
     if (x >= (uint64_t)sets * B) return;
     const uint32_t s = (uint32_t)(x / B), b = (uint32_t)(x % B);
     uint32_t base = row_ptr[x];
-    for (uint32_t t = set_tile0[s]; t < set_tile0[s + 1]; t++) {
-        const uint32_t v = M[(size_t)t * B + b];
-        M[(size_t)t * B + b] = base;
-        base += v;
+    const uint32_t t1 = set_tile0[s + 1];
+    for (uint32_t t0 = set_tile0[s]; t0 < t1; t0 += 16) {
+        // 16 counts loaded before any is overwritten: the loads do not wait on the stores
+        uint32_t v[16];
+#pragma unroll
+        for (uint32_t q = 0; q < 16; q++) v[q] = t0 + q < t1 ? M[(size_t)(t0 + q) * B + b] : 0u;
+#pragma unroll
+        for (uint32_t q = 0; q < 16; q++)
+            if (t0 + q < t1) {
+                M[(size_t)(t0 + q) * B + b] = base;
+                base += v[q];
+            }
     }
 }
 

@@ -30,6 +30,12 @@
 namespace zk {
 
 static constexpr int kNttThreads = 256;
+#ifndef ZK_NTT_MINB
+// resident CTAs per SM the pass kernels are compiled for: 2 (up to 128 registers) against 3
+// (85: the radix-4 steps then spill ~80 bytes) measured on GB300 with radix-4 steps: 2^20
+// 0.282 / 0.292 ms, 2^22 1.222 / 1.234 ms, 2^12 0.022 / 0.023 ms
+#define ZK_NTT_MINB 2
+#endif
 static constexpr int kMaxLogR = 11;       // 2048 elements * 32 B = 64 KB of shared memory
 static constexpr int kTileLogElems = 11;  // largest tile: R * T = 2048 elements per CTA
 // Default tile: 2^8 elements per CTA, or one radix-R column when R is larger. Measured on
@@ -120,8 +126,52 @@ __device__ __forceinline__ void ntt_pass_body(const NttPassParams& P, uint32_t t
     }
     __syncthreads();
 
-    // ---- R-point DFT per column: radix-2 DIF stages in shared memory ----
-    for (uint32_t st = 0; st < log_r; st++) {
+    // ---- R-point DFT per column: DIF stages in shared memory ----
+    // Pairs of radix-2 stages (st, st + 1) run as one radix-4 step: for j < h/2 (h = the
+    // half-size of stage st) the elements i0, i0 + h/2, i0 + h, i0 + 3h/2 of a block of 2h
+    // are closed under both stages, so one thread loads four, applies the four butterflies
+    // (the same products as two radix-2 stages) and stores four: half the shared-memory
+    // round trips, index computations and barriers. An odd stage count ends radix-2.
+    uint32_t st0 = 0;
+#ifndef ZK_NTT_RADIX2
+    // only while every thread has a radix-4 step: small tiles (E / 4 < blockDim) keep the
+    // radix-2 stages and all their threads busy (2^16 in 2^8-element tiles: 0.047 ms with
+    // radix-4 steps, 0.035 ms with radix-2)
+    for (; st0 + 1 < log_r && (E >> 2) >= blockDim.x; st0 += 2) {
+        const uint32_t log_h = log_r - st0 - 1;  // stage st0 pairs (x, x + h)
+        const uint32_t h = 1u << log_h, hq = h >> 1;
+        for (uint32_t qi = threadIdx.x; qi < (E >> 2); qi += blockDim.x) {
+            const uint32_t t = qi & (T - 1), b = qi >> log_t;
+            const uint32_t j = b & (hq - 1);
+            const uint32_t i0 = ((b >> (log_h - 1)) << (log_h + 1)) + j;
+            const uint32_t a0 = (swz(i0, log_r) << log_t) + t;
+            const uint32_t a1 = (swz(i0 + hq, log_r) << log_t) + t;
+            const uint32_t a2 = (swz(i0 + h, log_r) << log_t) + t;
+            const uint32_t a3 = (swz(i0 + h + hq, log_r) << log_t) + t;
+            const fe x0 = smem_get(s_lo, s_hi, a0), x1 = smem_get(s_lo, s_hi, a1);
+            const fe x2 = smem_get(s_lo, s_hi, a2), x3 = smem_get(s_lo, s_hi, a3);
+            // stage st0: (x0, x2) with twiddle index j, (x1, x3) with j + h/2
+            const fe p0 = fe_add<FrN>(x0, x2);
+            fe p2 = fe_sub<FrN>(x0, x2);
+            if (j != 0) p2 = fe_mul<FrN>(p2, fe_ldg(P.radix_tw + (j << st0)));
+            const fe p1 = fe_add<FrN>(x1, x3);
+            const fe p3 = fe_mul<FrN>(fe_sub<FrN>(x1, x3), fe_ldg(P.radix_tw + ((j + hq) << st0)));
+            // stage st0 + 1: (p0, p1) and (p2, p3), twiddle index j
+            fe q1 = fe_sub<FrN>(p0, p1), q3 = fe_sub<FrN>(p2, p3);
+            if (j != 0) {
+                const fe w = fe_ldg(P.radix_tw + (j << (st0 + 1)));
+                q1 = fe_mul<FrN>(q1, w);
+                q3 = fe_mul<FrN>(q3, w);
+            }
+            smem_put(s_lo, s_hi, a0, fe_add<FrN>(p0, p1));
+            smem_put(s_lo, s_hi, a1, q1);
+            smem_put(s_lo, s_hi, a2, fe_add<FrN>(p2, p3));
+            smem_put(s_lo, s_hi, a3, q3);
+        }
+        __syncthreads();
+    }
+#endif
+    for (uint32_t st = st0; st < log_r; st++) {
         const uint32_t log_h = log_r - st - 1;
         const uint32_t h = 1u << log_h;
         for (uint32_t bi = threadIdx.x; bi < (E >> 1); bi += blockDim.x) {
@@ -164,7 +214,7 @@ __device__ __forceinline__ void ntt_pass_body(const NttPassParams& P, uint32_t t
     }
 }
 
-__global__ void __launch_bounds__(kNttThreads, 3) ntt_pass_kernel(NttPassParams P) {
+__global__ void __launch_bounds__(kNttThreads, ZK_NTT_MINB) ntt_pass_kernel(NttPassParams P) {
     extern __shared__ uint4 smem[];
     ntt_pass_body(P, blockIdx.x, smem);
 }
@@ -172,7 +222,7 @@ __global__ void __launch_bounds__(kNttThreads, 3) ntt_pass_kernel(NttPassParams 
 // Batch: one launch runs the same pass level of many transforms. CTA b runs tile
 // b - first_tile[i] of item i, the largest i with first_tile[i] <= b; the item's
 // parameters are staged in shared memory once per CTA.
-__global__ void __launch_bounds__(kNttThreads, 3) ntt_pass_batch_kernel(const NttPassParams* __restrict__ items,
+__global__ void __launch_bounds__(kNttThreads, ZK_NTT_MINB) ntt_pass_batch_kernel(const NttPassParams* __restrict__ items,
                                                                        const uint32_t* __restrict__ first_tile,
                                                                        uint32_t nitems) {
     extern __shared__ uint4 smem[];
@@ -217,7 +267,7 @@ static constexpr uint32_t kQueueSmemEntries = 1024;
 static constexpr uint32_t kNone32 = 0xffffffffu;
 
 
-__global__ void __launch_bounds__(kNttThreads, 3) ntt_queue_kernel(const NttQueueEntry* __restrict__ entries,
+__global__ void __launch_bounds__(kNttThreads, ZK_NTT_MINB) ntt_queue_kernel(const NttQueueEntry* __restrict__ entries,
                                                                   uint32_t nentries, uint32_t nitems,
                                                                   uint32_t* state,
                                                                   const uint64_t* __restrict__ limit,
