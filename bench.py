@@ -307,6 +307,34 @@ def run_gpu(args, ranks: Ranks) -> dict:
     e2e_mpts, e2e_ok = timed_e2e(e2e_step)
     e2e_sep_mpts, e2e_sep_ok = timed_e2e(e2e_step_separate)
 
+    def timed_e2e_stream():
+        # a stream of host-buffer MSMs through zk_msm_g1_host_submit: step k + 1's uploads
+        # run while step k computes; every step uploads its points and scalars and reads its
+        # result back; wall clock from the first submit to the last result
+        for _ in range(args.warmup):
+            b = ctx.msm_g1_host_submit(pin_xy, pin_s, n)
+            b.wait()
+            b.destroy()
+        ranks.barrier()
+        ctx.memset(flush, 1)
+        ctx.sync()
+        ok = True
+        t0 = time.perf_counter()
+        pend = []
+        for _ in range(args.steps):
+            pend.append(ctx.msm_g1_host_submit(pin_xy, pin_s, n))
+            if len(pend) > 1:
+                b = pend.pop(0)
+                ok = ok and b.wait() == [res]
+                b.destroy()
+        for b in pend:
+            ok = ok and b.wait() == [res]
+            b.destroy()
+        t = ranks.max(time.perf_counter() - t0)
+        return n * args.steps * ranks.world / t / 1e6, ok
+
+    e2e_stream_mpts, e2e_stream_ok = timed_e2e_stream()
+
     ntt = run_gpu_ntt(ctx, args, ranks, 20, flush, imad_tops, hbm_peak)
     ntt22 = run_gpu_ntt(ctx, args, ranks, 22, flush, imad_tops, hbm_peak, brief=True)
     clocks = sampler.stop()
@@ -339,10 +367,14 @@ def run_gpu(args, ranks: Ranks) -> dict:
                    "csr_entries": entries, "l2": "flushed (256 MB memset) before every timed step",
                    "parallelism": f"replicas x{ranks.world}"},
         "msm_result": [hex(res[0]), hex(res[1])] if res else None,
-        "e2e": {"value": round(e2e_mpts, 3), "unit": "Mpts/s", "h2d_bytes_per_step": n * 96,
-                "d2h_bytes_per_step": 64 + 4, "result_ok": e2e_ok,
-                "path": "zk_msm_g1_host(pinned host affine points, pinned canonical scalars) -> host point "
-                        "(points uploaded on a second stream while the digits are sorted)",
+        "e2e": {"value": round(e2e_stream_mpts, 3), "unit": "Mpts/s", "h2d_bytes_per_step": n * 96,
+                "d2h_bytes_per_step": 64 + 4, "result_ok": e2e_stream_ok,
+                "path": "zk_msm_g1_host_submit per step (pinned host affine points and canonical scalars "
+                        "uploaded every step; the host point read back every step) as a stream: step k+1's "
+                        "uploads run while step k computes; wall clock from the first submit to the last result",
+                "one_call": {"value": round(e2e_mpts, 3), "result_ok": e2e_ok,
+                             "path": "zk_msm_g1_host, one synchronous call per step (points uploaded on a "
+                                     "second stream while the digits are sorted), device-event timed"},
                 "separate_calls": {"value": round(e2e_sep_mpts, 3), "result_ok": e2e_sep_ok,
                                    "path": "zk_bases_create + zk_h2d + zk_msm_g1"}},
         "gpu_launches": launches,

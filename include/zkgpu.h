@@ -38,6 +38,7 @@ extern "C" {
 
 typedef struct zk_ctx zk_ctx;
 typedef struct zk_bases zk_bases;
+typedef struct zk_batch zk_batch; /* an asynchronous MSM batch (zk_batch_wait / zk_batch_destroy) */
 
 /* Message of the last failure on this thread ("" if none). */
 const char *zk_last_error(void);
@@ -370,6 +371,21 @@ int zk_msm_g1_host(zk_ctx *ctx, const void *xy_canonical_host, const void *scala
                    int scalars_mont, uint32_t window_bits, uint8_t out_xy[64], int *out_is_inf);
 
 /*
+ * The same, asynchronous (a stream of host-buffer MSMs, as a serving loop issues them):
+ * returns once the work is enqueued, with a batch handle to pass to zk_batch_wait and then
+ * zk_batch_destroy;
+ * out_xy / out_is_inf are written when the batch completes, and the host buffers must stay
+ * valid (and unchanged) until then -- pinned memory keeps the copies asynchronous. The
+ * context keeps two device staging buffers and uses them in turn, so a call's uploads run
+ * while the previous call's MSM computes (the host link is otherwise idle then); a call
+ * waits for the MSM two calls back to release its buffer. Same result as zk_msm_g1_host. No
+ * reference counterpart (the reference's Metal MSM blocks per call).
+ */
+int zk_msm_g1_host_submit(zk_ctx *ctx, const void *xy_canonical_host, const void *scalars_host, size_t n,
+                          int scalars_mont, uint32_t window_bits, uint8_t *out_xy, int32_t *out_is_inf,
+                          zk_batch **out);
+
+/*
  * Batched G1 MSM: out[k] = sum_i scalars[k][i] * bases[k][offsets[k] + i] for i < sizes[k],
  * k < count. Replaces the per-instance loops of MSM_G1_BATCH and KZG_BATCH_COMMIT
  * (_msm_g1_batch / _kzg_batch_commit, runtime/kernels/cpu/kernels.py:441-496, which call
@@ -416,7 +432,6 @@ int zk_msm_g2_batch(zk_ctx *ctx, size_t count, const zk_bases *const *bases, con
  * must be destroyed before the context. Work enqueued on the context after a submit runs
  * after that batch's device part (one stream).
  */
-typedef struct zk_batch zk_batch;
 int zk_msm_g1_batch_submit(zk_ctx *ctx, size_t count, const zk_bases *const *bases, const uint64_t *offsets,
                            const void *const *scalars_dev, const uint64_t *sizes, int scalars_mont,
                            uint32_t window_bits, uint8_t *out_xy, int32_t *out_is_inf, zk_batch **out);

@@ -47,7 +47,7 @@ EXPORTED_SYMBOLS = (
     "zk_plonk_quotient_evals", "zk_ctx_create_prio", "zk_stream_priority_range", "zk_h2d_async", "zk_d2h_async",
     "zk_fence_record", "zk_fence_wait", "zk_fence_destroy", "zk_fr_r1cs_check_async",
     "zk_ntt_batch_set_queue", "zk_ntt_queue_status", "zk_ntt_queue_selftest", "zk_msm_batch_set_queue",
-    "zk_msm_queue_test_limit",
+    "zk_msm_queue_test_limit", "zk_msm_g1_host_submit",
 )
 
 _lib: Optional[ctypes.CDLL] = None
@@ -125,6 +125,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_ntt_plan_run": ([P], I),
             "zk_ntt_batch_set_queue": ([P, I], I),
             "zk_msm_batch_set_queue": ([P, I], I),
+            "zk_msm_g1_host_submit": ([P, P, P, S, I, U32, P, P, PP], I),
             "zk_msm_queue_test_limit": ([P, ctypes.c_uint64], I),
             "zk_ntt_queue_status": ([P], I),
             "zk_ntt_queue_selftest": ([P, ctypes.c_uint64, ctypes.POINTER(U32)], I),
@@ -731,6 +732,28 @@ class Context:
             return None
         b = bytes(out)
         return int.from_bytes(b[:32], "little"), int.from_bytes(b[32:], "little")
+
+    def msm_g1_host_submit(self, xy, scalars, n: int, *, scalars_mont: bool = False,
+                           window_bits: int = 0) -> "MsmBatch":
+        """msm_g1_host, asynchronous (zk_msm_g1_host_submit): returns an MsmBatch whose wait()
+        gives [point]. The host buffers stay referenced until the batch is destroyed; they
+        must not change before it completes (PinnedBuffer / pinned arrays keep the copies
+        asynchronous, so one call's uploads overlap the previous call's MSM)."""
+        keep = [xy, scalars]
+
+        def _ptr(a):
+            if hasattr(a, "ptr"):
+                return a.ptr
+            a = np.ascontiguousarray(a)
+            keep.append(a)
+            return a.ctypes.data
+        out = np.zeros((1, 64), dtype=np.uint8)
+        inf = np.zeros(1, dtype=np.int32)
+        h = ctypes.c_void_p()
+        check(load().zk_msm_g1_host_submit(self.handle, _ptr(xy), _ptr(scalars), int(n), 1 if scalars_mont else 0,
+                                           int(window_bits), out.ctypes.data, inf.ctypes.data, ctypes.byref(h)),
+              "zk_msm_g1_host_submit")
+        return MsmBatch(h.value, 1, False, out, inf, keep=keep)
 
     def msm_g1_host(self, xy, scalars, n: int, *, scalars_mont: bool = False, window_bits: int = 0):
         """One-call MSM from host memory (zk_msm_g1_host): ``xy`` canonical affine points

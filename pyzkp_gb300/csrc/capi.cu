@@ -213,6 +213,10 @@ int zk_ctx_destroy(zk_ctx* ctx) {
     for (cudaEvent_t ev : ctx->impl.chunk_ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->impl.inf_flag_dev) cudaFree(ctx->impl.inf_flag_dev);
+    for (auto& st : ctx->impl.host_stage) {
+        if (st.dev) cudaFree(st.dev);
+        if (st.free_ev) cudaEventDestroy(st.free_ev);
+    }
     if (ctx->impl.ntt_queue_err) cudaFree(ctx->impl.ntt_queue_err);
     for (auto& kv : ctx->impl.pinned_free) cudaFreeHost(kv.second);
     cudaStreamDestroy(ctx->impl.stream);
@@ -631,6 +635,53 @@ int zk_msm_g1(zk_ctx* ctx, const zk_bases* bases, size_t offset, const void* sca
                        bases->shifted_c, bases->n, /*glv=*/true, bases->has_inf);
 }
 
+// The lazily created resources of the host-buffer MSMs, each under its own check: a failure
+// part way leaves the rest to be created by the next call.
+static int host_msm_resources(Ctx* c) {
+    if (c->copy_stream == nullptr)
+        ZK_TRY_CUDA(cudaStreamCreateWithPriority(&c->copy_stream, cudaStreamNonBlocking, c->priority));
+    if (c->copy_go == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_go, cudaEventDisableTiming));
+    if (c->copy_done == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
+    for (cudaEvent_t& ev : c->chunk_ev)
+        if (ev == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    return ZK_OK;
+}
+
+// On the copy stream (after `wait`, an event on the main stream that orders the reuse of the
+// device buffers): the scalars first, alone on the link, in chunks whose digits the main
+// stream sorts as each arrives (one chunk below 2^18 scalars); then the points, converted
+// there too, with the infinity flag (only the accumulation, after the sort, waits for those:
+// copy_done). Sets c->scalar_chunks; returns the first CUDA error.
+static cudaError_t host_msm_upload(Ctx* c, cudaEvent_t wait, const void* xy_canonical_host,
+                                   const void* scalars_host, size_t n, void* bases, void* scalars,
+                                   uint32_t* inf_flag, int* rc) {
+    const size_t nchunks = n >= ((size_t)1 << 18) ? 4 : 1;
+    c->scalar_chunks.clear();
+    cudaError_t e = wait ? cudaStreamWaitEvent(c->copy_stream, wait, 0) : cudaSuccess;
+    for (size_t q = 0, j0 = 0; q < nchunks && e == cudaSuccess; q++) {
+        const size_t j1 = q + 1 == nchunks ? n : std::min(n, ((q + 1) * n / nchunks + 255) & ~(size_t)255);
+        e = cudaMemcpyAsync(static_cast<uint8_t*>(scalars) + j0 * 32, static_cast<const uint8_t*>(scalars_host) + j0 * 32,
+                            (j1 - j0) * 32, cudaMemcpyHostToDevice, c->copy_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(c->chunk_ev[q], c->copy_stream);
+        c->scalar_chunks.emplace_back((uint32_t)j1, c->chunk_ev[q]);
+        j0 = j1;
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(bases, xy_canonical_host, n * 64, cudaMemcpyHostToDevice, c->copy_stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(inf_flag, 0, 4, c->copy_stream);
+    if (e == cudaSuccess) {
+        // on the copy stream: mark infinity points, then convert and add the GLV images
+        const cudaStream_t main_stream = c->stream;
+        c->stream = c->copy_stream;
+        *rc = zk::mark_infinity(c, bases, n, false, inf_flag);
+        if (*rc == ZK_OK) *rc = zk::convert<zk::FqP, 1>(c, bases, bases, 2 * n);
+        if (*rc == ZK_OK) *rc = zk::glv_phi(c, static_cast<zk::affine_t*>(bases), n);
+        c->stream = main_stream;
+        e = cudaEventRecord(c->copy_done, c->copy_stream);
+    }
+    return e;
+}
+
 int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scalars_host, size_t n, int scalars_mont,
                    uint32_t window_bits, uint8_t out_xy[64], int* out_is_inf) {
     CTX_OR_FAIL(ctx);
@@ -644,52 +695,21 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
         return ZK_OK;
     }
     Ctx* c = &ctx->impl;
-    // each lazily created resource under its own check: a failure part way leaves the rest
-    // to be created by the next call
-    if (c->copy_stream == nullptr)
-        ZK_TRY_CUDA(cudaStreamCreateWithPriority(&c->copy_stream, cudaStreamNonBlocking, c->priority));
-    if (c->copy_go == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_go, cudaEventDisableTiming));
-    if (c->copy_done == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
-    for (cudaEvent_t& ev : c->chunk_ev)
-        if (ev == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    int rc = host_msm_resources(c);
+    if (rc != ZK_OK) return rc;
     if (c->inf_flag_dev == nullptr) ZK_TRY_CUDA(cudaMalloc(reinterpret_cast<void**>(&c->inf_flag_dev), 4));
     void* bases = nullptr;
     void* scalars = nullptr;
-    int rc = zk::scratch_alloc(c, 2 * n * sizeof(zk::affine_t), &bases);
-    if (rc != ZK_OK) return rc;
+    if ((rc = zk::scratch_alloc(c, 2 * n * sizeof(zk::affine_t), &bases)) != ZK_OK) return rc;
     if ((rc = zk::scratch_alloc(c, n * 32, &scalars)) != ZK_OK) {
         zk::scratch_free(c, bases);
         return rc;
     }
-    // copy stream (after the main stream's earlier work on the scratch): the scalars first,
-    // alone on the link, in chunks whose digits the main stream sorts as each arrives (one
-    // chunk below 2^18 scalars); then the points, converted there too (only the
-    // accumulation, after the sort, waits for those)
+    // the copies wait for the main stream's earlier work (the scratch may have served it)
     const cudaStream_t main_stream = c->stream;
-    const size_t nchunks = n >= ((size_t)1 << 18) ? 4 : 1;
-    c->scalar_chunks.clear();
     cudaError_t e = cudaEventRecord(c->copy_go, main_stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->copy_go, 0);
-    for (size_t q = 0, j0 = 0; q < nchunks && e == cudaSuccess; q++) {
-        const size_t j1 = q + 1 == nchunks ? n : std::min(n, ((q + 1) * n / nchunks + 255) & ~(size_t)255);
-        e = cudaMemcpyAsync(static_cast<uint8_t*>(scalars) + j0 * 32, static_cast<const uint8_t*>(scalars_host) + j0 * 32,
-                            (j1 - j0) * 32, cudaMemcpyHostToDevice, c->copy_stream);
-        if (e == cudaSuccess) e = cudaEventRecord(c->chunk_ev[q], c->copy_stream);
-        c->scalar_chunks.emplace_back((uint32_t)j1, c->chunk_ev[q]);
-        j0 = j1;
-    }
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(bases, xy_canonical_host, n * 64, cudaMemcpyHostToDevice, c->copy_stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(c->inf_flag_dev, 0, 4, c->copy_stream);
-    if (e == cudaSuccess) {
-        // on the copy stream: mark infinity points, then convert and add the GLV images
-        c->stream = c->copy_stream;
-        rc = zk::mark_infinity(c, bases, n, false, c->inf_flag_dev);
-        if (rc == ZK_OK) rc = zk::convert<zk::FqP, 1>(c, bases, bases, 2 * n);
-        if (rc == ZK_OK) rc = zk::glv_phi(c, static_cast<zk::affine_t*>(bases), n);
-        c->stream = main_stream;
-        e = cudaEventRecord(c->copy_done, c->copy_stream);
-    }
+        e = host_msm_upload(c, c->copy_go, xy_canonical_host, scalars_host, n, bases, scalars, c->inf_flag_dev, &rc);
     // main stream: digits and sort; the accumulation waits for copy_done (and with it for
     // the infinity flag)
     if (e == cudaSuccess && rc == ZK_OK) {
@@ -711,6 +731,84 @@ int zk_msm_g1_host(zk_ctx* ctx, const void* xy_canonical_host, const void* scala
         return ZK_ECUDA;
     }
     return rc;
+}
+
+int zk_msm_g1_host_submit(zk_ctx* ctx, const void* xy_canonical_host, const void* scalars_host, size_t n,
+                          int scalars_mont, uint32_t window_bits, uint8_t* out_xy, int32_t* out_is_inf,
+                          zk_batch** out) {
+    CTX_OR_FAIL(ctx);
+    if (out == nullptr || out_xy == nullptr || out_is_inf == nullptr ||
+        (n && (xy_canonical_host == nullptr || scalars_host == nullptr))) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    *out = nullptr;
+    Ctx* c = &ctx->impl;
+    zk::MsmJob job;
+    job.n = n;
+    job.stride = n;
+    job.glv = true;
+    zk::MsmAsync* impl = nullptr;
+    if (n == 0) {  // nothing to upload: a finished batch holding the identity
+        int rc = zk::msm_batch_submit(c, &job, 1, scalars_mont, window_bits, false, out_xy, out_is_inf, &impl);
+        if (rc != ZK_OK) return rc;
+        *out = new zk_batch{impl};
+        return ZK_OK;
+    }
+    int rc = host_msm_resources(c);
+    if (rc != ZK_OK) return rc;
+    // one of two staging buffers (points with their GLV images, scalars, infinity flag); its
+    // previous user (two calls back) released it with free_ev on the main stream
+    Ctx::HostStage& slot = c->host_stage[c->host_stage_next];
+    const size_t scal_at = 2 * n * sizeof(zk::affine_t), flag_at = scal_at + ((n * 32 + 255) & ~(size_t)255);
+    const size_t need = flag_at + 256;
+    if (slot.free_ev == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(&slot.free_ev, cudaEventDisableTiming));
+    if (slot.bytes < need) {
+        if (slot.dev != nullptr) {
+            ZK_TRY_CUDA(cudaEventSynchronize(slot.free_ev));
+            cudaFree(slot.dev);
+            slot.dev = nullptr;
+            slot.bytes = 0;
+        }
+        void* p = nullptr;
+        if (cudaMalloc(&p, need) != cudaSuccess) {
+            cudaGetLastError();
+            zk::set_error("zk_msm_g1_host_submit: device memory exhausted for the staging buffer");
+            return ZK_ENOMEM;
+        }
+        slot.dev = p;
+        slot.bytes = need;
+        slot.used = false;
+    }
+    c->host_stage_next ^= 1;
+    char* base = static_cast<char*>(slot.dev);
+    uint32_t* flag = reinterpret_cast<uint32_t*>(base + flag_at);
+    cudaError_t e = host_msm_upload(c, slot.used ? slot.free_ev : nullptr, xy_canonical_host, scalars_host, n, base,
+                                    base + scal_at, flag, &rc);
+    if (e == cudaSuccess && rc == ZK_OK) {
+        job.bases = reinterpret_cast<const zk::affine_t*>(base);
+        job.scalars = reinterpret_cast<const zk::fe*>(base + scal_at);
+        c->bases_wait = c->copy_done;
+        c->inf_flag = flag;
+        rc = zk::msm_batch_submit(c, &job, 1, scalars_mont, window_bits, false, out_xy, out_is_inf, &impl);
+        c->inf_flag = nullptr;
+        c->bases_wait = nullptr;
+    }
+    c->scalar_chunks.clear();
+    // the buffer is free again once the main stream has passed this MSM (and the copy stream
+    // its uploads, which the MSM waited for)
+    cudaStreamWaitEvent(c->stream, c->copy_done, 0);
+    cudaEventRecord(slot.free_ev, c->stream);
+    slot.used = true;
+    if (e != cudaSuccess) {
+        zk::set_error(std::string("zk_msm_g1_host_submit: ") + cudaGetErrorString(e));
+        cudaStreamSynchronize(c->stream);
+        if (impl) zk::msm_batch_release(impl);
+        return ZK_ECUDA;
+    }
+    if (rc != ZK_OK) return rc;
+    *out = new zk_batch{impl};
+    return ZK_OK;
 }
 
 int zk_g1_fixed_base_mul(zk_ctx* ctx, const uint8_t point_xy[64], const void* k_dev, size_t n, void* out_xy_dev) {

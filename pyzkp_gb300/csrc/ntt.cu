@@ -31,10 +31,16 @@ namespace zk {
 
 static constexpr int kNttThreads = 256;
 #ifndef ZK_NTT_MINB
-// resident CTAs per SM the pass kernels are compiled for: 2 (up to 128 registers) against 3
-// (85: the radix-4 steps then spill ~80 bytes) measured on GB300 with radix-4 steps: 2^20
-// 0.282 / 0.292 ms, 2^22 1.222 / 1.234 ms, 2^12 0.022 / 0.023 ms
+// resident CTAs per SM the single-transform pass kernel is compiled for: 2 (up to 128
+// registers) against 3 (85: the radix-4 steps then spill ~80 bytes) measured on GB300 with
+// radix-4 steps: 2^20 0.282 / 0.292 ms, 2^22 1.222 / 1.234 ms, 2^12 0.022 / 0.023 ms
 #define ZK_NTT_MINB 2
+#endif
+#ifndef ZK_NTT_BATCH_MINB
+// ... and the batch and queue kernels: their many small tiles (256-element tiles of 128
+// active threads) want the third CTA per SM (64 coset NTTs of 2^10..2^20: 2.87 ms at 3,
+// 3.00 ms at 2)
+#define ZK_NTT_BATCH_MINB 3
 #endif
 static constexpr int kMaxLogR = 11;       // 2048 elements * 32 B = 64 KB of shared memory
 static constexpr int kTileLogElems = 11;  // largest tile: R * T = 2048 elements per CTA
@@ -222,7 +228,7 @@ __global__ void __launch_bounds__(kNttThreads, ZK_NTT_MINB) ntt_pass_kernel(NttP
 // Batch: one launch runs the same pass level of many transforms. CTA b runs tile
 // b - first_tile[i] of item i, the largest i with first_tile[i] <= b; the item's
 // parameters are staged in shared memory once per CTA.
-__global__ void __launch_bounds__(kNttThreads, ZK_NTT_MINB) ntt_pass_batch_kernel(const NttPassParams* __restrict__ items,
+__global__ void __launch_bounds__(kNttThreads, ZK_NTT_BATCH_MINB) ntt_pass_batch_kernel(const NttPassParams* __restrict__ items,
                                                                        const uint32_t* __restrict__ first_tile,
                                                                        uint32_t nitems) {
     extern __shared__ uint4 smem[];
@@ -267,7 +273,7 @@ static constexpr uint32_t kQueueSmemEntries = 1024;
 static constexpr uint32_t kNone32 = 0xffffffffu;
 
 
-__global__ void __launch_bounds__(kNttThreads, ZK_NTT_MINB) ntt_queue_kernel(const NttQueueEntry* __restrict__ entries,
+__global__ void __launch_bounds__(kNttThreads, ZK_NTT_BATCH_MINB) ntt_queue_kernel(const NttQueueEntry* __restrict__ entries,
                                                                   uint32_t nentries, uint32_t nitems,
                                                                   uint32_t* state,
                                                                   const uint64_t* __restrict__ limit,

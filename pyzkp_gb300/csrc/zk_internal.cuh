@@ -116,6 +116,16 @@ struct Ctx {
     // is set, accumulations that test for infinity do so only if the word is non-zero
     uint32_t* inf_flag_dev = nullptr;
     const uint32_t* inf_flag = nullptr;
+    // zk_msm_g1_host_submit: two device staging buffers used in turn, so that one call's
+    // uploads overlap the previous call's MSM; free_ev (main stream) releases a buffer
+    struct HostStage {
+        void* dev = nullptr;
+        size_t bytes = 0;
+        cudaEvent_t free_ev = nullptr;
+        bool used = false;
+    };
+    HostStage host_stage[2];
+    int host_stage_next = 0;
     // MSM batches spread their pipelines over the context stream and these (fork / join
     // events); created on first use
     std::vector<cudaStream_t> side_streams;

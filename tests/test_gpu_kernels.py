@@ -396,6 +396,25 @@ def test_msm_g1_host_alternating_infinity_sets(gpu_ctx):
     for _ in range(2):
         assert gpu_ctx.msm_g1_host(pin_half, pin_s, n) == exp_half
         assert gpu_ctx.msm_g1_host(pin_full, pin_s, n) == exp_full
+    # the asynchronous form, several calls in flight (two staging buffers used in turn, each
+    # waiting for the MSM two calls back), then a larger call that grows a buffer, and a
+    # smaller one: every result the known answer
+    jobs = [gpu_ctx.msm_g1_host_submit(pin_half if j % 2 else pin_full, pin_s, n) for j in range(5)]
+    for j, b in enumerate(jobs):
+        assert b.wait() == [exp_half if j % 2 else exp_full], j
+        b.destroy()
+    m = (1 << 18) + 5
+    exp_m = O.affine_to_ints(O.msm_known_answer(k[:m], s[:m]))
+    first = gpu_ctx.msm_g1_host_submit(pin_full, pin_s, m)
+    second = gpu_ctx.msm_g1_host_submit(pin_full, pin_s, n)
+    third = gpu_ctx.msm_g1_host_submit(pin_half, pin_s, m)
+    assert first.wait() == [exp_m] and second.wait() == [exp_full]
+    assert third.wait() == [O.affine_to_ints(O.msm_known_answer(k_half[:m], s[:m]))]
+    for b in (first, second, third):
+        b.destroy()
+    empty = gpu_ctx.msm_g1_host_submit(pin_full, pin_s, 0)
+    assert empty.wait() == [None]
+    empty.destroy()
     for b in (pin_full, pin_half, pin_s):
         b.free()
 
