@@ -250,6 +250,7 @@ def run_gpu(args, ranks: Ranks) -> dict:
                         "32x32->64 multiply-accumulates, as lo+hi pairs (harmonic mean of the mad.lo and mad.hi "
                         "probes) or as mad.wide, counted as 2 IMAD each like the algorithmic work"),
         "imad_probes_T_per_s": imad_probes,
+        "peak_model": imad_model(ctx, acc_tops),
         "launch_ms": round(acc_ms_launch, 4),
         "share_of_step": round(acc_ms / max(1e-9, sum(v[1] for v in table.values())), 4),
         "traffic": traffic_of("msm_accumulate", log_n),
@@ -467,8 +468,45 @@ def run_gpu_ntt(ctx, args, ranks, log_n, flush, imad_tops, hbm_peak, brief=False
             e2e()
             ts.append(ctx.timer_stop())
         tot = ranks.max(sum(ts))
-        out["e2e"] = {"value": round(n * args.steps * ranks.world / (tot * 1e-3) / 1e6, 2), "unit": "Melem/s",
-                      "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 32}
+        one_call = n * args.steps * ranks.world / (tot * 1e-3) / 1e6
+        # a stream of host-buffer transforms (zk_ntt_host_submit): each step copies its input
+        # up and its output back; one step's output copy, the next step's input copy and a
+        # transform run at once. Two host buffer pairs in turn; wall clock.
+        pins = [(pin_in, pin_out), (ctx.pinned(n * 32), ctx.pinned(n * 32))]
+        pins[1][0].array[:] = pin_in.array
+        ref = None
+        for _ in range(args.warmup):
+            f = ctx.ntt_host_submit(N.NTT_EVALS_FROM_COEFFS, pin_out, pin_in, n, log_n, om)
+            f.wait()
+            f.destroy()
+            ref = bytes(pin_out.array[:64])
+        ranks.barrier()
+        ctx.memset(flush, 1)
+        ctx.sync()
+        ok = True
+        t0 = time.perf_counter()
+        pend = []
+        for k in range(args.steps):
+            pi, po = pins[k % 2]
+            pend.append((ctx.ntt_host_submit(N.NTT_EVALS_FROM_COEFFS, po, pi, n, log_n, om), po))
+            if len(pend) > 1:
+                f, po_done = pend.pop(0)
+                f.wait()
+                f.destroy()
+                ok = ok and bytes(po_done.array[:64]) == ref
+        for f, po_done in pend:
+            f.wait()
+            f.destroy()
+            ok = ok and bytes(po_done.array[:64]) == ref
+        stream_t = ranks.max(time.perf_counter() - t0)
+        out["e2e"] = {"value": round(n * args.steps * ranks.world / stream_t / 1e6, 2), "unit": "Melem/s",
+                      "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 32, "result_ok": ok,
+                      "path": "zk_ntt_host_submit per step (canonical pinned input up, canonical output back "
+                              "every step) as a stream: output copy, next input copy and transform at once; "
+                              "wall clock",
+                      "one_call": {"value": round(one_call, 2),
+                                   "path": "zk_h2d + zk_fr_to_mont + zk_ntt + zk_fr_from_mont + zk_d2h per step, "
+                                           "device-event timed"}}
     return out
 
 
@@ -564,6 +602,28 @@ def msm_model(n: int, ms: float, imad_tops: float) -> dict:
     tops = m * 272 / (ms * 1e-3) / 1e12
     return {"c_star": c_star, "fq_mults": m, "wide_macs": m * 136, "achieved_T_IMAD_s": round(tops, 3),
             "frac": round(tops / imad_tops, 4), "ms": round(ms, 4)}
+
+
+def imad_model(ctx, achieved_tops: float) -> dict:
+    """The denominator checked without the probe: SMs x SM clock x the nominal 64 32-bit
+    integer multiply-adds per clock per SM (the CUDA throughput table for compute capability
+    10.x). The probe's mad.wide rate counted as 2 IMAD per wide product exceeds it (about 82
+    per clock per SM), so the probe's peak is the stricter denominator and the one used."""
+    sms = ctx.num_sms()
+    mhz = None
+    try:
+        import subprocess
+
+        out = subprocess.run(["nvidia-smi", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits", "-i", "0"],
+                             capture_output=True, text=True, timeout=10).stdout.strip().splitlines()
+        mhz = float(out[0]) if out else None
+    except Exception:  # noqa: BLE001 -- no nvidia-smi: the model is left out
+        mhz = None
+    if not mhz:
+        return {"note": "SM clock unavailable"}
+    nominal = sms * mhz * 1e6 * 64 / 1e12
+    return {"sms": sms, "sm_max_mhz": mhz, "imad_per_clock_per_sm": 64, "T_IMAD_s": round(nominal, 2),
+            "frac_of_nominal": round(achieved_tops / nominal, 4)}
 
 
 def imad_peak(ctx):

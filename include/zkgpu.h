@@ -39,6 +39,7 @@ extern "C" {
 typedef struct zk_ctx zk_ctx;
 typedef struct zk_bases zk_bases;
 typedef struct zk_batch zk_batch; /* an asynchronous MSM batch (zk_batch_wait / zk_batch_destroy) */
+typedef struct zk_fence zk_fence; /* a point on a stream (zk_fence_wait / zk_fence_destroy) */
 
 /* Message of the last failure on this thread ("" if none). */
 const char *zk_last_error(void);
@@ -109,7 +110,6 @@ int zk_d2h_async(zk_ctx *ctx, void *dst_host, const void *src_dev, size_t bytes)
  * zk_fence_wait returns ZK_OK once the device has passed it, ZK_ETIMEOUT if timeout_ms
  * (>= 0; 0 = just ask) passes first; a negative timeout waits without a limit. No
  * counterpart in the reference (its Metal ops wait for completion inside every op). */
-typedef struct zk_fence zk_fence;
 int zk_fence_record(zk_ctx *ctx, zk_fence **out);
 int zk_fence_wait(zk_fence *f, int timeout_ms);
 int zk_fence_destroy(zk_fence *f);
@@ -166,6 +166,22 @@ int zk_fr_trimmed_len(zk_ctx *ctx, const void *a, size_t n, size_t *out);
 #define ZK_NTT_COSET_COEFFS_FROM_EVALS 3
 int zk_ntt(zk_ctx *ctx, int mode, void *out_dev, const void *in_dev, size_t in_len, uint32_t log_n,
            const uint8_t omega[32], const uint8_t shift[32]);
+
+/*
+ * The same transform between HOST buffers of canonical elements, asynchronous: in_host
+ * holds in_len canonical elements (32 bytes each), out_host receives n canonical elements.
+ * The shape of the reference's NTT ops, which take and return Python lists
+ * (runtime/kernels/cpu/kernels.py:175-250). Returns once the work is enqueued, with a fence
+ * (zk_fence_wait, then zk_fence_destroy) that passes when out_host is written; the host
+ * buffers must stay valid (and in_host unchanged) until then -- pinned memory keeps the
+ * copies asynchronous. The input copy, the transform (with the Montgomery conversions on
+ * either side) and the output copy run on three streams, and the context uses two device
+ * staging buffers in turn, so a stream of calls overlaps one call's output copy, the next
+ * call's input copy and a transform (the host link carries both directions at once). shift
+ * may be NULL (1). Errors as zk_ntt. No reference counterpart for the asynchrony.
+ */
+int zk_ntt_host_submit(zk_ctx *ctx, int mode, void *out_host, const void *in_host, size_t in_len, uint32_t log_n,
+                       const uint8_t omega[32], const uint8_t shift[32], zk_fence **done);
 
 /*
  * Batched NTTs: transform k is zk_ntt(modes[k], outs[k], ins[k], in_lens[k], log_ns[k],

@@ -47,7 +47,7 @@ EXPORTED_SYMBOLS = (
     "zk_plonk_quotient_evals", "zk_ctx_create_prio", "zk_stream_priority_range", "zk_h2d_async", "zk_d2h_async",
     "zk_fence_record", "zk_fence_wait", "zk_fence_destroy", "zk_fr_r1cs_check_async",
     "zk_ntt_batch_set_queue", "zk_ntt_queue_status", "zk_ntt_queue_selftest", "zk_msm_batch_set_queue",
-    "zk_msm_queue_test_limit", "zk_msm_g1_host_submit",
+    "zk_msm_queue_test_limit", "zk_msm_g1_host_submit", "zk_ntt_host_submit",
 )
 
 _lib: Optional[ctypes.CDLL] = None
@@ -126,6 +126,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
             "zk_ntt_batch_set_queue": ([P, I], I),
             "zk_msm_batch_set_queue": ([P, I], I),
             "zk_msm_g1_host_submit": ([P, P, P, S, I, U32, P, P, PP], I),
+            "zk_ntt_host_submit": ([P, I, P, P, S, U32, P, P, PP], I),
             "zk_msm_queue_test_limit": ([P, ctypes.c_uint64], I),
             "zk_ntt_queue_status": ([P], I),
             "zk_ntt_queue_selftest": ([P, ctypes.c_uint64, ctypes.POINTER(U32)], I),
@@ -515,6 +516,20 @@ class Context:
         self.handle = h.value
         self.device = device
         self.priority = priority
+
+    def ntt_host_submit(self, mode: int, out_host, in_host, in_len: int, log_n: int, omega: int,
+                        shift: int = 1) -> Fence:
+        """zk_ntt_host_submit: canonical host input (in_len x 32 bytes) -> canonical host output
+        (2^log_n x 32 bytes), asynchronous; the returned Fence passes when the output is
+        written. ``out_host`` / ``in_host``: PinnedBuffer or pinned arrays (anything with a
+        ``ptr``), which must stay alive and unchanged until then."""
+        om = np.frombuffer(_fr_bytes(omega), dtype=np.uint8).copy()
+        sh = np.frombuffer(_fr_bytes(shift), dtype=np.uint8).copy()
+        h = ctypes.c_void_p()
+        check(load().zk_ntt_host_submit(self.handle, int(mode), out_host.ptr, in_host.ptr if in_len else None,
+                                        int(in_len), int(log_n), om.ctypes.data, sh.ctypes.data, ctypes.byref(h)),
+              "zk_ntt_host_submit")
+        return Fence(h.value)
 
     def fence(self) -> Fence:
         h = ctypes.c_void_p()

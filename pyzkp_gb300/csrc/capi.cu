@@ -217,6 +217,15 @@ int zk_ctx_destroy(zk_ctx* ctx) {
         if (st.dev) cudaFree(st.dev);
         if (st.free_ev) cudaEventDestroy(st.free_ev);
     }
+    if (ctx->impl.d2h_stream) {
+        cudaStreamSynchronize(ctx->impl.d2h_stream);
+        cudaStreamDestroy(ctx->impl.d2h_stream);
+    }
+    for (auto& st : ctx->impl.ntt_stage) {
+        if (st.dev) cudaFree(st.dev);
+        for (cudaEvent_t ev : {st.free_ev, st.h2d_ev, st.comp_ev})
+            if (ev) cudaEventDestroy(ev);
+    }
     if (ctx->impl.ntt_queue_err) cudaFree(ctx->impl.ntt_queue_err);
     for (auto& kv : ctx->impl.pinned_free) cudaFreeHost(kv.second);
     cudaStreamDestroy(ctx->impl.stream);
@@ -1146,6 +1155,89 @@ int zk_ntt_plan_create(zk_ctx* ctx, size_t count, const int* modes, void* const*
                              (use_graph & ZK_NTT_PLAN_QUEUE) != 0, &impl);
     if (rc != ZK_OK) return rc;
     *out = new zk_ntt_plan{ctx, impl};
+    return ZK_OK;
+}
+
+int zk_ntt_host_submit(zk_ctx* ctx, int mode, void* out_host, const void* in_host, size_t in_len, uint32_t log_n,
+                       const uint8_t omega[32], const uint8_t shift[32], zk_fence** done) {
+    CTX_OR_FAIL(ctx);
+    if (done == nullptr || out_host == nullptr || omega == nullptr || (in_len && in_host == nullptr)) {
+        zk::set_error("null pointer");
+        return ZK_EINVAL;
+    }
+    *done = nullptr;
+    if (log_n > 28) {
+        zk::set_error("domain too large for BN254 root of unity (log2 n > 28)");
+        return ZK_EINVAL;
+    }
+    Ctx* c = &ctx->impl;
+    const size_t n = (size_t)1 << log_n, valid = in_len < n ? in_len : n;
+    const bool inverse = (mode == ZK_NTT_COEFFS_FROM_EVALS || mode == ZK_NTT_COSET_COEFFS_FROM_EVALS);
+    if (mode < 0 || mode > 3 || (inverse && in_len != n)) {
+        zk::set_error(mode < 0 || mode > 3 ? "invalid NTT mode" : "inverse transforms need len(evals) == n (a power of two)");
+        return ZK_EINVAL;
+    }
+    if (c->copy_stream == nullptr)
+        ZK_TRY_CUDA(cudaStreamCreateWithPriority(&c->copy_stream, cudaStreamNonBlocking, c->priority));
+    if (c->d2h_stream == nullptr)
+        ZK_TRY_CUDA(cudaStreamCreateWithPriority(&c->d2h_stream, cudaStreamNonBlocking, c->priority));
+    Ctx::NttStage& slot = c->ntt_stage[c->ntt_stage_next];
+    for (cudaEvent_t* ev : {&slot.free_ev, &slot.h2d_ev, &slot.comp_ev})
+        if (*ev == nullptr) ZK_TRY_CUDA(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
+    const size_t need = n * 32;
+    if (slot.bytes < need) {
+        if (slot.dev != nullptr) {
+            ZK_TRY_CUDA(cudaEventSynchronize(slot.free_ev));
+            cudaFree(slot.dev);
+            slot.dev = nullptr;
+            slot.bytes = 0;
+        }
+        void* p = nullptr;
+        if (cudaMalloc(&p, need) != cudaSuccess) {
+            cudaGetLastError();
+            zk::set_error("zk_ntt_host_submit: device memory exhausted for the staging buffer");
+            return ZK_ENOMEM;
+        }
+        slot.dev = p;
+        slot.bytes = need;
+        slot.used = false;
+    }
+    c->ntt_stage_next ^= 1;
+    std::unique_ptr<zk_fence> f(new zk_fence());
+    f->device = c->device;
+    ZK_TRY_CUDA(cudaEventCreateWithFlags(&f->ev, cudaEventDisableTiming));
+    auto* buf = static_cast<zk::fe*>(slot.dev);
+    // input copy (after the buffer's previous output copy), transform in place with the
+    // Montgomery conversions on either side, output copy
+    cudaError_t e = slot.used ? cudaStreamWaitEvent(c->copy_stream, slot.free_ev, 0) : cudaSuccess;
+    if (e == cudaSuccess && valid)
+        e = cudaMemcpyAsync(buf, in_host, valid * 32, cudaMemcpyHostToDevice, c->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(slot.h2d_ev, c->copy_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, slot.h2d_ev, 0);
+    int rc = ZK_OK;
+    if (e == cudaSuccess) {
+        static const uint8_t one[32] = {1};
+        rc = zk::convert<zk::FrP, 1>(c, buf, buf, valid);
+        if (rc == ZK_OK) rc = zk::ntt_run(c, mode, buf, buf, valid, log_n, omega, shift ? shift : one);
+        if (rc == ZK_OK) rc = zk::convert<zk::FrP, 0>(c, buf, buf, n);
+        e = cudaEventRecord(slot.comp_ev, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->d2h_stream, slot.comp_ev, 0);
+    if (e == cudaSuccess && rc == ZK_OK)
+        e = cudaMemcpyAsync(out_host, buf, n * 32, cudaMemcpyDeviceToHost, c->d2h_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(slot.free_ev, c->d2h_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(f->ev, c->d2h_stream);
+    slot.used = true;
+    if (e != cudaSuccess) {
+        zk::set_error(std::string("zk_ntt_host_submit: ") + cudaGetErrorString(e));
+        cudaEventDestroy(f->ev);
+        return ZK_ECUDA;
+    }
+    if (rc != ZK_OK) {
+        cudaEventDestroy(f->ev);
+        return rc;
+    }
+    *done = f.release();
     return ZK_OK;
 }
 

@@ -126,6 +126,18 @@ struct Ctx {
     };
     HostStage host_stage[2];
     int host_stage_next = 0;
+    // zk_ntt_host_submit: the same for host-buffer NTTs (input copy on copy_stream, the
+    // transform on the context stream, the output copy on d2h_stream); h2d_ev / comp_ev
+    // order the three, free_ev releases the buffer after its output copy
+    struct NttStage {
+        void* dev = nullptr;
+        size_t bytes = 0;
+        cudaEvent_t free_ev = nullptr, h2d_ev = nullptr, comp_ev = nullptr;
+        bool used = false;
+    };
+    NttStage ntt_stage[2];
+    int ntt_stage_next = 0;
+    cudaStream_t d2h_stream = nullptr;
     // MSM batches spread their pipelines over the context stream and these (fork / join
     // events); created on first use
     std::vector<cudaStream_t> side_streams;
