@@ -1063,16 +1063,21 @@ def run_gpu_serve(ctx, args, requests: int = 200, grid=tuple(x / 2 for x in rang
         sizes[i] = m
     setup_s = time.perf_counter() - t0
     prover = G.Prover(ctx)
-    svc = serve.ProverService(prover, keys, wits, budget_bytes=48 << 30, max_batch=64, slots=3)
+    # at most 24 requests per group: a burst spreads over the slots, so one group's latency-bound
+    # reductions overlap another's accumulation (128-request burst: 577 proofs/s at 24, 549 at 64)
+    svc = serve.ProverService(prover, keys, wits, budget_bytes=48 << 30, max_batch=24, slots=3)
     weights = [0.5] + [1.0] * (len(grid) - 2) + [0.5]
     svc.warm()
     # closed-loop capacity: a burst of requests all present at t = 0
-    closed = serve.poisson_trace(1e9, 64, list(keys), seed=2, weights=weights)
+    closed = serve.poisson_trace(1e9, 128, list(keys), seed=2, weights=weights)
     cap = {}
     for mode, tr in (("continuous", closed), ("batch", closed), ("plain", closed)):
-        t1 = time.perf_counter()
-        res = svc.run(tr, mode)
-        cap[mode] = len(tr) / (time.perf_counter() - t1)
+        runs = []
+        for _ in range(3):  # the median of three runs of the burst
+            t1 = time.perf_counter()
+            res = svc.run(tr, mode)
+            runs.append(len(tr) / (time.perf_counter() - t1))
+        cap[mode] = statistics.median(runs)
         if mode == "continuous":
             cap_proofs = res.proofs
     # The accumulation floor of the burst: its CSR entries (fixed-base mode: ceil(255 / c)

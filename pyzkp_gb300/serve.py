@@ -114,7 +114,7 @@ class ProverService:
     """Proves arrival traces for resident keys under a device-memory budget (module docstring)."""
 
     def __init__(self, prover: G.Prover, keys: dict, witnesses: dict, budget_bytes: int = 32 << 30,
-                 max_batch: int = 64, slots: int = 3, small_constraints: int = 1 << 14,
+                 max_batch: int = 24, slots: int = 3, small_constraints: int = 1 << 14,
                  contexts: Optional[list] = None, pin_witnesses: bool = True) -> None:
         """``contexts``: the slot contexts to use (default: created on first use, slot 0 at the
         most urgent stream priority); ``pin_witnesses``: keep page-locked copies of the
