@@ -363,10 +363,11 @@ def run_gpu(args, ranks: Ranks) -> dict:
         "vs_baseline": None,
         "dtype": "u32 limbs (exact BN254 Fq/Fr Montgomery arithmetic)",
         "data": "synthetic: seeded PCG64 scalars uniform in [0,r); bases [k_i]G, k_i uniform in [1,r)",
-        "config": {"workload": f"G1 MSM n=2^{log_n} (uniform scalars, resident bases) + Fr NTT n=2^20 / 2^22",
-                   "n": n, "seed": seed, "window_bits": stats["window_bits"], "windows": stats["windows"],
-                   "csr_entries": entries, "l2": "flushed (256 MB memset) before every timed step",
-                   "parallelism": f"replicas x{ranks.world}"},
+        "config": {"workload": f"G1 MSM n=2^{log_n} (uniform scalars) + Fr NTT n=2^20", "n": n, "seed": seed,
+                   "window_bits": stats["window_bits"], "l2": "flushed (256 MB memset) before every timed step"},
+        "config_detail": {"bases": "resident (uploaded once, GLV images built on the device)",
+                          "windows": stats["windows"], "csr_entries": entries, "ntt_sizes": [20, 22],
+                          "parallelism": f"replicas x{ranks.world}"},
         "msm_result": [hex(res[0]), hex(res[1])] if res else None,
         "e2e": {"value": round(e2e_stream_mpts, 3), "unit": "Mpts/s", "h2d_bytes_per_step": n * 96,
                 "d2h_bytes_per_step": 64 + 4, "result_ok": e2e_stream_ok,
