@@ -15,6 +15,7 @@ struct Field {
     uint64_t inv;  // -p^-1 mod 2^64
     uint64_t one[4];
     uint64_t r2[4];
+    uint64_t r3[4];  // R^3 mod p (turns a plain inverse of a Montgomery form into a Montgomery form)
 };
 
 struct F4 {
@@ -127,6 +128,8 @@ inline Field make_field(const uint64_t p[4]) {
     std::memcpy(F.one, t.v, 32);
     for (int i = 0; i < 256; i++) t = add(F, t, t);
     std::memcpy(F.r2, t.v, 32);
+    t = mul(F, t, t);  // R^2 R^2 / R
+    std::memcpy(F.r3, t.v, 32);
     return F;
 }
 
@@ -181,7 +184,60 @@ inline F4 pow_u64(const Field& F, const F4& a, uint64_t e) {
     return pow(F, a, ee);
 }
 
+inline bool is_one4(const uint64_t a[4]) { return a[0] == 1 && (a[1] | a[2] | a[3]) == 0; }
+
+// a >> 1 with `top` shifted into bit 255
+inline void shr1(uint64_t a[4], uint64_t top) {
+    a[0] = (a[0] >> 1) | (a[1] << 63);
+    a[1] = (a[1] >> 1) | (a[2] << 63);
+    a[2] = (a[2] >> 1) | (a[3] << 63);
+    a[3] = (a[3] >> 1) | (top << 63);
+}
+
+// x / 2 mod p for x < p (x + p < 2^255: no carry out of the 4 limbs)
+inline void half_mod(const Field& F, uint64_t x[4]) {
+    if (x[0] & 1) {
+        add4(x, x, F.p);
+        shr1(x, 0);
+    } else {
+        shr1(x, 0);
+    }
+}
+
+// Inverse of a Montgomery form a = A R: the Montgomery form R / A = R^2 a^-1 of A^-1 (zero for
+// zero). Binary extended Euclid on (a, p) with x1 a = u, x2 a = v (mod p) kept throughout;
+// variable time (the inputs are public values: MSM results, roots of unity, sizes).
 inline F4 inv(const Field& F, const F4& a) {
+    uint64_t u[4], v[4], x1[4] = {1, 0, 0, 0}, x2[4] = {0, 0, 0, 0};
+    std::memcpy(u, a.v, 32);
+    while (geq(u, F.p)) sub4(u, u, F.p);
+    if ((u[0] | u[1] | u[2] | u[3]) == 0) return F4{{0, 0, 0, 0}};
+    std::memcpy(v, F.p, 32);
+    while (!is_one4(u) && !is_one4(v)) {
+        while (!(u[0] & 1)) {
+            shr1(u, 0);
+            half_mod(F, x1);
+        }
+        while (!(v[0] & 1)) {
+            shr1(v, 0);
+            half_mod(F, x2);
+        }
+        if (geq(u, v)) {
+            sub4(u, u, v);
+            if (sub4(x1, x1, x2)) add4(x1, x1, F.p);
+        } else {
+            sub4(v, v, u);
+            if (sub4(x2, x2, x1)) add4(x2, x2, F.p);
+        }
+    }
+    F4 r, r3;
+    std::memcpy(r.v, is_one4(u) ? x1 : x2, 32);
+    std::memcpy(r3.v, F.r3, 32);
+    return mul(F, r, r3);  // a^-1 R^3 / R
+}
+
+// Fermat form of the same inverse, a^(p-2) (checks the binary form)
+inline F4 inv_pow(const Field& F, const F4& a) {
     uint64_t e[4];
     const uint64_t two[4] = {2, 0, 0, 0};
     sub4(e, F.p, two);

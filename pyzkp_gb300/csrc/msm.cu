@@ -1737,9 +1737,25 @@ class HostPool {
     }
 
     void run(size_t count, const std::function<void(size_t)>& fn) {
-        if (count == 0) return;
-        if (count == 1 || workers_ == 0 || count > kMaxTasks) {
+        if (count == 1 || workers_ == 0) {  // no helper: no shared state, no lock
             for (size_t i = 0; i < count; i++) fn(i);
+            return;
+        }
+        run_with(count, fn, [] {});
+    }
+
+    // run() in which the calling thread first executes own(): own() may take tasks itself
+    // through run_one() (the same ticket, so in the same index order as the workers), e.g.
+    // to consume results in order and compute whichever no worker has taken yet.
+    template <class Own>
+    void run_with(size_t count, const std::function<void(size_t)>& fn, Own&& own, size_t max_helpers = ~size_t(0)) {
+        if (count > kMaxTasks) {
+            for (size_t i = 0; i < count; i++) fn(i);
+            own();
+            return;
+        }
+        if (count == 0) {
+            own();
             return;
         }
         std::lock_guard<std::mutex> serial(run_mu_);
@@ -1747,12 +1763,20 @@ class HostPool {
         fn_ = &fn;
         done_.store(0, std::memory_order_relaxed);
         ticket_.store(gen_ << 48 | (uint64_t)count << 24, std::memory_order_release);
-        {
-            std::lock_guard<std::mutex> g(mu_);
-            wake_++;
+        const size_t helpers = std::min(std::min(count - 1, workers_), max_helpers);
+        if (helpers > 0) {
+            // the caller wakes up to kFanout workers and each woken worker up to kFanout more
+            // (a wake-up is a system call of a few microseconds: a tree of them instead of a
+            // row on the caller)
+            const size_t first = std::min(helpers, kFanout);
+            pending_.store((int64_t)(helpers - first), std::memory_order_relaxed);
+            {
+                std::lock_guard<std::mutex> g(mu_);
+                wake_++;
+            }
+            for (size_t i = 0; i < first; i++) cv_.notify_one();
         }
-        const size_t helpers = std::min(count - 1, workers_);
-        for (size_t i = 0; i < helpers; i++) cv_.notify_one();
+        own();
         work();
         // the tasks still running were claimed by awake workers; the wait re-checks every
         // millisecond, so even a lost wakeup of the condition variable only costs that much
@@ -1760,6 +1784,22 @@ class HostPool {
         while (done_.load(std::memory_order_acquire) < count)
             done_cv_.wait_for(g, std::chrono::milliseconds(1),
                               [&] { return done_.load(std::memory_order_acquire) >= count; });
+    }
+
+    // Claim and run the next task of the run in progress; false if none is left.
+    bool run_one() {
+        for (;;) {
+            uint64_t cur = ticket_.load(std::memory_order_acquire);
+            const uint64_t count = (cur >> 24) & kMaxTasks, i = cur & kMaxTasks;
+            if (i >= count) return false;
+            if (!ticket_.compare_exchange_weak(cur, cur + 1, std::memory_order_acq_rel)) continue;
+            (*fn_)(i);
+            if (done_.fetch_add(1, std::memory_order_acq_rel) + 1 == count) {
+                std::lock_guard<std::mutex> g(mu_);
+                done_cv_.notify_all();
+            }
+            return true;
+        }
     }
 
    private:
@@ -1779,6 +1819,8 @@ class HostPool {
                 cv_.wait(g, [&] { return wake_ != seen; });
                 seen = wake_;
             }
+            for (size_t i = 0; i < kFanout; i++)
+                if (pending_.fetch_sub(1, std::memory_order_acq_rel) > 0) cv_.notify_one();
             work();
         }
     }
@@ -1786,16 +1828,7 @@ class HostPool {
     // Claim and run tasks while the ticket has some left. A successful claim of task i means
     // the run that published the ticket is still waiting for task i, so fn_ is its function.
     void work() {
-        for (;;) {
-            uint64_t cur = ticket_.load(std::memory_order_acquire);
-            const uint64_t count = (cur >> 24) & kMaxTasks, i = cur & kMaxTasks;
-            if (i >= count) return;
-            if (!ticket_.compare_exchange_weak(cur, cur + 1, std::memory_order_acq_rel)) continue;
-            (*fn_)(i);
-            if (done_.fetch_add(1, std::memory_order_acq_rel) + 1 == count) {
-                std::lock_guard<std::mutex> g(mu_);
-                done_cv_.notify_all();
-            }
+        while (run_one()) {
         }
     }
 
@@ -1805,6 +1838,8 @@ class HostPool {
     const std::function<void(size_t)>* fn_ = nullptr;
     std::atomic<uint64_t> ticket_{0};
     std::atomic<size_t> done_{0};
+    std::atomic<int64_t> pending_{0};  // wake-ups the woken workers still have to pass on
+    static constexpr size_t kFanout = 2;
     uint64_t wake_ = 0;  // under mu_
     uint64_t gen_ = 0;   // under run_mu_
 };
@@ -1836,15 +1871,15 @@ static zkh::XyzzT<typename HostOf<C>::T> window_sum(const MsmPipeT<C>& p, uint32
 }
 
 // total = sum_w 2^(c w) S_w by Horner over the windows (one set in fixed-base mode, where
-// the window shifts are already in the bases), as canonical affine bytes.
-template <class C>
-static void horner_out(const MsmPipeT<C>& p, const zkh::XyzzT<typename HostOf<C>::T>* sw, uint8_t* out_xy,
-                       int32_t* out_is_inf) {
+// the window shifts are already in the bases), as canonical affine bytes; get(w) yields S_w,
+// asked for from the top window down.
+template <class C, class Get>
+static void horner_out(const MsmPipeT<C>& p, Get&& get, uint8_t* out_xy, int32_t* out_is_inf) {
     using H = typename HostOf<C>::T;
     zkh::XyzzT<H> total = zkh::xyzz_inf<H>();
     for (int w = (int)p.sh.Wr - 1; w >= 0; w--) {
         total = host_dbl_n(total, p.sh.c);
-        total = zkh::xyzz_add(total, sw[w]);
+        total = zkh::xyzz_add(total, get((uint32_t)w));
     }
     H x, y;
     *out_is_inf = zkh::xyzz_to_affine_canonical(total, &x, &y) ? 1 : 0;
@@ -1852,8 +1887,14 @@ static void horner_out(const MsmPipeT<C>& p, const zkh::XyzzT<typename HostOf<C>
     std::memcpy(out_xy + sizeof(H), &y, sizeof(H));
 }
 
+#ifndef ZK_COMBINE_HELPERS
+#define ZK_COMBINE_HELPERS 4
+#endif
+static constexpr size_t kCombineHelpers = ZK_COMBINE_HELPERS;  // pool workers of a one-instance combine
+
 // Combine every instance of `pipes`: the window sums of all instances in parallel on the
-// host pool, then each instance's Horner (in parallel across instances).
+// host pool, then each instance's Horner (in parallel across instances); a single instance
+// overlaps its Horner with its window sums.
 template <class C>
 static void combine_all(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, uint8_t* out_xy, int32_t* out_is_inf,
                         bool record = true) {
@@ -1876,15 +1917,42 @@ static void combine_all(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, uint8_t* 
     }
     std::vector<zkh::XyzzT<H>> sums(win.size());
     HostPool& pool = HostPool::get();
-    pool.run(win.size(), [&](size_t t) {
-        const Inst& in = insts[win[t].first];
-        sums[t] = window_sum<C>(pipes[in.q], in.k, win[t].second);
-    });
-    pool.run(insts.size(), [&](size_t t) {
-        const Inst& in = insts[t];
-        const size_t o = pipes[in.q].out_index[in.k];
-        horner_out<C>(pipes[in.q], sums.data() + in.first, out_xy + kOut * o, out_is_inf + o);
-    });
+    if (insts.size() == 1 && win.size() > 1) {
+        // One instance (the latency case): the calling thread runs the Horner from the top
+        // window down while woken workers compute the lower window sums; task t is window
+        // W-1-t, so tasks are claimed in the order the Horner consumes them, and the caller
+        // computes any window no worker has taken yet.
+        const MsmPipeT<C>& p = pipes[insts[0].q];
+        const uint32_t k = insts[0].k, W = (uint32_t)win.size();
+        std::unique_ptr<std::atomic<uint32_t>[]> ready(new std::atomic<uint32_t>[W]());
+        const std::function<void(size_t)> task = [&](size_t t) {
+            sums[t] = window_sum<C>(p, k, W - 1 - (uint32_t)t);
+            ready[t].store(1, std::memory_order_release);
+        };
+        const size_t o = p.out_index[k];
+        // a few helpers keep ahead of the Horner (a window sum costs about as much as 2-3
+        // windows of its doublings)
+        pool.run_with(W, task, [&] {
+            horner_out<C>(p, [&](uint32_t w) -> const zkh::XyzzT<H>& {
+                const uint32_t t = W - 1 - w;
+                while (!ready[t].load(std::memory_order_acquire))
+                    if (!pool.run_one()) std::this_thread::yield();  // a worker is on it
+                return sums[t];
+            }, out_xy + kOut * o, out_is_inf + o);
+        }, kCombineHelpers);
+    } else {
+        pool.run(win.size(), [&](size_t t) {
+            const Inst& in = insts[win[t].first];
+            sums[t] = window_sum<C>(pipes[in.q], in.k, win[t].second);
+        });
+        pool.run(insts.size(), [&](size_t t) {
+            const Inst& in = insts[t];
+            const size_t o = pipes[in.q].out_index[in.k];
+            const zkh::XyzzT<H>* sw = sums.data() + in.first;
+            horner_out<C>(pipes[in.q], [sw](uint32_t w) -> const zkh::XyzzT<H>& { return sw[w]; },
+                          out_xy + kOut * o, out_is_inf + o);
+        });
+    }
     if (!record) return;  // a worker thread of an asynchronous batch leaves the context's tables alone
     prof_host(c, "msm_host_combine",
               std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
