@@ -73,6 +73,16 @@ static constexpr uint32_t kBlockG = ZK_MSM_BLOCKG;    // buckets per block in th
 #define ZK_MSM_BLOCKG2 4
 #endif
 static constexpr uint32_t kBlockG2 = ZK_MSM_BLOCKG2;  // level-1 blocks per level-2 block
+// Straddling buckets over more than kFixupMax + 1 segments go to the long-bucket fixup (a
+// CTA tree per bucket); small pipelines, latency-bound, send them there from kFixupMaxSmall
+// + 2 segments on (a tree of log2(pieces) additions instead of a chain). Measured on GB300
+// (single MSMs, 4 against 8): 2^12 0.390 -> 0.371 ms, 2^16 0.767 -> 0.753 ms, 2^14 the same.
+static constexpr uint32_t kFixupMax = 8;
+#ifndef ZK_FIXUP_MAX_SMALL
+#define ZK_FIXUP_MAX_SMALL 4
+#endif
+static constexpr uint32_t kFixupMaxSmall = ZK_FIXUP_MAX_SMALL;
+static constexpr uint32_t kSmallBucketsPerSm = 512;  // "small": fewer buckets than this per SM
 
 struct MsmShape {
     uint32_t c;        // window bits
@@ -92,6 +102,7 @@ struct MsmShape {
     uint32_t glv;      // 1: each scalar is split k = k1 + k2 lambda (halves < 2^127, see glv_split);
                        // the phi(P) half of every instance's bases sits at bases + stride
     uint32_t seg;      // CSR entries per thread in the accumulation (kSegment, less for small pipelines)
+    uint32_t fixmax;   // a straddling bucket over more than fixmax + 1 segments goes to the long-bucket fixup
 };
 
 // One MSM of a pipeline: sum_{i < n} scalars[i] * bases[i] (fixed-base mode: bases holds the
@@ -126,6 +137,7 @@ static MsmShape make_shape(uint32_t c, bool glv = false) {
     s.B = 1u << (c - 1);
     shape_blocks(s, kBlockG);
     s.seg = kSegment;
+    s.fixmax = kFixupMax;
     s.shared = 0;
     s.Wr = s.W;
     s.inst = 1;
@@ -818,9 +830,8 @@ __global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_merge_kernel(const 
 // Fixup instead of merge rounds (when buckets are short): a bucket k whose entries
 // [row_ptr[k], row_ptr[k+1]) span units u0 < u1 left its pieces in slot 1 of unit u0 (the
 // bucket continues past the segment) and in slot 0 of every unit u0 < u <= u1 (the bucket
-// began before the segment). One thread per bucket adds up to kFixupMax + 1 pieces; longer
-// buckets are listed for msm_fixup_long_kernel, one CTA each.
-static constexpr uint32_t kFixupMax = 8;
+// began before the segment). One thread per bucket adds up to sh.fixmax + 1 pieces; longer
+// buckets are listed for msm_fixup_long_kernel (a CTA each).
 #ifndef ZK_FIXUP_DENSITY
 // measured on GB300: 2^20 plain (32 entries per bucket) fixup 0.32 vs rounds 0.48 ms; 2^20 GLV
 // (64) fixup 0.27 vs rounds 0.48 ms; 2^22 GLV (256) rounds 1.0 vs fixup 6.8 ms
@@ -829,14 +840,14 @@ static constexpr uint32_t kFixupMax = 8;
 static constexpr uint64_t kFixupDensity = ZK_FIXUP_DENSITY;  // CSR entries per bucket up to which the fixup is used
 
 template <class C, bool kL2>
-__device__ __forceinline__ void fixup_bucket(const uint32_t* __restrict__ row_ptr, uint32_t seg,
+__device__ __forceinline__ void fixup_bucket(const uint32_t* __restrict__ row_ptr, uint32_t seg, uint32_t fixmax,
                                              const typename C::P* slot_pts, typename C::P* buckets,
                                              uint32_t* long_list, uint32_t* long_count, uint32_t k) {
     const uint32_t b0 = row_ptr[k], b1 = row_ptr[k + 1];
     if (b1 == b0) return;
     const uint32_t u0 = b0 / seg, u1 = (b1 - 1) / seg;
     if (u0 == u1) return;  // final already (written by the accumulation)
-    if (u1 - u0 > kFixupMax) {
+    if (u1 - u0 > fixmax) {
         long_list[atomicAdd(long_count, 1u)] = k;
         return;
     }
@@ -847,17 +858,19 @@ __device__ __forceinline__ void fixup_bucket(const uint32_t* __restrict__ row_pt
 
 template <class C>
 __global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_fixup_kernel(const uint32_t* __restrict__ row_ptr, uint32_t nbuckets,
-                                                        uint32_t seg, const typename C::P* __restrict__ slot_pts,
+                                                        uint32_t seg, uint32_t fixmax,
+                                                        const typename C::P* __restrict__ slot_pts,
                                                         typename C::P* __restrict__ buckets,
                                                         uint32_t* __restrict__ long_list,
                                                         uint32_t* __restrict__ long_count) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nbuckets) return;
-    fixup_bucket<C, false>(row_ptr, seg, slot_pts, buckets, long_list, long_count, k);
+    fixup_bucket<C, false>(row_ptr, seg, fixmax, slot_pts, buckets, long_list, long_count, k);
 }
 
 // One CTA per listed bucket (items item0, item0 + stride, ...): strided partial sums, then a
-// shared-memory tree over `red` (blockDim points).
+// shared-memory tree over `red` (blockDim points). (One warp per bucket with a shuffle tree
+// measured slower: 2^14 single MSM 0.127 against 0.059 ms in this kernel.)
 template <class C, bool kL2>
 __device__ __forceinline__ void fixup_long_cta(const uint32_t* __restrict__ row_ptr, uint32_t seg,
                                                const typename C::P* slot_pts, typename C::P* buckets,
@@ -1175,7 +1188,8 @@ __global__ void __launch_bounds__(kMsmQThreads, 2) msm_queue_kernel(const MsmQPi
                 break;
             case kQFix:
                 if (i < q.nbuckets)
-                    fixup_bucket<C, true>(q.row_ptr, q.sh.seg, q.slot_pts[0], q.buckets, q.long_list, q.long_count, i);
+                    fixup_bucket<C, true>(q.row_ptr, q.sh.seg, q.sh.fixmax, q.slot_pts[0], q.buckets, q.long_list,
+                                          q.long_count, i);
                 break;
             case kQFixLong:
                 fixup_long_cta<C, true>(q.row_ptr, q.sh.seg, q.slot_pts[0], q.buckets, q.long_list, q.long_count, red,
@@ -1427,6 +1441,7 @@ static int pipe_init(MsmPipeT<C>& p, uint32_t c, bool fixed, bool glv, const std
     while (g > 2 && p.nbuckets / g < min_threads) g /= 2;
     while (g2 > 2 && p.nbuckets / g / g2 < min_threads / 2) g2 /= 2;
     shape_blocks(p.sh, g, g2);
+    if (p.nbuckets < (uint64_t)num_sms * kSmallBucketsPerSm) p.sh.fixmax = kFixupMaxSmall;
     p.units = (uint32_t)((p.max_entries + p.sh.seg - 1) / p.sh.seg);
     // tiled sort when a set's counters fit shared memory: set s = k Wr + w holds n_k halves
     // entries per window (n_k W in the fixed-base mode's one set), cut into tiles of at least
@@ -1483,7 +1498,7 @@ static size_t pipe_layout(MsmPipeT<C>& p, char* base) {
     p.slot_pts_a = reinterpret_cast<P*>(take((size_t)2 * p.units * sizeof(P)));
     p.slot_keys_b = reinterpret_cast<uint32_t*>(take(2 * first_out * 4));
     p.slot_pts_b = reinterpret_cast<P*>(take(2 * first_out * sizeof(P)));
-    p.long_list = reinterpret_cast<uint32_t*>(take(((size_t)p.units / kFixupMax + 2) * 4));
+    p.long_list = reinterpret_cast<uint32_t*>(take(((size_t)p.units / sh.fixmax + 2) * 4));
     p.long_count = reinterpret_cast<uint32_t*>(take(4));
     p.buckets = reinterpret_cast<P*>(take(p.nbuckets * sizeof(P)));
     p.Yb = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G * sizeof(P)));
@@ -1657,7 +1672,7 @@ static int pipe_enqueue_reduce(Ctx* c, MsmPipeT<C>& p) {
     if (p.max_entries <= (uint64_t)p.nbuckets * kFixupDensity) {
         ZK_TRY_CUDA(cudaMemsetAsync(p.long_count, 0, 4, st));
         ZK_LAUNCH(c, "msm_fixup", msm_fixup_kernel<C>, (unsigned)((p.nbuckets + 127) / 128), 128, 0, p.row_ptr,
-                  (uint32_t)p.nbuckets, sh.seg, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
+                  (uint32_t)p.nbuckets, sh.seg, sh.fixmax, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
         ZK_TRY_CUDA(cudaGetLastError());
         ZK_LAUNCH(c, "msm_fixup_long", msm_fixup_long_kernel<C>, (unsigned)(c->num_sms * 2), C::kFixupLongThreads, 0,
                   p.row_ptr, sh.seg, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
