@@ -174,11 +174,13 @@ int zk_ntt(zk_ctx *ctx, int mode, void *out_dev, const void *in_dev, size_t in_l
  * (runtime/kernels/cpu/kernels.py:175-250). Returns once the work is enqueued, with a fence
  * (zk_fence_wait, then zk_fence_destroy) that passes when out_host is written; the host
  * buffers must stay valid (and in_host unchanged) until then -- pinned memory keeps the
- * copies asynchronous. The input copy, the transform (with the Montgomery conversions on
- * either side) and the output copy run on three streams, and the context uses two device
- * staging buffers in turn, so a stream of calls overlaps one call's output copy, the next
- * call's input copy and a transform (the host link carries both directions at once). shift
- * may be NULL (1). Errors as zk_ntt. No reference counterpart for the asynchrony.
+ * copies asynchronous. The input copy, the transform (run on the canonical values
+ * directly: it is linear and its constants are Montgomery forms, so no conversion pass is
+ * needed; inputs of any 256 bits are reduced mod r) and the output copy run on three
+ * streams, and the context uses three device staging buffers in turn, so a stream of calls
+ * overlaps one call's output copy, the next call's input copy and a transform (the host
+ * link carries both directions at once). shift may be NULL (1). Errors as zk_ntt. No
+ * reference counterpart for the asynchrony.
  */
 int zk_ntt_host_submit(zk_ctx *ctx, int mode, void *out_host, const void *in_host, size_t in_len, uint32_t log_n,
                        const uint8_t omega[32], const uint8_t shift[32], zk_fence **done);

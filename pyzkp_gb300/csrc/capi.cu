@@ -1202,13 +1202,13 @@ int zk_ntt_host_submit(zk_ctx* ctx, int mode, void* out_host, const void* in_hos
         slot.bytes = need;
         slot.used = false;
     }
-    c->ntt_stage_next ^= 1;
+    c->ntt_stage_next = (c->ntt_stage_next + 1) % Ctx::kNttStages;
     std::unique_ptr<zk_fence> f(new zk_fence());
     f->device = c->device;
     ZK_TRY_CUDA(cudaEventCreateWithFlags(&f->ev, cudaEventDisableTiming));
     auto* buf = static_cast<zk::fe*>(slot.dev);
-    // input copy (after the buffer's previous output copy), transform in place with the
-    // Montgomery conversions on either side, output copy
+    // input copy (after the buffer's previous output copy), transform in place on the
+    // canonical values (no Montgomery conversion: ntt_run's canon_io), output copy
     cudaError_t e = slot.used ? cudaStreamWaitEvent(c->copy_stream, slot.free_ev, 0) : cudaSuccess;
     if (e == cudaSuccess && valid)
         e = cudaMemcpyAsync(buf, in_host, valid * 32, cudaMemcpyHostToDevice, c->copy_stream);
@@ -1217,9 +1217,7 @@ int zk_ntt_host_submit(zk_ctx* ctx, int mode, void* out_host, const void* in_hos
     int rc = ZK_OK;
     if (e == cudaSuccess) {
         static const uint8_t one[32] = {1};
-        rc = zk::convert<zk::FrP, 1>(c, buf, buf, valid);
-        if (rc == ZK_OK) rc = zk::ntt_run(c, mode, buf, buf, valid, log_n, omega, shift ? shift : one);
-        if (rc == ZK_OK) rc = zk::convert<zk::FrP, 0>(c, buf, buf, n);
+        rc = zk::ntt_run(c, mode, buf, buf, valid, log_n, omega, shift ? shift : one, /*canon_io=*/true);
         e = cudaEventRecord(slot.comp_ev, c->stream);
     }
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->d2h_stream, slot.comp_ev, 0);

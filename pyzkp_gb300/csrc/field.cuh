@@ -158,6 +158,38 @@ __device__ __forceinline__ fe fe_reduce_2p(const fe& t) {
     return r;
 }
 
+// limb i of 4p (4p < 2^256 for both moduli)
+template <class F>
+__host__ __device__ constexpr uint32_t p4_limb(int i) {
+    return (F::P(i) << 2) | (i ? (F::P(i - 1) >> 30) : 0u);
+}
+
+// r = t - 4p if t >= 4p else t, for any t < 2^256: r < 4p (2^256 < 6p), so fe_reduce_2p
+// after it brings any 256-bit value into [0, 2p).
+template <class F>
+__device__ __forceinline__ fe fe_reduce_4p(const fe& t) {
+    fe s;
+    uint32_t borrow;
+    asm("sub.cc.u32  %0, %9, %17;\n\t"
+        "subc.cc.u32 %1, %10, %18;\n\t"
+        "subc.cc.u32 %2, %11, %19;\n\t"
+        "subc.cc.u32 %3, %12, %20;\n\t"
+        "subc.cc.u32 %4, %13, %21;\n\t"
+        "subc.cc.u32 %5, %14, %22;\n\t"
+        "subc.cc.u32 %6, %15, %23;\n\t"
+        "subc.cc.u32 %7, %16, %24;\n\t"
+        "subc.u32    %8, 0, 0;"
+        : "=r"(s.v[0]), "=r"(s.v[1]), "=r"(s.v[2]), "=r"(s.v[3]), "=r"(s.v[4]), "=r"(s.v[5]), "=r"(s.v[6]),
+          "=r"(s.v[7]), "=r"(borrow)
+        : "r"(t.v[0]), "r"(t.v[1]), "r"(t.v[2]), "r"(t.v[3]), "r"(t.v[4]), "r"(t.v[5]), "r"(t.v[6]), "r"(t.v[7]),
+          "n"(p4_limb<F>(0)), "n"(p4_limb<F>(1)), "n"(p4_limb<F>(2)), "n"(p4_limb<F>(3)), "n"(p4_limb<F>(4)),
+          "n"(p4_limb<F>(5)), "n"(p4_limb<F>(6)), "n"(p4_limb<F>(7)));
+    fe r;
+#pragma unroll
+    for (int i = 0; i < 8; i++) r.v[i] = borrow ? t.v[i] : s.v[i];
+    return r;
+}
+
 // r = t - p if t >= p else t, for t < 2p (< 2^255).
 template <class F>
 __device__ __forceinline__ fe fe_reduce_once(const fe& t) {

@@ -66,6 +66,8 @@ struct NttPassParams {
     uint32_t log_l;
     uint32_t s_bits;
     uint32_t last;  // 1 on the last pass: outputs reduced to [0, r)
+    uint32_t reduce_in;  // 1 on the first pass of a transform of canonical values: inputs of any
+                         // 256 bits brought into [0, 2r) as they are loaded
 };
 
 // Butterflies, twiddles and scales run on lazy Fr values in [0, 2r) (FrLazyP); inputs are
@@ -123,6 +125,7 @@ __device__ __forceinline__ void ntt_pass_body(const NttPassParams& P, uint32_t t
         const uint32_t col = c0 + t;
         const uint32_t g = col + (m << stride_log);
         fe v = g < P.in_len ? (l2_in ? fe_ldcg(P.in + g) : fe_ldg(P.in + g)) : fe_zero();
+        if (P.reduce_in) v = fe_reduce_2p<FrN>(fe_reduce_4p<FrN>(v));
         if (P.pre_lo != nullptr && g < P.in_len) v = fe_mul<FrN>(v, lookup2(P.pre_lo, P.pre_hi, g, P.s_bits));
         if (P.log_l != 0) {
             const uint32_t e = (m * (col & l_mask)) << tw_shift;
@@ -576,7 +579,7 @@ static size_t pass_scratch_elems(const NttPlan* plan, const fe* out, const fe* i
 // passes go to scratch (and, out of place with 3+ passes, alternate with `out` so that
 // one scratch buffer suffices); the last pass writes `out`.
 static void make_passes(const NttPlan* plan, fe* out, const fe* in, uint32_t valid, fe* scratch,
-                        std::vector<PassLaunch>* launches) {
+                        std::vector<PassLaunch>* launches, bool canon_io = false) {
     const uint32_t log_n = plan->log_n;
     const uint64_t n = 1ull << log_n;
     launches->clear();
@@ -594,6 +597,7 @@ static void make_passes(const NttPlan* plan, fe* out, const fe* in, uint32_t val
         P.post_hi = plan->post_hi;
         P.in_len = valid;
         P.last = 1;
+        P.reduce_in = canon_io ? 1u : 0u;
         launches->push_back({P, 1, 32, 2 * 16});
         return;
     }
@@ -621,6 +625,7 @@ static void make_passes(const NttPlan* plan, fe* out, const fe* in, uint32_t val
         P.log_t = lt;
         P.log_l = log_l;
         P.last = remaining == 0 ? 1u : 0u;
+        P.reduce_in = canon_io && p == 0 ? 1u : 0u;
         const uint32_t elems = 1u << (lr + lt);
         const uint32_t threads = elems / 2 < (uint32_t)kNttThreads ? (elems / 2 < 32 ? 32 : elems / 2) : kNttThreads;
         launches->push_back({P, (uint32_t)(n >> (lr + lt)), threads, elems * 32});
@@ -639,8 +644,12 @@ static int check_job(int mode, const fe* out, const fe* in, size_t in_len, uint3
     return ZK_OK;
 }
 
+// canon_io: `in` holds canonical values and `out` receives canonical ones, with no
+// Montgomery conversion: the transform is linear and every constant it multiplies by is a
+// Montgomery form, so running it on x (read as the Montgomery form of x / R) yields the
+// Montgomery form of NTT(x) / R, which is NTT(x) itself.
 int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log_n, const uint8_t omega[32],
-            const uint8_t shift[32]) {
+            const uint8_t shift[32], bool canon_io) {
     int rc = check_job(mode, out, in, in_len, log_n);
     if (rc != ZK_OK) return rc;
     const uint64_t n = 1ull << log_n;
@@ -655,7 +664,7 @@ int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log
     const size_t se = pass_scratch_elems(plan, out, in);
     if (se && (rc = scratch_alloc(c, se * 32, reinterpret_cast<void**>(&scratch))) != ZK_OK) return rc;
     std::vector<PassLaunch> launches;
-    make_passes(plan, out, in, valid, scratch, &launches);
+    make_passes(plan, out, in, valid, scratch, &launches, canon_io);
     for (const PassLaunch& L : launches) {
         ZK_LAUNCH(c, "ntt_pass", ntt_pass_kernel, L.blocks, L.threads, L.smem, L.P);
         ZK_TRY_CUDA(cudaGetLastError());

@@ -128,14 +128,18 @@ struct Ctx {
     int host_stage_next = 0;
     // zk_ntt_host_submit: the same for host-buffer NTTs (input copy on copy_stream, the
     // transform on the context stream, the output copy on d2h_stream); h2d_ev / comp_ev
-    // order the three, free_ev releases the buffer after its output copy
+    // order the three, free_ev releases the buffer after its output copy. Three buffers: a
+    // buffer is held by its input copy, transform and output copy in turn, so with two the
+    // next input copy waited for an output copy and a stream of calls ran below the
+    // transform's rate.
     struct NttStage {
         void* dev = nullptr;
         size_t bytes = 0;
         cudaEvent_t free_ev = nullptr, h2d_ev = nullptr, comp_ev = nullptr;
         bool used = false;
     };
-    NttStage ntt_stage[2];
+    static constexpr int kNttStages = 3;
+    NttStage ntt_stage[kNttStages];
     int ntt_stage_next = 0;
     cudaStream_t d2h_stream = nullptr;
     // MSM batches spread their pipelines over the context stream and these (fork / join
@@ -196,7 +200,7 @@ void scratch_free(Ctx* c, void* p);
 
 // kernels implemented in the .cu files
 int ntt_run(Ctx* c, int mode, fe* out, const fe* in, size_t in_len, uint32_t log_n, const uint8_t omega[32],
-            const uint8_t shift[32]);
+            const uint8_t shift[32], bool canon_io = false);
 int msm_run(Ctx* c, const affine_t* bases, const fe* scalars, size_t n, int scalars_mont, uint32_t window_bits,
             uint8_t out_xy[64], int* out_is_inf, const affine_t* shifted = nullptr, uint32_t shifted_c = 0,
             uint64_t stride = 0, bool glv = false, bool inf_points = true);

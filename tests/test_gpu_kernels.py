@@ -132,7 +132,7 @@ def test_ntt_matches_oracle(gpu_ctx, log_n):
 
 def test_ntt_host_submit_stream_matches_oracle(gpu_ctx):
     """zk_ntt_host_submit: canonical host input -> canonical host output, several calls in
-    flight (two staging buffers in turn, three streams), sizes growing and shrinking, every
+    flight (three staging buffers in turn, three streams), sizes growing and shrinking, every
     mode, a zero-padded input, each result the oracle's."""
     cases = [(12, 0, 4096, 1), (16, 2, 65536, 5), (12, 1, 4096, 1), (20, 3, 1 << 20, 5), (10, 0, 700, 1),
              (16, 0, 50000, 1), (20, 0, 1 << 20, 1), (8, 2, 256, 5)]
@@ -152,6 +152,32 @@ def test_ntt_host_submit_stream_matches_oracle(gpu_ctx):
         f.destroy()
         got = pin_out.array[:n * 32].view("<u8").reshape(n, 4)
         assert (got == exp).all(), n
+        pin_in.free()
+        pin_out.free()
+
+
+def test_ntt_host_submit_reduces_noncanonical_input(gpu_ctx):
+    """zk_ntt_host_submit runs on the canonical values without Montgomery conversions; an
+    input of any 256 bits (r, 2r + 7, 4r + 3, 2^256 - 1, ...) transforms as its value mod r,
+    in every mode, at one and at two passes."""
+    r = synth.FR_MODULUS
+    for lg, mode, shift in ((10, 0, 1), (10, 3, 5), (14, 2, 5), (14, 1, 1)):
+        n = 1 << lg
+        base = synth.limbs_to_ints(synth.fr_uniform(9100 + lg + mode, n))
+        extra = [r, r + 1, 2 * r + 7, 4 * r + 3, 5 * r, (1 << 256) - 1, (1 << 255) + 11]
+        vals = [(v + r * (i % 5)) if (v + r * (i % 5)) < (1 << 256) else v for i, v in enumerate(base)]
+        vals[:len(extra)] = extra
+        raw = synth.ints_to_limbs(vals)
+        canon = synth.ints_to_limbs([v % r for v in vals])
+        pin_in = gpu_ctx.pinned(n * 32)
+        pin_in.array[:n * 32] = raw.view(np.uint8).reshape(-1)
+        pin_out = gpu_ctx.pinned(n * 32)
+        om = O.omega_for_size(n)
+        f = gpu_ctx.ntt_host_submit(mode, pin_out, pin_in, n, lg, om, shift)
+        f.wait()
+        f.destroy()
+        got = pin_out.array[:n * 32].view("<u8").reshape(n, 4)
+        assert (got == O.ntt_op(mode, canon, n, om, shift)).all(), (lg, mode)
         pin_in.free()
         pin_out.free()
 
