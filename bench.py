@@ -1081,7 +1081,7 @@ def run_gpu_serve(ctx, args, requests: int = 200, grid=tuple(x / 2 for x in rang
     setup_s = time.perf_counter() - t0
     prover = G.Prover(ctx)
     # at most 24 requests per group: a burst spreads over the slots, so one group's latency-bound
-    # reductions overlap another's accumulation (128-request burst: 577 proofs/s at 24, 549 at 64)
+    # reductions overlap another's accumulation (on the 128-request burst 24 measured ~5% above 64)
     svc = serve.ProverService(prover, keys, wits, budget_bytes=48 << 30, max_batch=24, slots=3)
     weights = [0.5] + [1.0] * (len(grid) - 2) + [0.5]
     svc.warm()
