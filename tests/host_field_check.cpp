@@ -4,7 +4,9 @@
 // writes, per record, mul(a, b), inv(a) (zero for a == 0), add(a, b), sub(a, b) and
 // to_mont(a) to argv[3]. With argv[1] "g1" a record (k, n) gives the affine canonical
 // coordinates of [2^(n mod 48)] P for P = [k mod 2^64] G1 (XYZZ double-and-add, then n XYZZ
-// doublings, as in the window combination). Built and checked by tests/test_host_field.py.
+// doublings, as in the window combination). With argv[1] "fq2" a record (a0, a1) of
+// canonical Fq values gives (a0 + a1 u)^2 in canonical form by csqr and by cmul (u^2 = -1).
+// Built and checked by tests/test_host_field.py.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -40,9 +42,19 @@ static int curve_mode(const std::vector<zkh::F4>& v, FILE* out) {
     return 0;
 }
 
+static int fq2_mode(const std::vector<zkh::F4>& v, FILE* out) {
+    for (size_t i = 0; i < v.size(); i += 2) {
+        const zkh::F2 a = {zkh::cto_mont(v[i]), zkh::cto_mont(v[i + 1])};
+        const zkh::F2 sq = zkh::cfrom_mont(zkh::csqr(a)), mu = zkh::cfrom_mont(zkh::cmul(a, a));
+        for (const zkh::F4* x : {&sq.c0, &sq.c1, &mu.c0, &mu.c1}) std::fwrite(x->v, 8, 4, out);
+    }
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc != 4) return 2;
     const bool curve = std::strcmp(argv[1], "g1") == 0;
+    const bool fq2 = std::strcmp(argv[1], "fq2") == 0;
     const zkh::Field& F = std::strcmp(argv[1], "fr") == 0 ? zkh::fr() : zkh::fq();
     FILE* in = std::fopen(argv[2], "rb");
     if (!in) return 3;
@@ -53,8 +65,8 @@ int main(int argc, char** argv) {
     if (v.size() % 2) return 4;
     FILE* out = std::fopen(argv[3], "wb");
     if (!out) return 5;
-    if (curve) {
-        const int rc = curve_mode(v, out);
+    if (curve || fq2) {
+        const int rc = curve ? curve_mode(v, out) : fq2_mode(v, out);
         std::fclose(out);
         return rc;
     }

@@ -93,3 +93,24 @@ def test_host_doubling_chain_matches_integers(tmp_path):
     for i, (k, n) in enumerate(recs):
         vals = [int.from_bytes(raw[64 * i + 32 * j:64 * i + 32 * j + 32], "little") for j in range(2)]
         assert vals == list(_affine_mul(k << n, q)), (i, k, n)
+
+
+def test_host_fq2_square_matches_integers(tmp_path):
+    """The host Fq2 square (2 products) against the product a * a and against (a0^2 - a1^2,
+    2 a0 a1) over the integers (u^2 = -1)."""
+    exe = _build(tmp_path)
+    q = MODULI["fq"]
+    rng = random.Random(0xF02)
+    recs = [(0, 0), (1, 0), (0, 1), (q - 1, q - 1), (q - 1, 1)] + [(rng.randrange(q), rng.randrange(q))
+                                                                   for _ in range(500)]
+    src = tmp_path / "in.bin"
+    dst = tmp_path / "out.bin"
+    src.write_bytes(b"".join(a.to_bytes(32, "little") + b.to_bytes(32, "little") for a, b in recs))
+    res = subprocess.run([str(exe), "fq2", str(src), str(dst)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    raw = dst.read_bytes()
+    assert len(raw) == 128 * len(recs)
+    for i, (a0, a1) in enumerate(recs):
+        vals = [int.from_bytes(raw[128 * i + 32 * j:128 * i + 32 * j + 32], "little") for j in range(4)]
+        want = [(a0 * a0 - a1 * a1) % q, 2 * a0 * a1 % q]
+        assert vals[:2] == want and vals[2:] == want, (i, a0, a1)
