@@ -159,14 +159,14 @@ def test_ntt_host_submit_stream_matches_oracle(gpu_ctx):
 def test_ntt_host_submit_reduces_noncanonical_input(gpu_ctx):
     """zk_ntt_host_submit runs on the canonical values without Montgomery conversions; an
     input of any 256 bits (r, 2r + 7, 4r + 3, 2^256 - 1, ...) transforms as its value mod r,
-    in every mode, at one and at two passes."""
+    in every mode, at n = 1 and 2 and at one and two passes."""
     r = synth.FR_MODULUS
-    for lg, mode, shift in ((10, 0, 1), (10, 3, 5), (14, 2, 5), (14, 1, 1)):
+    for lg, mode, shift in ((0, 0, 1), (0, 3, 5), (1, 1, 1), (1, 2, 5), (10, 0, 1), (10, 3, 5), (14, 2, 5), (14, 1, 1)):
         n = 1 << lg
         base = synth.limbs_to_ints(synth.fr_uniform(9100 + lg + mode, n))
         extra = [r, r + 1, 2 * r + 7, 4 * r + 3, 5 * r, (1 << 256) - 1, (1 << 255) + 11]
         vals = [(v + r * (i % 5)) if (v + r * (i % 5)) < (1 << 256) else v for i, v in enumerate(base)]
-        vals[:len(extra)] = extra
+        vals[:min(n, len(extra))] = extra[(lg + mode) % len(extra):][:n] if n < len(extra) else extra
         raw = synth.ints_to_limbs(vals)
         canon = synth.ints_to_limbs([v % r for v in vals])
         pin_in = gpu_ctx.pinned(n * 32)
