@@ -32,7 +32,7 @@ __device__ __forceinline__ fe c_mul_sub(const fe& a, const fe& b, const fe& c, c
     return fe_mul_sub<FqP>(a, b, c, d);
 }
 // zero mod q: the curve formulas keep Fq values lazy in [0, 2q) (field.cuh)
-__device__ __forceinline__ bool c_is_zero(const fe& a) { return fe_is_zero_mod<FqP>(a); }
+__device__ __forceinline__ bool c_is_zero(const fe& a) { return fe_is_zero_mod<FqP, true>(a); }
 __device__ __forceinline__ void c_set_zero(fe& a) { a = fe_zero(); }
 __device__ __forceinline__ void c_set_one(fe& a) { a = fe_one<FqP>(); }
 __device__ __forceinline__ fe c_ldg(const fe* p) { return fe_ldg(p); }
@@ -92,7 +92,9 @@ __device__ __forceinline__ fq2 c_sqr(const fq2& a) {
     const fe t1 = c_mul(a.c0, a.c1);
     return {t0, c_dbl(t1)};
 }
-__device__ __forceinline__ bool c_is_zero(const fq2& a) { return c_is_zero(a.c0) && c_is_zero(a.c1); }
+__device__ __forceinline__ bool c_is_zero(const fq2& a) {
+    return fe_is_zero_mod<FqP>(a.c0) && fe_is_zero_mod<FqP>(a.c1);
+}
 __device__ __forceinline__ void c_set_zero(fq2& a) {
     a.c0 = fe_zero();
     a.c1 = fe_zero();

@@ -117,9 +117,16 @@ __host__ __device__ constexpr uint32_t mod_limb(int i) {
     return F::LAZY ? p2_limb<F>(i) : F::P(i);
 }
 
-// a == 0 mod p for a value of the field's representation ([0, p), or [0, 2p) when lazy)
-template <class F>
+// a == 0 mod p for a value of the field's representation ([0, p), or [0, 2p) when lazy).
+// kEarly: limb 0 first (0 or p's limb 0 for either zero form): almost every value fails
+// there, so a test costs a compare and a branch instead of 16 logic ops. Measured on GB300:
+// G1 accumulation -0.4% / -0.6% at 2^20 / 2^22 with it, G2 +0.5% (its pairs of tests), so
+// the G1 coordinates take it and the Fq2 ones do not.
+template <class F, bool kEarly = false>
 __device__ __forceinline__ bool fe_is_zero_mod(const fe& a) {
+    if constexpr (kEarly) {
+        if (a.v[0] != 0u && (!F::LAZY || a.v[0] != F::P(0))) return false;
+    }
     if constexpr (F::LAZY) {
         uint32_t z = 0, e = 0;
 #pragma unroll
