@@ -444,7 +444,11 @@ def run_gpu_ntt(ctx, args, ranks, log_n, flush, imad_tops, hbm_peak, brief=False
                        "unit": "T IMAD/s", "frac": round(tops / imad_tops, 4), "passes": passes,
                        "launch_ms": round(pass_ms, 4), "traffic": traffic_of("ntt_pass", log_n),
                        "hbm": {"achieved": round(gbs, 1), "peak": hbm_peak, "unit": "GB/s",
-                               "frac": round(gbs / hbm_peak, 4)},
+                               "frac": round(gbs / hbm_peak, 4), "per": "pass (64 B/element each pass)"},
+                       "hbm_transform": {"achieved": round(64 * n / (passes * pass_ms * 1e-3) / 1e9, 1),
+                                         "peak": hbm_peak, "unit": "GB/s",
+                                         "frac": round(64 * n / (passes * pass_ms * 1e-3) / 1e9 / hbm_peak, 4),
+                                         "per": "transform (64 B/element in and out once, over all passes)"},
                        "algorithmic_work": "per pass 64 B/element; (n/2) log2(R) butterflies x 272 IMAD"}
     if not brief:
         # e2e: canonical host input -> device, to Montgomery, NTT, back to canonical, device -> host
