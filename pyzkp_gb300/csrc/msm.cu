@@ -649,6 +649,65 @@ __global__ void msm_hist_offsets_kernel(uint32_t* __restrict__ M, const uint32_t
     }
 }
 
+// Small pipelines: the bucket totals, their exclusive scan (row_ptr, the total at
+// row_ptr[sets B]) and the per-tile cursors in one CTA, instead of four or five launches of
+// a few microseconds each (the totals and cursors walk buckets strided by the CTA size, so
+// the count table is read and written coalesced; the scan takes contiguous runs).
+static constexpr uint32_t kMetaThreads = 1024;
+// Limits of the one-CTA form (measured on GB300: 2^12 single MSM 0.374 -> 0.360 ms with it;
+// at 2^14, 48 k counts, and in batches of 64 instances the one CTA ran as long as the
+// launches it replaces or longer)
+static constexpr uint64_t kMetaMaxBuckets = 1u << 13;  // row_ptr slots the one CTA handles
+static constexpr uint64_t kMetaMaxCounts = 1u << 14;   // per-tile counts (tiles x B) it walks
+
+__global__ void __launch_bounds__(kMetaThreads) msm_sort_meta_kernel(uint32_t* __restrict__ M,
+                                                                     const uint32_t* __restrict__ set_tile0,
+                                                                     uint32_t sets, uint32_t B,
+                                                                     uint32_t* __restrict__ row_ptr) {
+    __shared__ uint32_t part[kMetaThreads];
+    const uint32_t nb = sets * B;
+    // counts of bucket x over its set's tiles
+    for (uint32_t x = threadIdx.x; x < nb; x += blockDim.x) {
+        const uint32_t s = x / B, b = x % B;
+        uint32_t tot = 0;
+        for (uint32_t t = set_tile0[s]; t < set_tile0[s + 1]; t++) tot += M[(size_t)t * B + b];
+        row_ptr[x] = tot;
+    }
+    __syncthreads();
+    // exclusive scan: thread i sums the run [i per, (i + 1) per), the runs' sums are scanned
+    // in shared memory, then each run is rewritten as prefixes
+    const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
+    const uint32_t x0 = min(nb, threadIdx.x * per), x1 = min(nb, x0 + per);
+    uint32_t sum = 0;
+    for (uint32_t x = x0; x < x1; x++) sum += row_ptr[x];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {  // inclusive Hillis-Steele scan
+        const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t base = part[threadIdx.x] - sum;
+    for (uint32_t x = x0; x < x1; x++) {
+        const uint32_t cnt = row_ptr[x];
+        row_ptr[x] = base;
+        base += cnt;
+    }
+    if (threadIdx.x == blockDim.x - 1) row_ptr[nb] = part[blockDim.x - 1];
+    __syncthreads();
+    // cursors: M[t][b] := the first position of tile t's entries of bucket b
+    for (uint32_t x = threadIdx.x; x < nb; x += blockDim.x) {
+        const uint32_t s = x / B, b = x % B;
+        uint32_t cur = row_ptr[x];
+        for (uint32_t t = set_tile0[s]; t < set_tile0[s + 1]; t++) {
+            const uint32_t v = M[(size_t)t * B + b];
+            M[(size_t)t * B + b] = cur;
+            cur += v;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kTiledThreads) msm_scatter_tiles_kernel(const uint32_t* __restrict__ codes,
                                                                           const uint32_t* __restrict__ set_base,
                                                                           const uint32_t* __restrict__ set_tile0,
@@ -1614,16 +1673,22 @@ static int enqueue_tiled_sort(Ctx* c, MsmPipeT<C>& p, int scalars_mont) {
     ZK_LAUNCH(c, "msm_hist", msm_hist_kernel, p.tiles, kTiledThreads, smem, codes, p.set_base, p.set_tile0, sh.sets,
               p.te, sh.B, p.tile_hist);
     ZK_TRY_CUDA(cudaGetLastError());
-    const unsigned nb = (unsigned)((p.nbuckets + 255) / 256);
-    ZK_LAUNCH(c, "msm_hist_total", msm_hist_total_kernel, nb, 256, 0, p.tile_hist, p.set_tile0, sh.sets, sh.B,
-              p.row_ptr);
-    ZK_TRY_CUDA(cudaGetLastError());
-    // row_ptr[0..nbuckets) := exclusive scan; row_ptr[nbuckets] := total
-    rc = device_exclusive_scan(c, p.row_ptr, p.nbuckets, p.row_ptr + p.nbuckets, p.scan_tmp);
-    if (rc != ZK_OK) return rc;
-    ZK_LAUNCH(c, "msm_hist_offsets", msm_hist_offsets_kernel, nb, 256, 0, p.tile_hist, p.set_tile0, sh.sets, sh.B,
-              p.row_ptr);
-    ZK_TRY_CUDA(cudaGetLastError());
+    if (p.nbuckets <= kMetaMaxBuckets && (uint64_t)p.tiles * sh.B <= kMetaMaxCounts) {
+        ZK_LAUNCH(c, "msm_sort_meta", msm_sort_meta_kernel, 1, kMetaThreads, 0, p.tile_hist, p.set_tile0, sh.sets,
+                  sh.B, p.row_ptr);
+        ZK_TRY_CUDA(cudaGetLastError());
+    } else {
+        const unsigned nb = (unsigned)((p.nbuckets + 255) / 256);
+        ZK_LAUNCH(c, "msm_hist_total", msm_hist_total_kernel, nb, 256, 0, p.tile_hist, p.set_tile0, sh.sets, sh.B,
+                  p.row_ptr);
+        ZK_TRY_CUDA(cudaGetLastError());
+        // row_ptr[0..nbuckets) := exclusive scan; row_ptr[nbuckets] := total
+        rc = device_exclusive_scan(c, p.row_ptr, p.nbuckets, p.row_ptr + p.nbuckets, p.scan_tmp);
+        if (rc != ZK_OK) return rc;
+        ZK_LAUNCH(c, "msm_hist_offsets", msm_hist_offsets_kernel, nb, 256, 0, p.tile_hist, p.set_tile0, sh.sets,
+                  sh.B, p.row_ptr);
+        ZK_TRY_CUDA(cudaGetLastError());
+    }
     ZK_LAUNCH(c, "msm_scatter_tiles", msm_scatter_tiles_kernel, p.tiles, kTiledThreads, smem, codes, p.set_base,
               p.set_tile0, p.te, sh, p.d_inst, p.tile_hist, p.entries);
     ZK_TRY_CUDA(cudaGetLastError());
