@@ -1499,8 +1499,13 @@ static int pipe_init(MsmPipeT<C>& p, uint32_t c, bool fixed, bool glv, const std
     uint32_t g = kBlockG, g2 = kBlockG2;
     while (g > 2 && p.nbuckets / g < min_threads) g /= 2;
     while (g2 > 2 && p.nbuckets / g / g2 < min_threads / 2) g2 /= 2;
-    shape_blocks(p.sh, g, g2);
-    if (p.nbuckets < (uint64_t)num_sms * kSmallBucketsPerSm) p.sh.fixmax = kFixupMaxSmall;
+    // A small single MSM skips the level-2 blocks: the targets' trees get one level deeper,
+    // but a launch and its chain of 2 g2 additions go (measured on GB300: 2^10 / 2^12 /
+    // 2^14 0.327 / 0.365 / 0.490 -> 0.303 / 0.347 / 0.469 ms, 2^16 and larger the same);
+    // batches keep them (64 instances of 2^10..2^14: 1.6% slower without).
+    const bool small = p.nbuckets < (uint64_t)num_sms * kSmallBucketsPerSm;
+    shape_blocks(p.sh, g, small && jobs.size() == 1 ? 1u : g2);
+    if (small) p.sh.fixmax = kFixupMaxSmall;
     p.units = (uint32_t)((p.max_entries + p.sh.seg - 1) / p.sh.seg);
     // tiled sort when a set's counters fit shared memory: set s = k Wr + w holds n_k halves
     // entries per window (n_k W in the fixed-base mode's one set), cut into tiles of at least
