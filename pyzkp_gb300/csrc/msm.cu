@@ -76,10 +76,12 @@ static constexpr uint32_t kBlockG2 = ZK_MSM_BLOCKG2;  // level-1 blocks per leve
 // Straddling buckets over more than kFixupMax + 1 segments go to the long-bucket fixup (a
 // CTA tree per bucket); small pipelines, latency-bound, send them there from kFixupMaxSmall
 // + 2 segments on (a tree of log2(pieces) additions instead of a chain). Measured on GB300
-// (single MSMs, 4 against 8): 2^12 0.390 -> 0.371 ms, 2^16 0.767 -> 0.753 ms, 2^14 the same.
+// (single MSMs, 4 against 8): 2^12 0.390 -> 0.371 ms, 2^16 0.767 -> 0.753 ms, 2^14 the same;
+// then 3 against 4: 2^12 0.348 -> 0.331 ms, 2^10 / 2^14 / 2^16 -0.5..-1.5% (2 is slower: the
+// CTA trees of many 4-piece buckets, 2^16 0.98 ms).
 static constexpr uint32_t kFixupMax = 8;
 #ifndef ZK_FIXUP_MAX_SMALL
-#define ZK_FIXUP_MAX_SMALL 4
+#define ZK_FIXUP_MAX_SMALL 3
 #endif
 static constexpr uint32_t kFixupMaxSmall = ZK_FIXUP_MAX_SMALL;
 static constexpr uint32_t kSmallBucketsPerSm = 512;  // "small": fewer buckets than this per SM
