@@ -587,7 +587,7 @@ def sort_kernels(table: dict, steps: int, n: int, entries: int, hbm_peak: float)
     again and writes one 4-byte entry each (its per-tile counters are not counted). Atomic
     sort (bucket sets over 2^15): msm_digits reads the scalars and writes the two 32-byte
     GLV halves; msm_scatter reads the halves and writes the entries. `stage`: every sort
-    kernel together (scan and per-tile counter passes included) against the stage's own
+    kernel together (scan and per-tile counter passes, or their one-CTA form, included) against the stage's own
     minimum, the scalars in and the entries out."""
     out = {}
     for name, nbytes in (("msm_codes", n * 32 + entries * 4), ("msm_hist", entries * 4),
@@ -599,8 +599,8 @@ def sort_kernels(table: dict, steps: int, n: int, entries: int, hbm_peak: float)
         t = ms / la
         gbs = nbytes / (t * 1e-3) / 1e9
         out[name] = {"ms": round(t, 4), "bytes": nbytes, "GB_s": round(gbs, 1), "frac": round(gbs / hbm_peak, 4)}
-    names = ("msm_codes", "msm_hist", "msm_hist_total", "msm_hist_offsets", "msm_scatter_tiles", "msm_digits",
-             "msm_scatter", "scan_tiles", "scan_add")
+    names = ("msm_codes", "msm_hist", "msm_hist_total", "msm_hist_offsets", "msm_sort_meta", "msm_scatter_tiles",
+             "msm_digits", "msm_scatter", "scan_tiles", "scan_add")
     t = sum(table[k][1] / steps for k in names if k in table and table[k][0])
     if t > 0:
         nbytes = n * 32 + entries * 4
