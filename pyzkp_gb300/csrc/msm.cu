@@ -900,14 +900,31 @@ __global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_merge_kernel(const 
 #endif
 static constexpr uint64_t kFixupDensity = ZK_FIXUP_DENSITY;  // CSR entries per bucket up to which the fixup is used
 
+// Buckets of at least kHugePieces pieces (a hot digit: 10% of the scalars equal to 1 put
+// ~3300 pieces into one bucket at 2^20) are summed in chunks of about kChunkPieces pieces by
+// many CTAs, at most kMaxChunks per bucket, the last CTA to finish one adding its chunk sums
+// (one CTA for the whole bucket took 0.5 ms). Their list, count and per-bucket chunk
+// counters share the long list's count block: counts[0] long buckets, counts[1] huge
+// buckets, counts[2 .. 2 + hcap) chunks done per huge bucket, counts[2 + hcap ..] the huge
+// buckets' keys; hcap bounds the huge buckets (units / kHugePieces + 2).
+static constexpr uint32_t kHugePieces = 2048;
+static constexpr uint32_t kChunkPieces = 256;
+static constexpr uint32_t kMaxChunks = 64;
+
+__host__ __device__ inline uint32_t huge_cap(uint32_t units) { return units / kHugePieces + 2; }
+
 template <class C, bool kL2>
 __device__ __forceinline__ void fixup_bucket(const uint32_t* __restrict__ row_ptr, uint32_t seg, uint32_t fixmax,
                                              const typename C::P* slot_pts, typename C::P* buckets,
-                                             uint32_t* long_list, uint32_t* long_count, uint32_t k) {
+                                             uint32_t* long_list, uint32_t* long_count, uint32_t hcap, uint32_t k) {
     const uint32_t b0 = row_ptr[k], b1 = row_ptr[k + 1];
     if (b1 == b0) return;
     const uint32_t u0 = b0 / seg, u1 = (b1 - 1) / seg;
     if (u0 == u1) return;  // final already (written by the accumulation)
+    if (u1 - u0 >= kHugePieces) {
+        long_count[2 + hcap + atomicAdd(long_count + 1, 1u)] = k;
+        return;
+    }
     if (u1 - u0 > fixmax) {
         long_list[atomicAdd(long_count, 1u)] = k;
         return;
@@ -923,23 +940,105 @@ __global__ void __launch_bounds__(128, C::kRedMinBlocks) msm_fixup_kernel(const 
                                                         const typename C::P* __restrict__ slot_pts,
                                                         typename C::P* __restrict__ buckets,
                                                         uint32_t* __restrict__ long_list,
-                                                        uint32_t* __restrict__ long_count) {
+                                                        uint32_t* __restrict__ long_count, uint32_t hcap) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nbuckets) return;
-    fixup_bucket<C, false>(row_ptr, seg, fixmax, slot_pts, buckets, long_list, long_count, k);
+    fixup_bucket<C, false>(row_ptr, seg, fixmax, slot_pts, buckets, long_list, long_count, hcap, k);
 }
 
-// One CTA per listed bucket (items item0, item0 + stride, ...): strided partial sums, then a
-// shared-memory tree over `red` (blockDim points). (One warp per bucket with a shuffle tree
-// measured slower: 2^14 single MSM 0.127 against 0.059 ms in this kernel.)
+// The sum of the pieces of units [ua, ub] of a bucket whose first unit is u0 (its piece is
+// slot 1, the others' slot 0), or of `n` consecutive points at `pts` when pts is given, by
+// the CTA: strided partial sums, then a shared-memory tree over `red` (blockDim points)
+// spanning the next power of two of the terms. The result is valid in thread 0.
+template <class C, bool kL2>
+__device__ __forceinline__ typename C::P cta_sum(const typename C::P* slot_pts, uint32_t u0, uint32_t ua, uint32_t ub,
+                                                 const typename C::P* pts, uint32_t n, typename C::P* red) {
+    using P = typename C::P;
+    const uint32_t terms = pts != nullptr ? n : ub - ua + 1;
+    uint32_t width = 1;
+    while (width < terms && width < blockDim.x) width <<= 1;
+    P acc = xyzz_inf<typename C::T>();
+    if (threadIdx.x < width)
+        for (uint32_t t = threadIdx.x; t < terms; t += width) {
+            const P* src = pts != nullptr ? pts + t : slot_pts + 2 * (size_t)(ua + t) + (ua + t == u0 ? 1 : 0);
+            acc = xyzz_add(acc, pts != nullptr ? xyzz_ldcg(src) : xyzz_get<kL2>(src));
+        }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (uint32_t off = width / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < off) red[threadIdx.x] = xyzz_add(red[threadIdx.x], red[threadIdx.x + off]);
+        __syncthreads();
+    }
+    acc = red[0];
+    __syncthreads();  // red free again
+    return acc;
+}
+
+// Units item0, item0 + stride, ... of the CTAs: first the chunks of the huge buckets (unit
+// h kMaxChunks + ch: chunk ch of huge bucket h), then one CTA per listed long bucket. A chunk
+// sum goes to chunk_pts (h kMaxChunks + ch); the CTA whose chunk completes a bucket (counted
+// after a fence) adds the bucket's chunk sums, read through L2. Nothing waits on another CTA.
+// (One warp per long bucket with a shuffle tree measured slower: 2^14 single MSM 0.127
+// against 0.059 ms in this kernel.)
+// The chunks of the huge buckets (units item0, item0 + stride, ... of the CTAs: unit
+// h kMaxChunks + ch is chunk ch of huge bucket h). A chunk sum goes to chunk_pts
+// (h kMaxChunks + ch); the CTA whose chunk completes a bucket (counted after a fence) adds
+// the bucket's chunk sums, read through L2. Nothing waits on another CTA. Not inlined: the
+// long buckets' code around its call stays as it was without it (inlined, the long-bucket
+// kernel ran 2^12 single MSMs 8 us slower).
+template <class C, bool kL2>
+__device__ __noinline__ void fixup_huge_units(const uint32_t* __restrict__ row_ptr, uint32_t seg,
+                                              const typename C::P* slot_pts, typename C::P* buckets,
+                                              uint32_t* long_count, uint32_t hcap, uint32_t huge,
+                                              typename C::P* chunk_pts, typename C::P* red, uint32_t* s_last,
+                                              uint32_t item0, uint32_t stride) {
+    using P = typename C::P;
+    for (uint32_t unit = item0; unit < huge * kMaxChunks; unit += stride) {
+        const uint32_t h = unit / kMaxChunks, ch = unit % kMaxChunks;
+        const uint32_t k = kL2 ? __ldcg(long_count + 2 + hcap + h) : long_count[2 + hcap + h];
+        const uint32_t u0 = row_ptr[k] / seg, u1 = (row_ptr[k + 1] - 1) / seg;
+        const uint32_t pieces = u1 - u0 + 1;
+        const uint32_t nch = min(kMaxChunks, (pieces + kChunkPieces - 1) / kChunkPieces);
+        if (ch >= nch) continue;  // the same for the whole CTA
+        const uint32_t per = (pieces + nch - 1) / nch;
+        const uint32_t ua = u0 + ch * per, ub = min(u1, ua + per - 1);
+        P r = cta_sum<C, kL2>(slot_pts, u0, ua, ub, nullptr, 0, red);
+        if (threadIdx.x == 0) {
+            xyzz_store(chunk_pts + (size_t)h * kMaxChunks + ch, r);
+            __threadfence();  // the chunk sum is visible before it is counted
+            *s_last = atomicAdd(long_count + 2 + h, 1u) == nch - 1 ? 1u : 0u;
+        }
+        __syncthreads();
+        if (*s_last) {  // every chunk of bucket k is done: add their sums
+            __threadfence();
+            r = cta_sum<C, kL2>(nullptr, 0, 0, 0, chunk_pts + (size_t)h * kMaxChunks, nch, red);
+            if (threadIdx.x == 0) xyzz_store(buckets + k, r);
+        }
+        __syncthreads();  // s_last read by every thread before it is written again
+    }
+}
+
+// The huge buckets' chunks, then one CTA per listed long bucket: strided partial sums, then a
+// shared-memory tree over `red` (blockDim points). Long bucket i goes to CTA
+// (i + huge kMaxChunks) mod stride, past the CTAs of the chunk units, so that the two kinds
+// of work run side by side. (One warp per long bucket with a shuffle tree measured slower:
+// 2^14 single MSM 0.127 against 0.059 ms in this kernel; the chunks in a kernel of their own
+// before this one serialised the two, witness-like 2^20 0.25 against 0.14 ms.)
 template <class C, bool kL2>
 __device__ __forceinline__ void fixup_long_cta(const uint32_t* __restrict__ row_ptr, uint32_t seg,
                                                const typename C::P* slot_pts, typename C::P* buckets,
-                                               const uint32_t* long_list, const uint32_t* long_count,
-                                               typename C::P* red, uint32_t item0, uint32_t stride) {
+                                               const uint32_t* long_list, uint32_t* long_count, uint32_t hcap,
+                                               typename C::P* chunk_pts, typename C::P* red, uint32_t item0,
+                                               uint32_t stride) {
     using P = typename C::P;
+    __shared__ uint32_t s_last;
+    const uint32_t huge = kL2 ? __ldcg(long_count + 1) : long_count[1];
+    if (huge != 0)
+        fixup_huge_units<C, kL2>(row_ptr, seg, slot_pts, buckets, long_count, hcap, huge, chunk_pts, red, &s_last,
+                                 item0, stride);
     const uint32_t count = kL2 ? __ldcg(long_count) : *long_count;
-    for (uint32_t item = item0; item < count; item += stride) {
+    const uint32_t shift = (uint32_t)(((uint64_t)huge * kMaxChunks) % stride);
+    for (uint32_t item = (item0 + stride - shift) % stride; item < count; item += stride) {
         const uint32_t k = kL2 ? __ldcg(long_list + item) : long_list[item];
         const uint32_t u0 = row_ptr[k] / seg, u1 = (row_ptr[k + 1] - 1) / seg;
         // the tree spans the next power of two of the pieces (at most the CTA): a bucket of 16
@@ -967,9 +1066,12 @@ __global__ void __launch_bounds__(C::kFixupLongThreads, C::kFixupLongMinBlocks) 
                                                                            const typename C::P* __restrict__ slot_pts,
                                                                            typename C::P* __restrict__ buckets,
                                                                            const uint32_t* __restrict__ long_list,
-                                                                           const uint32_t* __restrict__ long_count) {
+                                                                           uint32_t* __restrict__ long_count,
+                                                                           uint32_t hcap,
+                                                                           typename C::P* __restrict__ chunk_pts) {
     __shared__ typename C::P red[C::kFixupLongThreads];
-    fixup_long_cta<C, false>(row_ptr, seg, slot_pts, buckets, long_list, long_count, red, blockIdx.x, gridDim.x);
+    fixup_long_cta<C, false>(row_ptr, seg, slot_pts, buckets, long_list, long_count, hcap, chunk_pts, red, blockIdx.x,
+                             gridDim.x);
 }
 
 // ---- 5. window reduction ----------------------------------------------------------------
@@ -1139,10 +1241,10 @@ struct MsmQPipe {
     uint32_t* slot_keys[2];
     P* slot_pts[2];
     uint32_t* long_list;
-    uint32_t* long_count;
+    uint32_t* long_count;  // the count block (see fixup_bucket), hcap huge buckets at most
     P *Yb, *Eb, *Y2, *E2, *F2, *tgt_out, *tgt;
     MsmShape sh;
-    uint32_t units, nbuckets, parts, skip_inf;
+    uint32_t units, nbuckets, parts, skip_inf, hcap;
 };
 
 struct MsmQEntry {
@@ -1250,11 +1352,11 @@ __global__ void __launch_bounds__(kMsmQThreads, 2) msm_queue_kernel(const MsmQPi
             case kQFix:
                 if (i < q.nbuckets)
                     fixup_bucket<C, true>(q.row_ptr, q.sh.seg, q.sh.fixmax, q.slot_pts[0], q.buckets, q.long_list,
-                                          q.long_count, i);
+                                          q.long_count, q.hcap, i);
                 break;
             case kQFixLong:
-                fixup_long_cta<C, true>(q.row_ptr, q.sh.seg, q.slot_pts[0], q.buckets, q.long_list, q.long_count, red,
-                                        b, sE.items);
+                fixup_long_cta<C, true>(q.row_ptr, q.sh.seg, q.slot_pts[0], q.buckets, q.long_list, q.long_count,
+                                        q.hcap, q.slot_pts[1], red, b, sE.items);
                 break;
             case kQBlk1:
                 if (i < q.sh.sets * q.sh.G) blocks_thread<C, true>(q.buckets, q.sh, q.Yb, q.Eb, i);
@@ -1565,7 +1667,8 @@ static size_t pipe_layout(MsmPipeT<C>& p, char* base) {
     p.slot_keys_b = reinterpret_cast<uint32_t*>(take(2 * first_out * 4));
     p.slot_pts_b = reinterpret_cast<P*>(take(2 * first_out * sizeof(P)));
     p.long_list = reinterpret_cast<uint32_t*>(take(((size_t)p.units / sh.fixmax + 2) * 4));
-    p.long_count = reinterpret_cast<uint32_t*>(take(4));
+    // the count block: long and huge counts, the huge buckets' chunk counters and keys
+    p.long_count = reinterpret_cast<uint32_t*>(take((2 + 2 * (size_t)huge_cap(p.units)) * 4));
     p.buckets = reinterpret_cast<P*>(take(p.nbuckets * sizeof(P)));
     p.Yb = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G * sizeof(P)));
     p.Eb = reinterpret_cast<P*>(take((size_t)sh.sets * sh.G * sizeof(P)));
@@ -1742,12 +1845,15 @@ static int pipe_enqueue_reduce(Ctx* c, MsmPipeT<C>& p) {
     // Partial sums of straddling buckets: short buckets (up to ~3 segments on average) by one
     // fixup pass, longer ones by merge rounds (kFixupDensity).
     if (p.max_entries <= (uint64_t)p.nbuckets * kFixupDensity) {
-        ZK_TRY_CUDA(cudaMemsetAsync(p.long_count, 0, 4, st));
+        const uint32_t hcap = huge_cap(p.units);
+        // counts and chunk counters to zero (the keys are written before they are read)
+        ZK_TRY_CUDA(cudaMemsetAsync(p.long_count, 0, (2 + (size_t)hcap) * 4, st));
         ZK_LAUNCH(c, "msm_fixup", msm_fixup_kernel<C>, (unsigned)((p.nbuckets + 127) / 128), 128, 0, p.row_ptr,
-                  (uint32_t)p.nbuckets, sh.seg, sh.fixmax, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
+                  (uint32_t)p.nbuckets, sh.seg, sh.fixmax, p.slot_pts_a, p.buckets, p.long_list, p.long_count, hcap);
         ZK_TRY_CUDA(cudaGetLastError());
+        // the chunk sums of huge buckets go to slot_pts_b (merge-round space, unused in fixup mode)
         ZK_LAUNCH(c, "msm_fixup_long", msm_fixup_long_kernel<C>, (unsigned)(c->num_sms * 2), C::kFixupLongThreads, 0,
-                  p.row_ptr, sh.seg, p.slot_pts_a, p.buckets, p.long_list, p.long_count);
+                  p.row_ptr, sh.seg, p.slot_pts_a, p.buckets, p.long_list, p.long_count, hcap, p.slot_pts_b);
         ZK_TRY_CUDA(cudaGetLastError());
     } else {
         uint64_t span = sh.seg;
@@ -2295,6 +2401,7 @@ static int queue_fill(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, MsmQueueT<C
         d.slot_pts[1] = p.slot_pts_b;
         d.long_list = p.long_list;
         d.long_count = p.long_count;
+        d.hcap = huge_cap(p.units);
         d.Yb = p.Yb;
         d.Eb = p.Eb;
         d.Y2 = p.Y2;
@@ -2323,7 +2430,8 @@ static int queue_launch(Ctx* c, const std::vector<MsmPipeT<C>>& pipes, MsmQueueT
     uint32_t* state = reinterpret_cast<uint32_t*>(q.dev + q.state_at);
     ZK_TRY_CUDA(cudaMemsetAsync(state, 0, (kQueueDone + q.qe.size()) * 4, c->stream));
     for (size_t k = 0; k < pipes.size(); k++)
-        if (q.fixup_mode[k]) ZK_TRY_CUDA(cudaMemsetAsync(pipes[k].long_count, 0, 4, c->stream));
+        if (q.fixup_mode[k])
+            ZK_TRY_CUDA(cudaMemsetAsync(pipes[k].long_count, 0, (2 + (size_t)huge_cap(pipes[k].units)) * 4, c->stream));
     if (c->bases_wait != nullptr) ZK_TRY_CUDA(cudaStreamWaitEvent(c->stream, c->bases_wait, 0));
     if constexpr (kQueueForm<C>) {
         ZK_LAUNCH(c, "msm_queue", msm_queue_kernel<C>, q.grid, kMsmQThreads, 0,

@@ -369,6 +369,31 @@ def test_msm_2_20_known_answer(gpu_ctx):
     assert gpu_ctx.msm_g1(bases, ds, m, offset=7) == exp2
 
 
+@pytest.mark.parametrize("log_n,c", [(16, 0), (16, 13), (18, 0), (20, 0)])
+def test_msm_hot_digit_known_answer(gpu_ctx, log_n, c):
+    """Scalars that crowd one bucket: all 1 (every entry in bucket 1 of window 0), then 1 and
+    -1 with a share of uniform scalars. The hot bucket spans thousands of accumulation
+    segments, so its pieces are summed in chunks by many CTAs and the chunk sums by the last
+    of them; the result is the known answer [sum k_i s_i]G."""
+    n = 1 << log_n
+    seed = synth.seed_for(7, log_n)
+    k = synth.base_dlogs(seed, n)
+    dk = gpu_ctx.to_device(k)
+    dxy = gpu_ctx.alloc(n * 64)
+    gpu_ctx.g1_fixed_base_mul((1, 2), dk, n, dxy)
+    bases = gpu_ctx.bases_from_device(dxy, n)
+    ones = synth.ints_to_limbs([1] * n)
+    rng = np.random.default_rng(seed)
+    mixed_ints = synth.limbs_to_ints(synth.fr_uniform(seed + 1, n))
+    pick = rng.random(n)
+    mixed_ints = [1 if u < 0.45 else (R - 1 if u < 0.9 else v) for u, v in zip(pick, mixed_ints)]
+    mixed = synth.ints_to_limbs(mixed_ints)
+    for s in (ones, mixed):
+        ds = gpu_ctx.to_device(s)
+        gpu_ctx.fr_to_mont(ds, ds, n)
+        assert gpu_ctx.msm_g1(bases, ds, n, window_bits=c) == O.affine_to_ints(O.msm_known_answer(k, s)), c
+
+
 def test_msm_2_24_known_answer(gpu_ctx):
     """A large MSM (2^24 points: 2^25 GLV halves x 8 windows = 2^28 CSR entries) against the
     known answer; bases generated on the device."""
