@@ -974,12 +974,6 @@ __device__ __forceinline__ typename C::P cta_sum(const typename C::P* slot_pts, 
     return acc;
 }
 
-// Units item0, item0 + stride, ... of the CTAs: first the chunks of the huge buckets (unit
-// h kMaxChunks + ch: chunk ch of huge bucket h), then one CTA per listed long bucket. A chunk
-// sum goes to chunk_pts (h kMaxChunks + ch); the CTA whose chunk completes a bucket (counted
-// after a fence) adds the bucket's chunk sums, read through L2. Nothing waits on another CTA.
-// (One warp per long bucket with a shuffle tree measured slower: 2^14 single MSM 0.127
-// against 0.059 ms in this kernel.)
 // The chunks of the huge buckets (units item0, item0 + stride, ... of the CTAs: unit
 // h kMaxChunks + ch is chunk ch of huge bucket h). A chunk sum goes to chunk_pts
 // (h kMaxChunks + ch); the CTA whose chunk completes a bucket (counted after a fence) adds
