@@ -335,13 +335,15 @@ __device__ __forceinline__ void xyzz_store(XyzzT<T>* p, const XyzzT<T>& a) {
 #endif
 // Threads of the CTA that sums one long bucket's pieces (strided partial sums, then a
 // shared-memory tree of the threads' partials); G2 points (256 B) keep it at 128 so that
-// the tree fits 32 KB of static shared memory. G1 runs 256 threads with two CTAs per SM
-// (128 registers, a few spilled): measured on GB300 the kernel takes 0.50 ms for the one
-// bucket of ~1600 segments that the 0/1 values of witness-like scalars make at 2^20 (MSM
-// 355 Mpts/s), against 0.54 ms with one 256-thread CTA per SM (350) and 0.66 ms with 128
-// threads (337); with ~500 long buckets of a 2^16 MSM it takes 0.080 / 0.121 / 0.084 ms.
+// the tree fits 32 KB of static shared memory. G1 runs 128 threads with four CTAs per SM
+// (a grid of as many): since huge buckets are summed in chunks by many CTAs, the CTA size
+// serves the long buckets of small pipelines, whose few pieces leave most of a wide CTA
+// idle. Measured on GB300 against 256 threads at two CTAs per SM: single MSMs 2^14 / 2^16
+// 0.476 / 0.758 -> 0.466 / 0.713 ms, 64 instances of 2^10..2^14 4.41 -> 4.28 ms; 2^18
+// +0.5%, witness-like 2^20 fixup 0.139 -> 0.158 ms. (Before the chunks, 256 threads had
+// won: one CTA summed the ~1600-segment bucket that witness-like 0/1 values make at 2^20.)
 #ifndef ZK_FIXUP_LONG_G1
-#define ZK_FIXUP_LONG_G1 256
+#define ZK_FIXUP_LONG_G1 128
 #endif
 // Minimum resident 128-thread CTAs per SM asked of the G1 merge and fixup kernels (G2 keeps
 // 1: its points need the registers).
@@ -349,7 +351,7 @@ __device__ __forceinline__ void xyzz_store(XyzzT<T>* p, const XyzzT<T>& a) {
 #define ZK_RED_MINB 1
 #endif
 #ifndef ZK_FIXUP_LONG_MINB_G1
-#define ZK_FIXUP_LONG_MINB_G1 2
+#define ZK_FIXUP_LONG_MINB_G1 4
 #endif
 struct CurveG1 {
     using T = fe;

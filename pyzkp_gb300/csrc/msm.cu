@@ -1846,7 +1846,9 @@ static int pipe_enqueue_reduce(Ctx* c, MsmPipeT<C>& p) {
                   (uint32_t)p.nbuckets, sh.seg, sh.fixmax, p.slot_pts_a, p.buckets, p.long_list, p.long_count, hcap);
         ZK_TRY_CUDA(cudaGetLastError());
         // the chunk sums of huge buckets go to slot_pts_b (merge-round space, unused in fixup mode)
-        ZK_LAUNCH(c, "msm_fixup_long", msm_fixup_long_kernel<C>, (unsigned)(c->num_sms * 2), C::kFixupLongThreads, 0,
+        // as many CTAs as fit at once (at least 2 per SM)
+        ZK_LAUNCH(c, "msm_fixup_long", msm_fixup_long_kernel<C>,
+                  (unsigned)(c->num_sms * std::max(2, C::kFixupLongMinBlocks)), C::kFixupLongThreads, 0,
                   p.row_ptr, sh.seg, p.slot_pts_a, p.buckets, p.long_list, p.long_count, hcap, p.slot_pts_b);
         ZK_TRY_CUDA(cudaGetLastError());
     } else {
